@@ -1,0 +1,333 @@
+"""Benchmark: MI estimates/s at N=1e6, k=3 on one GB300.
+
+Workload (one "step" = one batch through the C ABI): the large-sample
+precision configuration -- four bivariate Gaussian KSG MI estimates with
+rho in {0, 0.3, 0.6, 0.9} and one Frenzel-Pompe conditional MI of a 3-D
+Gaussian (corr(x,y)=0.5, corr(x,z)=corr(y,z)=0.4), all float64, N=1,000,000,
+k=3, seeded synthetic data (no dataset involved).
+
+Arms:
+  default          this library: batched FP32 tiles + FP64 recheck.
+                   `value`   = estimates/s with inputs resident in HBM
+                               (device-pointer batch), CUDA events per step;
+                   `e2e`     = the same through the C ABI with host buffers
+                               (H2D of the inputs and D2H of the results timed);
+                   `plain`   = the all-FP64 comparator, one task per call;
+                   `cpu_baseline` = the reference algorithm (SciPy cKDTree,
+                               oracle/ref_port.py) on a bounded query sample.
+  --impl reference the reference's CPU path (cKDTree calls of
+                   ennemi/_entropy_estimators.py, oracle/ref_port.py) with all
+                   host threads, each step a bounded sample of the workload.
+
+L2 (129 MB) is flushed between timed steps by writing a 512 MB buffer,
+outside the timed events.  Under torchrun each rank runs its own replica of
+the batch (tasks are independent; no collective on the data path) and rank 0
+prints the aggregate.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "MI estimates/s, N=1e6 k=3: batched FP32+recheck vs plain GPU; counts bit-exact"
+UNIT = "MI estimates/s"
+RHOS = (0.0, 0.3, 0.6, 0.9)
+CMI_COV = [[1, 0.5, 0.4], [0.5, 1, 0.4], [0.4, 0.4, 1]]
+
+
+def make_workload(n: int, seed: int = 0):
+    """[(kind, [columns])] -- kind 'mi' (x, y) or 'cmi' (x, y, z)."""
+    rng = np.random.default_rng(seed)
+    work = []
+    for rho in RHOS:
+        d = rng.multivariate_normal([0, 0], [[1, rho], [rho, 1]], size=n)
+        work.append(("mi", [np.ascontiguousarray(d[:, 0]), np.ascontiguousarray(d[:, 1])]))
+    d = rng.multivariate_normal([0, 0, 0], CMI_COV, size=n)
+    work.append(("cmi", [np.ascontiguousarray(d[:, c]) for c in range(3)]))
+    return work
+
+
+def make_tasks(work, k, cols_of=lambda c: c):
+    from ennemi_gb300 import _native as N
+    tasks = []
+    for kind, cols in work:
+        cs = [cols_of(c) for c in cols]
+        n = len(cols[0])
+        if kind == "mi":
+            tasks.append(N.Task(N.MI, k, [cs[0]], [cs[1]], n=n))
+        else:
+            tasks.append(N.Task(N.CMI, k, [cs[0]], [cs[1]], [cs[2]], n=n))
+    return tasks
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.dev = device_index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_bench_{os.getpid()}.csv")
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.dev}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.fh, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), float(parts[3]), parts[4:]))
+            except ValueError:
+                continue
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in rows:
+            for name, flag in zip(names, r[3][1:]):
+                if flag.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
+                "power_w_max": max(r[2] for r in rows), "samples": len(rows),
+                "reasons": sorted(reasons)}
+
+
+def flush_l2(buf):
+    buf.add_(1.0)
+
+
+def timed_steps(run, steps, torch, flush_buf):
+    """Sum of CUDA-event times of `steps` calls of run(), L2 flushed between."""
+    total = 0.0
+    per = []
+    for _ in range(steps):
+        flush_l2(flush_buf)
+        torch.cuda.synchronize()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record()
+        run()
+        b.record()
+        torch.cuda.synchronize()
+        ms = a.elapsed_time(b)
+        per.append(ms)
+        total += ms
+    return total, per
+
+
+def cpu_baseline(work, k, fraction, threads):
+    from oracle import ref_port
+    tasks = [(kind, tuple(cols)) for kind, cols in work]
+    t0 = time.perf_counter()
+    r = ref_port.sample_rate(tasks, k, fraction, threads=threads)
+    wall = time.perf_counter() - t0
+    return {"value": len(tasks) / r["extrapolated_s"], "unit": UNIT, "cores": r["threads"],
+            "kind": "port",
+            "sample": (f"SciPy cKDTree (the reference's calls), trees built over all N, "
+                       f"{r['fraction']:.3f} of the query points searched/counted, time scaled to "
+                       f"the full batch; measured {wall:.1f} s"),
+            "seconds_per_batch_extrapolated": r["extrapolated_s"]}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    work = make_workload(args.n, args.seed)
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup if args.warmup < 1 else 1):
+        cpu_baseline(make_workload(20000, args.seed), args.k, 0.05, threads)
+    vals, secs = [], []
+    for _ in range(args.steps):
+        cb = cpu_baseline(work, args.k, args.ref_fraction, threads)
+        vals.append(cb["value"])
+        secs.append(cb["seconds_per_batch_extrapolated"])
+    value = len(work) / (sum(secs) / len(secs))
+    cb["value"] = value
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1000.0 * sum(secs) / len(secs), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": "4x bivariate Gaussian KSG MI (rho 0/.3/.6/.9) + 1x 3-D Gaussian CMI",
+                       "n": args.n, "k": args.k, "tasks_per_step": len(work),
+                       "host_threads": threads},
+            "cpu_baseline": cb,
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=1_000_000)
+    ap.add_argument("--k", type=int, default=3)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-fraction", type=float, default=0.01)
+    ap.add_argument("--ref-fraction", type=float, default=0.01)
+    ap.add_argument("--profile", action="store_true", help="device-resident steps only (ncu)")
+    args = ap.parse_args()
+
+    if args.impl == "reference":
+        run_reference(args)
+        return
+
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    dev = torch.cuda.current_device()
+
+    from ennemi_gb300 import _native as N
+    ctx = N.context(dev)
+    ctx.set_stream(torch.cuda.current_stream().cuda_stream)
+
+    work = make_workload(args.n, args.seed + rank)
+    dcols = [[torch.from_numpy(c).cuda() for c in cols] for _, cols in work]
+    dev_tasks = make_tasks([(kind, dc) for (kind, _), dc in zip(work, dcols)], args.k)
+    host_tasks = make_tasks(work, args.k)
+    ntask = len(dev_tasks)
+    flush_buf = torch.zeros(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def step_dev():
+        N.run_tasks(dev_tasks, flags=N.INPUT_DEVICE, device=dev)
+
+    def step_host():
+        N.run_tasks(host_tasks, flags=0, device=dev)
+
+    for _ in range(max(args.warmup, 0)):
+        step_dev()
+    if args.profile:
+        torch.cuda.synchronize()
+        for _ in range(args.steps):
+            step_dev()
+        torch.cuda.synchronize()
+        return
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    barrier()
+    with ClockSampler(dev) as clk:
+        dev_ms, per = timed_steps(step_dev, args.steps, torch, flush_buf)
+    barrier()
+    clocks = clk.summary()
+
+    # end to end through the C ABI with host buffers
+    for _ in range(max(1, args.warmup // 2)):
+        step_host()
+    barrier()
+    e2e_ms, _ = timed_steps(step_host, args.steps, torch, flush_buf)
+    barrier()
+    h2d, d2h = ctx.transfer_bytes()
+
+    # per-phase device times of one more step
+    res = []
+    N.run_tasks(dev_tasks, flags=N.INPUT_DEVICE | N.TIMING, device=dev, results_out=res)
+    phases = ctx.timings()
+
+    ms_dev = dev_ms / args.steps
+    ms_e2e = e2e_ms / args.steps
+    if world > 1:
+        t = torch.tensor([ms_dev, ms_e2e], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms_dev, ms_e2e = t.tolist()
+    value = world * ntask / (ms_dev / 1000.0)
+    e2e_value = world * ntask / (ms_e2e / 1000.0)
+
+    plain = None
+    if not args.no_plain:
+        # the plain comparator: all-FP64 distances, one task per call
+        def step_plain():
+            for t in dev_tasks:
+                N.run_tasks([t], flags=N.INPUT_DEVICE | N.PLAIN_FP64, device=dev)
+        step_plain()
+        p_ms, _ = timed_steps(step_plain, 1, torch, flush_buf)
+        plain = {"value": ntask / (p_ms / 1000.0), "unit": UNIT, "ms_per_step": p_ms,
+                 "form": "all-FP64 distances, one task per egb_run_batch call, device inputs"}
+
+    if rank != 0:
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return
+
+    cpu = None
+    if not args.no_cpu:
+        cpu = cpu_baseline(work, args.k, args.cpu_fraction, os.cpu_count())
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_dev, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+        "config": {"workload": "4x bivariate Gaussian KSG MI (rho 0/.3/.6/.9) + 1x 3-D Gaussian CMI "
+                               "(corr .5/.4/.4), float64, seeded",
+                   "n": args.n, "k": args.k, "tasks_per_step": ntask,
+                   "l2": "flushed between timed steps (512 MB write)"},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "ms_per_step": ms_e2e},
+        "gpu_launches": None,
+        "phases_ms": phases,
+        "estimates": [r.value for r in res],
+        "clocks": clocks,
+        "plain": plain,
+        "speedup_vs_plain": (value / plain["value"]) if plain else None,
+        "cpu_baseline": cpu,
+        "per_step_ms": per,
+    }
+    print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

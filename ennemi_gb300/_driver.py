@@ -1,0 +1,557 @@
+"""Public API with the signatures and behaviour of ennemi/_driver.py.
+
+What differs is how the work runs.  The reference hands every (lag, variable)
+or (i, j) task to a thread pool, each task building its own cKDTrees
+(_driver.py:736-785).  Here every call collects its tasks first -- lagging,
+masking, validation and rescaling stay on the host in NumPy, so the inputs
+are bit-identical to the reference's -- and then evaluates all of them in one
+batched GPU launch sequence (``_native.run_tasks``).  Callbacks fire after
+that batch, once per task, in task order.  ``max_threads`` is accepted for
+compatibility and has no effect: there is no host thread pool.
+
+Errors and warnings are those of the reference, raised at the same points.
+"""
+
+from __future__ import annotations
+
+import sys
+import threading
+from typing import Callable, List, Optional, Sequence, Tuple, TypeVar, Union
+from warnings import warn
+
+import numpy as np
+import numpy.typing as npt
+
+from . import _native
+from ._entropy_estimators import (
+    _estimate_conditional_discrete_mi, _estimate_discrete_entropy, _estimate_discrete_mi,
+    cmi_task, conditional_semidiscrete_task, entropy_task, mi_task, semidiscrete_task)
+
+FloatArray = npt.NDArray[np.float64]
+ArrayLike = npt.ArrayLike
+GenArrayLike = TypeVar("GenArrayLike", Sequence[float], Sequence[Sequence[float]], FloatArray)
+
+DISCRETE_NORMALIZATION_WARNING = \
+    "You have set normalize=True while at least one variable is discrete. " +\
+    "The correlation coefficient formula assumes both variables to be continuous, " +\
+    "and the results are not comparable across different discrete variables. " +\
+    "Compare the raw MI against entropy of the discrete variable instead. " +\
+    "If you really want to calculate correlation coefficients, you can suppress " +\
+    "this warning by setting normalize=False and calling normalize_mi() on the results."
+
+PREPROCESS_CONSTANT_DATA_WARNING = \
+    "A variable not marked as discrete takes only a single value, " +\
+    "or values in a very small numerical range. " +\
+    "If this is intentional, you can suppress this warning by passing preprocess=False. " +\
+    "Note that this disables rescaling on all other variables as well."
+
+NAN_MSG = "input contains NaNs (after applying the mask), pass drop_nan=True to ignore"
+K_TOO_LARGE_MSG = "k must be smaller than number of observations (after lag and mask)"
+MIXED_COND_MSG = ("Conditioning is not supported with mixed discrete and continuous data. " +
+                  "This is a limitation that can be lifted in the future (see " +
+                  "https://github.com/polsys/ennemi/issues/87).")
+
+# Seed of the preprocessing noise: digits of e, as in _driver.py:874.
+NOISE_SEED = 2_718281828
+NOISE_SCALE = 1e-10
+
+
+# --------------------------------------------------------------- batching --
+
+class _Batch:
+    """Collects estimator tasks and host-side values; evaluates all GPU work
+    in one call and hands back the values in submission order."""
+
+    def __init__(self):
+        self.tasks: List[_native.Task] = []
+        self.slots: List[Tuple[str, object]] = []
+
+    def add_task(self, task: _native.Task) -> int:
+        self.slots.append(("gpu", len(self.tasks)))
+        self.tasks.append(task)
+        return len(self.slots) - 1
+
+    def add_value(self, value: float) -> int:
+        self.slots.append(("host", float(value)))
+        return len(self.slots) - 1
+
+    def run(self) -> np.ndarray:
+        gpu = _native.run_tasks(self.tasks) if self.tasks else np.empty(0)
+        out = np.empty(len(self.slots))
+        for i, (kind, v) in enumerate(self.slots):
+            out[i] = gpu[v] if kind == "gpu" else v
+        return out
+
+
+class _NoiseStream:
+    """Standard normals of default_rng(NOISE_SEED), cached and grown on demand.
+
+    The reference draws rng.normal(0, 1e-10, shape) from a fresh generator for
+    each task, in the order x, y, z (_driver.py:874-900).  Consecutive draws
+    of one generator are consecutive slices of the same stream, and
+    normal(0, s) is 0 + s * standard_normal, so slicing this cache gives the
+    same doubles bit for bit.
+    """
+
+    def __init__(self):
+        self._s = np.empty(0)
+        self._lock = threading.Lock()
+
+    def take(self, start: int, shape) -> np.ndarray:
+        count = int(np.prod(shape))
+        with self._lock:
+            if self._s.size < start + count:
+                size = max(start + count, 2 * self._s.size)
+                self._s = np.random.default_rng(NOISE_SEED).standard_normal(size)
+            s = self._s
+        return (0.0 + NOISE_SCALE * s[start:start + count]).reshape(shape)
+
+
+_noise = _NoiseStream()
+
+
+# ------------------------------------------------------------ normalise --
+
+def normalize_mi(mi: Union[float, GenArrayLike]) -> GenArrayLike:
+    """Normalize mutual information values to the unit interval.
+
+    Equivalent to passing `normalize=True` to the estimation methods: the
+    result is sqrt(1 - exp(-2 MI)), the correlation coefficient of a Gaussian
+    pair with that MI.  Non-positive values are returned unchanged.  Pandas
+    `DataFrame`/`Series` inputs keep their columns and indices.
+    """
+    if "pandas" in sys.modules:
+        import pandas
+        if isinstance(mi, (pandas.DataFrame, pandas.Series)):
+            return mi.map(_normalize)
+    return np.vectorize(_normalize, otypes=[float])(mi)
+
+
+def _normalize(mi: float) -> float:
+    if mi <= 0.0:
+        return mi
+    return np.sqrt(1 - np.exp(-2 * mi))
+
+
+# -------------------------------------------------------------- entropy --
+
+def estimate_entropy(x: ArrayLike,
+                     *, k: int = 3,
+                     multidim: bool = False,
+                     discrete: bool = False,
+                     mask: Optional[ArrayLike] = None,
+                     cond: Optional[ArrayLike] = None,
+                     drop_nan: bool = False) -> FloatArray:
+    """Estimate the entropy of one or more continuous random variables (nats).
+
+    Same parameters and results as ennemi.estimate_entropy (_driver.py:84-162):
+    each column of a 2-D `x` separately, or all columns as one variable with
+    `multidim=True`; `mask` selects observations; `cond` gives the conditional
+    entropy H(X|Y) = H(X,Y) - H(Y); `discrete=True` uses the plug-in formula;
+    `drop_nan=True` drops rows with NaNs.  All continuous estimates of the call
+    run in one batched GPU launch.
+    """
+    x_arr = np.asarray(x)
+    if mask is not None:
+        mask = np.asarray(mask)
+        _validate_mask(mask, x_arr.shape[0])
+    if not 1 <= x_arr.ndim <= 2:
+        raise ValueError("x must be one- or two-dimensional")
+    _validate_k_type(k)
+
+    if cond is None:
+        result = _estimate_entropy(x_arr, k, multidim, mask, discrete, drop_nan)
+    else:
+        cond_arr = np.asarray(cond)
+        _validate_cond(cond_arr, x_arr.shape[0])
+        result = _estimate_conditional_entropy(x_arr, cond_arr, k, multidim, mask, discrete, drop_nan)
+
+    if not multidim and "pandas" in sys.modules:
+        import pandas
+        if isinstance(x, pandas.DataFrame):
+            return pandas.DataFrame(np.atleast_2d(result), columns=x.columns)
+        elif isinstance(x, pandas.Series):
+            return pandas.DataFrame(np.atleast_2d(result), columns=[x.name])
+    return result
+
+
+def _entropy_slots(batch: _Batch, x: FloatArray, k: int, multidim: bool,
+                   mask, discrete: bool, drop_nan: bool) -> List[int]:
+    if multidim or x.ndim == 1:
+        xs = _mask_and_validate_entropy(x, mask, drop_nan, discrete, k)
+        return [_entropy_slot(batch, xs, k, discrete)]
+    return [_entropy_slot(batch, _mask_and_validate_entropy(x[:, i], mask, drop_nan, discrete, k),
+                          k, discrete) for i in range(x.shape[1])]
+
+
+def _estimate_entropy(x: FloatArray, k: int, multidim: bool,
+                      mask, discrete: bool, drop_nan: bool) -> FloatArray:
+    batch = _Batch()
+    slots = _entropy_slots(batch, x, k, multidim, mask, discrete, drop_nan)
+    values = batch.run()
+    if multidim or x.ndim == 1:
+        return np.asarray(values[slots[0]])
+    return values[slots]
+
+
+def _mask_and_validate_entropy(x: FloatArray, mask, drop_nan: bool, discrete: bool,
+                               k: int) -> FloatArray:
+    if mask is not None:
+        x = x[np.asanyarray(mask)]
+    if drop_nan and not discrete:
+        x = x[~np.max(np.isnan(x), axis=1)] if x.ndim > 1 else x[~np.isnan(x)]
+    if k >= x.shape[0]:
+        raise ValueError(K_TOO_LARGE_MSG)
+    if not discrete and np.any(np.isnan(x)):
+        raise ValueError(NAN_MSG)
+    return x
+
+
+def _entropy_slot(batch: _Batch, xs: FloatArray, k: int, discrete: bool) -> int:
+    if discrete:
+        return batch.add_value(_estimate_discrete_entropy(xs))
+    return batch.add_task(entropy_task(xs, k))
+
+
+def _estimate_conditional_entropy(x: FloatArray, cond: FloatArray, k: int, multidim: bool,
+                                  mask, discrete: bool, drop_nan: bool) -> FloatArray:
+    """H(X|Y) = H(X,Y) - H(Y), both terms in the same batch (_driver.py:202-220)."""
+    batch = _Batch()
+    marginal = _entropy_slots(batch, cond, k, True, mask, discrete, drop_nan)[0]
+    if multidim or x.ndim == 1:
+        xs = _mask_and_validate_entropy(np.column_stack((x, cond)), mask, drop_nan, discrete, k)
+        joint = [_entropy_slot(batch, xs, k, discrete)]
+    else:
+        joint = []
+        for i in range(x.shape[1]):
+            xs = _mask_and_validate_entropy(np.column_stack((x[:, i], cond)), mask, drop_nan,
+                                            discrete, k)
+            joint.append(_entropy_slot(batch, xs, k, discrete))
+    values = batch.run()
+    if multidim or x.ndim == 1:
+        return np.asarray(values[joint[0]] - values[marginal])
+    return values[joint] - values[marginal]
+
+
+# ------------------------------------------------------------------- MI --
+
+def estimate_mi(y: ArrayLike, x: ArrayLike,
+                lag: Union[Sequence[int], ArrayLike, int] = 0,
+                *, k: int = 3,
+                cond: Optional[ArrayLike] = None,
+                cond_lag: Union[Sequence[int], Sequence[Sequence[int]], ArrayLike, int] = 0,
+                mask: Optional[ArrayLike] = None,
+                discrete_y: bool = False,
+                discrete_x: bool = False,
+                preprocess: bool = True,
+                drop_nan: bool = False,
+                normalize: bool = False,
+                max_threads: Optional[int] = None,
+                callback: Optional[Callable[[int, int], None]] = None) -> FloatArray:
+    """Estimate the mutual information between y and each x variable (nats).
+
+    Same parameters and result as ennemi.estimate_mi (_driver.py:229-360): a
+    (len(lag), n_x) array; lags follow y(t) ~ x(t - lag) | z(t - cond_lag);
+    `cond` selects conditional MI, `discrete_y` / `discrete_x` the Ross
+    estimators, `preprocess` the unit-variance rescaling with fixed-seed
+    1e-10 noise, `normalize` the correlation scale.  Every (lag, variable)
+    task of the call runs in one batched GPU launch; `callback(var, lag)`
+    fires once per task after it.  `max_threads` has no effect.
+    """
+    x_arr = np.asarray(x)
+    y_arr = np.asarray(y)
+    if cond is not None:
+        cond_arr = np.column_stack((np.asarray(cond),))
+        ncond = cond_arr.shape[1]
+    else:
+        cond_arr = None
+        ncond = 1
+    mask_arr = None if mask is None else np.asarray(mask)
+
+    lag_arr = np.atleast_1d(lag)
+    cond_lag_arr = np.broadcast_to(np.column_stack((cond_lag,)), (lag_arr.shape[0], ncond))
+
+    result = _estimate_mi(y_arr, x_arr, lag_arr, k, cond_arr, cond_lag_arr, mask_arr,
+                          discrete_x, discrete_y, preprocess, drop_nan, max_threads, callback)
+
+    if normalize:
+        if discrete_x or discrete_y:
+            warn(DISCRETE_NORMALIZATION_WARNING)
+        result = normalize_mi(result)
+
+    if "pandas" in sys.modules:
+        import pandas
+        if isinstance(x, pandas.DataFrame):
+            return pandas.DataFrame(result, index=lag_arr, columns=x.columns)
+        elif isinstance(x, pandas.Series):
+            return pandas.DataFrame(result, index=lag_arr, columns=[x.name])
+    return result
+
+
+def estimate_corr(y: ArrayLike, x: ArrayLike,
+                  lag: Union[Sequence[int], ArrayLike, int] = 0,
+                  *, k: int = 3,
+                  cond: Optional[ArrayLike] = None,
+                  cond_lag: Union[Sequence[int], Sequence[Sequence[int]], ArrayLike, int] = 0,
+                  mask: Optional[ArrayLike] = None,
+                  preprocess: bool = True,
+                  drop_nan: bool = False,
+                  max_threads: Optional[int] = None,
+                  callback: Optional[Callable[[int, int], None]] = None) -> FloatArray:
+    """MI correlation between continuous variables: estimate_mi(..., normalize=True)."""
+    return estimate_mi(y, x, lag, k=k, cond=cond, cond_lag=cond_lag, mask=mask,
+                       preprocess=preprocess, drop_nan=drop_nan, normalize=True,
+                       max_threads=max_threads, callback=callback)
+
+
+def _estimate_mi(y: FloatArray, x: FloatArray, lag: FloatArray, k: int,
+                 cond: Optional[FloatArray], cond_lag: FloatArray,
+                 mask: Optional[FloatArray], discrete_x: bool, discrete_y: bool,
+                 preprocess: bool, drop_nan: bool, max_threads: Optional[int],
+                 callback: Optional[Callable[[int, int], None]]) -> FloatArray:
+    _check_parameters(x, y, k, cond, mask)
+    min_lag = min(np.min(lag), np.min(cond_lag))
+    max_lag = max(np.max(lag), np.max(cond_lag))
+    if max_lag - min_lag >= y.size or max_lag >= y.size or min_lag <= -y.size:
+        raise ValueError("lag is too large, no observations left")
+
+    nvar = 1 if x.ndim == 1 else x.shape[1]
+    indices = [(li, vi) for li in range(len(lag)) for vi in range(nvar)]
+    batch = _Batch()
+    slots = []
+    for li, vi in indices:
+        xv = x if x.ndim == 1 else x[:, vi]
+        slots.append(_lagged_mi_slot(batch, xv, y, lag[li], max_lag, min_lag, k, mask, cond,
+                                     cond_lag[li], discrete_x, discrete_y, preprocess, drop_nan))
+    values = batch.run()
+    result = np.empty((len(lag), nvar))
+    for (li, vi), s in zip(indices, slots):
+        result[li, vi] = values[s]
+        if callback is not None:
+            callback(vi, lag[li])
+    return result
+
+
+def _check_parameters(x: FloatArray, y: Optional[FloatArray], k: int,
+                      cond: Optional[FloatArray], mask: Optional[FloatArray]) -> None:
+    _validate_k_type(k)
+    if not 1 <= len(x.shape) <= 2:
+        raise ValueError("x must be one- or two-dimensional")
+    if y is not None:
+        if len(y.shape) > 1:
+            raise ValueError("y must be one-dimensional")
+        if x.shape[0] != y.shape[0]:
+            raise ValueError("x and y must have same length")
+    if mask is not None:
+        _validate_mask(mask, x.shape[0])
+    if cond is not None:
+        _validate_cond(cond, x.shape[0])
+
+
+def _validate_k_type(k: int) -> None:
+    if not isinstance(k, int):
+        raise TypeError("k must be int")
+    if k <= 0:
+        raise ValueError("k must be greater than zero")
+
+
+def _validate_mask(mask: FloatArray, input_len: int) -> None:
+    if len(mask.shape) > 1:
+        raise ValueError("mask must be one-dimensional")
+    if len(mask) != input_len:
+        raise ValueError("mask length does not match input length")
+    if mask.dtype != bool:
+        raise TypeError("mask must contain only booleans")
+
+
+def _validate_cond(cond: FloatArray, input_len: int) -> None:
+    if not 1 <= cond.ndim <= 2:
+        raise ValueError("cond must be one- or two-dimensional")
+    if input_len != len(cond):
+        raise ValueError("x and cond must have same length")
+
+
+# ------------------------------------------------------------- pairwise --
+
+def pairwise_mi(data: ArrayLike,
+                *, k: int = 3,
+                cond: Optional[ArrayLike] = None,
+                mask: Optional[ArrayLike] = None,
+                discrete: ArrayLike = False,
+                preprocess: bool = True,
+                drop_nan: bool = False,
+                normalize: bool = False,
+                max_threads: Optional[int] = None,
+                callback: Optional[Callable[[int, int], None]] = None) -> FloatArray:
+    """Pairwise MI between the columns of `data` (nats); NaN diagonal.
+
+    Same parameters and result as ennemi.pairwise_mi (_driver.py:540-623).
+    All i < j pairs run in one batched GPU launch; `callback(i, j)` fires once
+    per pair after it.  `max_threads` has no effect.
+    """
+    data_arr = np.asarray(data)
+    cond_arr = None if cond is None else np.column_stack((np.asarray(cond),))
+    mask_arr = None if mask is None else np.asarray(mask)
+
+    if data_arr.ndim == 1 or data_arr.shape[1] == 1:
+        return np.full((1, 1), np.nan)
+
+    discrete_arr = np.broadcast_to(discrete, data_arr.shape[1])
+    result = _pairwise_mi(data_arr, k, cond_arr, preprocess, drop_nan, mask_arr, discrete_arr,
+                          max_threads, callback)
+
+    if normalize:
+        if discrete_arr.any():
+            warn(DISCRETE_NORMALIZATION_WARNING)
+        result = normalize_mi(result)
+
+    if "pandas" in sys.modules:
+        import pandas
+        if isinstance(data, pandas.DataFrame):
+            return pandas.DataFrame(result, index=data.columns, columns=data.columns)
+    return result
+
+
+def pairwise_corr(data: ArrayLike,
+                  *, k: int = 3,
+                  cond: Optional[ArrayLike] = None,
+                  mask: Optional[ArrayLike] = None,
+                  preprocess: bool = True,
+                  drop_nan: bool = False,
+                  max_threads: Optional[int] = None,
+                  callback: Optional[Callable[[int, int], None]] = None) -> FloatArray:
+    """Pairwise MI correlation: pairwise_mi(..., normalize=True)."""
+    return pairwise_mi(data, k=k, cond=cond, mask=mask, preprocess=preprocess,
+                       drop_nan=drop_nan, normalize=True, max_threads=max_threads,
+                       callback=callback)
+
+
+def _pairwise_mi(data: FloatArray, k: int, cond: Optional[FloatArray], preprocess: bool,
+                 drop_nan: bool, mask: Optional[FloatArray], discrete: FloatArray,
+                 max_threads: Optional[int],
+                 callback: Optional[Callable[[int, int], None]]) -> FloatArray:
+    _check_parameters(data, None, k, cond, mask)
+    if (not (np.all(discrete) or np.all(~discrete))) and (cond is not None):
+        raise ValueError(MIXED_COND_MSG)
+    nvar = data.shape[1]
+    cond_lag = np.full(cond.shape[1], 0) if cond is not None else np.asarray(0)
+
+    batch = _Batch()
+    pairs = []
+    slots = []
+    for i in range(nvar):
+        for j in range(i + 1, nvar):
+            pairs.append((i, j))
+            slots.append(_lagged_mi_slot(batch, data[:, i], data[:, j], 0, 0, 0, k, mask, cond,
+                                         cond_lag, discrete[i], discrete[j], preprocess,
+                                         drop_nan))
+    values = batch.run()
+    result = np.full((nvar, nvar), np.nan)
+    for (i, j), s in zip(pairs, slots):
+        result[i, j] = values[s]
+        result[j, i] = values[s]
+        if callback is not None:
+            callback(i, j)
+    return result
+
+
+# ------------------------------------------------------- per-task prep --
+
+def _lagged_mi_slot(batch: _Batch, x: FloatArray, y: FloatArray, lag: int, max_lag: int,
+                    min_lag: int, k: int, mask: Optional[FloatArray], cond: Optional[FloatArray],
+                    cond_lag: FloatArray, discrete_x: bool, discrete_y: bool, preprocess: bool,
+                    drop_nan: bool) -> int:
+    """One task of _lagged_mi (_driver.py:788-832): slice, mask, validate,
+    rescale, then queue the estimator (or evaluate a discrete one)."""
+    min_lag = min(min_lag, 0)
+    max_lag = max(max_lag, 0)
+    xs = x[max_lag - lag: len(x) - lag + min_lag]
+    ys = y[max_lag: len(y) + min_lag]
+    if cond is not None:
+        zs = np.column_stack([cond[max_lag - cond_lag[i]: len(cond) - cond_lag[i] + min_lag, i]
+                              for i in range(len(cond_lag))])
+    else:
+        zs = None
+
+    xs, ys, zs = _apply_masks(xs, ys, zs, mask, min_lag, max_lag, drop_nan)
+    _validate_masked_data(xs, ys, zs, k, discrete_x, discrete_y)
+    if preprocess:
+        xs, ys, zs = _rescale_data(xs, ys, zs, discrete_x, discrete_y)
+
+    if zs is None:
+        if discrete_x and discrete_y:
+            return batch.add_value(_estimate_discrete_mi(xs, ys))
+        if discrete_x:
+            return batch.add_task(semidiscrete_task(ys, xs, k))
+        if discrete_y:
+            return batch.add_task(semidiscrete_task(xs, ys, k))
+        return batch.add_task(mi_task(xs, ys, k))
+    if discrete_x and discrete_y:
+        return batch.add_value(_estimate_conditional_discrete_mi(xs, ys, zs))
+    if discrete_x:
+        return batch.add_task(conditional_semidiscrete_task(ys, xs, zs, k))
+    if discrete_y:
+        return batch.add_task(conditional_semidiscrete_task(xs, ys, zs, k))
+    return batch.add_task(cmi_task(xs, ys, zs, k))
+
+
+def _apply_masks(xs: FloatArray, ys: FloatArray, zs: Optional[FloatArray],
+                 mask: Optional[FloatArray], min_lag: int, max_lag: int,
+                 drop_nan: bool) -> Tuple[FloatArray, FloatArray, Optional[FloatArray]]:
+    """The mask is indexed in y's time frame (_driver.py:834-854)."""
+    if mask is not None:
+        sub = mask[max_lag: len(mask) + min_lag]
+        xs, ys = xs[sub], ys[sub]
+        if zs is not None:
+            zs = zs[sub]
+    if drop_nan:
+        keep = ~(np.isnan(xs) | np.isnan(ys))
+        if zs is not None:
+            keep &= ~np.max(np.isnan(zs), axis=1)
+            zs = zs[keep]
+        xs, ys = xs[keep], ys[keep]
+    return xs, ys, zs
+
+
+def _validate_masked_data(xs: FloatArray, ys: FloatArray, zs: Optional[FloatArray], k: int,
+                          discrete_x: bool, discrete_y: bool) -> None:
+    if len(ys) <= k:
+        raise ValueError(K_TOO_LARGE_MSG)
+    if (not discrete_x or xs.dtype.kind in "iufc") and np.isnan(xs).any():
+        raise ValueError(NAN_MSG)
+    if (not discrete_y or ys.dtype.kind in "iufc") and np.isnan(ys).any():
+        raise ValueError(NAN_MSG)
+    if not (discrete_x and discrete_y) and zs is not None and np.isnan(zs).any():
+        raise ValueError(NAN_MSG)
+
+
+def _rescale_data(xs: FloatArray, ys: FloatArray, zs: Optional[FloatArray],
+                  discrete_x: bool, discrete_y: bool):
+    """Unit variance plus 1e-10 noise, drawn in the order x, y, z from the
+    fixed-seed stream (_driver.py:871-902).  Constant data is left as is,
+    with a warning, and draws no noise."""
+    pos = 0
+    if not discrete_x:
+        std = xs.std()
+        if np.abs(std) < 1e-20:
+            warn(PREPROCESS_CONSTANT_DATA_WARNING)
+        else:
+            xs = (xs - xs.mean()) / std
+            xs += _noise.take(pos, xs.shape)
+            pos += xs.size
+    if not discrete_y:
+        std = ys.std()
+        if np.abs(std) < 1e-20:
+            warn(PREPROCESS_CONSTANT_DATA_WARNING)
+        else:
+            ys = (ys - ys.mean()) / std
+            ys += _noise.take(pos, ys.shape)
+            pos += ys.size
+    if zs is not None and not (discrete_x and discrete_y):
+        std = zs.std(axis=0)
+        if np.any(np.abs(std) < 1e-20):
+            warn(PREPROCESS_CONSTANT_DATA_WARNING)
+        else:
+            zs = (zs - zs.mean(axis=0)) / std
+            zs += _noise.take(pos, zs.shape)
+    return xs, ys, zs

@@ -1,0 +1,250 @@
+"""ctypes binding of libennemi_gb.so (include/ennemi_gb.h).
+
+This is the only way the package reaches the GPU: there is no CPU fallback.
+If the library is missing or no CUDA device is visible, every estimator call
+raises ``RuntimeError``.
+
+``run_tasks`` evaluates a list of :class:`Task` in one ``egb_run_batch`` call.
+Columns may be NumPy arrays (host memory; uploaded by the library, each
+distinct address range once) or CUDA tensors exposing ``data_ptr()`` (device
+memory, used in place); one batch uses one kind.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+from dataclasses import dataclass, field
+from typing import List, Optional, Sequence
+
+import numpy as np
+
+from . import _build
+
+MI, CMI, SEMI, CSEMI, ENTROPY = 0, 1, 2, 3, 4
+
+INPUT_DEVICE = 1 << 0
+PLAIN_FP64 = 1 << 1
+TIMING = 1 << 2
+FORCE_BRUTE = 1 << 3
+KEEP_INTERNALS = 1 << 4
+FORCE_SLAB = 1 << 5
+
+PHASES = ("upload", "prepare", "sort", "knn", "counts", "combine", "total")
+
+
+class EgbColumn(ctypes.Structure):
+    _fields_ = [("data", ctypes.c_void_p), ("stride", ctypes.c_int64)]
+
+
+class EgbTask(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int32), ("k", ctypes.c_int32), ("n", ctypes.c_int64),
+                ("dx", ctypes.c_int32), ("dy", ctypes.c_int32), ("dz", ctypes.c_int32),
+                ("nclass", ctypes.c_int32), ("cols", ctypes.POINTER(EgbColumn)),
+                ("labels", ctypes.POINTER(ctypes.c_int32))]
+
+
+class EgbResult(ctypes.Structure):
+    _fields_ = [("value", ctypes.c_double), ("term_sum", ctypes.c_double),
+                ("zero_mask", ctypes.c_uint32), ("status", ctypes.c_int32)]
+
+
+_lib = None
+_lib_lock = threading.Lock()
+_ctx = {}
+
+
+def lib_path() -> str:
+    return _build.LIB_PATH
+
+
+def load():
+    """Load libennemi_gb.so (building it first if the sources are newer)."""
+    global _lib
+    with _lib_lock:
+        if _lib is not None:
+            return _lib
+        if _build.needs_build():
+            _build.build()
+        lib = ctypes.CDLL(_build.LIB_PATH)
+        vp, i32, i64 = ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64
+        dp = ctypes.POINTER(ctypes.c_double)
+        lib.egb_create.argtypes = [ctypes.c_int, ctypes.POINTER(vp)]
+        lib.egb_create.restype = ctypes.c_int
+        lib.egb_destroy.argtypes = [vp]
+        lib.egb_destroy.restype = None
+        lib.egb_set_stream.argtypes = [vp, vp]
+        lib.egb_set_stream.restype = ctypes.c_int
+        lib.egb_last_error.argtypes = [vp]
+        lib.egb_last_error.restype = ctypes.c_char_p
+        lib.egb_run_batch.argtypes = [vp, ctypes.POINTER(EgbTask), i32, i32, ctypes.POINTER(EgbResult)]
+        lib.egb_run_batch.restype = ctypes.c_int
+        lib.egb_fetch.argtypes = [vp, i32, i32, vp]
+        lib.egb_fetch.restype = ctypes.c_int
+        lib.egb_knn_eps.argtypes = [vp, vp, i64, i32, i32, i32, vp]
+        lib.egb_knn_eps.restype = ctypes.c_int
+        lib.egb_ball_count.argtypes = [vp, vp, i64, i32, vp, i32, vp]
+        lib.egb_ball_count.restype = ctypes.c_int
+        lib.egb_timings.argtypes = [vp, dp, i32]
+        lib.egb_timings.restype = ctypes.c_int
+        lib.egb_last_transfer.argtypes = [vp, ctypes.POINTER(i64), ctypes.POINTER(i64)]
+        lib.egb_last_transfer.restype = ctypes.c_int
+        lib.egb_version.argtypes = []
+        lib.egb_version.restype = ctypes.c_char_p
+        _lib = lib
+        return lib
+
+
+class Context:
+    """One library context (device, stream, arena).  Calls are serialised."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load()
+        self.device = device
+        h = ctypes.c_void_p()
+        rc = self.lib.egb_create(device, ctypes.byref(h))
+        if rc != 0:
+            raise RuntimeError(f"egb_create(device={device}) failed ({rc}): no usable CUDA device")
+        self.h = h
+        self.lock = threading.Lock()
+
+    def close(self):
+        if self.h:
+            self.lib.egb_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def error(self) -> str:
+        return self.lib.egb_last_error(self.h).decode()
+
+    def check(self, rc: int, what: str):
+        if rc != 0:
+            raise RuntimeError(f"{what} failed ({rc}): {self.error()}")
+
+    def set_stream(self, stream_handle: int | None):
+        self.check(self.lib.egb_set_stream(self.h, ctypes.c_void_p(stream_handle or 0)), "egb_set_stream")
+
+    def transfer_bytes(self):
+        a, b = ctypes.c_int64(), ctypes.c_int64()
+        self.lib.egb_last_transfer(self.h, ctypes.byref(a), ctypes.byref(b))
+        return a.value, b.value
+
+    def timings(self) -> dict:
+        buf = (ctypes.c_double * 8)()
+        n = self.lib.egb_timings(self.h, buf, 8)
+        return {PHASES[i]: buf[i] for i in range(n)}
+
+
+def context(device: int = 0) -> Context:
+    ctx = _ctx.get(device)
+    if ctx is None:
+        ctx = Context(device)
+        _ctx[device] = ctx
+    return ctx
+
+
+@dataclass
+class Task:
+    """One estimator invocation: columns are x first, then y, then z."""
+    kind: int
+    k: int
+    x: Sequence
+    y: Sequence = ()
+    z: Sequence = ()
+    labels: Optional[np.ndarray] = None   # int32 class index per sample (SEMI/CSEMI)
+    nclass: int = 0
+    n: int = 0
+    keep: List = field(default_factory=list)
+
+
+def as_columns(a) -> list:
+    """Split a float64 array (1-D or n x d) into a list of 1-D column views."""
+    a = np.asarray(a, dtype=np.float64)
+    if a.ndim == 1:
+        return [a]
+    return [a[:, c] for c in range(a.shape[1])]
+
+
+def _col_struct(col, device: bool):
+    if device:
+        stride = col.stride(0) if col.dim() == 1 else col.stride(0)
+        return EgbColumn(col.data_ptr(), int(stride)), col
+    c = np.asarray(col, dtype=np.float64)
+    if c.ndim != 1:
+        raise ValueError("columns must be one-dimensional")
+    s = c.strides[0]
+    if s <= 0 or s % 8 != 0 or not c.flags.aligned:
+        c = np.ascontiguousarray(c)
+        s = 8
+    return EgbColumn(c.ctypes.data, s // 8), c
+
+
+def run_tasks(tasks: List[Task], flags: int = 0, device: int = 0,
+              results_out: Optional[list] = None) -> np.ndarray:
+    """Evaluate the tasks in one batched call; returns the estimates."""
+    if not tasks:
+        return np.empty(0)
+    ctx = context(device)
+    is_dev = bool(flags & INPUT_DEVICE)
+    ctasks = (EgbTask * len(tasks))()
+    keep = []
+    for i, t in enumerate(tasks):
+        cols = list(t.x) + list(t.y) + list(t.z)
+        arr = (EgbColumn * len(cols))()
+        for c, col in enumerate(cols):
+            arr[c], ref = _col_struct(col, is_dev)
+            keep.append(ref)
+        keep.append(arr)
+        n = t.n or (cols[0].shape[0])
+        ct = ctasks[i]
+        ct.kind, ct.k, ct.n = t.kind, int(t.k), int(n)
+        ct.dx, ct.dy, ct.dz = len(t.x), len(t.y), len(t.z)
+        ct.cols = arr
+        if t.labels is not None:
+            lab = np.ascontiguousarray(t.labels, dtype=np.int32)
+            keep.append(lab)
+            ct.labels = lab.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+            ct.nclass = int(t.nclass)
+    res = (EgbResult * len(tasks))()
+    with ctx.lock:
+        rc = ctx.lib.egb_run_batch(ctx.h, ctasks, len(tasks), flags, res)
+        ctx.check(rc, "egb_run_batch")
+    if results_out is not None:
+        results_out.extend(res)
+    return np.array([r.value for r in res], dtype=np.float64)
+
+
+def fetch(task_index: int, which: int, n: int, device: int = 0) -> np.ndarray:
+    """eps (which=0) or count slot which-1 of the last batch run with KEEP_INTERNALS."""
+    ctx = context(device)
+    out = np.empty(n, dtype=np.float64 if which == 0 else np.int64)
+    with ctx.lock:
+        ctx.check(ctx.lib.egb_fetch(ctx.h, task_index, which, out.ctypes.data), "egb_fetch")
+    return out
+
+
+def knn_eps(points, k: int, flags: int = 0, device: int = 0) -> np.ndarray:
+    """cKDTree(points).query(points, k=[k+1], p=inf)[0].ravel() on the GPU."""
+    ctx = context(device)
+    p = np.ascontiguousarray(points, dtype=np.float64)
+    if p.ndim == 1:
+        p = p.reshape(-1, 1)
+    out = np.empty(p.shape[0])
+    with ctx.lock:
+        ctx.check(ctx.lib.egb_knn_eps(ctx.h, p.ctypes.data, p.shape[0], p.shape[1], int(k),
+                                      flags & ~INPUT_DEVICE, out.ctypes.data), "egb_knn_eps")
+    return out
+
+
+def ball_count(points, radius, flags: int = 0, device: int = 0) -> np.ndarray:
+    """cKDTree(points).query_ball_point(points, radius, p=inf, return_length=True)."""
+    ctx = context(device)
+    p = np.ascontiguousarray(points, dtype=np.float64)
+    if p.ndim == 1:
+        p = p.reshape(-1, 1)
+    r = np.ascontiguousarray(np.broadcast_to(np.asarray(radius, dtype=np.float64), (p.shape[0],)))
+    out = np.empty(p.shape[0], dtype=np.int64)
+    with ctx.lock:
+        ctx.check(ctx.lib.egb_ball_count(ctx.h, p.ctypes.data, p.shape[0], p.shape[1], r.ctypes.data,
+                                         flags & ~INPUT_DEVICE, out.ctypes.data), "egb_ball_count")
+    return out

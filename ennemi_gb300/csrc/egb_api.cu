@@ -1,0 +1,959 @@
+// egb_api.cu -- host planner and C ABI of libennemi_gb.so (include/ennemi_gb.h).
+//
+// One egb_run_batch() call turns a list of estimator invocations into a fixed
+// sequence of batched launches on one stream:
+//
+//   upload      caller columns (host memory: each distinct address range once)
+//               and the descriptor tables (one pinned copy)
+//   gather      -> per-task working FP64 columns (class-grouped for the
+//               semidiscrete estimators)
+//   prepare     column midranges (centres of the FP32 copies)
+//   sort        every 1-D space and the first column of every slab job, one
+//               segmented LSD radix sort for the whole batch
+//   materialise multi-D job blocks (FP64 + centred FP32, working or sorted)
+//   kNN         1-D: merge on sorted keys; multi-D: tile kernels (brute force
+//               or slab), any-K select for k + 1 > 32
+//   radius      rad = eps - 1e-12
+//   counts      1-D: gallop + bisect on sorted keys; multi-D: tile kernels
+//   combine     per-task term sums (psi table / log) + zero flags
+//   download    partial sums, flags, device error word
+//
+// The spaces each estimator searches follow ennemi/_entropy_estimators.py:
+//   MI     kNN (x,y) all;  counts x, y                          (:69-113)
+//   CMI    kNN (x,y,z);    counts (x,z), (y,z), z               (:116-156)
+//   SEMI   kNN x per class of y;  count x over all samples      (:159-200)
+//   CSEMI  kNN (x,z) per class;   counts (x,z) all, z within the
+//          class, z all                                          (:203-247)
+//   ENT    kNN x                                                 (:21-42)
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "egb_internal.cuh"
+#include "ennemi_gb.h"
+
+using namespace egb;
+
+namespace {
+
+constexpr int KIND_KNN_ONLY = 100;    // egb_knn_eps
+constexpr int KIND_COUNT_ONLY = 101;  // egb_ball_count
+constexpr int SLAB_MIN = 4096;        // shorter multi-D segments use brute force
+constexpr int NPHASE = 7;
+
+// Digamma of a positive integer with the reference's formula
+// (ennemi/_entropy_estimators.py:341-348): the SciPy constant for psi(1),
+// otherwise the asymptotic expansion in the same order of operations.
+double psi_int(double y) {
+  if (y == 1.0) return -0.5772156649015331;
+  return std::log(y) -
+         std::pow(y, -6) * (std::pow(y, 2) * (std::pow(y, 2) * (y / 2 + 1.0 / 12) - 1.0 / 120) +
+                            1.0 / 252);
+}
+
+size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+int64_t round32(int64_t n) { return (n + 31) / 32 * 32; }
+
+struct Layout {
+  size_t off = 0;
+  size_t take(size_t bytes, size_t align = 256) {
+    off = align_up(off, align);
+    const size_t o = off;
+    off += bytes;
+    return o;
+  }
+};
+
+struct TaskPlan {
+  int kind = 0, k = 0, K = 0;
+  int64_t n = 0, ld = 0;
+  int dx = 0, dy = 0, dz = 0, ncol = 0, nclass = 0, nslot = 0;
+  std::vector<int32_t> perm;      // working -> caller index; empty = identity
+  std::vector<int64_t> cls_off;   // class segment starts (nclass + 1)
+  size_t off_x64 = 0, off_eps = 0, off_rad = 0, off_cnt[3] = {0, 0, 0};
+  size_t tab_perm = 0;            // offset of perm inside the table blob
+  size_t tab_rad = 0;             // KIND_COUNT_ONLY: caller radii (host input)
+  int center0 = 0;                // first column of the task in the centre array
+};
+
+struct SegKey {
+  int task, col;
+  int64_t b, e;
+  bool operator<(const SegKey& o) const {
+    return std::tie(task, col, b, e) < std::tie(o.task, o.col, o.b, o.e);
+  }
+};
+
+struct Space {
+  int task;
+  int64_t b, e;
+  SpaceCols sp;
+  int K;     // kNN: k + 1
+  int slot;  // counts
+};
+
+}  // namespace
+
+struct egb_ctx {
+  int device = 0;
+  int num_sms = 1;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  void* arena = nullptr;
+  size_t arena_cap = 0;
+  void* pinned = nullptr;
+  size_t pinned_cap = 0;
+  double* psi_d = nullptr;
+  int64_t psi_len = 0;
+  cudaEvent_t ev[NPHASE + 1] = {};
+  double timings[NPHASE] = {};
+  int ntimings = 0;
+  int64_t h2d_bytes = 0, d2h_bytes = 0;
+  // internals of the last batch (egb_fetch)
+  bool kept = false;
+  std::vector<TaskPlan> keep;
+};
+
+namespace {
+
+int fail(egb_ctx* ctx, int code, const std::string& msg) {
+  if (ctx) ctx->err = msg;
+  return code;
+}
+
+#define EGB_CUDA(call)                                                                 \
+  do {                                                                                 \
+    cudaError_t e_ = (call);                                                           \
+    if (e_ != cudaSuccess)                                                             \
+      return fail(ctx, EGB_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+int ensure_arena(egb_ctx* ctx, size_t bytes) {
+  if (bytes <= ctx->arena_cap) return EGB_OK;
+  if (ctx->arena) cudaFree(ctx->arena);
+  ctx->arena = nullptr;
+  ctx->arena_cap = 0;
+  const size_t want = align_up(bytes + bytes / 8, 1 << 20);
+  if (cudaMalloc(&ctx->arena, want) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(ctx, EGB_ERR_NOMEM, "device allocation of " + std::to_string(want) + " bytes failed");
+  }
+  ctx->arena_cap = want;
+  return EGB_OK;
+}
+
+int ensure_pinned(egb_ctx* ctx, size_t bytes) {
+  if (bytes <= ctx->pinned_cap) return EGB_OK;
+  if (ctx->pinned) cudaFreeHost(ctx->pinned);
+  ctx->pinned = nullptr;
+  ctx->pinned_cap = 0;
+  const size_t want = align_up(bytes + bytes / 8, 1 << 16);
+  if (cudaMallocHost(&ctx->pinned, want) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(ctx, EGB_ERR_NOMEM, "pinned host allocation of " + std::to_string(want) + " bytes failed");
+  }
+  ctx->pinned_cap = want;
+  return EGB_OK;
+}
+
+int ensure_psi(egb_ctx* ctx, int64_t need) {
+  if (need <= ctx->psi_len) return EGB_OK;
+  int64_t len = std::max<int64_t>(need, 1 << 16);
+  std::vector<double> tab((size_t)len);
+  tab[0] = 0.0;  // placeholder: zero counts are flagged, never looked up
+  for (int64_t i = 1; i < len; ++i) tab[(size_t)i] = psi_int((double)i);
+  double* d = nullptr;
+  if (cudaMalloc(&d, sizeof(double) * (size_t)len) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(ctx, EGB_ERR_NOMEM, "device allocation of the digamma table failed");
+  }
+  EGB_CUDA(cudaMemcpyAsync(d, tab.data(), sizeof(double) * (size_t)len, cudaMemcpyHostToDevice,
+                           ctx->stream));
+  EGB_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (ctx->psi_d) cudaFree(ctx->psi_d);
+  ctx->psi_d = d;
+  ctx->psi_len = len;
+  return EGB_OK;
+}
+
+void set_cols(SpaceCols& sp, std::initializer_list<std::pair<int, int>> ranges) {
+  sp.d = 0;
+  std::memset(sp.cols, 0, sizeof(sp.cols));
+  for (auto r : ranges)
+    for (int c = r.first; c < r.first + r.second; ++c) sp.cols[sp.d++] = (int8_t)c;
+}
+
+// extra: per-task extras for the internal kinds (radius for KIND_COUNT_ONLY)
+int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_result* results,
+              const double* count_radius) {
+  if (!ctx) return EGB_ERR_ARG;
+  if (ntasks < 0 || (ntasks > 0 && !tasks)) return fail(ctx, EGB_ERR_ARG, "invalid task list");
+  if (ntasks == 0) return EGB_OK;
+  const bool dev_in = (flags & EGB_INPUT_DEVICE) != 0;
+  const int plain = (flags & EGB_PLAIN_FP64) ? 1 : 0;
+  const bool force_brute = (flags & EGB_FORCE_BRUTE) != 0;
+  const bool force_slab = (flags & EGB_FORCE_SLAB) != 0 && !force_brute;
+  const bool timing = (flags & EGB_TIMING) != 0;
+  cudaStream_t st = ctx->stream;
+  ctx->kept = false;
+  ctx->keep.clear();
+
+  // ------------------------------------------------------------ validate --
+  std::vector<TaskPlan> P((size_t)ntasks);
+  int64_t max_n = 1, max_ld = 32;
+  int ncols_total = 0;
+  for (int t = 0; t < ntasks; ++t) {
+    const egb_task& T = tasks[t];
+    TaskPlan& p = P[(size_t)t];
+    const std::string who = "task " + std::to_string(t) + ": ";
+    p.kind = T.kind;
+    p.k = T.k;
+    p.n = T.n;
+    p.dx = T.dx;
+    p.dy = T.dy;
+    p.dz = T.dz;
+    p.ncol = T.dx + T.dy + T.dz;
+    const bool internal = T.kind == KIND_KNN_ONLY || T.kind == KIND_COUNT_ONLY;
+    if (!(T.kind >= EGB_MI && T.kind <= EGB_ENTROPY) && !internal)
+      return fail(ctx, EGB_ERR_ARG, who + "unknown estimator kind");
+    if (T.n < 1 || T.n > (int64_t)0x3fffffff) return fail(ctx, EGB_ERR_ARG, who + "n out of range");
+    if (T.k < 1 && T.kind != KIND_COUNT_ONLY) return fail(ctx, EGB_ERR_ARG, who + "k must be greater than zero");
+    if (T.dx < 1 || T.dy < 0 || T.dz < 0 || p.ncol > EGB_DMAX)
+      return fail(ctx, EGB_ERR_ARG, who + "column counts out of range (at most 32 columns)");
+    const bool needs_y = T.kind == EGB_MI || T.kind == EGB_CMI;
+    const bool needs_z = T.kind == EGB_CMI || T.kind == EGB_CSEMI;
+    if ((needs_y != (T.dy > 0)) || (needs_z != (T.dz > 0)))
+      return fail(ctx, EGB_ERR_ARG, who + "column counts do not match the estimator kind");
+    if (!T.cols) return fail(ctx, EGB_ERR_ARG, who + "null column list");
+    for (int c = 0; c < p.ncol; ++c)
+      if (!T.cols[c].data || T.cols[c].stride < 1)
+        return fail(ctx, EGB_ERR_ARG, who + "invalid column " + std::to_string(c));
+    p.K = T.k + 1;
+    p.ld = round32(T.n);
+    p.center0 = ncols_total;
+    ncols_total += p.ncol;
+    max_n = std::max(max_n, T.n);
+    max_ld = std::max(max_ld, p.ld);
+    p.nslot = T.kind == EGB_MI ? 2 : (T.kind == EGB_CMI || T.kind == EGB_CSEMI) ? 3
+              : (T.kind == EGB_SEMI || T.kind == KIND_COUNT_ONLY) ? 1 : 0;
+    if (T.kind == EGB_SEMI || T.kind == EGB_CSEMI) {
+      if (!T.labels || T.nclass < 1) return fail(ctx, EGB_ERR_ARG, who + "labels required");
+      p.nclass = T.nclass;
+      std::vector<int64_t> cnt((size_t)T.nclass + 1, 0);
+      for (int64_t i = 0; i < T.n; ++i) {
+        const int32_t c = T.labels[i];
+        if (c < 0 || c >= T.nclass) return fail(ctx, EGB_ERR_ARG, who + "label out of range");
+        ++cnt[(size_t)c + 1];
+      }
+      p.cls_off.assign((size_t)T.nclass + 1, 0);
+      for (int c = 0; c < T.nclass; ++c) p.cls_off[(size_t)c + 1] = p.cls_off[(size_t)c] + cnt[(size_t)c + 1];
+      std::vector<int64_t> pos(p.cls_off.begin(), p.cls_off.end() - 1);
+      p.perm.resize((size_t)T.n);
+      for (int64_t i = 0; i < T.n; ++i) p.perm[(size_t)pos[(size_t)T.labels[i]]++] = (int32_t)i;
+    } else {
+      p.nclass = 1;
+      p.cls_off = {0, T.n};
+    }
+  }
+
+  // ------------------------------------------------------------- spaces --
+  std::vector<Space> knn, cnt;
+  for (int t = 0; t < ntasks; ++t) {
+    const TaskPlan& p = P[(size_t)t];
+    Space s{};
+    s.task = t;
+    s.K = p.K;
+    const int X = 0, Y = p.dx, Z = p.dx + p.dy;
+    switch (p.kind) {
+      case EGB_MI:
+        s.b = 0; s.e = p.n;
+        set_cols(s.sp, {{X, p.dx}, {Y, p.dy}}); knn.push_back(s);
+        set_cols(s.sp, {{X, p.dx}}); s.slot = 0; cnt.push_back(s);
+        set_cols(s.sp, {{Y, p.dy}}); s.slot = 1; cnt.push_back(s);
+        break;
+      case EGB_CMI:
+        s.b = 0; s.e = p.n;
+        set_cols(s.sp, {{X, p.dx}, {Y, p.dy}, {Z, p.dz}}); knn.push_back(s);
+        set_cols(s.sp, {{X, p.dx}, {Z, p.dz}}); s.slot = 0; cnt.push_back(s);
+        set_cols(s.sp, {{Y, p.dy}, {Z, p.dz}}); s.slot = 1; cnt.push_back(s);
+        set_cols(s.sp, {{Z, p.dz}}); s.slot = 2; cnt.push_back(s);
+        break;
+      case EGB_SEMI:
+        set_cols(s.sp, {{X, p.dx}});
+        for (int c = 0; c < p.nclass; ++c) {
+          s.b = p.cls_off[(size_t)c]; s.e = p.cls_off[(size_t)c + 1];
+          if (s.e > s.b) knn.push_back(s);
+        }
+        s.b = 0; s.e = p.n; s.slot = 0; cnt.push_back(s);
+        break;
+      case EGB_CSEMI:
+        set_cols(s.sp, {{X, p.dx}, {Z, p.dz}});
+        for (int c = 0; c < p.nclass; ++c) {
+          s.b = p.cls_off[(size_t)c]; s.e = p.cls_off[(size_t)c + 1];
+          if (s.e > s.b) knn.push_back(s);
+        }
+        s.b = 0; s.e = p.n; s.slot = 0; cnt.push_back(s);
+        set_cols(s.sp, {{Z, p.dz}}); s.slot = 1;
+        for (int c = 0; c < p.nclass; ++c) {
+          s.b = p.cls_off[(size_t)c]; s.e = p.cls_off[(size_t)c + 1];
+          if (s.e > s.b) cnt.push_back(s);
+        }
+        s.b = 0; s.e = p.n; s.slot = 2; cnt.push_back(s);
+        break;
+      case EGB_ENTROPY:
+      case KIND_KNN_ONLY:
+        s.b = 0; s.e = p.n;
+        set_cols(s.sp, {{X, p.dx}}); knn.push_back(s);
+        break;
+      case KIND_COUNT_ONLY:
+        s.b = 0; s.e = p.n;
+        set_cols(s.sp, {{X, p.dx}}); s.slot = 0; cnt.push_back(s);
+        break;
+    }
+  }
+
+  // ------------------------------------------------------ sort segments --
+  std::map<SegKey, int> seg_index;
+  std::vector<SortSeg> segs;
+  auto seg_for = [&](int task, int col, int64_t b, int64_t e) {
+    const SegKey key{task, col, b, e};
+    auto it = seg_index.find(key);
+    if (it != seg_index.end()) return it->second;
+    SortSeg s{};
+    s.task = task;
+    s.col = col;
+    s.src_begin = (int32_t)b;
+    s.len = (int32_t)(e - b);
+    const int id = (int)segs.size();
+    segs.push_back(s);
+    seg_index[key] = id;
+    return id;
+  };
+
+  // kNN: 1-D sorted jobs, multi-D tile jobs, any-K select jobs
+  struct MJob { Space s; bool is_knn; int slab; int sort_seg; int sel; };
+  std::vector<std::pair<int, Space>> sorted_knn, sorted_cnt;  // (seg, space)
+  std::vector<MJob> mjobs;
+  for (const Space& s : knn) {
+    if (s.sp.d == 1) {
+      sorted_knn.push_back({seg_for(s.task, s.sp.cols[0], s.b, s.e), s});
+    } else {
+      MJob m{s, true, 0, -1, 0};
+      if (s.K > EGB_KREG_MAX) m.sel = 1;
+      else if (force_slab || (!force_brute && s.e - s.b >= SLAB_MIN)) m.slab = 1;
+      if (m.slab) m.sort_seg = seg_for(s.task, s.sp.cols[0], s.b, s.e);
+      mjobs.push_back(m);
+    }
+  }
+  for (const Space& s : cnt) {
+    if (s.sp.d == 1) {
+      sorted_cnt.push_back({seg_for(s.task, s.sp.cols[0], s.b, s.e), s});
+    } else {
+      MJob m{s, false, 0, -1, 0};
+      if (force_slab || (!force_brute && s.e - s.b >= SLAB_MIN)) m.slab = 1;
+      if (m.slab) m.sort_seg = seg_for(s.task, s.sp.cols[0], s.b, s.e);
+      mjobs.push_back(m);
+    }
+  }
+  int64_t sort_total = 0;
+  int nblk_sort = 0;
+  for (SortSeg& s : segs) {
+    s.out_base = sort_total;
+    s.blk0 = nblk_sort;
+    s.nblk = (s.len + SORT_TILE - 1) / SORT_TILE;
+    sort_total += s.len;
+    nblk_sort += s.nblk;
+  }
+  if (sort_total >= ((int64_t)1 << 31)) return fail(ctx, EGB_ERR_ARG, "batch too large for one sort");
+
+  // ------------------------------------------------------------- layout --
+  Layout dl;  // device arena
+  Layout tl;  // table blob (pinned host, copied to the device as one block)
+  // caller data ranges (host input): dedupe by address range
+  struct Range { uintptr_t lo, hi; size_t dev_off; };
+  std::vector<Range> ranges;
+  if (!dev_in) {
+    std::vector<std::pair<uintptr_t, uintptr_t>> rs;
+    for (int t = 0; t < ntasks; ++t)
+      for (int c = 0; c < P[(size_t)t].ncol; ++c) {
+        const egb_column& col = tasks[t].cols[c];
+        const uintptr_t lo = (uintptr_t)col.data;
+        const uintptr_t hi = lo + (uintptr_t)(((tasks[t].n - 1) * col.stride + 1) * sizeof(double));
+        rs.push_back({lo, hi});
+      }
+    std::sort(rs.begin(), rs.end());
+    for (auto& r : rs) {
+      if (!ranges.empty() && r.first <= ranges.back().hi) ranges.back().hi = std::max(ranges.back().hi, r.second);
+      else ranges.push_back({r.first, r.second, 0});
+    }
+    for (auto& r : ranges) {
+      // keep the element alignment of the source within the 256-byte block
+      const size_t mis = r.lo & 255u;
+      r.dev_off = dl.take(r.hi - r.lo + mis) + mis;
+    }
+  }
+  auto dev_col = [&](int t, int c) -> const double* {
+    const egb_column& col = tasks[t].cols[c];
+    if (dev_in) return col.data;
+    const uintptr_t a = (uintptr_t)col.data;
+    for (const Range& r : ranges)
+      if (a >= r.lo && a < r.hi) return (const double*)((char*)ctx->arena + r.dev_off + (a - r.lo));
+    return nullptr;
+  };
+
+  for (int t = 0; t < ntasks; ++t) {
+    TaskPlan& p = P[(size_t)t];
+    p.off_x64 = dl.take(sizeof(double) * (size_t)(p.ncol * p.ld));
+    p.off_eps = dl.take(sizeof(double) * (size_t)p.ld);
+    p.off_rad = dl.take(sizeof(double) * (size_t)p.ld);
+    for (int s = 0; s < p.nslot; ++s) p.off_cnt[s] = dl.take(sizeof(int32_t) * (size_t)p.ld);
+    if (!p.perm.empty()) p.tab_perm = tl.take(sizeof(int32_t) * p.perm.size());
+    if (p.kind == KIND_COUNT_ONLY && !dev_in) p.tab_rad = tl.take(sizeof(double) * (size_t)p.n);
+  }
+  const size_t off_centers = dl.take(sizeof(double) * (size_t)ncols_total);
+  const size_t off_minmax = dl.take(sizeof(unsigned long long) * 2 * (size_t)ncols_total);
+  const size_t off_keys_a = dl.take(sizeof(uint64_t) * (size_t)std::max<int64_t>(sort_total, 1));
+  const size_t off_keys_b = dl.take(sizeof(uint64_t) * (size_t)std::max<int64_t>(sort_total, 1));
+  const size_t off_vals_a = dl.take(sizeof(int32_t) * (size_t)std::max<int64_t>(sort_total, 1));
+  const size_t off_vals_b = dl.take(sizeof(int32_t) * (size_t)std::max<int64_t>(sort_total, 1));
+  const size_t off_hist = dl.take(sizeof(uint32_t) * 256 * (size_t)std::max(nblk_sort, 1));
+  const size_t off_scan = dl.take(sizeof(uint32_t) * sort_scan_tmp_elems(std::max(nblk_sort, 1)));
+
+  // multi-D job blocks
+  std::vector<JobDev> jobs(mjobs.size());
+  int64_t max_lds = 32;
+  for (size_t j = 0; j < mjobs.size(); ++j) {
+    const MJob& m = mjobs[j];
+    JobDev& J = jobs[j];
+    std::memset(&J, 0, sizeof(J));
+    const int64_t len = m.s.e - m.s.b;
+    J.lds = round32(len);
+    max_lds = std::max(max_lds, J.lds);
+    J.task = m.s.task;
+    J.seg_begin = (int32_t)m.s.b;
+    J.len = (int32_t)len;
+    J.K = m.is_knn ? m.s.K : 0;
+    J.slab = m.slab;
+    J.sort_seg = m.sort_seg;
+    J.sp = m.s.sp;
+    const int d = m.s.sp.d;
+    J.c64 = (double*)(uintptr_t)dl.take(sizeof(double) * (size_t)(d * J.lds));
+    J.c32 = (float*)(uintptr_t)dl.take(sizeof(float) * (size_t)(d * J.lds));
+    J.idx = (int32_t*)(uintptr_t)dl.take(sizeof(int32_t) * (size_t)J.lds);
+    J.center = (double*)(uintptr_t)dl.take(sizeof(double) * (size_t)d);
+  }
+
+  // sorted jobs
+  std::vector<SortedJob> sj_knn, sj_cnt;
+  int blk_knn = 0, blk_cnt = 0;
+  for (auto& pr : sorted_knn) {
+    const SortSeg& sg = segs[(size_t)pr.first];
+    SortedJob j{};
+    j.task = pr.second.task; j.kind = 0; j.slot = 0; j.K = pr.second.K;
+    j.base = sg.out_base; j.len = sg.len; j.blk0 = blk_knn;
+    blk_knn += (sg.len + SORTED_BLOCK - 1) / SORTED_BLOCK;
+    sj_knn.push_back(j);
+  }
+  for (auto& pr : sorted_cnt) {
+    const SortSeg& sg = segs[(size_t)pr.first];
+    SortedJob j{};
+    j.task = pr.second.task; j.kind = 1; j.slot = pr.second.slot; j.K = 0;
+    j.base = sg.out_base; j.len = sg.len; j.blk0 = blk_cnt;
+    blk_cnt += (sg.len + SORTED_BLOCK - 1) / SORTED_BLOCK;
+    sj_cnt.push_back(j);
+  }
+
+  // tile launch groups
+  struct Group {
+    int is_knn, sel, kclass, dclass, slab, dmax;
+    std::vector<WorkItem> items;
+    size_t tab_items = 0;
+    int64_t defer_cap = 0;   // slab groups: every query may be deferred once
+    size_t off_defer = 0;
+  };
+  std::vector<Group> groups;
+  std::map<std::tuple<int, int, int, int, int>, int> gidx;
+  std::vector<size_t> order(mjobs.size());
+  for (size_t j = 0; j < order.size(); ++j) order[j] = j;
+  std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) { return jobs[a].len > jobs[b].len; });
+  for (size_t oi = 0; oi < order.size(); ++oi) {
+    const size_t j = order[oi];
+    const MJob& m = mjobs[j];
+    const int d = m.s.sp.d;
+    const int dclass = (d >= 2 && d <= 4) ? d : 0;
+    int kclass = 0;
+    if (m.is_knn && !m.sel) kclass = m.s.K <= 4 ? 4 : m.s.K <= 8 ? 8 : m.s.K <= 16 ? 16 : 32;
+    const auto key = std::make_tuple(m.is_knn, m.sel, kclass, dclass, m.slab);
+    auto it = gidx.find(key);
+    int g;
+    if (it == gidx.end()) {
+      g = (int)groups.size();
+      gidx[key] = g;
+      Group G;
+      G.is_knn = m.is_knn; G.sel = m.sel; G.kclass = kclass; G.dclass = dclass; G.slab = m.slab; G.dmax = d;
+      groups.push_back(G);
+    } else {
+      g = it->second;
+    }
+    groups[(size_t)g].dmax = std::max(groups[(size_t)g].dmax, d);
+  }
+  for (size_t oi = 0; oi < order.size(); ++oi) {
+    const size_t j = order[oi];
+    const MJob& m = mjobs[j];
+    const int d = m.s.sp.d;
+    const int dclass = (d >= 2 && d <= 4) ? d : 0;
+    int kclass = 0;
+    if (m.is_knn && !m.sel) kclass = m.s.K <= 4 ? 4 : m.s.K <= 8 ? 8 : m.s.K <= 16 ? 16 : 32;
+    Group& G = groups[(size_t)gidx[std::make_tuple(m.is_knn, m.sel, kclass, dclass, m.slab)]];
+    int qb;
+    if (G.sel) qb = SELECT_WARPS;
+    else if (G.is_knn) qb = knn_shape(G.kclass, G.dclass, plain, G.slab, G.dmax).queries();
+    else qb = count_shape(G.dclass, plain, G.slab, G.dmax).queries();
+    for (int64_t q0 = 0; q0 < jobs[j].len; q0 += qb) G.items.push_back({(int32_t)j, (int32_t)q0});
+    if (G.slab) G.defer_cap += jobs[j].len;
+  }
+  for (Group& G : groups)
+    if (G.defer_cap > 0) G.off_defer = dl.take(sizeof(DeferEntry) * (size_t)G.defer_cap);
+
+  // combine
+  std::vector<CombineJob> cjobs;
+  std::vector<int32_t> chunk_job;
+  for (int t = 0; t < ntasks; ++t) {
+    const TaskPlan& p = P[(size_t)t];
+    if (p.kind == KIND_KNN_ONLY || p.kind == KIND_COUNT_ONLY) continue;
+    CombineJob c{};
+    c.task = t;
+    c.kind = p.kind;
+    c.chunk0 = (int32_t)chunk_job.size();
+    c.nchunk = (int32_t)((p.n + COMBINE_CHUNK - 1) / COMBINE_CHUNK);
+    for (int i = 0; i < c.nchunk; ++i) chunk_job.push_back((int32_t)cjobs.size());
+    cjobs.push_back(c);
+  }
+  const int nchunks = (int)chunk_job.size();
+
+  // tables (pinned blob -> device)
+  std::vector<GatherCol> gcols;
+  std::vector<int32_t> col_task, col_idx;
+  const size_t tab_tasks = tl.take(sizeof(TaskDev) * (size_t)ntasks);
+  const size_t tab_gcols = tl.take(sizeof(GatherCol) * (size_t)ncols_total);
+  const size_t tab_coltask = tl.take(sizeof(int32_t) * (size_t)ncols_total);
+  const size_t tab_colidx = tl.take(sizeof(int32_t) * (size_t)ncols_total);
+  const size_t tab_segs = tl.take(sizeof(SortSeg) * std::max<size_t>(segs.size(), 1));
+  const size_t tab_blkseg = tl.take(sizeof(int32_t) * (size_t)std::max(nblk_sort, 1));
+  const size_t tab_sjk = tl.take(sizeof(SortedJob) * std::max<size_t>(sj_knn.size(), 1));
+  const size_t tab_sjc = tl.take(sizeof(SortedJob) * std::max<size_t>(sj_cnt.size(), 1));
+  const size_t tab_jobs = tl.take(sizeof(JobDev) * std::max<size_t>(jobs.size(), 1));
+  for (Group& G : groups) G.tab_items = tl.take(sizeof(WorkItem) * G.items.size());
+  const size_t tab_cjobs = tl.take(sizeof(CombineJob) * std::max<size_t>(cjobs.size(), 1));
+  const size_t tab_chunkjob = tl.take(sizeof(int32_t) * (size_t)std::max(nchunks, 1));
+  const size_t tab_bytes = align_up(tl.off, 256);
+  const size_t off_tab = dl.take(tab_bytes);
+  // zero-initialised region: counters, job flags, zero flags, error word
+  const int ncounters = 2 * (int)groups.size();  // work counter + deferred count
+  const size_t zr_counters = 0;
+  const size_t zr_jflags = align_up(zr_counters + sizeof(int) * (size_t)std::max(ncounters, 1), 16);
+  const size_t zr_zero = align_up(zr_jflags + sizeof(uint32_t) * std::max<size_t>(jobs.size(), 1), 16);
+  const size_t zr_err = align_up(zr_zero + sizeof(uint32_t) * (size_t)ntasks, 16);
+  const size_t zr_bytes = align_up(zr_err + 16, 256);
+  const size_t off_zr = dl.take(zr_bytes);
+  // readback region: partial sums, then a copy of zero flags + error word
+  const size_t off_partial = dl.take(sizeof(double) * (size_t)std::max(nchunks, 1));
+  const size_t arena_bytes = align_up(dl.off, 256);
+
+  // pinned: table blob + readback
+  const size_t pin_rb = align_up(tab_bytes, 256);
+  const size_t pin_bytes = pin_rb + sizeof(double) * (size_t)std::max(nchunks, 1) + zr_bytes;
+  int rc = ensure_arena(ctx, arena_bytes);
+  if (rc) return rc;
+  rc = ensure_pinned(ctx, pin_bytes);
+  if (rc) return rc;
+  rc = ensure_psi(ctx, max_n + 1);
+  if (rc) return rc;
+  char* A = (char*)ctx->arena;
+  char* H = (char*)ctx->pinned;
+
+  // ------------------------------------------------------- fill tables --
+  auto devp = [&](size_t off) { return (void*)(A + off); };
+  std::vector<TaskDev> tdev((size_t)ntasks);
+  for (int t = 0; t < ntasks; ++t) {
+    TaskPlan& p = P[(size_t)t];
+    TaskDev& D = tdev[(size_t)t];
+    std::memset(&D, 0, sizeof(D));
+    D.x64 = (const double*)devp(p.off_x64);
+    D.center = (const double*)(A + off_centers) + p.center0;
+    D.eps = (double*)devp(p.off_eps);
+    D.rad = (double*)devp(p.off_rad);
+    for (int s = 0; s < p.nslot; ++s) D.cnt[s] = (int32_t*)devp(p.off_cnt[s]);
+    D.ld = p.ld;
+    D.n = (int32_t)p.n;
+    D.ncol = p.ncol;
+    D.rad_given = p.kind == KIND_COUNT_ONLY ? 1 : 0;
+    const int32_t* perm_dev = p.perm.empty() ? nullptr : (const int32_t*)(A + off_tab + p.tab_perm);
+    if (!p.perm.empty()) std::memcpy(H + p.tab_perm, p.perm.data(), sizeof(int32_t) * p.perm.size());
+    if (p.kind == KIND_COUNT_ONLY && !dev_in)
+      std::memcpy(H + p.tab_rad, count_radius, sizeof(double) * (size_t)p.n);
+    for (int c = 0; c < p.ncol; ++c) {
+      GatherCol g{};
+      g.src = dev_col(t, c);
+      g.stride = tasks[t].cols[c].stride;
+      g.perm = perm_dev;
+      g.task = t;
+      g.col = c;
+      gcols.push_back(g);
+      col_task.push_back(t);
+      col_idx.push_back(c);
+    }
+  }
+  std::memcpy(H + tab_tasks, tdev.data(), sizeof(TaskDev) * tdev.size());
+  std::memcpy(H + tab_gcols, gcols.data(), sizeof(GatherCol) * gcols.size());
+  std::memcpy(H + tab_coltask, col_task.data(), sizeof(int32_t) * col_task.size());
+  std::memcpy(H + tab_colidx, col_idx.data(), sizeof(int32_t) * col_idx.size());
+  if (!segs.empty()) std::memcpy(H + tab_segs, segs.data(), sizeof(SortSeg) * segs.size());
+  {
+    int32_t* bs = (int32_t*)(H + tab_blkseg);
+    for (size_t s = 0; s < segs.size(); ++s)
+      for (int b = 0; b < segs[s].nblk; ++b) bs[segs[s].blk0 + b] = (int32_t)s;
+  }
+  if (!sj_knn.empty()) std::memcpy(H + tab_sjk, sj_knn.data(), sizeof(SortedJob) * sj_knn.size());
+  if (!sj_cnt.empty()) std::memcpy(H + tab_sjc, sj_cnt.data(), sizeof(SortedJob) * sj_cnt.size());
+  for (size_t j = 0; j < jobs.size(); ++j) {
+    JobDev J = jobs[j];
+    const TaskDev& D = tdev[(size_t)J.task];
+    J.c64 = (double*)(A + (uintptr_t)J.c64);
+    J.c32 = (float*)(A + (uintptr_t)J.c32);
+    J.idx = (int32_t*)(A + (uintptr_t)J.idx);
+    J.center = (double*)(A + (uintptr_t)J.center);
+    J.jflags = (uint32_t*)(A + off_zr + zr_jflags) + j;
+    J.eps = D.eps;
+    J.rad = D.rad;
+    J.cnt = mjobs[j].is_knn ? nullptr : D.cnt[mjobs[j].s.slot];
+    std::memcpy(H + tab_jobs + sizeof(JobDev) * j, &J, sizeof(JobDev));
+  }
+  for (Group& G : groups)
+    if (!G.items.empty()) std::memcpy(H + G.tab_items, G.items.data(), sizeof(WorkItem) * G.items.size());
+  if (!cjobs.empty()) std::memcpy(H + tab_cjobs, cjobs.data(), sizeof(CombineJob) * cjobs.size());
+  if (nchunks) std::memcpy(H + tab_chunkjob, chunk_job.data(), sizeof(int32_t) * (size_t)nchunks);
+
+  auto dtab = [&](size_t off) { return (void*)(A + off_tab + off); };
+  const TaskDev* tasks_d = (const TaskDev*)dtab(tab_tasks);
+  int* counters = (int*)(A + off_zr + zr_counters);
+  uint32_t* zero_d = (uint32_t*)(A + off_zr + zr_zero);
+  uint32_t* err_d = (uint32_t*)(A + off_zr + zr_err);
+
+  // ------------------------------------------------------------ launch --
+  ctx->h2d_bytes = (int64_t)tab_bytes;
+  ctx->d2h_bytes = (int64_t)(zr_bytes + sizeof(double) * (size_t)nchunks);
+  if (!dev_in)
+    for (const Range& r : ranges) ctx->h2d_bytes += (int64_t)(r.hi - r.lo);
+  if (timing) EGB_CUDA(cudaEventRecord(ctx->ev[0], st));
+  if (!dev_in)
+    for (const Range& r : ranges)
+      EGB_CUDA(cudaMemcpyAsync(A + r.dev_off, (const void*)r.lo, r.hi - r.lo, cudaMemcpyHostToDevice, st));
+  EGB_CUDA(cudaMemcpyAsync(A + off_tab, H, tab_bytes, cudaMemcpyHostToDevice, st));
+  EGB_CUDA(cudaMemsetAsync(A + off_zr, 0, zr_bytes, st));
+  if (dev_in)
+    for (int t = 0; t < ntasks; ++t)
+      if (P[(size_t)t].kind == KIND_COUNT_ONLY)
+        EGB_CUDA(cudaMemcpyAsync(tdev[(size_t)t].rad, count_radius, sizeof(double) * (size_t)P[(size_t)t].n,
+                                 cudaMemcpyDeviceToDevice, st));
+  if (!dev_in)
+    for (int t = 0; t < ntasks; ++t)
+      if (P[(size_t)t].kind == KIND_COUNT_ONLY)
+        EGB_CUDA(cudaMemcpyAsync(tdev[(size_t)t].rad, A + off_tab + P[(size_t)t].tab_rad,
+                                 sizeof(double) * (size_t)P[(size_t)t].n, cudaMemcpyDeviceToDevice, st));
+  if (timing) EGB_CUDA(cudaEventRecord(ctx->ev[1], st));
+
+  launch_gather(tasks_d, (const GatherCol*)dtab(tab_gcols), ncols_total, max_ld, st);
+  launch_prepare(tasks_d, (const int32_t*)dtab(tab_coltask), (const int32_t*)dtab(tab_colidx),
+                 ncols_total, (unsigned long long*)(A + off_minmax), (double*)(A + off_centers), st);
+  if (timing) EGB_CUDA(cudaEventRecord(ctx->ev[2], st));
+
+  uint64_t* keys = (uint64_t*)(A + off_keys_a);
+  int32_t* vals = (int32_t*)(A + off_vals_a);
+  launch_sort(tasks_d, (const SortSeg*)dtab(tab_segs), (const int32_t*)dtab(tab_blkseg), nblk_sort,
+              keys, (uint64_t*)(A + off_keys_b), vals, (int32_t*)(A + off_vals_b),
+              (uint32_t*)(A + off_hist), (uint32_t*)(A + off_scan), st);
+  launch_materialize(tasks_d, (const JobDev*)dtab(tab_jobs), (int)jobs.size(), vals,
+                     (const SortSeg*)dtab(tab_segs), max_lds, st);
+  if (timing) EGB_CUDA(cudaEventRecord(ctx->ev[3], st));
+
+  launch_sorted_jobs(tasks_d, (const SortedJob*)dtab(tab_sjk), (int)sj_knn.size(), blk_knn, keys, vals, st);
+  for (size_t g = 0; g < groups.size(); ++g) {
+    Group& G = groups[g];
+    if (!G.is_knn || G.items.empty()) continue;
+    if (G.sel)
+      launch_knn_select((const JobDev*)dtab(tab_jobs), (const WorkItem*)dtab(G.tab_items),
+                        (int)G.items.size(), err_d, ctx->num_sms, st);
+    else
+      launch_knn_tile((const JobDev*)dtab(tab_jobs), (const WorkItem*)dtab(G.tab_items),
+                      (int)G.items.size(), G.kclass, G.dclass, plain, G.slab, G.dmax,
+                      counters + 2 * g, err_d, (DeferEntry*)(A + G.off_defer),
+                      counters + 2 * g + 1, ctx->num_sms, st);
+  }
+  for (size_t g = 0; g < groups.size(); ++g) {
+    Group& G = groups[g];
+    if (!G.is_knn || G.sel || !G.slab || G.items.empty()) continue;
+    launch_knn_defer((const JobDev*)dtab(tab_jobs), (const DeferEntry*)(A + G.off_defer),
+                     counters + 2 * g + 1, (int)G.defer_cap, G.kclass, G.dclass, plain,
+                     ctx->num_sms, st);
+  }
+  if (timing) EGB_CUDA(cudaEventRecord(ctx->ev[4], st));
+
+  launch_radius(tasks_d, ntasks, max_ld, st);
+  launch_sorted_jobs(tasks_d, (const SortedJob*)dtab(tab_sjc), (int)sj_cnt.size(), blk_cnt, keys, vals, st);
+  for (size_t g = 0; g < groups.size(); ++g) {
+    Group& G = groups[g];
+    if (G.is_knn || G.items.empty()) continue;
+    launch_count_tile((const JobDev*)dtab(tab_jobs), (const WorkItem*)dtab(G.tab_items),
+                      (int)G.items.size(), G.dclass, plain, G.slab, G.dmax, counters + 2 * g,
+                      err_d, (DeferEntry*)(A + G.off_defer), counters + 2 * g + 1, ctx->num_sms,
+                      st);
+  }
+  for (size_t g = 0; g < groups.size(); ++g) {
+    Group& G = groups[g];
+    if (G.is_knn || !G.slab || G.items.empty()) continue;
+    launch_count_defer((const JobDev*)dtab(tab_jobs), (const DeferEntry*)(A + G.off_defer),
+                       counters + 2 * g + 1, (int)G.defer_cap, G.dclass, plain, ctx->num_sms, st);
+  }
+  if (timing) EGB_CUDA(cudaEventRecord(ctx->ev[5], st));
+
+  launch_combine(tasks_d, (const CombineJob*)dtab(tab_cjobs), (const int32_t*)dtab(tab_chunkjob),
+                 nchunks, ctx->psi_d, ctx->psi_len, (double*)(A + off_partial), zero_d, err_d, st);
+  EGB_CUDA(cudaGetLastError());
+  if (nchunks)
+    EGB_CUDA(cudaMemcpyAsync(H + pin_rb, A + off_partial, sizeof(double) * (size_t)nchunks,
+                             cudaMemcpyDeviceToHost, st));
+  const size_t pin_zr = pin_rb + sizeof(double) * (size_t)std::max(nchunks, 1);
+  EGB_CUDA(cudaMemcpyAsync(H + pin_zr, A + off_zr, zr_bytes, cudaMemcpyDeviceToHost, st));
+  if (timing) EGB_CUDA(cudaEventRecord(ctx->ev[6], st));
+  EGB_CUDA(cudaStreamSynchronize(st));
+
+  if (timing) {
+    float ms = 0.f;
+    for (int i = 0; i < NPHASE - 1; ++i) {
+      cudaEventElapsedTime(&ms, ctx->ev[i], ctx->ev[i + 1]);
+      ctx->timings[i] = ms;
+    }
+    cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[NPHASE - 1]);
+    ctx->timings[NPHASE - 1] = ms;
+    ctx->ntimings = NPHASE;
+  }
+
+  const uint32_t dev_err = *(const uint32_t*)(H + pin_zr + zr_err);
+  if (dev_err) {
+    char buf[128];
+    std::snprintf(buf, sizeof buf, "device error word 0x%x (%s)", dev_err,
+                  (dev_err & DERR_WAIT_TIMEOUT) ? "bounded wait gave up" : "index guard");
+    return fail(ctx, EGB_ERR_DEVICE, buf);
+  }
+
+  // ----------------------------------------------------------- results --
+  const double* partial = (const double*)(H + pin_rb);
+  const uint32_t* zf = (const uint32_t*)(H + pin_zr + zr_zero);
+  const double INF = HUGE_VAL;
+  int ci = 0;
+  for (int t = 0; t < ntasks; ++t) {
+    const TaskPlan& p = P[(size_t)t];
+    egb_result r{};
+    r.status = EGB_OK;
+    if (p.kind == KIND_KNN_ONLY || p.kind == KIND_COUNT_ONLY) {
+      if (results) results[t] = r;
+      continue;
+    }
+    const CombineJob& c = cjobs[(size_t)ci++];
+    double S = 0.0;
+    for (int i = 0; i < c.nchunk; ++i) S += partial[c.chunk0 + i];
+    const uint32_t z = zf[t];
+    const double N = (double)p.n;
+    const double mean = S / N;
+    double v = 0.0;
+    switch (p.kind) {
+      case EGB_MI:
+        // psi(nx) or psi(ny) is the scalar +inf when it holds a zero
+        v = z ? -INF : psi_int(N) + psi_int(p.k) - mean;
+        break;
+      case EGB_CMI:
+      case EGB_CSEMI: {
+        const bool a = (z & 3u) != 0, b = (z & 4u) != 0;
+        if (a && b) v = NAN;          // inf - inf
+        else if (a) v = -INF;         // psi(k) - (+inf)
+        else if (b) v = INF;          // psi(k) - (-inf)
+        else v = psi_int(p.k) - mean;
+        break;
+      }
+      case EGB_SEMI: {
+        double w = 0.0;  // sum over classes of psi(c) * c / N
+        for (int cl = 0; cl < p.nclass; ++cl) {
+          const double cc = (double)(p.cls_off[(size_t)cl + 1] - p.cls_off[(size_t)cl]);
+          w += psi_int(cc) * (cc / N);
+        }
+        v = z ? -INF : psi_int(N) + psi_int(p.k) - mean - w;
+        break;
+      }
+      case EGB_ENTROPY:
+        v = psi_int(N) - psi_int(p.k) + (double)p.ncol * (mean + std::log(2.0));
+        break;
+    }
+    r.value = v;
+    r.term_sum = S;
+    r.zero_mask = z;
+    if (results) results[t] = r;
+  }
+  if (flags & EGB_KEEP_INTERNALS) {
+    ctx->keep = std::move(P);
+    ctx->kept = true;
+  }
+  return EGB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int egb_create(int device, egb_ctx** out) {
+  if (!out) return EGB_ERR_ARG;
+  *out = nullptr;
+  egb_ctx* ctx = new egb_ctx();
+  ctx->device = device;
+  if (cudaSetDevice(device) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking) != cudaSuccess) {
+    cudaGetLastError();
+    delete ctx;
+    return EGB_ERR_CUDA;
+  }
+  ctx->stream = ctx->own_stream;
+  cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
+  if (ctx->num_sms < 1) ctx->num_sms = 1;
+  for (auto& e : ctx->ev) cudaEventCreate(&e);
+  *out = ctx;
+  return EGB_OK;
+}
+
+void egb_destroy(egb_ctx* ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->device);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  if (ctx->arena) cudaFree(ctx->arena);
+  if (ctx->pinned) cudaFreeHost(ctx->pinned);
+  if (ctx->psi_d) cudaFree(ctx->psi_d);
+  for (auto& e : ctx->ev)
+    if (e) cudaEventDestroy(e);
+  if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+  delete ctx;
+}
+
+int egb_set_stream(egb_ctx* ctx, void* stream) {
+  if (!ctx) return EGB_ERR_ARG;
+  ctx->stream = stream ? (cudaStream_t)stream : ctx->own_stream;
+  return EGB_OK;
+}
+
+const char* egb_last_error(const egb_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int egb_run_batch(egb_ctx* ctx, const egb_task* tasks, int32_t ntasks, int32_t flags,
+                  egb_result* results) {
+  if (!ctx) return EGB_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  for (int t = 0; t < ntasks && tasks; ++t)
+    if (tasks[t].kind > EGB_ENTROPY || tasks[t].kind < EGB_MI)
+      return fail(ctx, EGB_ERR_ARG, "task " + std::to_string(t) + ": unknown estimator kind");
+  return run_batch(ctx, tasks, ntasks, flags, results, nullptr);
+}
+
+int egb_fetch(egb_ctx* ctx, int32_t task, int32_t which, void* host_out) {
+  if (!ctx || !host_out) return EGB_ERR_ARG;
+  if (!ctx->kept) return fail(ctx, EGB_ERR_STATE, "no batch internals kept (run with EGB_KEEP_INTERNALS)");
+  if (task < 0 || task >= (int)ctx->keep.size()) return fail(ctx, EGB_ERR_ARG, "task index out of range");
+  const TaskPlan& p = ctx->keep[(size_t)task];
+  if (which < 0 || which > p.nslot) return fail(ctx, EGB_ERR_ARG, "no such internal array");
+  cudaSetDevice(ctx->device);
+  const size_t n = (size_t)p.n;
+  std::vector<char> buf(n * 8);
+  const char* src = (const char*)ctx->arena + (which == 0 ? p.off_eps : p.off_cnt[which - 1]);
+  const size_t esz = which == 0 ? 8 : 4;
+  EGB_CUDA(cudaMemcpyAsync(buf.data(), src, n * esz, cudaMemcpyDeviceToHost, ctx->stream));
+  EGB_CUDA(cudaStreamSynchronize(ctx->stream));
+  for (size_t w = 0; w < n; ++w) {
+    const size_t i = p.perm.empty() ? w : (size_t)p.perm[w];
+    if (which == 0) ((double*)host_out)[i] = ((const double*)buf.data())[w];
+    else ((int64_t*)host_out)[i] = ((const int32_t*)buf.data())[w];
+  }
+  return EGB_OK;
+}
+
+int egb_knn_eps(egb_ctx* ctx, const double* points, int64_t n, int32_t d, int32_t k,
+                int32_t flags, double* eps) {
+  if (!ctx) return EGB_ERR_ARG;
+  if (!points || !eps || n < 1 || d < 1 || d > EGB_DMAX || k < 1)
+    return fail(ctx, EGB_ERR_ARG, "egb_knn_eps: invalid arguments");
+  cudaSetDevice(ctx->device);
+  std::vector<egb_column> cols((size_t)d);
+  for (int c = 0; c < d; ++c) cols[(size_t)c] = {points + c, (int64_t)d};
+  egb_task t{};
+  t.kind = KIND_KNN_ONLY;
+  t.k = k;
+  t.n = n;
+  t.dx = d;
+  t.cols = cols.data();
+  int rc = run_batch(ctx, &t, 1, flags | EGB_KEEP_INTERNALS, nullptr, nullptr);
+  if (rc) return rc;
+  const TaskPlan& p = ctx->keep[0];
+  const cudaMemcpyKind kind = (flags & EGB_INPUT_DEVICE) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  EGB_CUDA(cudaMemcpyAsync(eps, (const char*)ctx->arena + p.off_eps, sizeof(double) * (size_t)n, kind,
+                           ctx->stream));
+  EGB_CUDA(cudaStreamSynchronize(ctx->stream));
+  return EGB_OK;
+}
+
+int egb_ball_count(egb_ctx* ctx, const double* points, int64_t n, int32_t d, const double* radius,
+                   int32_t flags, int64_t* count) {
+  if (!ctx) return EGB_ERR_ARG;
+  if (!points || !radius || !count || n < 1 || d < 1 || d > EGB_DMAX)
+    return fail(ctx, EGB_ERR_ARG, "egb_ball_count: invalid arguments");
+  cudaSetDevice(ctx->device);
+  std::vector<egb_column> cols((size_t)d);
+  for (int c = 0; c < d; ++c) cols[(size_t)c] = {points + c, (int64_t)d};
+  egb_task t{};
+  t.kind = KIND_COUNT_ONLY;
+  t.k = 1;
+  t.n = n;
+  t.dx = d;
+  t.cols = cols.data();
+  int rc = run_batch(ctx, &t, 1, flags | EGB_KEEP_INTERNALS, nullptr, radius);
+  if (rc) return rc;
+  if (flags & EGB_INPUT_DEVICE) {
+    // widen int32 -> int64 through the host (test-sized path)
+    std::vector<int64_t> tmp((size_t)n);
+    rc = egb_fetch(ctx, 0, 1, tmp.data());
+    if (rc) return rc;
+    EGB_CUDA(cudaMemcpy(count, tmp.data(), sizeof(int64_t) * (size_t)n, cudaMemcpyHostToDevice));
+    return EGB_OK;
+  }
+  return egb_fetch(ctx, 0, 1, count);
+}
+
+int egb_timings(const egb_ctx* ctx, double* ms, int32_t max) {
+  if (!ctx || !ms) return 0;
+  const int n = std::min<int>(max, ctx->ntimings);
+  for (int i = 0; i < n; ++i) ms[i] = ctx->timings[i];
+  return n;
+}
+
+int egb_last_transfer(const egb_ctx* ctx, int64_t* h2d_bytes, int64_t* d2h_bytes) {
+  if (!ctx) return EGB_ERR_ARG;
+  if (h2d_bytes) *h2d_bytes = ctx->h2d_bytes;
+  if (d2h_bytes) *d2h_bytes = ctx->d2h_bytes;
+  return EGB_OK;
+}
+
+const char* egb_version(void) { return "ennemi_gb300 0.1.0 (sm_103a)"; }
+
+}  // extern "C"

@@ -1,0 +1,252 @@
+// egb_internal.cuh -- device structures and helpers shared by the kernels of
+// libennemi_gb.so.
+//
+// Layout of one batch in HBM (all inside one arena):
+//   * task t owns ncol_t float64 columns in *working order* (samples of a
+//     class-partitioned task grouped by class, stable); column c lives at
+//     x64 + c*ld with ld a multiple of 32 elements, so every column start is
+//     256-byte aligned relative to the arena;
+//   * eps[ld] (float64), rad[ld] = fl64(eps - 1e-12) or a caller radius, and
+//     up to three int32 count arrays cnt[s][ld];
+//   * per sorted 1-D space: the order-preserving uint64 keys and the working
+//     index of each key, concatenated over all spaces of the batch;
+//   * per multi-D job: its columns copied into one SoA block (see JobDev),
+//     with an FP32 copy fl32(x - center_c) (center_c = the task column's
+//     midrange) read by the FP32 distance filters.
+// All distances are max-norm.  Every decision that fixes a neighbour count or
+// a k-th distance is taken on the exact FP64 distance max_c fl64(|a_c - b_c|)
+// -- the value scipy's cKDTree compares -- either directly or behind an FP32
+// filter whose guard band is proven below (band()).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#define EGB_DMAX 32        // most columns in one space
+#define EGB_KREG_MAX 32    // largest k+1 kept in registers by the tile kernels
+
+namespace egb {
+
+// Device-side error word: kernels OR bits in, the host reads it after a batch.
+enum DevErr : uint32_t {
+  DERR_NONE = 0,
+  DERR_WAIT_TIMEOUT = 1u << 0,  // a bounded mbarrier wait gave up
+  DERR_BAD_INDEX = 1u << 1,     // an index guard tripped
+};
+
+// Per-job flag bits (JobDev::jflags).
+enum JobFlag : uint32_t {
+  TF_UNSAFE32 = 1u << 0,  // some centred value does not fit FP32 comfortably:
+                          // every candidate of the job is checked in FP64
+};
+
+// ------------------------------------------------------------ key helpers --
+// Order-preserving map float64 -> uint64 (after folding -0.0 into +0.0).
+__host__ __device__ __forceinline__ uint64_t key_of(double v) {
+  v = v + 0.0;  // -0.0 + 0.0 = +0.0 in round-to-nearest
+  uint64_t u;
+#ifdef __CUDA_ARCH__
+  u = (uint64_t)__double_as_longlong(v);
+#else
+  __builtin_memcpy(&u, &v, 8);
+#endif
+  return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
+}
+__host__ __device__ __forceinline__ double value_of(uint64_t k) {
+  uint64_t u = (k >> 63) ? (k & 0x7fffffffffffffffull) : ~k;
+  double v;
+#ifdef __CUDA_ARCH__
+  v = __longlong_as_double((long long)u);
+#else
+  __builtin_memcpy(&v, &u, 8);
+#endif
+  return v;
+}
+
+#ifdef __CUDACC__
+// fl64(|a - b|) as the bit pattern of a non-negative double.  Non-negative
+// doubles order like their bit patterns, so the max over coordinates and the
+// comparisons run on the integer pipe; only the subtraction is FP64.
+__device__ __forceinline__ uint64_t absdiff_bits(double a, double b) {
+  return (uint64_t)__double_as_longlong(a - b) & 0x7fffffffffffffffull;
+}
+__device__ __forceinline__ double bits_to_double(uint64_t u) {
+  return __longlong_as_double((long long)u);
+}
+
+// FP32 guard band.
+// Let c be a column centre (a double), q the query, p a candidate, and
+// D = max_c |p_c - q_c| the exact max-norm distance.  The filter works on
+// f = fl32(fl64(v - c)) per coordinate and d32 = max_c fl32(|f_p - f_q|).
+// With u = 2^-24 and M = max_c |q_c - c|:
+//   |f - (v - c)| <= (u + 2^-53 + u 2^-53)|v - c| + 2^-150   (subnormals),
+//   |p_c - c| <= M + D,   |q_c - c| <= M,
+//   the FP32 subtraction adds at most u |f_p - f_q|,
+// so |d32 - D| <= 2^-23 (M + D)(1 + 2^-20) + 2^-148, and the FP64 distance
+// fl64(D) is within 2^-53 D of D.  band(M, t) = 2^-21 (M + t) + 2^-100 is
+// four times that bound for every D <= t (1 + 2^-20):
+//   kNN:    a candidate with fl64 distance < t has d32 <= t + band(M, t);
+//   counts: d32 <= r - band(M, r)  =>  fl64 distance <= r,
+//           d32 >  r + band(M, r)  =>  fl64 distance >  r.
+// Everything in between is decided in FP64.
+__device__ __forceinline__ double band(double m, double t) {
+  return 0x1p-21 * (m + t) + 0x1p-100;
+}
+#endif
+
+constexpr uint64_t INF_BITS = 0x7ff0000000000000ull;
+
+// ------------------------------------------------------------ job structs --
+struct TaskDev {          // per-task device view
+  const double* x64;      // working FP64 columns, column c at x64 + c*ld
+  const double* center;   // [ncol] column midranges (FP32 copies are x - center)
+  double* eps;            // [ld]
+  double* rad;            // [ld] count radius per sample
+  int32_t* cnt[3];        // count slots (working order)
+  int64_t ld;
+  int32_t n;
+  int32_t ncol;
+  int32_t rad_given;      // 1: rad holds caller radii (egb_ball_count)
+  int32_t pad_;
+};
+
+struct SpaceCols {        // the columns of one (sub)space of a task
+  int32_t d;
+  int8_t cols[EGB_DMAX];
+};
+
+// A multi-D job: the samples [seg_begin, seg_end) of one task restricted to
+// the columns `sp`, materialised as a contiguous structure-of-arrays block
+// (FP64 and FP32 copies, column c at +c*lds).  Brute-force jobs keep working
+// order; slab jobs are sorted by their first column, so that the candidates
+// within distance t of a query lie in a contiguous run around it.  Queries
+// and candidates are the same point set (every kNN and ball-count query of
+// the reference searches the set it belongs to).
+struct JobDev {
+  double* c64;            // [d][lds]
+  float* c32;             // [d][lds] fl32(c64 - center)
+  int32_t* idx;           // [lds] position -> working index of the task
+  double* center;         // [d]
+  uint32_t* jflags;       // TF_* bits of this job (set by materialise)
+  double* eps;            // task eps  (kNN: written; counts: unused)
+  const double* rad;      // task radius (counts)
+  int32_t* cnt;           // task count slot (counts)
+  int64_t lds;
+  int32_t task;
+  int32_t seg_begin;
+  int32_t len;            // seg_end - seg_begin
+  int32_t K;              // k + 1 (kNN) or 0 (count)
+  int32_t slab;           // 1: sorted by the first column
+  int32_t sort_seg;       // slab: index of the sort segment of column 0
+  SpaceCols sp;
+};
+
+struct WorkItem {         // one tile of queries of one job
+  int32_t job;
+  int32_t q0;
+};
+
+// A slab query whose search a tile work item left unfinished (it needed a
+// much wider window than the rest of its item); finished one warp per query.
+struct DeferEntry {
+  int32_t job;
+  int32_t pos;
+};
+constexpr int DEFER_FRAC = 8;    // an item stops when <= 1/8 of its threads
+                                 // still have unfinished queries
+constexpr int SIDE_CAP = 128;    // ... or after this many tiles beyond home
+
+// 1-D jobs on sorted arrays: one thread per sorted position.
+struct SortedJob {
+  int32_t task;
+  int32_t kind;           // 0 = kNN (writes eps), 1 = count (writes cnt[slot])
+  int32_t slot;
+  int32_t K;              // k + 1 for kNN
+  int64_t base;           // offset of the sorted segment in the key buffer
+  int32_t len;            // its length
+  int32_t blk0;           // first block of this job in the launch
+};
+
+struct SortSeg {          // one segment of the batched radix sort
+  int64_t out_base;       // offset into the concatenated key buffer
+  int32_t len;
+  int32_t blk0;           // first tile (block) of the segment
+  int32_t nblk;
+  int32_t task;
+  int32_t col;            // source column of the task
+  int32_t src_begin;      // first working index of the segment
+};
+
+struct GatherCol {        // working column <- caller column (strided, permuted)
+  const double* src;
+  int64_t stride;
+  const int32_t* perm;    // working -> caller index, or null (identity)
+  int32_t task;
+  int32_t col;
+};
+
+struct CombineJob {       // per-task reduction of per-sample terms
+  int32_t task;
+  int32_t kind;           // egb_kind
+  int32_t chunk0;         // first partial-sum slot of the task
+  int32_t nchunk;
+};
+constexpr int COMBINE_CHUNK = 4096;
+
+// ----------------------------------------------------------- entry points --
+// Launch wrappers implemented in the kernel translation units.  Every wrapper
+// launches on `st` and never synchronises.
+
+// egb_prep.cu
+void launch_gather(const TaskDev* tasks_d, const GatherCol* cols_d, int ncols,
+                   int64_t max_ld, cudaStream_t st);
+void launch_prepare(const TaskDev* tasks_d, const int32_t* col_task_d, const int32_t* col_idx_d,
+                    int ncols_total, unsigned long long* minmax_d, double* centers_d,
+                    cudaStream_t st);
+void launch_materialize(const TaskDev* tasks_d, const JobDev* jobs_d, int njobs,
+                        const int32_t* sorted_vals, const SortSeg* segs_d, int64_t max_lds,
+                        cudaStream_t st);
+void launch_radius(const TaskDev* tasks_d, int ntasks, int64_t max_ld, cudaStream_t st);
+void launch_combine(const TaskDev* tasks_d, const CombineJob* jobs_d, const int32_t* chunk_job_d,
+                    int nchunks, const double* psi_tab, int64_t psi_len, double* partial,
+                    uint32_t* zero_flags, uint32_t* err, cudaStream_t st);
+
+// egb_sort.cu
+constexpr int SORT_TILE = 2048;
+size_t sort_scan_tmp_elems(int nblk);
+void launch_sort(const TaskDev* tasks_d, const SortSeg* segs_d, const int32_t* blk_seg_d,
+                 int nblk, uint64_t* keys_a, uint64_t* keys_b, int32_t* vals_a,
+                 int32_t* vals_b, uint32_t* hist, uint32_t* scan_tmp, cudaStream_t st);
+constexpr int SORTED_BLOCK = 256;
+void launch_sorted_jobs(const TaskDev* tasks_d, const SortedJob* jobs_d, int njobs,
+                        int total_blocks, const uint64_t* keys, const int32_t* perm,
+                        cudaStream_t st);
+
+// egb_knn.cu / egb_count.cu: tile kernels over materialised jobs.
+// dclass in {2, 3, 4} or 0 (generic d <= EGB_DMAX); kclass in {4, 8, 16, 32}.
+struct TileShape {
+  int threads;            // CTA size
+  int qpt;                // queries per thread
+  int tile;               // candidates per shared-memory tile
+  size_t smem;            // dynamic shared memory bytes
+  int queries() const { return threads * qpt; }
+};
+TileShape knn_shape(int kclass, int dclass, int plain, int slab, int dmax);
+void launch_knn_tile(const JobDev* jobs_d, const WorkItem* items_d, int nitems, int kclass,
+                     int dclass, int plain, int slab, int dmax, int* counter, uint32_t* err,
+                     DeferEntry* defer, int* defer_count, int num_sms, cudaStream_t st);
+void launch_knn_defer(const JobDev* jobs_d, const DeferEntry* defer, const int* defer_count,
+                      int defer_cap, int kclass, int dclass, int plain, int num_sms,
+                      cudaStream_t st);
+TileShape count_shape(int dclass, int plain, int slab, int dmax);
+void launch_count_tile(const JobDev* jobs_d, const WorkItem* items_d, int nitems, int dclass,
+                       int plain, int slab, int dmax, int* counter, uint32_t* err,
+                       DeferEntry* defer, int* defer_count, int num_sms, cudaStream_t st);
+void launch_count_defer(const JobDev* jobs_d, const DeferEntry* defer, const int* defer_count,
+                        int defer_cap, int dclass, int plain, int num_sms, cudaStream_t st);
+
+// egb_select.cu: any K (one warp per query, radix select on FP64 bits)
+constexpr int SELECT_WARPS = 8;
+void launch_knn_select(const JobDev* jobs_d, const WorkItem* items_d, int nitems, uint32_t* err,
+                       int num_sms, cudaStream_t st);
+
+}  // namespace egb

@@ -1,0 +1,4 @@
+// FP32-filter slab (k+1)-NN tile kernels (see egb_knn.cuh).
+#include "egb_knn.cuh"
+EGB_KNN_TU(false, true)
+EGB_KNN_DEFER_TU(false)

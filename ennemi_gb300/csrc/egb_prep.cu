@@ -1,0 +1,263 @@
+// egb_prep.cu -- data movement around the search kernels.
+//
+// gather       caller columns (strided, optionally class-permuted) -> the
+//              task's working FP64 columns, zero padded up to ld;
+// prepare      per working column the midrange centre (min/max over the
+//              order-preserving integer keys, so -0.0/+0.0 and any finite
+//              values compare exactly);
+// materialize  per multi-D job: its columns copied into one SoA block in
+//              working or sorted order, with the FP32 centred copy and the
+//              job's "FP32 unsafe" flag (a centred value >= 1e37 or not
+//              finite: every candidate of that job is then decided in FP64);
+// radius       rad = fl64(eps - 1e-12): the reference's count radius
+//              (ennemi/_entropy_estimators.py:109-110, :152-154, :196,
+//              :243-245);
+// combine      per-sample estimator term summed in fixed 4096-sample chunks
+//              (deterministic order), plus per-slot "a count was zero" flags.
+//              Terms, from ennemi/_entropy_estimators.py:
+//                MI     psi(nx) + psi(ny)                       (:113)
+//                CMI    psi(nxz) + psi(nyz) - psi(nz)           (:156)
+//                SEMI   psi(n)                                  (:200)
+//                CSEMI  psi(nxz) + psi(nyz) - psi(nz)           (:247)
+//                ENT    log(eps)                                (:42)
+//              psi comes from an FP64 table indexed by the integer count.
+#include "egb_internal.cuh"
+#include "ennemi_gb.h"
+
+namespace egb {
+
+namespace {
+
+constexpr int PREP_THREADS = 256;
+
+int grid_x_for(int64_t n) {
+  int64_t b = (n + PREP_THREADS - 1) / PREP_THREADS;
+  if (b > 2048) b = 2048;
+  return (int)(b < 1 ? 1 : b);
+}
+int grid_y_for(int n) { return n > 65535 ? 65535 : (n < 1 ? 1 : n); }
+
+__global__ void gather_kernel(const TaskDev* __restrict__ tasks,
+                              const GatherCol* __restrict__ cols, int ncols) {
+  for (int g = blockIdx.y; g < ncols; g += gridDim.y) {
+    const GatherCol gc = cols[g];
+    const TaskDev t = tasks[gc.task];
+    double* dst = const_cast<double*>(t.x64) + (int64_t)gc.col * t.ld;
+    for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < t.ld;
+         w += (int64_t)gridDim.x * blockDim.x) {
+      double v = 0.0;
+      if (w < t.n) {
+        const int64_t s = gc.perm ? (int64_t)gc.perm[w] : w;
+        v = gc.src[s * gc.stride];
+      }
+      dst[w] = v;
+    }
+  }
+}
+
+__global__ void minmax_kernel(const TaskDev* __restrict__ tasks,
+                              const int32_t* __restrict__ col_task,
+                              const int32_t* __restrict__ col_idx, int ncols,
+                              unsigned long long* __restrict__ minmax) {
+  for (int g = blockIdx.y; g < ncols; g += gridDim.y) {
+    const TaskDev t = tasks[col_task[g]];
+    const double* x = t.x64 + (int64_t)col_idx[g] * t.ld;
+    unsigned long long lo = ~0ull, hi = 0ull;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < t.n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+      const unsigned long long k = key_of(x[i]);
+      lo = k < lo ? k : lo;
+      hi = k > hi ? k : hi;
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+      const unsigned long long a = __shfl_xor_sync(0xffffffffu, lo, o);
+      const unsigned long long b = __shfl_xor_sync(0xffffffffu, hi, o);
+      lo = a < lo ? a : lo;
+      hi = b > hi ? b : hi;
+    }
+    if ((threadIdx.x & 31) == 0) {
+      atomicMin(&minmax[2 * g], lo);
+      atomicMax(&minmax[2 * g + 1], hi);
+    }
+  }
+}
+
+__global__ void center_kernel(const unsigned long long* __restrict__ minmax, int ncols,
+                              double* __restrict__ centers) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= ncols) return;
+  const double lo = value_of(minmax[2 * g]);
+  const double hi = value_of(minmax[2 * g + 1]);
+  centers[g] = 0.5 * lo + 0.5 * hi;
+}
+
+__global__ void materialize_kernel(const TaskDev* __restrict__ tasks,
+                                   const JobDev* __restrict__ jobs, int njobs,
+                                   const int32_t* __restrict__ sorted_vals,
+                                   const SortSeg* __restrict__ segs) {
+  for (int jb = blockIdx.y; jb < njobs; jb += gridDim.y) {
+    const JobDev J = jobs[jb];
+    const TaskDev t = tasks[J.task];
+    const int d = J.sp.d;
+    if (blockIdx.x == 0 && threadIdx.x < d) J.center[threadIdx.x] = t.center[J.sp.cols[threadIdx.x]];
+    const int32_t* sv = J.slab ? sorted_vals + segs[J.sort_seg].out_base : nullptr;
+    bool bad = false;
+    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < J.lds;
+         p += (int64_t)gridDim.x * blockDim.x) {
+      if (p < J.len) {
+        const int32_t w = sv ? sv[p] : J.seg_begin + (int32_t)p;
+        J.idx[p] = w;
+        for (int c = 0; c < d; ++c) {
+          const int tc = J.sp.cols[c];
+          const double v = t.x64[(int64_t)tc * t.ld + w];
+          const double cv = v - t.center[tc];
+          bad |= !(fabs(cv) < 1e37);
+          J.c64[(int64_t)c * J.lds + p] = v;
+          // clamped so that FP32 distances stay finite; a job with a clamped
+          // value never trusts its FP32 copy (TF_UNSAFE32)
+          J.c32[(int64_t)c * J.lds + p] = __double2float_rn(fmin(fmax(cv, -1e37), 1e37));
+        }
+      } else {
+        J.idx[p] = J.seg_begin;
+        for (int c = 0; c < d; ++c) {
+          J.c64[(int64_t)c * J.lds + p] = 0.0;
+          J.c32[(int64_t)c * J.lds + p] = 0.0f;
+        }
+      }
+    }
+    if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(J.jflags, (uint32_t)TF_UNSAFE32);
+  }
+}
+
+__global__ void radius_kernel(const TaskDev* __restrict__ tasks, int ntasks) {
+  for (int ti = blockIdx.y; ti < ntasks; ti += gridDim.y) {
+    const TaskDev t = tasks[ti];
+    if (t.rad_given) continue;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < t.n;
+         i += (int64_t)gridDim.x * blockDim.x)
+      t.rad[i] = t.eps[i] - 1e-12;
+  }
+}
+
+__device__ __forceinline__ double psi_of(const double* __restrict__ tab, int64_t len, int32_t n,
+                                         uint32_t& bad) {
+  if (n < 0 || n >= len) {
+    bad = 1u;
+    return 0.0;
+  }
+  return tab[n];  // entry 0 is a placeholder; zero counts are flagged
+}
+
+__global__ void combine_kernel(const TaskDev* __restrict__ tasks,
+                               const CombineJob* __restrict__ jobs,
+                               const int32_t* __restrict__ chunk_job,
+                               const double* __restrict__ psi_tab, int64_t psi_len,
+                               double* __restrict__ partial, uint32_t* __restrict__ zero_flags,
+                               uint32_t* __restrict__ err) {
+  const int chunk = blockIdx.x;
+  const CombineJob jb = jobs[chunk_job[chunk]];
+  const TaskDev t = tasks[jb.task];
+  const int64_t p0 = (int64_t)(chunk - jb.chunk0) * COMBINE_CHUNK;
+  const int64_t p1 = p0 + COMBINE_CHUNK < (int64_t)t.n ? p0 + COMBINE_CHUNK : (int64_t)t.n;
+  double acc = 0.0;
+  uint32_t zf = 0, bad = 0;
+  for (int64_t i = p0 + threadIdx.x; i < p1; i += blockDim.x) {
+    double term;
+    switch (jb.kind) {
+      case EGB_MI: {
+        const int32_t a = t.cnt[0][i], b = t.cnt[1][i];
+        zf |= (a == 0 ? 1u : 0u) | (b == 0 ? 2u : 0u);
+        term = psi_of(psi_tab, psi_len, a, bad) + psi_of(psi_tab, psi_len, b, bad);
+        break;
+      }
+      case EGB_CMI:
+      case EGB_CSEMI: {
+        const int32_t a = t.cnt[0][i], b = t.cnt[1][i], c = t.cnt[2][i];
+        zf |= (a == 0 ? 1u : 0u) | (b == 0 ? 2u : 0u) | (c == 0 ? 4u : 0u);
+        term = (psi_of(psi_tab, psi_len, a, bad) + psi_of(psi_tab, psi_len, b, bad)) -
+               psi_of(psi_tab, psi_len, c, bad);
+        break;
+      }
+      case EGB_SEMI: {
+        const int32_t a = t.cnt[0][i];
+        zf |= (a == 0 ? 1u : 0u);
+        term = psi_of(psi_tab, psi_len, a, bad);
+        break;
+      }
+      default: {  // EGB_ENTROPY: log(0) = -inf propagates exactly as in NumPy
+        const double e = t.eps[i];
+        zf |= (e == 0.0 ? 1u : 0u);
+        term = log(e);
+        break;
+      }
+    }
+    acc += term;
+  }
+  // fixed-order block reduction: warp shuffles, then warp 0 over warp sums
+  __shared__ double wsum[32];
+#pragma unroll
+  for (int o = 16; o; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  zf = __reduce_or_sync(0xffffffffu, zf);
+  bad = __reduce_or_sync(0xffffffffu, bad);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) wsum[warp] = acc;
+  if (lane == 0 && zf) atomicOr(&zero_flags[jb.task], zf);
+  if (lane == 0 && bad) atomicOr(err, (uint32_t)DERR_BAD_INDEX);
+  __syncthreads();
+  if (warp == 0) {
+    const int nw = blockDim.x >> 5;
+    double v = lane < nw ? wsum[lane] : 0.0;
+#pragma unroll
+    for (int o = 16; o; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) partial[chunk] = v;
+  }
+}
+
+}  // namespace
+
+void launch_gather(const TaskDev* tasks_d, const GatherCol* cols_d, int ncols, int64_t max_ld,
+                   cudaStream_t st) {
+  if (ncols <= 0) return;
+  dim3 grid(grid_x_for(max_ld), grid_y_for(ncols));
+  gather_kernel<<<grid, PREP_THREADS, 0, st>>>(tasks_d, cols_d, ncols);
+}
+
+void launch_prepare(const TaskDev* tasks_d, const int32_t* col_task_d, const int32_t* col_idx_d,
+                    int ncols_total, unsigned long long* minmax_d, double* centers_d,
+                    cudaStream_t st) {
+  if (ncols_total <= 0) return;
+  // slot 2g holds the min key (starts all-ones), slot 2g+1 the max key
+  // (starts at zero)
+  cudaMemsetAsync(minmax_d, 0, sizeof(unsigned long long) * 2 * ncols_total, st);
+  cudaMemset2DAsync(minmax_d, 2 * sizeof(unsigned long long), 0xff, sizeof(unsigned long long),
+                    ncols_total, st);
+  dim3 grid(64, grid_y_for(ncols_total));
+  minmax_kernel<<<grid, PREP_THREADS, 0, st>>>(tasks_d, col_task_d, col_idx_d, ncols_total,
+                                                minmax_d);
+  center_kernel<<<(ncols_total + 255) / 256, 256, 0, st>>>(minmax_d, ncols_total, centers_d);
+}
+
+void launch_materialize(const TaskDev* tasks_d, const JobDev* jobs_d, int njobs,
+                        const int32_t* sorted_vals, const SortSeg* segs_d, int64_t max_lds,
+                        cudaStream_t st) {
+  if (njobs <= 0) return;
+  dim3 grid(grid_x_for(max_lds), grid_y_for(njobs));
+  materialize_kernel<<<grid, PREP_THREADS, 0, st>>>(tasks_d, jobs_d, njobs, sorted_vals, segs_d);
+}
+
+void launch_radius(const TaskDev* tasks_d, int ntasks, int64_t max_ld, cudaStream_t st) {
+  if (ntasks <= 0) return;
+  dim3 grid(grid_x_for(max_ld), grid_y_for(ntasks));
+  radius_kernel<<<grid, PREP_THREADS, 0, st>>>(tasks_d, ntasks);
+}
+
+void launch_combine(const TaskDev* tasks_d, const CombineJob* jobs_d, const int32_t* chunk_job_d,
+                    int nchunks, const double* psi_tab, int64_t psi_len, double* partial,
+                    uint32_t* zero_flags, uint32_t* err, cudaStream_t st) {
+  if (nchunks <= 0) return;
+  combine_kernel<<<nchunks, 256, 0, st>>>(tasks_d, jobs_d, chunk_job_d, psi_tab, psi_len,
+                                          partial, zero_flags, err);
+}
+
+}  // namespace egb

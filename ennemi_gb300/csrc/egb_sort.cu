@@ -1,0 +1,324 @@
+// egb_sort.cu -- batched segmented LSD radix sort of FP64 columns, and the
+// 1-D estimator kernels that run on the sorted arrays.
+//
+// Sort.  Every requested (task, column, segment) is one segment of a single
+// concatenated key array.  Keys are the order-preserving uint64 image of the
+// FP64 value (key_of), the payload is the working index of the point.  Eight
+// stable 8-bit LSD passes; each pass is histogram -> exclusive scan ->
+// stable scatter.  Per-block histograms are laid out segment-major,
+// digit-next, block-minor, so ONE global exclusive scan yields absolute
+// output positions that never leave a segment.
+//
+// 1-D kNN (entropy of one column, Ross MI with 1-D x): for the point at
+// sorted position p the (k+1)-th smallest |x_j - x_p| (self included) is
+// found by merging outward from p -- the exact FP64 distances, as cKDTree.
+//
+// 1-D counts (marginal spaces of KSG / CMI): #{j : fl64(|x_j - q|) <= r},
+// r = fl64(eps - 1e-12).  fl64(s_j - q) is monotone in s_j (rounding is
+// monotone), so on each side of q the predicate holds on one contiguous run
+// of sorted positions.  Its ends are found by galloping out from p and
+// bisecting, evaluating the exact FP64 predicate only -- O(log count) probes.
+#include "egb_internal.cuh"
+
+namespace egb {
+
+namespace {
+
+constexpr int SORT_THREADS = 256;
+constexpr int SCAN_THREADS = 256;
+constexpr int SCAN_ITEMS = 16;
+constexpr int SCAN_CHUNK = SCAN_THREADS * SCAN_ITEMS;
+constexpr int SORTED_THREADS = SORTED_BLOCK;
+
+__global__ void sort_load_kernel(const TaskDev* __restrict__ tasks,
+                                 const SortSeg* __restrict__ segs,
+                                 const int32_t* __restrict__ blk_seg,
+                                 uint64_t* __restrict__ keys,
+                                 int32_t* __restrict__ vals) {
+  const int b = blockIdx.x;
+  const SortSeg s = segs[blk_seg[b]];
+  const TaskDev t = tasks[s.task];
+  const double* x = t.x64 + (int64_t)s.col * t.ld + s.src_begin;
+  const int i0 = (b - s.blk0) * SORT_TILE;
+  const int i1 = min(i0 + SORT_TILE, s.len);
+  for (int i = i0 + threadIdx.x; i < i1; i += SORT_THREADS) {
+    keys[s.out_base + i] = key_of(x[i]);
+    vals[s.out_base + i] = s.src_begin + i;
+  }
+}
+
+__global__ void sort_hist_kernel(const SortSeg* __restrict__ segs,
+                                 const int32_t* __restrict__ blk_seg,
+                                 const uint64_t* __restrict__ keys, int shift,
+                                 uint32_t* __restrict__ hist) {
+  __shared__ uint32_t h[256];
+  const int b = blockIdx.x;
+  const SortSeg s = segs[blk_seg[b]];
+  h[threadIdx.x] = 0;
+  __syncthreads();
+  const int i0 = (b - s.blk0) * SORT_TILE;
+  const int i1 = min(i0 + SORT_TILE, s.len);
+  for (int i = i0 + threadIdx.x; i < i1; i += SORT_THREADS) {
+    const uint32_t dgt = (uint32_t)(keys[s.out_base + i] >> shift) & 255u;
+    atomicAdd(&h[dgt], 1u);
+  }
+  __syncthreads();
+  const int lb = b - s.blk0;
+  hist[(int64_t)256 * s.blk0 + (int64_t)threadIdx.x * s.nblk + lb] = h[threadIdx.x];
+}
+
+// Stable scatter: the tile is consumed in rounds of 256 consecutive keys
+// (one per thread, in order).  Inside a round a key's rank is
+//   (earlier rounds, same digit) + (earlier warps, same digit)
+//   + (earlier lanes of its warp, same digit; via match_any).
+// offs[] already holds absolute positions in the concatenated buffer.
+__global__ void sort_scatter_kernel(const SortSeg* __restrict__ segs,
+                                    const int32_t* __restrict__ blk_seg,
+                                    const uint64_t* __restrict__ kin,
+                                    const int32_t* __restrict__ vin, int shift,
+                                    const uint32_t* __restrict__ offs,
+                                    uint64_t* __restrict__ kout,
+                                    int32_t* __restrict__ vout) {
+  constexpr int NW = SORT_THREADS / 32;
+  __shared__ uint32_t base[256];
+  __shared__ uint32_t wcnt[NW][256];
+  __shared__ uint32_t rtot[256];
+  const int b = blockIdx.x;
+  const SortSeg s = segs[blk_seg[b]];
+  const int lb = b - s.blk0;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  base[tid] = offs[(int64_t)256 * s.blk0 + (int64_t)tid * s.nblk + lb];
+  for (int w = 0; w < NW; ++w) wcnt[w][tid] = 0;
+  __syncthreads();
+  const int i0 = lb * SORT_TILE;
+  const int i1 = min(i0 + SORT_TILE, s.len);
+  const uint32_t lt_mask = (1u << lane) - 1u;
+  for (int r0 = i0; r0 < i1; r0 += SORT_THREADS) {
+    const int i = r0 + tid;
+    const bool valid = i < i1;
+    uint64_t key = 0;
+    int32_t val = 0;
+    uint32_t dgt = 256u + (uint32_t)lane;  // invalid lanes never match valid ones
+    if (valid) {
+      key = kin[s.out_base + i];
+      val = vin[s.out_base + i];
+      dgt = (uint32_t)(key >> shift) & 255u;
+    }
+    const uint32_t peers = __match_any_sync(0xffffffffu, dgt);
+    const uint32_t wrank = __popc(peers & lt_mask);
+    if (valid && wrank == 0) wcnt[warp][dgt] = __popc(peers);
+    __syncthreads();
+    {  // exclusive scan over warps for digit `tid`
+      uint32_t run = 0;
+#pragma unroll
+      for (int w = 0; w < NW; ++w) {
+        const uint32_t c = wcnt[w][tid];
+        wcnt[w][tid] = run;
+        run += c;
+      }
+      rtot[tid] = run;
+    }
+    __syncthreads();
+    if (valid) {
+      const uint32_t pos = base[dgt] + wcnt[warp][dgt] + wrank;
+      kout[pos] = key;
+      vout[pos] = val;
+    }
+    __syncthreads();
+    base[tid] += rtot[tid];
+#pragma unroll
+    for (int w = 0; w < NW; ++w) wcnt[w][tid] = 0;
+    __syncthreads();
+  }
+}
+
+// ------------------------------------------------------------------ scan --
+__device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* total) {
+  __shared__ uint32_t ws[SCAN_THREADS / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) ws[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t w = lane < SCAN_THREADS / 32 ? ws[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    if (lane < SCAN_THREADS / 32) ws[lane] = w;
+  }
+  __syncthreads();
+  const uint32_t wprefix = warp ? ws[warp - 1] : 0;
+  if (total) *total = ws[SCAN_THREADS / 32 - 1];
+  const uint32_t r = wprefix + x - v;
+  __syncthreads();
+  return r;
+}
+
+__global__ void scan_reduce_kernel(const uint32_t* __restrict__ in, int64_t n,
+                                   uint32_t* __restrict__ sums) {
+  const int64_t c0 = (int64_t)blockIdx.x * SCAN_CHUNK;
+  uint32_t s = 0;
+  for (int j = 0; j < SCAN_ITEMS; ++j) {
+    const int64_t i = c0 + (int64_t)j * SCAN_THREADS + threadIdx.x;
+    if (i < n) s += in[i];
+  }
+  uint32_t tot;
+  block_excl_scan(s, &tot);
+  if (threadIdx.x == 0) sums[blockIdx.x] = tot;
+}
+
+__global__ void scan_top_kernel(uint32_t* __restrict__ sums, int nchunks) {
+  uint32_t carry = 0;
+  for (int c0 = 0; c0 < nchunks; c0 += SCAN_THREADS) {
+    const int i = c0 + threadIdx.x;
+    const uint32_t v = i < nchunks ? sums[i] : 0;
+    uint32_t tot;
+    const uint32_t ex = block_excl_scan(v, &tot);
+    if (i < nchunks) sums[i] = carry + ex;
+    carry += tot;
+  }
+}
+
+__global__ void scan_down_kernel(uint32_t* __restrict__ data, int64_t n,
+                                 const uint32_t* __restrict__ sums) {
+  const int64_t c0 = (int64_t)blockIdx.x * SCAN_CHUNK;
+  // blocked arrangement: thread t owns items [t*ITEMS, (t+1)*ITEMS)
+  uint32_t v[SCAN_ITEMS];
+  uint32_t s = 0;
+#pragma unroll
+  for (int j = 0; j < SCAN_ITEMS; ++j) {
+    const int64_t i = c0 + (int64_t)threadIdx.x * SCAN_ITEMS + j;
+    v[j] = i < n ? data[i] : 0;
+    s += v[j];
+  }
+  uint32_t run = block_excl_scan(s, nullptr) + sums[blockIdx.x];
+#pragma unroll
+  for (int j = 0; j < SCAN_ITEMS; ++j) {
+    const int64_t i = c0 + (int64_t)threadIdx.x * SCAN_ITEMS + j;
+    if (i < n) data[i] = run;
+    run += v[j];
+  }
+}
+
+// --------------------------------------------------------- sorted jobs ----
+__global__ void sorted_jobs_kernel(const TaskDev* __restrict__ tasks,
+                                   const SortedJob* __restrict__ jobs, int njobs,
+                                   const uint64_t* __restrict__ keys_all,
+                                   const int32_t* __restrict__ perm_all) {
+  // the job of this block: last j with jobs[j].blk0 <= blockIdx.x
+  int lo = 0, hi = njobs;
+  while (hi - lo > 1) {
+    const int m = (lo + hi) >> 1;
+    if (jobs[m].blk0 <= (int)blockIdx.x) lo = m; else hi = m;
+  }
+  const SortedJob jb = jobs[lo];
+  const int64_t p = (int64_t)((int)blockIdx.x - jb.blk0) * SORTED_THREADS + threadIdx.x;
+  const int64_t len = jb.len;
+  if (p >= len) return;
+  const uint64_t* __restrict__ keys = keys_all + jb.base;
+  const int32_t i = perm_all[jb.base + p];
+  const TaskDev t = tasks[jb.task];
+  const double q = value_of(keys[p]);
+  const double INF = __longlong_as_double((long long)INF_BITS);
+
+  if (jb.kind == 0) {  // (k+1)-NN distance, self included; +inf if too few
+    int64_t L = p - 1, R = p + 1;
+    double d = (jb.K <= len) ? 0.0 : INF;
+    if (jb.K <= len) {
+      for (int s = 1; s < jb.K; ++s) {
+        const double dl = L >= 0 ? q - value_of(keys[L]) : INF;
+        const double dr = R < len ? value_of(keys[R]) - q : INF;
+        if (dl <= dr) { d = dl; --L; } else { d = dr; ++R; }
+      }
+    }
+    t.eps[i] = d;
+    return;
+  }
+
+  const double r = t.rad[i];
+  int32_t count;
+  if (!(r >= 0.0)) {
+    count = 0;
+  } else if (r == INF) {
+    count = (int32_t)len;
+  } else {
+    // right end: last j >= p with fl64(s_j - q) <= r   (true at j = p)
+    int64_t a = p, step = 1;
+    while (a + step < len && value_of(keys[a + step]) - q <= r) {
+      a += step;
+      step <<= 1;
+    }
+    int64_t b = a + step < len ? a + step : len;  // first index known false (or len)
+    while (b - a > 1) {
+      const int64_t m = a + ((b - a) >> 1);
+      if (value_of(keys[m]) - q <= r) a = m; else b = m;
+    }
+    const int64_t R = a;
+    // left end: first j <= p with fl64(q - s_j) <= r   (true at j = p)
+    a = p;
+    step = 1;
+    while (a - step >= 0 && q - value_of(keys[a - step]) <= r) {
+      a -= step;
+      step <<= 1;
+    }
+    b = a - step >= 0 ? a - step : -1;  // last index known false (or -1)
+    while (a - b > 1) {
+      const int64_t m = b + ((a - b) >> 1);
+      if (q - value_of(keys[m]) <= r) a = m; else b = m;
+    }
+    count = (int32_t)(R - a + 1);
+  }
+  t.cnt[jb.slot][i] = count;
+}
+
+}  // namespace
+
+size_t sort_scan_tmp_elems(int nblk) {
+  const int64_t n = (int64_t)256 * nblk;
+  return (size_t)((n + SCAN_CHUNK - 1) / SCAN_CHUNK) + 1;
+}
+
+static void excl_scan(uint32_t* data, int64_t n, uint32_t* tmp, cudaStream_t st) {
+  const int nchunks = (int)((n + SCAN_CHUNK - 1) / SCAN_CHUNK);
+  scan_reduce_kernel<<<nchunks, SCAN_THREADS, 0, st>>>(data, n, tmp);
+  scan_top_kernel<<<1, SCAN_THREADS, 0, st>>>(tmp, nchunks);
+  scan_down_kernel<<<nchunks, SCAN_THREADS, 0, st>>>(data, n, tmp);
+}
+
+void launch_sort(const TaskDev* tasks_d, const SortSeg* segs_d, const int32_t* blk_seg_d,
+                 int nblk, uint64_t* keys_a, uint64_t* keys_b, int32_t* vals_a,
+                 int32_t* vals_b, uint32_t* hist, uint32_t* scan_tmp, cudaStream_t st) {
+  if (nblk <= 0) return;
+  sort_load_kernel<<<nblk, SORT_THREADS, 0, st>>>(tasks_d, segs_d, blk_seg_d, keys_a, vals_a);
+  uint64_t* kin = keys_a;
+  uint64_t* kout = keys_b;
+  int32_t* vin = vals_a;
+  int32_t* vout = vals_b;
+  for (int pass = 0; pass < 8; ++pass) {
+    const int shift = 8 * pass;
+    sort_hist_kernel<<<nblk, SORT_THREADS, 0, st>>>(segs_d, blk_seg_d, kin, shift, hist);
+    excl_scan(hist, (int64_t)256 * nblk, scan_tmp, st);
+    sort_scatter_kernel<<<nblk, SORT_THREADS, 0, st>>>(segs_d, blk_seg_d, kin, vin, shift,
+                                                       hist, kout, vout);
+    uint64_t* tk = kin; kin = kout; kout = tk;
+    int32_t* tv = vin; vin = vout; vout = tv;
+  }
+  // eight passes: the sorted keys and values are back in keys_a / vals_a
+}
+
+void launch_sorted_jobs(const TaskDev* tasks_d, const SortedJob* jobs_d, int njobs,
+                        int total_blocks, const uint64_t* keys, const int32_t* perm,
+                        cudaStream_t st) {
+  if (njobs <= 0 || total_blocks <= 0) return;
+  sorted_jobs_kernel<<<(unsigned)total_blocks, SORTED_THREADS, 0, st>>>(tasks_d, jobs_d, njobs,
+                                                                        keys, perm);
+}
+
+}  // namespace egb

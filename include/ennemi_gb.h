@@ -1,0 +1,178 @@
+/*
+ * ennemi_gb.h -- C ABI of libennemi_gb.so, the GB300 (sm_103a) nearest-
+ * neighbour estimator library behind ennemi_gb300.
+ *
+ * What it replaces.  ennemi's estimators (ennemi/_entropy_estimators.py) do
+ * all their neighbour arithmetic through scipy.spatial.cKDTree:
+ *
+ *   eps = tree.query(pts, k=[k+1], p=inf)[0]           (:39, :108, :142, :194, :240)
+ *   n   = tree.query_ball_point(pts, eps - 1e-12, p=inf, return_length=True)
+ *                                                      (:109-110, :152-154, :196, :243-245)
+ *
+ * followed by a digamma combination of the counts (:42, :113, :156, :200,
+ * :247).  One call of egb_run_batch() evaluates a whole list of such
+ * estimator invocations -- the tasks that ennemi/_driver.py:477-483 and
+ * :701-707 fan out to a thread pool (_driver.py:736-785) -- on one GPU and
+ * returns one estimate per task, computed with the reference's formulas.
+ * egb_knn_eps() and egb_ball_count() are the two cKDTree queries on their own.
+ *
+ * Semantics kept from the reference (bit for bit):
+ *   - distances are max-norm, each coordinate difference rounded to nearest
+ *     in IEEE-754 binary64, exactly the value cKDTree compares;
+ *   - eps_i is the (k+1)-th smallest such distance from point i to the points
+ *     of its search set, the point itself included (distance 0); +inf when
+ *     the set has k or fewer points;
+ *   - counts are inclusive: #{j : dist(i, j) <= fl64(eps_i - 1e-12)}, the
+ *     point itself included when that radius is >= 0;
+ *   - a zero count makes the reference's _psi() return a scalar +inf
+ *     (_entropy_estimators.py:338-339); the per-slot zero flags reproduce the
+ *     resulting -inf / +inf / NaN estimates.
+ *
+ * Threading: a context is used by one host thread at a time.  All calls
+ * return 0 on success or a negative EGB_ERR_* code; egb_last_error() gives a
+ * message for the last failure on that context.
+ */
+#ifndef ENNEMI_GB_H
+#define ENNEMI_GB_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Estimator kinds; each names the reference function it replaces. */
+enum egb_kind {
+  EGB_MI = 0,     /* _estimate_single_mi                    _entropy_estimators.py:69-113  */
+  EGB_CMI = 1,    /* _estimate_conditional_mi               _entropy_estimators.py:116-156 */
+  EGB_SEMI = 2,   /* _estimate_semidiscrete_mi              _entropy_estimators.py:159-200 */
+  EGB_CSEMI = 3,  /* _estimate_conditional_semidiscrete_mi  _entropy_estimators.py:203-247 */
+  EGB_ENTROPY = 4 /* _estimate_single_entropy               _entropy_estimators.py:21-42   */
+};
+
+/* Status codes. */
+enum egb_status {
+  EGB_OK = 0,
+  EGB_ERR_ARG = -1,      /* invalid argument (message says which)            */
+  EGB_ERR_CUDA = -2,     /* a CUDA runtime call failed                        */
+  EGB_ERR_DEVICE = -3,   /* a kernel reported an error (bounded wait gave up,
+                            index guard tripped)                               */
+  EGB_ERR_NOMEM = -4,    /* device or pinned host allocation failed           */
+  EGB_ERR_STATE = -5     /* call out of order (e.g. fetch before a batch)     */
+};
+
+/* Flags for egb_run_batch / egb_knn_eps / egb_ball_count. */
+enum egb_flags {
+  EGB_INPUT_DEVICE = 1 << 0, /* column pointers are device pointers (else host) */
+  EGB_PLAIN_FP64 = 1 << 1,   /* every distance evaluated in FP64 (the plain
+                                comparator); default is FP32 distance tiles with
+                                an FP64 recheck of every borderline candidate   */
+  EGB_TIMING = 1 << 2,       /* record per-phase CUDA-event timings             */
+  EGB_FORCE_BRUTE = 1 << 3,  /* never use the sorted-slab variant for multi-D
+                                spaces (plain brute force over the segment)     */
+  EGB_KEEP_INTERNALS = 1 << 4, /* keep eps / counts for egb_fetch()             */
+  EGB_FORCE_SLAB = 1 << 5      /* use the sorted-slab variant for every multi-D
+                                  space, whatever its size (tests)               */
+};
+
+/* One float64 column: sample i at data[i * stride] (stride in elements). */
+typedef struct egb_column {
+  const double* data;
+  int64_t stride;
+} egb_column;
+
+/*
+ * One estimator invocation.  Columns are listed x first, then y, then z:
+ *   EGB_MI       dx >= 1, dy >= 1, dz = 0      (x, y continuous)
+ *   EGB_CMI      dx >= 1, dy >= 1, dz >= 1     (cond = z)
+ *   EGB_SEMI     dx >= 1, dy = 0,  dz = 0      (discrete y given as labels)
+ *   EGB_CSEMI    dx >= 1, dy = 0,  dz >= 1     (discrete y given as labels)
+ *   EGB_ENTROPY  dx >= 1, dy = 0,  dz = 0
+ * labels (host memory, SEMI/CSEMI only): class index of each sample in
+ * [0, nclass); the caller maps the reference's np.unique(y) values to 0..C-1
+ * in sorted order.
+ */
+typedef struct egb_task {
+  int32_t kind;
+  int32_t k;
+  int64_t n;
+  int32_t dx, dy, dz;
+  int32_t nclass;
+  const egb_column* cols;  /* dx + dy + dz entries */
+  const int32_t* labels;   /* SEMI / CSEMI: n entries, host memory */
+} egb_task;
+
+/*
+ * Result of one task.  value is the estimate in nats with the reference
+ * formula; term_sum is the sum over samples of the per-sample term
+ * (psi(nx)+psi(ny), psi(nxz)+psi(nyz)-psi(nz), psi(n) or log(eps)), and
+ * zero_mask has bit s set when count slot s held a zero (for EGB_ENTROPY:
+ * bit 0 = some eps was 0).
+ */
+typedef struct egb_result {
+  double value;
+  double term_sum;
+  uint32_t zero_mask;
+  int32_t status;
+} egb_result;
+
+typedef struct egb_ctx egb_ctx;
+
+/* Create a context on CUDA device `device` (its own non-blocking stream). */
+int egb_create(int device, egb_ctx** out);
+void egb_destroy(egb_ctx* ctx);
+/* Launch on `stream` (a cudaStream_t, e.g. torch's current stream); NULL
+ * restores the context's own stream. */
+int egb_set_stream(egb_ctx* ctx, void* stream);
+const char* egb_last_error(const egb_ctx* ctx);
+
+/*
+ * Evaluate `ntasks` estimator invocations and write one result each.
+ * Replaces the per-task calls of _lagged_mi (_driver.py:788-832) and
+ * _call_entropy_func (_driver.py:222-226) into the estimators.  Blocks until
+ * the results are on the host.
+ */
+int egb_run_batch(egb_ctx* ctx, const egb_task* tasks, int32_t ntasks, int32_t flags,
+                  egb_result* results);
+
+/*
+ * Internals of the last batch run with EGB_KEEP_INTERNALS, in the caller's
+ * sample order: which = 0 -> eps (double[n]); which = 1 + s -> count slot s
+ * (int64[n]).  Slots: MI nx, ny; CMI nxz, nyz, nz; SEMI n; CSEMI nxz, nyz, nz.
+ */
+int egb_fetch(egb_ctx* ctx, int32_t task, int32_t which, void* host_out);
+
+/*
+ * cKDTree(points).query(points, k=[k+1], p=inf)[0] for a row-major (n x d)
+ * float64 array: eps[i] = (k+1)-th smallest max-norm distance (self
+ * included).  points and eps in host memory unless EGB_INPUT_DEVICE.
+ */
+int egb_knn_eps(egb_ctx* ctx, const double* points, int64_t n, int32_t d, int32_t k,
+                int32_t flags, double* eps);
+
+/*
+ * cKDTree(points).query_ball_point(points, radius, p=inf, return_length=True):
+ * count[i] = #{j : maxnorm(points_j - points_i) <= radius[i]}.
+ */
+int egb_ball_count(egb_ctx* ctx, const double* points, int64_t n, int32_t d,
+                   const double* radius, int32_t flags, int64_t* count);
+
+/*
+ * Per-phase device times of the last batch run with EGB_TIMING, in ms:
+ * [0] upload, [1] gather+prepare, [2] sort, [3] kNN, [4] counts,
+ * [5] combine+download, [6] whole batch.  Returns the number written.
+ */
+int egb_timings(const egb_ctx* ctx, double* ms, int32_t max);
+
+/* Bytes the last batch copied host -> device (inputs, descriptor tables) and
+ * device -> host (partial sums, flags); returns 0. */
+int egb_last_transfer(const egb_ctx* ctx, int64_t* h2d_bytes, int64_t* d2h_bytes);
+
+/* Library version string. */
+const char* egb_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ENNEMI_GB_H */

@@ -1,0 +1,67 @@
+"""The C ABI library builds, loads and exports what include/*.h declares.
+
+No compute calls here (no GPU needed): symbols, struct layouts shared with
+the ctypes binding, and loud failure without a device.
+"""
+
+import ctypes
+import glob
+import os
+import re
+
+import pytest
+
+from conftest import ROOT
+from ennemi_gb300 import _build, _native
+
+
+def declared_functions():
+    names = set()
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        text = open(h).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        for m in re.finditer(r"\b(egb_[a-z0-9_]+)\s*\(", text):
+            names.add(m.group(1))
+    return sorted(names)
+
+
+@pytest.fixture(scope="module")
+def lib():
+    _build.build()
+    return ctypes.CDLL(_build.LIB_PATH)
+
+
+def test_header_declares_entry_points():
+    names = declared_functions()
+    for n in ["egb_create", "egb_destroy", "egb_run_batch", "egb_fetch", "egb_knn_eps",
+              "egb_ball_count", "egb_last_error", "egb_set_stream", "egb_timings"]:
+        assert n in names
+
+
+def test_library_exports_every_declared_symbol(lib):
+    missing = [n for n in declared_functions() if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_version_string(lib):
+    lib.egb_version.restype = ctypes.c_char_p
+    assert b"sm_103a" in lib.egb_version()
+
+
+def test_struct_layouts_match_header():
+    # egb_column {ptr, i64}; egb_task {i32,i32,i64,4*i32,ptr,ptr}; egb_result {f64,f64,u32,i32}
+    assert ctypes.sizeof(_native.EgbColumn) == 16
+    assert ctypes.sizeof(_native.EgbTask) == 48
+    assert _native.EgbTask.cols.offset == 32
+    assert ctypes.sizeof(_native.EgbResult) == 24
+
+
+def test_null_arguments_rejected_without_device(lib):
+    lib.egb_run_batch.restype = ctypes.c_int
+    assert lib.egb_run_batch(None, None, 0, 0, None) == -1
+    lib.egb_create.argtypes = [ctypes.c_int, ctypes.c_void_p]
+    assert lib.egb_create(0, None) == -1
+
+
+def test_library_is_built_for_sm103a():
+    assert "arch=compute_103a,code=sm_103a" in " ".join(_build.NVCC_FLAGS)

@@ -1,0 +1,175 @@
+"""Host-side logic of the public API, on the CPU.
+
+The GPU evaluation (``_native.run_tasks``) is swapped for the CPU oracle in
+these tests only, so that lagging, masking, validation, rescaling, batching
+and result assembly can be checked against the reference's own outputs
+(tests/golden/golden_driver.npz) without a device.  The product path never
+does this: without the CUDA library it raises (last test).
+"""
+
+import warnings
+
+import numpy as np
+import pytest
+
+import ennemi_gb300 as eg
+from ennemi_gb300 import _driver, _native
+from conftest import driver_cases
+
+DCASES = driver_cases()
+
+
+def _py(v):
+    v = np.asarray(v)
+    return v.item() if v.ndim == 0 else v
+
+
+@pytest.fixture
+def on_oracle(oracle, monkeypatch):
+    calls = []
+
+    def run(tasks, flags=0, device=0, results_out=None):
+        calls.append(len(tasks))
+        out = []
+        for t in tasks:
+            x = np.column_stack(t.x)
+            y = np.column_stack(t.y) if len(t.y) else None
+            z = np.column_stack(t.z) if len(t.z) else None
+            with np.errstate(all="ignore"):
+                if t.kind == _native.MI:
+                    v = oracle.ksg_mi(x, y, t.k)[0]
+                elif t.kind == _native.CMI:
+                    v = oracle.cmi(x, y, z, t.k)[0]
+                elif t.kind == _native.SEMI:
+                    v = oracle.semidiscrete_mi(x, t.labels, t.k)[0]
+                elif t.kind == _native.CSEMI:
+                    v = oracle.conditional_semidiscrete_mi(x, t.labels, z, t.k)[0]
+                else:
+                    v = oracle.entropy(x, t.k)[0]
+            out.append(v)
+        return np.array(out)
+
+    monkeypatch.setattr(_native, "run_tasks", run)
+    return calls
+
+
+@pytest.mark.parametrize("case", DCASES, ids=[c["name"] for c in DCASES])
+def test_driver_matches_reference(on_oracle, case):
+    fn = getattr(eg, str(case["func"]))
+    args = [_py(case[f"arg{i}"]) for i in range(4) if f"arg{i}" in case]
+    kw = {k[3:]: _py(v) for k, v in case.items() if k.startswith("kw_")}
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        res = np.asarray(fn(*args, **kw), dtype=np.float64)
+    gold = case["result"]
+    assert res.shape == gold.shape
+    assert np.allclose(res, gold, rtol=0, atol=1e-12, equal_nan=True), (res, gold)
+    # every call is one batch
+    assert len(on_oracle) <= 1
+
+
+def test_noise_stream_is_the_reference_draw_sequence():
+    for n, dz in [(1, 1), (17, 2), (5000, 3)]:
+        rng = np.random.default_rng(_driver.NOISE_SEED)
+        a = rng.normal(0.0, 1e-10, n)
+        b = rng.normal(0.0, 1e-10, n)
+        c = rng.normal(0.0, 1e-10, (n, dz))
+        assert np.array_equal(_driver._noise.take(0, (n,)), a)
+        assert np.array_equal(_driver._noise.take(n, (n,)), b)
+        assert np.array_equal(_driver._noise.take(2 * n, (n, dz)), c)
+
+
+def test_rescale_matches_reference_formula():
+    rng = np.random.default_rng(3)
+    x, y, z = rng.normal(5, 3, 300), rng.gamma(2, size=300), rng.normal(size=(300, 2))
+    xs, ys, zs = _driver._rescale_data(x, y, z, False, False)
+    r = np.random.default_rng(2_718281828)
+    ex = (x - x.mean()) / x.std()
+    ex += r.normal(0.0, 1e-10, ex.shape)
+    ey = (y - y.mean()) / y.std()
+    ey += r.normal(0.0, 1e-10, ey.shape)
+    ez = (z - z.mean(axis=0)) / z.std(axis=0)
+    ez += r.normal(0.0, 1e-10, ez.shape)
+    assert np.array_equal(xs, ex) and np.array_equal(ys, ey) and np.array_equal(zs, ez)
+
+
+def test_constant_variable_warns_and_draws_no_noise():
+    x = np.ones(50)
+    y = np.arange(50.0)
+    with pytest.warns(UserWarning):
+        xs, ys, _ = _driver._rescale_data(x, y, None, False, False)
+    assert np.array_equal(xs, x)
+    r = np.random.default_rng(2_718281828)
+    ey = (y - y.mean()) / y.std()
+    ey += r.normal(0.0, 1e-10, ey.shape)  # y gets the first draw
+    assert np.array_equal(ys, ey)
+
+
+@pytest.mark.parametrize("call,exc,msg", [
+    (lambda: eg.estimate_mi(np.zeros(10), np.zeros(10), k=0), ValueError, "k must be greater than zero"),
+    (lambda: eg.estimate_mi(np.zeros(10), np.zeros(10), k=3.0), TypeError, "k must be int"),
+    (lambda: eg.estimate_mi(np.zeros(10), np.zeros(9)), ValueError, "x and y must have same length"),
+    (lambda: eg.estimate_mi(np.zeros((10, 2)), np.zeros(10)), ValueError, "y must be one-dimensional"),
+    (lambda: eg.estimate_mi(np.zeros(10), np.zeros((10, 2, 2))), ValueError, "x must be one- or two-dimensional"),
+    (lambda: eg.estimate_mi(np.zeros(10), np.zeros(10), mask=np.ones(9, bool)), ValueError,
+     "mask length does not match input length"),
+    (lambda: eg.estimate_mi(np.zeros(10), np.zeros(10), mask=np.ones(10)), TypeError,
+     "mask must contain only booleans"),
+    (lambda: eg.estimate_mi(np.zeros(10), np.zeros(10), mask=np.ones((10, 2), bool)), ValueError,
+     "mask must be one-dimensional"),
+    (lambda: eg.estimate_mi(np.zeros(10), np.zeros(10), cond=np.zeros(9)), ValueError,
+     "x and cond must have same length"),
+    (lambda: eg.estimate_mi(np.zeros(10), np.zeros(10), lag=10), ValueError,
+     "lag is too large, no observations left"),
+    (lambda: eg.estimate_mi(np.zeros(10), np.zeros(10), k=10), ValueError,
+     "k must be smaller than number of observations (after lag and mask)"),
+    (lambda: eg.estimate_mi(np.r_[np.nan, np.zeros(9)], np.zeros(10)), ValueError,
+     "input contains NaNs (after applying the mask), pass drop_nan=True to ignore"),
+    (lambda: eg.estimate_entropy(np.zeros(5), k=5), ValueError,
+     "k must be smaller than number of observations (after lag and mask)"),
+    (lambda: eg.estimate_entropy(np.zeros((5, 2, 2))), ValueError, "x must be one- or two-dimensional"),
+    (lambda: eg.pairwise_mi(np.zeros((10, 3)), cond=np.zeros(10), discrete=[True, False, False]),
+     ValueError, "Conditioning is not supported with mixed discrete and continuous data."),
+])
+def test_validation_messages(call, exc, msg):
+    with pytest.raises(exc) as ei:
+        call()
+    assert str(ei.value).startswith(msg)
+
+
+def test_callbacks_once_per_task_after_one_batch(on_oracle):
+    rng = np.random.default_rng(0)
+    x, y = rng.normal(size=(400, 3)), rng.normal(size=400)
+    seen = []
+    eg.estimate_mi(y, x, [0, 1, 2], callback=lambda v, l: seen.append((v, l)))
+    assert sorted(seen) == sorted((v, l) for l in [0, 1, 2] for v in range(3))
+    assert on_oracle == [9]
+    seen.clear()
+    eg.pairwise_mi(x, callback=lambda i, j: seen.append((i, j)))
+    assert seen == [(0, 1), (0, 2), (1, 2)]
+
+
+def test_aliases_exactly_equal(on_oracle):
+    rng = np.random.default_rng(1)
+    data = rng.normal(size=(300, 3))
+    assert np.array_equal(eg.estimate_corr(data[:, 0], data[:, 1:], [0, 1]),
+                          eg.estimate_mi(data[:, 0], data[:, 1:], [0, 1], normalize=True))
+    assert np.array_equal(eg.pairwise_corr(data), eg.pairwise_mi(data, normalize=True), equal_nan=True)
+
+
+def test_normalize_mi():
+    assert eg.normalize_mi(-0.5) == -0.5
+    assert np.isclose(eg.normalize_mi(-0.5 * np.log(1 - 0.36)), 0.6)
+
+
+def test_trivial_pairwise():
+    assert np.isnan(eg.pairwise_mi(np.zeros(10))).all()
+
+
+def test_fails_loudly_without_gpu():
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a CUDA device is present")
+    x = np.random.default_rng(0).normal(size=100)
+    with pytest.raises(RuntimeError):
+        eg.estimate_mi(x, x + 1)

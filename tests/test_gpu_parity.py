@@ -1,0 +1,168 @@
+"""GPU parity: eps bit for bit, counts exactly, estimates within 1e-10 nats.
+
+Against (1) the golden vectors made by the live reference (cKDTree) and (2)
+the CPU oracle at sizes that have no fixture, for every kernel variant: the
+FP32 filter with FP64 recheck (default) and all-FP64 (plain), each as brute
+force and as sorted slab.
+"""
+
+import numpy as np
+import pytest
+
+from ennemi_gb300 import _entropy_estimators as E
+from ennemi_gb300 import _native as N
+from conftest import estimator_cases, inputs_of, outputs_of
+
+pytestmark = pytest.mark.gpu
+
+CASES = estimator_cases()
+VARIANTS = {
+    "fp32": 0,
+    "fp32-brute": N.FORCE_BRUTE,
+    "fp32-slab": N.FORCE_SLAB,
+    "fp64-brute": N.PLAIN_FP64 | N.FORCE_BRUTE,
+    "fp64-slab": N.PLAIN_FP64 | N.FORCE_SLAB,
+}
+SLOTS = {"mi": ["nx", "ny"], "cmi": ["nxz", "nyz", "nz"], "semi": ["n"],
+         "csemi": ["nxz", "nyz", "nz"], "ent": []}
+TOL = 1e-10  # nats
+
+
+def make_task(kind, k, inp):
+    if kind == "mi":
+        return E.mi_task(inp["x"], inp["y"], k)
+    if kind == "cmi":
+        return E.cmi_task(inp["x"], inp["y"], inp["z"], k)
+    if kind == "semi":
+        return E.semidiscrete_task(inp["x"], inp["y"], k)
+    if kind == "csemi":
+        return E.conditional_semidiscrete_task(inp["x"], inp["y"], inp["z"], k)
+    return E.entropy_task(inp["x"], k)
+
+
+def same_value(a, b, tol=TOL):
+    if np.isnan(a) or np.isnan(b):
+        return np.isnan(a) and np.isnan(b)
+    if np.isinf(a) or np.isinf(b):
+        return a == b
+    return abs(a - b) <= tol
+
+
+def check_internals(i, kind, n, eps_ref, counts_ref):
+    eps = N.fetch(i, 0, n)
+    assert np.array_equal(eps.view(np.uint64), np.asarray(eps_ref, np.float64).view(np.uint64)), \
+        f"eps differs at {np.flatnonzero(eps != eps_ref)[:10]}"
+    for s, name in enumerate(SLOTS[kind]):
+        c = N.fetch(i, 1 + s, n)
+        ref = np.asarray(counts_ref[name]).astype(np.int64)
+        assert np.array_equal(c, ref), f"{name} differs at {np.flatnonzero(c != ref)[:10]}"
+
+
+@pytest.mark.parametrize("variant", list(VARIANTS))
+@pytest.mark.parametrize("case", CASES, ids=[c["name"] for c in CASES])
+def test_golden_estimators(case, variant):
+    kind, k = str(case["kind"]), int(case["k"])
+    inp = inputs_of(case)
+    task = make_task(kind, k, inp)
+    vals = N.run_tasks([task], flags=VARIANTS[variant] | N.KEEP_INTERNALS)
+    gold = outputs_of(case)
+    check_internals(0, kind, task.n, gold["eps"], gold)
+    assert same_value(vals[0], float(case["value"])), (vals[0], float(case["value"]))
+
+
+@pytest.mark.parametrize("variant", ["fp32", "fp64-slab"])
+def test_golden_all_in_one_batch(variant):
+    tasks = [make_task(str(c["kind"]), int(c["k"]), inputs_of(c)) for c in CASES]
+    vals = N.run_tasks(tasks, flags=VARIANTS[variant] | N.KEEP_INTERNALS)
+    for i, c in enumerate(CASES):
+        gold = outputs_of(c)
+        check_internals(i, str(c["kind"]), tasks[i].n, gold["eps"], gold)
+        assert same_value(vals[i], float(c["value"])), c["name"]
+
+
+def _oracle_case(O, kind, k, inp):
+    with np.errstate(all="ignore"):
+        if kind == "mi":
+            return O.ksg_mi(inp["x"], inp["y"], k)
+        if kind == "cmi":
+            return O.cmi(inp["x"], inp["y"], inp["z"], k)
+        if kind == "semi":
+            return O.semidiscrete_mi(inp["x"], inp["y"], k)
+        if kind == "csemi":
+            return O.conditional_semidiscrete_mi(inp["x"], inp["y"], inp["z"], k)
+        return O.entropy(inp["x"], k)
+
+
+def _medium_cases():
+    rng = np.random.default_rng(2024)
+    n = 20000
+    g = rng.multivariate_normal([0, 0], [[1, 0.6], [0.6, 1]], size=n)
+    yield "mi_gauss_20k", "mi", 3, dict(x=g[:, 0], y=g[:, 1])
+    t = rng.standard_t(3, size=n)
+    yield "mi_t3_lognormal_20k", "mi", 3, dict(x=t, y=np.exp(rng.normal(size=n)) + 0.1 * t)
+    c3 = rng.multivariate_normal([0, 0, 0], [[1, .5, .4], [.5, 1, .4], [.4, .4, 1]], size=n)
+    yield "cmi_gauss3_20k", "cmi", 3, dict(x=c3[:, 0], y=c3[:, 1], z=c3[:, 2:])
+    c4 = rng.normal(size=(12000, 4))
+    yield "cmi_dz2_12k_k5", "cmi", 5, dict(x=c4[:, 0], y=c4[:, 1] + c4[:, 0], z=c4[:, 2:])
+    cls = rng.choice(5, p=[0.5, 0.2, 0.2, 0.08, 0.02], size=n)
+    yield "semi_x2_5cls_20k", "semi", 3, dict(x=rng.normal(size=(n, 2)) + cls[:, None] * 0.3, y=cls)
+    cls2 = (rng.uniform(size=15000) * 3).astype(int)
+    yield "csemi_15k", "csemi", 2, dict(x=rng.normal(size=15000) + cls2, y=cls2,
+                                          z=rng.normal(size=(15000, 1)))
+    yield "ent_3d_20k", "ent", 3, dict(x=rng.normal(size=(n, 3)))
+    yield "ent_1d_20k_k40", "ent", 40, dict(x=rng.normal(size=n))
+    yield "mi_k40_8k", "mi", 40, dict(x=g[:8000, 0], y=g[:8000, 1])
+    yield "mi_rounded_20k", "mi", 3, dict(x=np.round(g[:, 0], 2), y=np.round(g[:, 1], 2))
+    yield "ent_9d_3k", "ent", 4, dict(x=rng.normal(size=(3000, 9)))
+    big = rng.normal(size=(5000, 2))
+    yield "mi_huge_unsafe32_5k", "mi", 3, dict(x=1e300 * big[:, 0], y=big[:, 1])
+
+
+MEDIUM = list(_medium_cases())
+
+
+@pytest.mark.parametrize("variant", ["fp32", "fp32-brute", "fp64-slab"])
+@pytest.mark.parametrize("case", MEDIUM, ids=[c[0] for c in MEDIUM])
+def test_medium_against_oracle(oracle, case, variant):
+    name, kind, k, inp = case
+    ref_value, ref = _oracle_case(oracle, kind, k, inp)
+    task = make_task(kind, k, inp)
+    vals = N.run_tasks([task], flags=VARIANTS[variant] | N.KEEP_INTERNALS)
+    check_internals(0, kind, task.n, ref["eps"], ref)
+    assert same_value(vals[0], ref_value), (vals[0], ref_value)
+
+
+def test_primitives_against_oracle(oracle):
+    rng = np.random.default_rng(5)
+    for d in [1, 2, 3, 6]:
+        pts = rng.normal(size=(7000, d))
+        for k in [1, 3, 50]:
+            eps = N.knn_eps(pts, k)
+            assert np.array_equal(eps, oracle.knn_eps(pts, k)), (d, k)
+        r = np.abs(rng.normal(0.05, 0.05, size=7000))
+        r[::97] = -1e-13
+        r[5] = np.inf
+        cnt = N.ball_count(pts, r)
+        assert np.array_equal(cnt, oracle.ball_count(pts, r)), d
+
+
+def test_device_input_matches_host_input():
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(7)
+    x = rng.normal(size=30000)
+    y = 0.5 * x + rng.normal(size=30000)
+    host = N.run_tasks([E.mi_task(x, y, 3)])
+    xd = torch.from_numpy(x).cuda()
+    yd = torch.from_numpy(y).cuda()
+    dev = N.run_tasks([N.Task(N.MI, 3, [xd], [yd], n=30000)], flags=N.INPUT_DEVICE)
+    assert host[0] == dev[0]
+
+
+def test_public_estimators_on_gpu():
+    rng = np.random.default_rng(0)
+    cov = [[1, 0.6], [0.6, 1]]
+    d = rng.multivariate_normal([0, 0], cov, size=4000)
+    mi = E._estimate_single_mi(d[:, 0], d[:, 1], 3)
+    assert abs(mi - (-0.5 * np.log(1 - 0.36))) < 0.03
+    h = E._estimate_single_entropy(d[:, 0])
+    assert abs(h - 0.5 * np.log(2 * np.pi * np.e)) < 0.05
