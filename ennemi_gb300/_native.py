@@ -90,6 +90,8 @@ def load():
         lib.egb_timings.restype = ctypes.c_int
         lib.egb_last_transfer.argtypes = [vp, ctypes.POINTER(i64), ctypes.POINTER(i64)]
         lib.egb_last_transfer.restype = ctypes.c_int
+        lib.egb_last_stats.argtypes = [vp, ctypes.POINTER(i64), i32]
+        lib.egb_last_stats.restype = ctypes.c_int
         lib.egb_version.argtypes = []
         lib.egb_version.restype = ctypes.c_char_p
         _lib = lib
@@ -128,6 +130,13 @@ class Context:
         a, b = ctypes.c_int64(), ctypes.c_int64()
         self.lib.egb_last_transfer(self.h, ctypes.byref(a), ctypes.byref(b))
         return a.value, b.value
+
+    def stats(self) -> dict:
+        buf = (ctypes.c_int64 * 6)()
+        n = self.lib.egb_last_stats(self.h, buf, 6)
+        names = ("knn_tile_pairs", "knn_defer_pairs", "knn_deferred",
+                 "count_tile_pairs", "count_defer_pairs", "count_deferred")
+        return {names[i]: int(buf[i]) for i in range(n)}
 
     def timings(self) -> dict:
         buf = (ctypes.c_double * 8)()

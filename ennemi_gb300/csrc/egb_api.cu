@@ -117,6 +117,7 @@ struct egb_ctx {
   double timings[NPHASE] = {};
   int ntimings = 0;
   int64_t h2d_bytes = 0, d2h_bytes = 0;
+  int64_t stats[8] = {};  // kNN: tile pairs, deferred pairs, deferred queries; counts: same
   // internals of the last batch (egb_fetch)
   bool kept = false;
   std::vector<TaskPlan> keep;
@@ -339,17 +340,20 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   };
 
   // kNN: 1-D sorted jobs, multi-D tile jobs, any-K select jobs
-  struct MJob { Space s; bool is_knn; int slab; int sort_seg; int sel; };
+  struct MJob { Space s; bool is_knn; int slab; int sort_seg; int sel; int sort_seg_b; };
   std::vector<std::pair<int, Space>> sorted_knn, sorted_cnt;  // (seg, space)
   std::vector<MJob> mjobs;
   for (const Space& s : knn) {
     if (s.sp.d == 1) {
       sorted_knn.push_back({seg_for(s.task, s.sp.cols[0], s.b, s.e), s});
     } else {
-      MJob m{s, true, 0, -1, 0};
+      MJob m{s, true, 0, -1, 0, -1};
       if (s.K > EGB_KREG_MAX) m.sel = 1;
       else if (force_slab || (!force_brute && s.e - s.b >= SLAB_MIN)) m.slab = 1;
-      if (m.slab) m.sort_seg = seg_for(s.task, s.sp.cols[0], s.b, s.e);
+      if (m.slab) {
+        m.sort_seg = seg_for(s.task, s.sp.cols[0], s.b, s.e);
+        m.sort_seg_b = seg_for(s.task, s.sp.cols[1], s.b, s.e);
+      }
       mjobs.push_back(m);
     }
   }
@@ -357,9 +361,12 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
     if (s.sp.d == 1) {
       sorted_cnt.push_back({seg_for(s.task, s.sp.cols[0], s.b, s.e), s});
     } else {
-      MJob m{s, false, 0, -1, 0};
+      MJob m{s, false, 0, -1, 0, -1};
       if (force_slab || (!force_brute && s.e - s.b >= SLAB_MIN)) m.slab = 1;
-      if (m.slab) m.sort_seg = seg_for(s.task, s.sp.cols[0], s.b, s.e);
+      if (m.slab) {
+        m.sort_seg = seg_for(s.task, s.sp.cols[0], s.b, s.e);
+        m.sort_seg_b = seg_for(s.task, s.sp.cols[1], s.b, s.e);
+      }
       mjobs.push_back(m);
     }
   }
@@ -445,10 +452,16 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
     J.sort_seg = m.sort_seg;
     J.sp = m.s.sp;
     const int d = m.s.sp.d;
+    J.sort_seg_b = m.sort_seg_b;
     J.c64 = (double*)(uintptr_t)dl.take(sizeof(double) * (size_t)(d * J.lds));
     J.c32 = (float*)(uintptr_t)dl.take(sizeof(float) * (size_t)(d * J.lds));
     J.idx = (int32_t*)(uintptr_t)dl.take(sizeof(int32_t) * (size_t)J.lds);
     J.center = (double*)(uintptr_t)dl.take(sizeof(double) * (size_t)d);
+    if (m.slab) {
+      J.c64b = (double*)(uintptr_t)dl.take(sizeof(double) * (size_t)(d * J.lds));
+      J.c32b = (float*)(uintptr_t)dl.take(sizeof(float) * (size_t)(d * J.lds));
+      J.idxb = (int32_t*)(uintptr_t)dl.take(sizeof(int32_t) * (size_t)J.lds);
+    }
   }
 
   // sorted jobs
@@ -523,6 +536,16 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   for (Group& G : groups)
     if (G.defer_cap > 0) G.off_defer = dl.take(sizeof(DeferEntry) * (size_t)G.defer_cap);
 
+  std::vector<int> job_group(mjobs.size(), 0);
+  for (size_t j = 0; j < mjobs.size(); ++j) {
+    const MJob& m = mjobs[j];
+    const int d = m.s.sp.d;
+    const int dclass = (d >= 2 && d <= 4) ? d : 0;
+    int kclass = 0;
+    if (m.is_knn && !m.sel) kclass = m.s.K <= 4 ? 4 : m.s.K <= 8 ? 8 : m.s.K <= 16 ? 16 : 32;
+    job_group[j] = gidx[std::make_tuple(m.is_knn, m.sel, kclass, dclass, m.slab)];
+  }
+
   // combine
   std::vector<CombineJob> cjobs;
   std::vector<int32_t> chunk_job;
@@ -558,7 +581,8 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   const size_t off_tab = dl.take(tab_bytes);
   // zero-initialised region: counters, job flags, zero flags, error word
   const int ncounters = 2 * (int)groups.size();  // work counter + deferred count
-  const size_t zr_counters = 0;
+  const size_t zr_stats = 0;  // 4 x u64 per group
+  const size_t zr_counters = align_up(zr_stats + 32 * std::max<size_t>(groups.size(), 1), 16);
   const size_t zr_jflags = align_up(zr_counters + sizeof(int) * (size_t)std::max(ncounters, 1), 16);
   const size_t zr_zero = align_up(zr_jflags + sizeof(uint32_t) * std::max<size_t>(jobs.size(), 1), 16);
   const size_t zr_err = align_up(zr_zero + sizeof(uint32_t) * (size_t)ntasks, 16);
@@ -631,7 +655,13 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
     J.c32 = (float*)(A + (uintptr_t)J.c32);
     J.idx = (int32_t*)(A + (uintptr_t)J.idx);
     J.center = (double*)(A + (uintptr_t)J.center);
+    if (J.c64b) {
+      J.c64b = (double*)(A + (uintptr_t)J.c64b);
+      J.c32b = (float*)(A + (uintptr_t)J.c32b);
+      J.idxb = (int32_t*)(A + (uintptr_t)J.idxb);
+    }
     J.jflags = (uint32_t*)(A + off_zr + zr_jflags) + j;
+    J.stats = (unsigned long long*)(A + off_zr + zr_stats) + 4 * job_group[j];
     J.eps = D.eps;
     J.rad = D.rad;
     J.cnt = mjobs[j].is_knn ? nullptr : D.cnt[mjobs[j].s.slot];
@@ -747,6 +777,14 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
     ctx->ntimings = NPHASE;
   }
 
+  {
+    const unsigned long long* st4 = (const unsigned long long*)(H + pin_zr + zr_stats);
+    for (int i = 0; i < 8; ++i) ctx->stats[i] = 0;
+    for (size_t g = 0; g < groups.size(); ++g) {
+      const int base = groups[g].is_knn ? 0 : 3;
+      for (int i = 0; i < 3; ++i) ctx->stats[base + i] += (int64_t)st4[4 * g + i];
+    }
+  }
   const uint32_t dev_err = *(const uint32_t*)(H + pin_zr + zr_err);
   if (dev_err) {
     char buf[128];
@@ -952,6 +990,13 @@ int egb_last_transfer(const egb_ctx* ctx, int64_t* h2d_bytes, int64_t* d2h_bytes
   if (h2d_bytes) *h2d_bytes = ctx->h2d_bytes;
   if (d2h_bytes) *d2h_bytes = ctx->d2h_bytes;
   return EGB_OK;
+}
+
+int egb_last_stats(const egb_ctx* ctx, int64_t* out, int32_t max) {
+  if (!ctx || !out) return 0;
+  const int n = std::min<int>(max, 6);
+  for (int i = 0; i < n; ++i) out[i] = ctx->stats[i];
+  return n;
 }
 
 const char* egb_version(void) { return "ennemi_gb300 0.1.0 (sm_103a)"; }

@@ -129,6 +129,8 @@ count_tile_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ 
     TileSched<TILE, SLAB> sc;
     sc.init(len, q0, min(q0 + THREADS * QPT, len));
     const int nhome = sc.h1 - sc.home + 1;
+    const int nq_item = min(THREADS * QPT, len - q0);
+    unsigned long long pairs = 0;  // thread 0: candidates x queries screened
     int citem = 0;
     bool stop = false;
 #pragma unroll 1
@@ -154,44 +156,54 @@ count_tile_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ 
       const int A = t * TILE;
       const int cnt = min(TILE, len - A);
       const T* tl = tiles + (size_t)buf * DM * TILE;
-      if constexpr (D == 0) {
-        for (int j = 0; j < cnt; ++j) {
+      pairs += (unsigned long long)cnt * (unsigned long long)nq_item;
+      // Groups of 4 candidates: the FP32 screen counts the sure-inside ones
+      // and only marks borderline ones in a bit mask (bit 4q + u); those are
+      // decided in FP64 afterwards in a data-dependent loop, which keeps the
+      // FP64 work off the hot path (see the kNN kernel).
+      for (int g0 = 0; g0 < cnt; g0 += 4) {
+        const bool full = g0 + 4 <= cnt;
+        uint32_t border = 0;
+        if constexpr (D == 0) {
 #pragma unroll
-          for (int q = 0; q < QPT; ++q) {
-            if constexpr (!PLAIN) {
-              float dist = 0.0f;
+          for (int u = 0; u < 4; ++u) {
+            const bool in = g0 + u < cnt;
+            const int j = in ? g0 + u : cnt - 1;
 #pragma unroll
-              for (int c = 0; c < DQ; ++c) {
-                if (c >= d) break;
-                dist = fmaxf(dist, fabsf(tl[c * TILE + j] - qv[q][c]));
+            for (int q = 0; q < QPT; ++q) {
+              if constexpr (!PLAIN) {
+                float dist = 0.0f;
+#pragma unroll
+                for (int c = 0; c < DQ; ++c) {
+                  if (c >= d) break;
+                  dist = fmaxf(dist, fabsf(tl[c * TILE + j] - qv[q][c]));
+                }
+                cntq[q] += (in && dist <= lo[q]) ? 1 : 0;
+                border |= ((in && dist > lo[q] && dist <= hi[q]) ? 1u : 0u) << (4 * q + u);
+              } else {
+                uint64_t mm = 0;
+#pragma unroll
+                for (int c = 0; c < DQ; ++c) {
+                  if (c >= d) break;
+                  const uint64_t v = absdiff_bits(tl[c * TILE + j], qv[q][c]);
+                  mm = v > mm ? v : mm;
+                }
+                cntq[q] += (in && qok[q] && mm <= rbits[q]) ? 1 : 0;
               }
-              cntq[q] += (dist <= lo[q]) ? 1 : 0;
-              if (dist > lo[q] && dist <= hi[q]) recheck(q, A + j);
-            } else {
-              uint64_t mm = 0;
-#pragma unroll
-              for (int c = 0; c < DQ; ++c) {
-                if (c >= d) break;
-                const uint64_t v = absdiff_bits(tl[c * TILE + j], qv[q][c]);
-                mm = v > mm ? v : mm;
-              }
-              cntq[q] += (qok[q] && mm <= rbits[q]) ? 1 : 0;
             }
           }
-        }
-      } else if constexpr (!PLAIN) {
-        for (int g0 = 0; g0 < cnt; g0 += 4) {
+        } else if constexpr (!PLAIN) {
           float4 cv[D];
 #pragma unroll
           for (int c = 0; c < D; ++c) cv[c] = *reinterpret_cast<const float4*>(tl + c * TILE + g0);
-          if (g0 + 4 <= cnt) {
+          if (full) {
 #define EGB_CNT_LANE(U)                                                         \
   _Pragma("unroll") for (int q = 0; q < QPT; ++q) {                             \
     float dist = fabsf(pick4<U>(cv[0]) - qv[q][0]);                             \
     _Pragma("unroll") for (int c = 1; c < D; ++c)                               \
         dist = fmaxf(dist, fabsf(pick4<U>(cv[c]) - qv[q][c]));                  \
     cntq[q] += (dist <= lo[q]) ? 1 : 0;                                         \
-    if (dist > lo[q] && dist <= hi[q]) recheck(q, A + g0 + U);                  \
+    border |= ((dist > lo[q]) && (dist <= hi[q]) ? 1u : 0u) << (4 * q + U);     \
   }
             EGB_CNT_LANE(0)
             EGB_CNT_LANE(1)
@@ -199,7 +211,9 @@ count_tile_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ 
             EGB_CNT_LANE(3)
 #undef EGB_CNT_LANE
           } else {
-            for (int u = 0; g0 + u < cnt; ++u) {
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+              const bool in = g0 + u < cnt;
 #pragma unroll
               for (int q = 0; q < QPT; ++q) {
                 float dist = 0.0f;
@@ -208,21 +222,21 @@ count_tile_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ 
                   const float cu = u == 0 ? cv[c].x : u == 1 ? cv[c].y : u == 2 ? cv[c].z : cv[c].w;
                   dist = fmaxf(dist, fabsf(cu - qv[q][c]));
                 }
-                cntq[q] += (dist <= lo[q]) ? 1 : 0;
-                if (dist > lo[q] && dist <= hi[q]) recheck(q, A + g0 + u);
+                cntq[q] += (in && dist <= lo[q]) ? 1 : 0;
+                border |= ((in && dist > lo[q] && dist <= hi[q]) ? 1u : 0u) << (4 * q + u);
               }
             }
           }
-        }
-      } else {
-        for (int g0 = 0; g0 < cnt; g0 += 2) {
-          double2 cv[D];
+        } else {
 #pragma unroll
-          for (int c = 0; c < D; ++c) cv[c] = *reinterpret_cast<const double2*>(tl + c * TILE + g0);
-          const int nu = min(2, cnt - g0);
+          for (int h = 0; h < 2; ++h) {
+            double2 cv[D];
 #pragma unroll
-          for (int u = 0; u < 2; ++u) {
-            if (u < nu) {
+            for (int c = 0; c < D; ++c)
+              cv[c] = *reinterpret_cast<const double2*>(tl + c * TILE + g0 + 2 * h);
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+              const bool in = g0 + 2 * h + u < cnt;
 #pragma unroll
               for (int q = 0; q < QPT; ++q) {
                 uint64_t mm = 0;
@@ -231,8 +245,19 @@ count_tile_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ 
                   const uint64_t v = absdiff_bits(u ? cv[c].y : cv[c].x, qv[q][c]);
                   mm = v > mm ? v : mm;
                 }
-                cntq[q] += (qok[q] && mm <= rbits[q]) ? 1 : 0;
+                cntq[q] += (in && qok[q] && mm <= rbits[q]) ? 1 : 0;
               }
+            }
+          }
+        }
+        if (__builtin_expect(border != 0u, 0)) {
+#pragma unroll
+          for (int q = 0; q < QPT; ++q) {
+            uint32_t bq = (border >> (4 * q)) & 0xFu;
+            while (bq) {
+              const int u = __ffs(bq) - 1;
+              bq &= bq - 1u;
+              recheck(q, A + g0 + u);
             }
           }
         }
@@ -291,10 +316,12 @@ count_tile_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ 
           sj.cnt[sj.idx[qp[q]]] = qok[q] ? cntq[q] : 0;
         } else {
           const int slot = atomicAdd(defer_count, 1);
-          defer[slot] = DeferEntry{job, qp[q]};
+          atomicAdd(sj.stats + 2, 1ull);
+          defer[slot] = DeferEntry{job, qp[q], qr[q]};
         }
       }
     }
+    if (tid == 0) atomicAdd(sj.stats + 0, pairs);
     __syncthreads();
   }
 }
@@ -318,20 +345,24 @@ count_defer_kernel(const JobDev* __restrict__ jobs, const DeferEntry* __restrict
     const int d = D ? D : J->sp.d;
     const int len = J->len;
     const int64_t lds = J->lds;
-    const double* __restrict__ c64 = J->c64;
-    const T* g = PLAIN ? reinterpret_cast<const T*>(J->c64) : reinterpret_cast<const T*>(J->c32);
+    const double* __restrict__ q64 = J->c64;
+    const T* qg = PLAIN ? reinterpret_cast<const T*>(J->c64) : reinterpret_cast<const T*>(J->c32);
     const int pos = en.pos;
-    const double r = J->rad[J->idx[pos]];  // deferred queries have r >= 0
+    const double r = en.tb;  // the radius; deferred queries have r >= 0
     const uint64_t rbits = (uint64_t)__double_as_longlong(r);
     const bool unsafe = !PLAIN && ((*J->jflags & TF_UNSAFE32) != 0u);
+    const ScanOrder<T> o = choose_order<T, PLAIN>(J, pos, r);
+    const double* __restrict__ c64 = o.c64;
+    const T* g = o.g;
+    const double* scol = c64 + (int64_t)o.col * lds;
     T qv[DQ];
     double m = 0.0;
 #pragma unroll
     for (int c = 0; c < DQ; ++c) {
       if (D == 0 && c >= d) break;
-      qv[c] = g[(int64_t)c * lds + pos];
+      qv[c] = qg[(int64_t)c * lds + pos];
       if (!PLAIN) {
-        const double v = fabs(c64[(int64_t)c * lds + pos] - J->center[c]);
+        const double v = fabs(q64[(int64_t)c * lds + pos] - J->center[c]);
         m = v > m ? v : m;
       }
     }
@@ -347,9 +378,9 @@ count_defer_kernel(const JobDev* __restrict__ jobs, const DeferEntry* __restrict
         hi = __double2float_ru(r + b);
       }
     }
-    const double qx = c64[pos];
     int cnt = 0;
-    auto eval = [&](int j) {
+    // screen: 0 = outside, 1 = inside, 2 = borderline (FP64 decides)
+    auto screen = [&](int j) -> int {
       if constexpr (PLAIN) {
         uint64_t mm = 0;
 #pragma unroll
@@ -358,7 +389,7 @@ count_defer_kernel(const JobDev* __restrict__ jobs, const DeferEntry* __restrict
           const uint64_t v = absdiff_bits(g[(int64_t)c * lds + j], qv[c]);
           mm = v > mm ? v : mm;
         }
-        cnt += mm <= rbits ? 1 : 0;
+        return mm <= rbits ? 1 : 0;
       } else {
         float dist = 0.0f;
 #pragma unroll
@@ -366,39 +397,58 @@ count_defer_kernel(const JobDev* __restrict__ jobs, const DeferEntry* __restrict
           if (D == 0 && c >= d) break;
           dist = fmaxf(dist, fabsf(g[(int64_t)c * lds + j] - qv[c]));
         }
-        if (dist <= lo) {
-          ++cnt;
-        } else if (dist <= hi) {
-          uint64_t mm = 0;
-#pragma unroll
-          for (int c = 0; c < DQ; ++c) {
-            if (D == 0 && c >= d) break;
-            const int64_t off = (int64_t)c * lds;
-            const uint64_t v = absdiff_bits(c64[off + j], c64[off + pos]);
-            mm = v > mm ? v : mm;
-          }
-          cnt += mm <= rbits ? 1 : 0;
-        }
+        return dist <= lo ? 1 : (dist <= hi ? 2 : 0);
       }
     };
-    int nr = pos, nl = pos - 1;
-    bool doneR = false, doneL = nl < 0;
+    auto resolve = [&](int j) {
+      uint64_t mm = 0;
+#pragma unroll
+      for (int c = 0; c < DQ; ++c) {
+        if (D == 0 && c >= d) break;
+        const int64_t off = (int64_t)c * lds;
+        const uint64_t v = absdiff_bits(c64[off + j], q64[off + pos]);
+        mm = v > mm ? v : mm;
+      }
+      cnt += mm <= rbits ? 1 : 0;
+    };
+    int nr = o.start, nl = o.start - 1;
+    bool doneR = nr >= len, doneL = nl < 0;
     while (!doneR || !doneL) {
+      uint32_t border = 0;
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int jr = nr + lane + 32 * u;
+        const int jl = nl - lane - 32 * u;
+        if (!doneR && jr < len) {
+          const int sres = screen(jr);
+          cnt += sres == 1 ? 1 : 0;
+          border |= (sres == 2 ? 1u : 0u) << u;
+        }
+        if (!doneL && jl >= 0) {
+          const int sres = screen(jl);
+          cnt += sres == 1 ? 1 : 0;
+          border |= (sres == 2 ? 16u : 0u) << u;
+        }
+      }
+      while (border) {
+        const int b = __ffs(border) - 1;
+        border &= border - 1u;
+        resolve(b < 4 ? nr + lane + 32 * b : nl - lane - 32 * (b - 4));
+      }
       if (!doneR) {
-        const int j = nr + lane;
-        if (j < len) eval(j);
-        nr += 32;
-        doneR = nr >= len || (c64[nr] - qx > r);
+        nr += 128;
+        doneR = nr >= len || (scol[nr] - o.qs > r);
       }
       if (!doneL) {
-        const int j = nl - lane;
-        if (j >= 0) eval(j);
-        nl -= 32;
-        doneL = nl < 0 || (qx - c64[nl] > r);
+        nl -= 128;
+        doneL = nl < 0 || (o.qs - scol[nl] > r);
       }
     }
     const int total = __reduce_add_sync(0xffffffffu, cnt);
-    if (lane == 0) J->cnt[J->idx[pos]] = total;
+    if (lane == 0) {
+      J->cnt[J->idx[pos]] = total;
+      atomicAdd(J->stats + 1, (unsigned long long)(nr - nl - 1));
+    }
   }
 }
 

@@ -63,6 +63,19 @@ __host__ __device__ __forceinline__ double value_of(uint64_t k) {
 }
 
 #ifdef __CUDACC__
+// Smallest float >= the non-negative double with bit pattern u (integer
+// operations only: GB300 issues FP64 at 2 lanes per clock per SM, so this
+// keeps conversions off that pipe).
+__device__ __forceinline__ float f32_up_of_bits(uint64_t u) {
+  const int e = (int)(u >> 52);                       // biased exponent (sign is 0)
+  if (e >= 1023 + 128) return __int_as_float(0x7f800000);
+  if (e < 1023 - 126) return __int_as_float(0x00800000);  // 2^-126 bounds it
+  const uint64_t mant = u & 0xfffffffffffffull;
+  uint32_t b = ((uint32_t)(e - 1023 + 127) << 23) | (uint32_t)(mant >> 29);
+  b += (mant & 0x1fffffffull) ? 1u : 0u;              // carry into the exponent is exact
+  return __int_as_float((int)b);
+}
+
 // fl64(|a - b|) as the bit pattern of a non-negative double.  Non-negative
 // doubles order like their bit patterns, so the max over coordinates and the
 // comparisons run on the integer pipe; only the subtraction is FP64.
@@ -137,6 +150,16 @@ struct JobDev {
   int32_t K;              // k + 1 (kNN) or 0 (count)
   int32_t slab;           // 1: sorted by the first column
   int32_t sort_seg;       // slab: index of the sort segment of column 0
+  int32_t sort_seg_b;     // slab: sort segment of column 1 (second order)
+  int32_t pad_;
+  // slab jobs: a second copy sorted by column 1, scanned by deferred queries
+  // whose column-1 slab is narrower than their column-0 slab
+  double* c64b;
+  float* c32b;
+  int32_t* idxb;
+  // work counters of this job's launch group: [0] pairs screened by tile
+  // items, [1] pairs screened by deferred-query warps, [2] queries deferred
+  unsigned long long* stats;
   SpaceCols sp;
 };
 
@@ -149,7 +172,9 @@ struct WorkItem {         // one tile of queries of one job
 // much wider window than the rest of its item); finished one warp per query.
 struct DeferEntry {
   int32_t job;
-  int32_t pos;
+  int32_t pos;      // position in the job's first-column order
+  double tb;        // upper bound of the query's threshold (kNN: K-th distance
+                    // so far; counts: the radius)
 };
 constexpr int DEFER_FRAC = 8;    // an item stops when <= 1/8 of its threads
                                  // still have unfinished queries

@@ -36,10 +36,14 @@ __device__ __forceinline__ void insert_sorted(uint64_t (&top)[KMAX], uint64_t v)
   }
 }
 
+// FP32 screen threshold for K-th distance t (bits) and query magnitude mq:
+// an upward-rounded evaluation of t + band(mq, t) = t + 2^-21 (mq + t) + 2^-100
+// in FP32 (every operation rounds toward +inf, so the result bounds the exact
+// value from above).
 __device__ __forceinline__ float thr_from(uint64_t kth_bits, float mq) {
   if (kth_bits >= INF_BITS) return __int_as_float(0x7f800000);
-  const double t = bits_to_double(kth_bits);
-  return __double2float_ru(t + band((double)mq, t));
+  const float tu = f32_up_of_bits(kth_bits);
+  return __fmaf_ru(tu, 1.0f + 0x1p-21f, __fmaf_ru(mq, 0x1p-21f, 0x1p-100f));
 }
 
 template <int U>
@@ -140,6 +144,8 @@ knn_tile_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ it
     TileSched<TILE, SLAB> sc;
     sc.init(len, q0, min(q0 + THREADS * QPT, len));
     const int nhome = sc.h1 - sc.home + 1;
+    const int nq_item = min(THREADS * QPT, len - q0);
+    unsigned long long pairs = 0;  // thread 0: candidates x queries screened
     int citem = 0;      // tiles consumed by this item
     bool stop = false;  // slab: no further tiles; unfinished queries deferred
 #pragma unroll 1
@@ -165,57 +171,63 @@ knn_tile_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ it
       const int A = t * TILE;
       const int cnt = min(TILE, len - A);
       const T* tl = tiles + (size_t)buf * DM * TILE;
-      if constexpr (D == 0) {
-        for (int j = 0; j < cnt; ++j) {
+      pairs += (unsigned long long)cnt * (unsigned long long)nq_item;
+      // Candidates go in groups of 4.  The FP32 (or FP64) screen of a group
+      // only sets bits of a hit mask (bit 4q + u: query q, candidate u); the
+      // rare hits are resolved afterwards in a data-dependent loop, so the
+      // FP64 recheck and the list insertion stay off the hot path instead
+      // of being if-converted into it (the FP64 pipe has 2 lanes per SM).
+      for (int g0 = 0; g0 < cnt; g0 += 4) {
+        uint32_t hits = 0;
+        if constexpr (D == 0) {
 #pragma unroll
-          for (int q = 0; q < QPT; ++q) {
-            if constexpr (!PLAIN) {
-              float dist = 0.0f;
+          for (int u = 0; u < 4; ++u) {
+            const int j = g0 + u < cnt ? g0 + u : cnt - 1;
 #pragma unroll
-              for (int c = 0; c < DQ; ++c) {
-                if (c >= d) break;
-                dist = fmaxf(dist, fabsf(tl[c * TILE + j] - qv[q][c]));
+            for (int q = 0; q < QPT; ++q) {
+              if constexpr (!PLAIN) {
+                float dist = 0.0f;
+#pragma unroll
+                for (int c = 0; c < DQ; ++c) {
+                  if (c >= d) break;
+                  dist = fmaxf(dist, fabsf(tl[c * TILE + j] - qv[q][c]));
+                }
+                hits |= (dist <= thr[q] ? 1u : 0u) << (4 * q + u);
+              } else {
+                uint64_t m = 0;
+#pragma unroll
+                for (int c = 0; c < DQ; ++c) {
+                  if (c >= d) break;
+                  const uint64_t v = absdiff_bits(tl[c * TILE + j], qv[q][c]);
+                  m = v > m ? v : m;
+                }
+                hits |= (m < top[q][KMAX - 1] ? 1u : 0u) << (4 * q + u);
               }
-              if (dist <= thr[q]) recheck(q, A + j);
-            } else {
-              uint64_t m = 0;
-#pragma unroll
-              for (int c = 0; c < DQ; ++c) {
-                if (c >= d) break;
-                const uint64_t v = absdiff_bits(tl[c * TILE + j], qv[q][c]);
-                m = v > m ? v : m;
-              }
-              if (m < top[q][KMAX - 1]) insert_sorted<KMAX>(top[q], m);
             }
           }
-        }
-      } else if constexpr (!PLAIN) {
-        for (int g0 = 0; g0 < cnt; g0 += 4) {
+        } else if constexpr (!PLAIN) {
           float4 cv[D];
 #pragma unroll
           for (int c = 0; c < D; ++c) cv[c] = *reinterpret_cast<const float4*>(tl + c * TILE + g0);
-          const bool edge = g0 + 4 > cnt;
 #define EGB_KNN_LANE(U)                                                         \
   _Pragma("unroll") for (int q = 0; q < QPT; ++q) {                             \
     float dist = fabsf(pick4<U>(cv[0]) - qv[q][0]);                             \
     _Pragma("unroll") for (int c = 1; c < D; ++c)                               \
         dist = fmaxf(dist, fabsf(pick4<U>(cv[c]) - qv[q][c]));                  \
-    if (dist <= thr[q]) {                                                       \
-      if (!edge || g0 + U < cnt) recheck(q, A + g0 + U);                        \
-    }                                                                           \
+    hits |= (dist <= thr[q] ? 1u : 0u) << (4 * q + U);                          \
   }
           EGB_KNN_LANE(0)
           EGB_KNN_LANE(1)
           EGB_KNN_LANE(2)
           EGB_KNN_LANE(3)
 #undef EGB_KNN_LANE
-        }
-      } else {
-        for (int g0 = 0; g0 < cnt; g0 += 2) {
-          double2 cv[D];
+        } else {
 #pragma unroll
-          for (int c = 0; c < D; ++c) cv[c] = *reinterpret_cast<const double2*>(tl + c * TILE + g0);
-          const bool edge = g0 + 2 > cnt;
+          for (int h = 0; h < 2; ++h) {
+            double2 cv[D];
+#pragma unroll
+            for (int c = 0; c < D; ++c)
+              cv[c] = *reinterpret_cast<const double2*>(tl + c * TILE + g0 + 2 * h);
 #define EGB_KNN_LANE64(U)                                                       \
   _Pragma("unroll") for (int q = 0; q < QPT; ++q) {                             \
     uint64_t m = absdiff_bits(pick2<U>(cv[0]), qv[q][0]);                       \
@@ -223,13 +235,24 @@ knn_tile_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ it
       const uint64_t v = absdiff_bits(pick2<U>(cv[c]), qv[q][c]);               \
       m = v > m ? v : m;                                                        \
     }                                                                           \
-    if (m < top[q][KMAX - 1]) {                                                 \
-      if (!edge || g0 + U < cnt) insert_sorted<KMAX>(top[q], m);                \
-    }                                                                           \
+    hits |= (m < top[q][KMAX - 1] ? 1u : 0u) << (4 * q + 2 * h + U);            \
   }
-          EGB_KNN_LANE64(0)
-          EGB_KNN_LANE64(1)
+            EGB_KNN_LANE64(0)
+            EGB_KNN_LANE64(1)
 #undef EGB_KNN_LANE64
+          }
+        }
+        if (g0 + 4 > cnt) hits &= ((1u << (cnt - g0)) - 1u) * 0x1111u;  // partial group
+        if (__builtin_expect(hits != 0u, 0)) {
+#pragma unroll
+          for (int q = 0; q < QPT; ++q) {
+            uint32_t hq = (hits >> (4 * q)) & 0xFu;
+            while (hq) {
+              const int u = __ffs(hq) - 1;
+              hq &= hq - 1u;
+              recheck(q, A + g0 + u);
+            }
+          }
         }
       }
       __syncthreads();  // every thread is done with this buffer
@@ -290,10 +313,12 @@ knn_tile_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ it
           sj.eps[sj.idx[qp[q]]] = t;
         } else {
           const int slot = atomicAdd(defer_count, 1);
-          defer[slot] = DeferEntry{job, qp[q]};
+          atomicAdd(sj.stats + 2, 1ull);
+          defer[slot] = DeferEntry{job, qp[q], t};
         }
       }
     }
+    if (tid == 0) atomicAdd(sj.stats + 0, pairs);
     __syncthreads();  // sj and s_item are rewritten by the next fetch
   }
 }
@@ -330,30 +355,37 @@ knn_defer_kernel(const JobDev* __restrict__ jobs, const DeferEntry* __restrict__
     const int d = D ? D : J->sp.d;
     const int len = J->len;
     const int64_t lds = J->lds;
-    const double* __restrict__ c64 = J->c64;
-    const T* g = PLAIN ? reinterpret_cast<const T*>(J->c64) : reinterpret_cast<const T*>(J->c32);
+    const double* __restrict__ q64 = J->c64;  // query coordinates (first order)
+    const T* qg = PLAIN ? reinterpret_cast<const T*>(J->c64) : reinterpret_cast<const T*>(J->c32);
     const int pos = en.pos;
     const int K = J->K;
     const bool unsafe = !PLAIN && ((*J->jflags & TF_UNSAFE32) != 0u);
+    const ScanOrder<T> o = choose_order<T, PLAIN>(J, pos, en.tb);
+    const double* __restrict__ c64 = o.c64;  // candidates, in the scan order
+    const T* g = o.g;
+    const double* scol = c64 + (int64_t)o.col * lds;
     T qv[DQ];
     double m = 0.0;
 #pragma unroll
     for (int c = 0; c < DQ; ++c) {
       if (D == 0 && c >= d) break;
-      qv[c] = g[(int64_t)c * lds + pos];
+      qv[c] = qg[(int64_t)c * lds + pos];
       if (!PLAIN) {
-        const double v = fabs(c64[(int64_t)c * lds + pos] - J->center[c]);
+        const double v = fabs(q64[(int64_t)c * lds + pos] - J->center[c]);
         m = v > m ? v : m;
       }
     }
     const float mq = __double2float_ru(m);
-    const double qx = c64[pos];
     uint64_t top[KMAX];
 #pragma unroll
     for (int s = 0; s < KMAX; ++s) top[s] = s >= KMAX - K ? INF_BITS : 0ull;
-    uint64_t tw = INF_BITS;
-    float thr = __int_as_float(0x7f800000);
-    auto eval = [&](int j) {
+    // tb bounds the final K-th distance from above: candidates beyond it can
+    // neither screen in nor keep a side open
+    const uint64_t tb_bits = (uint64_t)__double_as_longlong(en.tb);
+    uint64_t tw = tb_bits < INF_BITS ? tb_bits : INF_BITS;
+    float thr = (PLAIN || unsafe) ? __int_as_float(0x7f800000) : thr_from(tw, mq);
+    // screen of one candidate: FP32 (or FP64 for PLAIN) only
+    auto screen = [&](int j) -> bool {
       if constexpr (PLAIN) {
         uint64_t mm = 0;
 #pragma unroll
@@ -362,7 +394,7 @@ knn_defer_kernel(const JobDev* __restrict__ jobs, const DeferEntry* __restrict__
           const uint64_t v = absdiff_bits(g[(int64_t)c * lds + j], qv[c]);
           mm = v > mm ? v : mm;
         }
-        if (mm < top[KMAX - 1]) insert_sorted<KMAX>(top, mm);
+        return mm < top[KMAX - 1] && mm <= tw;
       } else {
         float dist = 0.0f;
 #pragma unroll
@@ -370,37 +402,45 @@ knn_defer_kernel(const JobDev* __restrict__ jobs, const DeferEntry* __restrict__
           if (D == 0 && c >= d) break;
           dist = fmaxf(dist, fabsf(g[(int64_t)c * lds + j] - qv[c]));
         }
-        if (dist <= thr) {
-          uint64_t mm = 0;
-#pragma unroll
-          for (int c = 0; c < DQ; ++c) {
-            if (D == 0 && c >= d) break;
-            const int64_t off = (int64_t)c * lds;
-            const uint64_t v = absdiff_bits(c64[off + j], c64[off + pos]);
-            mm = v > mm ? v : mm;
-          }
-          if (mm < top[KMAX - 1]) insert_sorted<KMAX>(top, mm);
-        }
+        return dist <= thr;
       }
     };
-    int nr = pos, nl = pos - 1;
-    bool doneR = false, doneL = nl < 0;
+    auto resolve = [&](int j) {
+      uint64_t mm = 0;
+#pragma unroll
+      for (int c = 0; c < DQ; ++c) {
+        if (D == 0 && c >= d) break;
+        const int64_t off = (int64_t)c * lds;
+        const uint64_t v = absdiff_bits(c64[off + j], q64[off + pos]);
+        mm = v > mm ? v : mm;
+      }
+      if (mm < top[KMAX - 1]) insert_sorted<KMAX>(top, mm);
+    };
+    // each step: 4 positions per lane on each open side (128 per side)
+    int nr = o.start, nl = o.start - 1;
+    bool doneR = nr >= len, doneL = nl < 0;
     while (!doneR || !doneL) {
-      if (!doneR) {
-        const int j = nr + lane;
-        if (j < len) eval(j);
-        nr += 32;
+      uint32_t hits = 0;
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int jr = nr + lane + 32 * u;
+        const int jl = nl - lane - 32 * u;
+        if (!doneR && jr < len && screen(jr)) hits |= 1u << u;
+        if (!doneL && jl >= 0 && screen(jl)) hits |= 16u << u;
       }
-      if (!doneL) {
-        const int j = nl - lane;
-        if (j >= 0) eval(j);
-        nl -= 32;
+      while (hits) {
+        const int b = __ffs(hits) - 1;
+        hits &= hits - 1u;
+        resolve(b < 4 ? nr + lane + 32 * b : nl - lane - 32 * (b - 4));
       }
-      tw = warp_min_u64(top[KMAX - 1]);
+      if (!doneR) nr += 128;
+      if (!doneL) nl -= 128;
+      const uint64_t lw = warp_min_u64(top[KMAX - 1]);
+      tw = lw < tw ? lw : tw;
       if (!PLAIN) thr = unsafe ? __int_as_float(0x7f800000) : thr_from(tw, mq);
-      const double tb = bits_to_double(tw);
-      if (!doneR) doneR = nr >= len || (c64[nr] - qx > tb);
-      if (!doneL) doneL = nl < 0 || (qx - c64[nl] > tb);
+      const double tbd = bits_to_double(tw);
+      if (!doneR) doneR = nr >= len || (scol[nr] - o.qs > tbd);
+      if (!doneL) doneL = nl < 0 || (o.qs - scol[nl] > tbd);
     }
     // K-th smallest of the union of the lane lists
     uint64_t lst[KMAX];
@@ -423,7 +463,10 @@ knn_defer_kernel(const JobDev* __restrict__ jobs, const DeferEntry* __restrict__
       kth = v;
       if (lane == who) ++h;
     }
-    if (lane == 0) J->eps[J->idx[pos]] = bits_to_double(kth);
+    if (lane == 0) {
+      J->eps[J->idx[pos]] = bits_to_double(kth);
+      atomicAdd(J->stats + 1, (unsigned long long)(nr - nl - 1));
+    }
   }
 }
 

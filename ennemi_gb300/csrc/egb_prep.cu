@@ -92,6 +92,36 @@ __global__ void center_kernel(const unsigned long long* __restrict__ minmax, int
   centers[g] = 0.5 * lo + 0.5 * hi;
 }
 
+__device__ __forceinline__ bool materialize_copy(const TaskDev& t, const JobDev& J, int d,
+                                                 double* c64, float* c32, int32_t* idx,
+                                                 const int32_t* sv) {
+  bool bad = false;
+  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < J.lds;
+       p += (int64_t)gridDim.x * blockDim.x) {
+    if (p < J.len) {
+      const int32_t w = sv ? sv[p] : J.seg_begin + (int32_t)p;
+      idx[p] = w;
+      for (int c = 0; c < d; ++c) {
+        const int tc = J.sp.cols[c];
+        const double v = t.x64[(int64_t)tc * t.ld + w];
+        const double cv = v - t.center[tc];
+        bad |= !(fabs(cv) < 1e37);
+        c64[(int64_t)c * J.lds + p] = v;
+        // clamped so that FP32 distances stay finite; a job with a clamped
+        // value never trusts its FP32 copy (TF_UNSAFE32)
+        c32[(int64_t)c * J.lds + p] = __double2float_rn(fmin(fmax(cv, -1e37), 1e37));
+      }
+    } else {
+      idx[p] = J.seg_begin;
+      for (int c = 0; c < d; ++c) {
+        c64[(int64_t)c * J.lds + p] = 0.0;
+        c32[(int64_t)c * J.lds + p] = 0.0f;
+      }
+    }
+  }
+  return bad;
+}
+
 __global__ void materialize_kernel(const TaskDev* __restrict__ tasks,
                                    const JobDev* __restrict__ jobs, int njobs,
                                    const int32_t* __restrict__ sorted_vals,
@@ -102,30 +132,9 @@ __global__ void materialize_kernel(const TaskDev* __restrict__ tasks,
     const int d = J.sp.d;
     if (blockIdx.x == 0 && threadIdx.x < d) J.center[threadIdx.x] = t.center[J.sp.cols[threadIdx.x]];
     const int32_t* sv = J.slab ? sorted_vals + segs[J.sort_seg].out_base : nullptr;
-    bool bad = false;
-    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < J.lds;
-         p += (int64_t)gridDim.x * blockDim.x) {
-      if (p < J.len) {
-        const int32_t w = sv ? sv[p] : J.seg_begin + (int32_t)p;
-        J.idx[p] = w;
-        for (int c = 0; c < d; ++c) {
-          const int tc = J.sp.cols[c];
-          const double v = t.x64[(int64_t)tc * t.ld + w];
-          const double cv = v - t.center[tc];
-          bad |= !(fabs(cv) < 1e37);
-          J.c64[(int64_t)c * J.lds + p] = v;
-          // clamped so that FP32 distances stay finite; a job with a clamped
-          // value never trusts its FP32 copy (TF_UNSAFE32)
-          J.c32[(int64_t)c * J.lds + p] = __double2float_rn(fmin(fmax(cv, -1e37), 1e37));
-        }
-      } else {
-        J.idx[p] = J.seg_begin;
-        for (int c = 0; c < d; ++c) {
-          J.c64[(int64_t)c * J.lds + p] = 0.0;
-          J.c32[(int64_t)c * J.lds + p] = 0.0f;
-        }
-      }
-    }
+    bool bad = materialize_copy(t, J, d, J.c64, J.c32, J.idx, sv);
+    if (J.c64b != nullptr)  // second copy, sorted by column 1 (same values)
+      materialize_copy(t, J, d, J.c64b, J.c32b, J.idxb, sorted_vals + segs[J.sort_seg_b].out_base);
     if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(J.jflags, (uint32_t)TF_UNSAFE32);
   }
 }

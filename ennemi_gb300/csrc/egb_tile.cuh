@@ -92,7 +92,63 @@ __device__ __forceinline__ void stage_tile(T* tiles, int DM, int buf, const T* g
     bulk_g2s(tiles + ((size_t)buf * DM + c) * TILE, g + (int64_t)c * lds + A, bytes, bar);
 }
 
-// Copy a job descriptor into shared memory (thread 0).
-__device__ __forceinline__ void copy_job(JobDev& dst, const JobDev& src) { dst = src; }
+// Number of positions p of a sorted column with |col[p] - v| <= t (within
+// rounding; used only to choose a scan order), and the first position with
+// col[p] >= v.
+__device__ __forceinline__ int lower_bound_d(const double* col, int len, double v) {
+  int lo = 0, hi = len;
+  while (lo < hi) {
+    const int m = (lo + hi) >> 1;
+    if (col[m] < v) lo = m + 1; else hi = m;
+  }
+  return lo;
+}
+__device__ __forceinline__ int upper_bound_d(const double* col, int len, double v) {
+  int lo = 0, hi = len;
+  while (lo < hi) {
+    const int m = (lo + hi) >> 1;
+    if (col[m] <= v) lo = m + 1; else hi = m;
+  }
+  return lo;
+}
+
+// Scan order for a deferred slab query: its first-column slab or, when the
+// job has a second copy sorted by column 1 and that slab is narrower, the
+// second.  Returns the arrays to scan, the start position, the sorted
+// column's query value and the column index used for termination.
+template <typename T>
+struct ScanOrder {
+  const double* c64;
+  const T* g;
+  int start;       // first position to the right (inclusive)
+  int col;         // sorted column (0 or 1)
+  double qs;       // query value in that column
+};
+
+template <typename T, bool PLAIN>
+__device__ __forceinline__ ScanOrder<T> choose_order(const JobDev* J, int pos, double tb) {
+  ScanOrder<T> o;
+  o.c64 = J->c64;
+  o.g = PLAIN ? reinterpret_cast<const T*>(J->c64) : reinterpret_cast<const T*>(J->c32);
+  o.start = pos;
+  o.col = 0;
+  o.qs = J->c64[pos];
+  if (J->c64b == nullptr || J->sp.d < 2 || !(tb < __longlong_as_double((long long)INF_BITS)))
+    return o;
+  const int len = J->len;
+  const double* x = J->c64;
+  const double* y = J->c64b + J->lds;  // column 1 of the second copy, sorted
+  const double qy = J->c64[J->lds + pos];
+  const int w0 = upper_bound_d(x, len, o.qs + tb) - lower_bound_d(x, len, o.qs - tb);
+  const int w1 = upper_bound_d(y, len, qy + tb) - lower_bound_d(y, len, qy - tb);
+  if (w1 < w0) {
+    o.c64 = J->c64b;
+    o.g = PLAIN ? reinterpret_cast<const T*>(J->c64b) : reinterpret_cast<const T*>(J->c32b);
+    o.start = lower_bound_d(y, len, qy);
+    o.col = 1;
+    o.qs = qy;
+  }
+  return o;
+}
 
 }  // namespace egb

@@ -168,6 +168,12 @@ int egb_timings(const egb_ctx* ctx, double* ms, int32_t max);
  * device -> host (partial sums, flags); returns 0. */
 int egb_last_transfer(const egb_ctx* ctx, int64_t* h2d_bytes, int64_t* d2h_bytes);
 
+/* Work counters of the last batch: [0] kNN candidate-query pairs screened by
+ * tile work items, [1] kNN pairs screened for deferred queries, [2] kNN
+ * queries deferred, [3..5] the same for the multi-D counts.  Returns the
+ * number written. */
+int egb_last_stats(const egb_ctx* ctx, int64_t* out, int32_t max);
+
 /* Library version string. */
 const char* egb_version(void);
 
