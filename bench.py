@@ -275,7 +275,7 @@ def main():
     res = []
     N.run_tasks(dev_tasks, flags=N.INPUT_DEVICE | N.TIMING, device=dev, results_out=res)
     phases = ctx.timings()
-    work = ctx.stats()
+    work_stats = ctx.stats()
 
     ms_dev = dev_ms / args.steps
     ms_e2e = e2e_ms / args.steps
@@ -318,7 +318,7 @@ def main():
                 "d2h_bytes_per_step": d2h, "ms_per_step": ms_e2e},
         "gpu_launches": None,
         "phases_ms": phases,
-        "work": work,
+        "work": work_stats,
         "estimates": [r.value for r in res],
         "clocks": clocks,
         "plain": plain,
