@@ -174,6 +174,39 @@ int egb_last_transfer(const egb_ctx* ctx, int64_t* h2d_bytes, int64_t* d2h_bytes
  * number written. */
 int egb_last_stats(const egb_ctx* ctx, int64_t* out, int32_t max);
 
+/*
+ * egb_knn_eps_noalloc -- egb_knn_eps() for callers that may not allocate
+ * device memory.  It has no counterpart in the reference; it exists for
+ * callers such as a plugin inside a larger GPU application that owns a fixed,
+ * pre-reserved memory pool, a latency-bound loop that cannot accept the
+ * implicit device synchronisation of cudaMalloc/cudaFree, or a process near
+ * the device's memory limit where an allocation could fail mid-run.
+ *
+ * points: device pointer to a row-major (n x d) float64 array; eps: device
+ * pointer to n float64 outputs, eps[i] = the (k+1)-th smallest max-norm
+ * distance from point i (self included), bit-identical to egb_knn_eps().
+ * stream: the cudaStream_t to launch on (NULL = the legacy default stream);
+ * the call returns after the stream has finished the work.
+ *
+ * All intermediate data lives in one file-scope __device__ array of
+ * EGB_NOALLOC_SCRATCH_BYTES bytes, which every GPU that loads the library
+ * keeps until the process exits.  Limits: n <= EGB_NOALLOC_MAX_POINTS,
+ * d <= EGB_NOALLOC_MAX_DIM, k + 1 <= 32; anything larger returns EGB_ERR_ARG
+ * without launching.  No cudaMalloc, cudaFree or allocating library routine
+ * is called.
+ *
+ * The first call on a device looks up the device address of the scratch
+ * array (cudaGetSymbolAddress) with that device current; make that first
+ * call before any stream capture.  Every call on a device shares the one
+ * scratch array: calls that overlap on the GPU (different streams, different
+ * host threads) race and must be serialised by the caller.
+ */
+#define EGB_NOALLOC_MAX_POINTS 16384
+#define EGB_NOALLOC_MAX_DIM 8
+#define EGB_NOALLOC_SCRATCH_BYTES (1152u * 1024u)
+int egb_knn_eps_noalloc(const double* points, int64_t n, int32_t d, int32_t k, double* eps,
+                        void* stream);
+
 /* Library version string. */
 const char* egb_version(void);
 
