@@ -277,6 +277,31 @@ def main():
     phases = ctx.timings()
     work_stats = ctx.stats()
 
+    # roofline of the dominant multi-D kernel (FP32/INT-pipe bound): counted
+    # algorithmic operations ((2d+1) per candidate-query pair) over its own
+    # event-timed duration, against the nominal FP32 lane rate of the part
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    max_mhz = clocks.get("sm_max_mhz") or peaks.get("sm_max_mhz") or 2070.0
+    peak_ops = sms * 128 * max_mhz * 1e6
+    cand = [("count_tile_kernel", phases.get("count_tile", 0.0), work_stats.get("count_tile_ops", 0),
+             work_stats.get("count_tile_pairs", 0)),
+            ("knn_tile_kernel", phases.get("knn_tile", 0.0), work_stats.get("knn_tile_ops", 0),
+             work_stats.get("knn_tile_pairs", 0))]
+    kname, kms, kops, kpairs = max(cand, key=lambda c: c[1])
+    achieved = kops / (kms / 1000.0) if kms > 0 else 0.0
+    roofline = {"bound": "alu", "kernel": kname, "achieved": achieved / 1e9,
+                "peak": peak_ops / 1e9, "unit": "Gop/s", "frac": achieved / peak_ops,
+                "traffic": None, "ms": kms, "pairs": kpairs,
+                "peak_source": (f"nominal FP32 lane rate: {sms} SMs x 128 lanes x {max_mhz:.0f} MHz "
+                                "(MEASURED_PEAKS.json holds only HBM and bf16 figures)"),
+                "ops_per_pair": "2d+1 (d differences, d max-of-abs, 1 compare)",
+                "hbm_peak_gbs": peaks.get("hbm_gbs")}
+
     ms_dev = dev_ms / args.steps
     ms_e2e = e2e_ms / args.steps
     if world > 1:
@@ -316,7 +341,8 @@ def main():
                    "l2": "flushed between timed steps (512 MB write)"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": ms_e2e},
-        "gpu_launches": None,
+        "gpu_launches": work_stats.get("kernel_launches"),
+        "roofline": roofline,
         "phases_ms": phases,
         "work": work_stats,
         "estimates": [r.value for r in res],

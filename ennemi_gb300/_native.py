@@ -31,7 +31,8 @@ FORCE_BRUTE = 1 << 3
 KEEP_INTERNALS = 1 << 4
 FORCE_SLAB = 1 << 5
 
-PHASES = ("upload", "prepare", "sort", "knn", "counts", "combine", "total")
+PHASES = ("upload", "prepare", "sort", "knn", "counts", "combine", "total",
+          "knn_tile", "knn_defer", "count_tile", "count_defer")
 
 
 class EgbColumn(ctypes.Structure):
@@ -132,15 +133,16 @@ class Context:
         return a.value, b.value
 
     def stats(self) -> dict:
-        buf = (ctypes.c_int64 * 6)()
-        n = self.lib.egb_last_stats(self.h, buf, 6)
         names = ("knn_tile_pairs", "knn_defer_pairs", "knn_deferred",
-                 "count_tile_pairs", "count_defer_pairs", "count_deferred")
+                 "count_tile_pairs", "count_defer_pairs", "count_deferred",
+                 "knn_tile_ops", "count_tile_ops", "kernel_launches")
+        buf = (ctypes.c_int64 * len(names))()
+        n = self.lib.egb_last_stats(self.h, buf, len(names))
         return {names[i]: int(buf[i]) for i in range(n)}
 
     def timings(self) -> dict:
-        buf = (ctypes.c_double * 8)()
-        n = self.lib.egb_timings(self.h, buf, 8)
+        buf = (ctypes.c_double * len(PHASES))()
+        n = self.lib.egb_timings(self.h, buf, len(PHASES))
         return {PHASES[i]: buf[i] for i in range(n)}
 
 

@@ -28,6 +28,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -42,11 +43,19 @@
 using namespace egb;
 
 namespace {
+std::atomic<long long> g_launches{0};
+}  // namespace
+
+void egb::count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+namespace {
 
 constexpr int KIND_KNN_ONLY = 100;    // egb_knn_eps
 constexpr int KIND_COUNT_ONLY = 101;  // egb_ball_count
 constexpr int SLAB_MIN = 4096;        // shorter multi-D segments use brute force
 constexpr int NPHASE = 7;
+constexpr int NKTIME = 4;   // kNN tile, kNN deferred, count tile, count deferred
+constexpr int NSTATS = 9;
 
 // Digamma of a positive integer with the reference's formula
 // (ennemi/_entropy_estimators.py:341-348): the SciPy constant for psi(1),
@@ -114,10 +123,13 @@ struct egb_ctx {
   double* psi_d = nullptr;
   int64_t psi_len = 0;
   cudaEvent_t ev[NPHASE + 1] = {};
-  double timings[NPHASE] = {};
+  cudaEvent_t kev[2 * NKTIME] = {};
+  double timings[NPHASE + NKTIME] = {};
   int ntimings = 0;
   int64_t h2d_bytes = 0, d2h_bytes = 0;
-  int64_t stats[8] = {};  // kNN: tile pairs, deferred pairs, deferred queries; counts: same
+  // kNN: tile pairs, deferred pairs, deferred queries; counts: the same;
+  // [6] kNN tile ops, [7] count tile ops ((2d+1) per pair); [8] kernels launched
+  int64_t stats[NSTATS] = {};
   // internals of the last batch (egb_fetch)
   bool kept = false;
   std::vector<TaskPlan> keep;
@@ -204,6 +216,7 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   const bool force_slab = (flags & EGB_FORCE_SLAB) != 0 && !force_brute;
   const bool timing = (flags & EGB_TIMING) != 0;
   cudaStream_t st = ctx->stream;
+  const long long launches0 = g_launches.load();
   ctx->kept = false;
   ctx->keep.clear();
 
@@ -716,6 +729,7 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   if (timing) EGB_CUDA(cudaEventRecord(ctx->ev[3], st));
 
   launch_sorted_jobs(tasks_d, (const SortedJob*)dtab(tab_sjk), (int)sj_knn.size(), blk_knn, keys, vals, st);
+  if (timing) EGB_CUDA(cudaEventRecord(ctx->kev[0], st));
   for (size_t g = 0; g < groups.size(); ++g) {
     Group& G = groups[g];
     if (!G.is_knn || G.items.empty()) continue;
@@ -728,6 +742,8 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
                       counters + 2 * g, err_d, (DeferEntry*)(A + G.off_defer),
                       counters + 2 * g + 1, ctx->num_sms, st);
   }
+  if (timing) EGB_CUDA(cudaEventRecord(ctx->kev[1], st));
+  if (timing) EGB_CUDA(cudaEventRecord(ctx->kev[2], st));
   for (size_t g = 0; g < groups.size(); ++g) {
     Group& G = groups[g];
     if (!G.is_knn || G.sel || !G.slab || G.items.empty()) continue;
@@ -735,10 +751,12 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
                      counters + 2 * g + 1, (int)G.defer_cap, G.kclass, G.dclass, plain,
                      ctx->num_sms, st);
   }
+  if (timing) EGB_CUDA(cudaEventRecord(ctx->kev[3], st));
   if (timing) EGB_CUDA(cudaEventRecord(ctx->ev[4], st));
 
   launch_radius(tasks_d, ntasks, max_ld, st);
   launch_sorted_jobs(tasks_d, (const SortedJob*)dtab(tab_sjc), (int)sj_cnt.size(), blk_cnt, keys, vals, st);
+  if (timing) EGB_CUDA(cudaEventRecord(ctx->kev[4], st));
   for (size_t g = 0; g < groups.size(); ++g) {
     Group& G = groups[g];
     if (G.is_knn || G.items.empty()) continue;
@@ -747,12 +765,15 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
                       err_d, (DeferEntry*)(A + G.off_defer), counters + 2 * g + 1, ctx->num_sms,
                       st);
   }
+  if (timing) EGB_CUDA(cudaEventRecord(ctx->kev[5], st));
+  if (timing) EGB_CUDA(cudaEventRecord(ctx->kev[6], st));
   for (size_t g = 0; g < groups.size(); ++g) {
     Group& G = groups[g];
     if (G.is_knn || !G.slab || G.items.empty()) continue;
     launch_count_defer((const JobDev*)dtab(tab_jobs), (const DeferEntry*)(A + G.off_defer),
                        counters + 2 * g + 1, (int)G.defer_cap, G.dclass, plain, ctx->num_sms, st);
   }
+  if (timing) EGB_CUDA(cudaEventRecord(ctx->kev[7], st));
   if (timing) EGB_CUDA(cudaEventRecord(ctx->ev[5], st));
 
   launch_combine(tasks_d, (const CombineJob*)dtab(tab_cjobs), (const int32_t*)dtab(tab_chunkjob),
@@ -774,16 +795,23 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
     }
     cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[NPHASE - 1]);
     ctx->timings[NPHASE - 1] = ms;
-    ctx->ntimings = NPHASE;
+    for (int i = 0; i < NKTIME; ++i) {
+      cudaEventElapsedTime(&ms, ctx->kev[2 * i], ctx->kev[2 * i + 1]);
+      ctx->timings[NPHASE + i] = ms;
+    }
+    ctx->ntimings = NPHASE + NKTIME;
   }
 
   {
     const unsigned long long* st4 = (const unsigned long long*)(H + pin_zr + zr_stats);
-    for (int i = 0; i < 8; ++i) ctx->stats[i] = 0;
+    for (int i = 0; i < NSTATS; ++i) ctx->stats[i] = 0;
     for (size_t g = 0; g < groups.size(); ++g) {
       const int base = groups[g].is_knn ? 0 : 3;
       for (int i = 0; i < 3; ++i) ctx->stats[base + i] += (int64_t)st4[4 * g + i];
+      const int d = groups[g].dclass ? groups[g].dclass : groups[g].dmax;
+      ctx->stats[groups[g].is_knn ? 6 : 7] += (int64_t)st4[4 * g] * (2 * d + 1);
     }
+    ctx->stats[8] = (int64_t)(g_launches.load() - launches0);
   }
   const uint32_t dev_err = *(const uint32_t*)(H + pin_zr + zr_err);
   if (dev_err) {
@@ -871,6 +899,7 @@ int egb_create(int device, egb_ctx** out) {
   cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
   if (ctx->num_sms < 1) ctx->num_sms = 1;
   for (auto& e : ctx->ev) cudaEventCreate(&e);
+  for (auto& e : ctx->kev) cudaEventCreate(&e);
   *out = ctx;
   return EGB_OK;
 }
@@ -883,6 +912,8 @@ void egb_destroy(egb_ctx* ctx) {
   if (ctx->pinned) cudaFreeHost(ctx->pinned);
   if (ctx->psi_d) cudaFree(ctx->psi_d);
   for (auto& e : ctx->ev)
+    if (e) cudaEventDestroy(e);
+  for (auto& e : ctx->kev)
     if (e) cudaEventDestroy(e);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
   delete ctx;
@@ -994,7 +1025,7 @@ int egb_last_transfer(const egb_ctx* ctx, int64_t* h2d_bytes, int64_t* d2h_bytes
 
 int egb_last_stats(const egb_ctx* ctx, int64_t* out, int32_t max) {
   if (!ctx || !out) return 0;
-  const int n = std::min<int>(max, 6);
+  const int n = std::min<int>(max, NSTATS);
   for (int i = 0; i < n; ++i) out[i] = ctx->stats[i];
   return n;
 }

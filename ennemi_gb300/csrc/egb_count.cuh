@@ -487,6 +487,7 @@ void launch_count_t(const JobDev* jobs, const WorkItem* items, int nitems, int* 
   if (grid < 1) return;
   kern<<<grid, C::THREADS, s.smem, st>>>(jobs, items, nitems, counter, err, dmax,
                                          SLAB ? defer : nullptr, defer_count);
+  count_launch();
 }
 
 template <int D, bool PLAIN>
@@ -497,6 +498,7 @@ void launch_count_defer_t(const JobDev* jobs, const DeferEntry* list, const int*
   if (grid > num_sms * 8) grid = num_sms * 8;
   if (grid < 1) return;
   count_defer_kernel<D, PLAIN><<<grid, 32 * warps_per_block, 0, st>>>(jobs, list, count, cap);
+  count_launch();
 }
 
 template <bool PLAIN, bool SLAB>

@@ -217,6 +217,10 @@ struct CombineJob {       // per-task reduction of per-sample terms
 };
 constexpr int COMBINE_CHUNK = 4096;
 
+// Kernels launched by this library since the counter was last read (every
+// <<<>>> site calls count_launch(); the planner reports the count per batch).
+void count_launch();
+
 // ----------------------------------------------------------- entry points --
 // Launch wrappers implemented in the kernel translation units.  Every wrapper
 // launches on `st` and never synchronises.

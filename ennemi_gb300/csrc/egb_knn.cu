@@ -180,6 +180,7 @@ void launch_knn_select(const JobDev* jobs_d, const WorkItem* items_d, int nitems
   (void)num_sms;
   if (nitems <= 0) return;
   knn_select_kernel<<<nitems, SELECT_WARPS * 32, 0, st>>>(jobs_d, items_d, nitems);
+  count_launch();
 }
 
 }  // namespace egb

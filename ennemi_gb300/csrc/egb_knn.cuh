@@ -508,6 +508,7 @@ void launch_knn_t(const JobDev* jobs, const WorkItem* items, int nitems, int* co
   if (grid < 1) return;
   kern<<<grid, C::THREADS, s.smem, st>>>(jobs, items, nitems, counter, err, dmax,
                                          SLAB ? defer : nullptr, defer_count);
+  count_launch();
 }
 
 template <int D, int KMAX, bool PLAIN>
@@ -518,6 +519,7 @@ void launch_knn_defer_t(const JobDev* jobs, const DeferEntry* list, const int* c
   if (grid > num_sms * 8) grid = num_sms * 8;
   if (grid < 1) return;
   knn_defer_kernel<D, KMAX, PLAIN><<<grid, 32 * warps_per_block, 0, st>>>(jobs, list, count, cap);
+  count_launch();
 }
 
 // Dispatch over (dclass, kclass) for one (PLAIN, SLAB) pair.

@@ -230,6 +230,7 @@ void launch_gather(const TaskDev* tasks_d, const GatherCol* cols_d, int ncols, i
   if (ncols <= 0) return;
   dim3 grid(grid_x_for(max_ld), grid_y_for(ncols));
   gather_kernel<<<grid, PREP_THREADS, 0, st>>>(tasks_d, cols_d, ncols);
+  count_launch();
 }
 
 void launch_prepare(const TaskDev* tasks_d, const int32_t* col_task_d, const int32_t* col_idx_d,
@@ -244,7 +245,9 @@ void launch_prepare(const TaskDev* tasks_d, const int32_t* col_task_d, const int
   dim3 grid(64, grid_y_for(ncols_total));
   minmax_kernel<<<grid, PREP_THREADS, 0, st>>>(tasks_d, col_task_d, col_idx_d, ncols_total,
                                                 minmax_d);
+  count_launch();
   center_kernel<<<(ncols_total + 255) / 256, 256, 0, st>>>(minmax_d, ncols_total, centers_d);
+  count_launch();
 }
 
 void launch_materialize(const TaskDev* tasks_d, const JobDev* jobs_d, int njobs,
@@ -253,12 +256,14 @@ void launch_materialize(const TaskDev* tasks_d, const JobDev* jobs_d, int njobs,
   if (njobs <= 0) return;
   dim3 grid(grid_x_for(max_lds), grid_y_for(njobs));
   materialize_kernel<<<grid, PREP_THREADS, 0, st>>>(tasks_d, jobs_d, njobs, sorted_vals, segs_d);
+  count_launch();
 }
 
 void launch_radius(const TaskDev* tasks_d, int ntasks, int64_t max_ld, cudaStream_t st) {
   if (ntasks <= 0) return;
   dim3 grid(grid_x_for(max_ld), grid_y_for(ntasks));
   radius_kernel<<<grid, PREP_THREADS, 0, st>>>(tasks_d, ntasks);
+  count_launch();
 }
 
 void launch_combine(const TaskDev* tasks_d, const CombineJob* jobs_d, const int32_t* chunk_job_d,
@@ -267,6 +272,7 @@ void launch_combine(const TaskDev* tasks_d, const CombineJob* jobs_d, const int3
   if (nchunks <= 0) return;
   combine_kernel<<<nchunks, 256, 0, st>>>(tasks_d, jobs_d, chunk_job_d, psi_tab, psi_len,
                                           partial, zero_flags, err);
+  count_launch();
 }
 
 }  // namespace egb

@@ -288,8 +288,11 @@ size_t sort_scan_tmp_elems(int nblk) {
 static void excl_scan(uint32_t* data, int64_t n, uint32_t* tmp, cudaStream_t st) {
   const int nchunks = (int)((n + SCAN_CHUNK - 1) / SCAN_CHUNK);
   scan_reduce_kernel<<<nchunks, SCAN_THREADS, 0, st>>>(data, n, tmp);
+  count_launch();
   scan_top_kernel<<<1, SCAN_THREADS, 0, st>>>(tmp, nchunks);
+  count_launch();
   scan_down_kernel<<<nchunks, SCAN_THREADS, 0, st>>>(data, n, tmp);
+  count_launch();
 }
 
 void launch_sort(const TaskDev* tasks_d, const SortSeg* segs_d, const int32_t* blk_seg_d,
@@ -297,6 +300,7 @@ void launch_sort(const TaskDev* tasks_d, const SortSeg* segs_d, const int32_t* b
                  int32_t* vals_b, uint32_t* hist, uint32_t* scan_tmp, cudaStream_t st) {
   if (nblk <= 0) return;
   sort_load_kernel<<<nblk, SORT_THREADS, 0, st>>>(tasks_d, segs_d, blk_seg_d, keys_a, vals_a);
+  count_launch();
   uint64_t* kin = keys_a;
   uint64_t* kout = keys_b;
   int32_t* vin = vals_a;
@@ -304,9 +308,11 @@ void launch_sort(const TaskDev* tasks_d, const SortSeg* segs_d, const int32_t* b
   for (int pass = 0; pass < 8; ++pass) {
     const int shift = 8 * pass;
     sort_hist_kernel<<<nblk, SORT_THREADS, 0, st>>>(segs_d, blk_seg_d, kin, shift, hist);
+    count_launch();
     excl_scan(hist, (int64_t)256 * nblk, scan_tmp, st);
     sort_scatter_kernel<<<nblk, SORT_THREADS, 0, st>>>(segs_d, blk_seg_d, kin, vin, shift,
                                                        hist, kout, vout);
+    count_launch();
     uint64_t* tk = kin; kin = kout; kout = tk;
     int32_t* tv = vin; vin = vout; vout = tv;
   }
@@ -319,6 +325,7 @@ void launch_sorted_jobs(const TaskDev* tasks_d, const SortedJob* jobs_d, int njo
   if (njobs <= 0 || total_blocks <= 0) return;
   sorted_jobs_kernel<<<(unsigned)total_blocks, SORTED_THREADS, 0, st>>>(tasks_d, jobs_d, njobs,
                                                                         keys, perm);
+  count_launch();
 }
 
 }  // namespace egb

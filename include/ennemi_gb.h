@@ -159,8 +159,10 @@ int egb_ball_count(egb_ctx* ctx, const double* points, int64_t n, int32_t d,
 
 /*
  * Per-phase device times of the last batch run with EGB_TIMING, in ms:
- * [0] upload, [1] gather+prepare, [2] sort, [3] kNN, [4] counts,
- * [5] combine+download, [6] whole batch.  Returns the number written.
+ * [0] upload, [1] gather+prepare, [2] sort+materialise, [3] kNN, [4] counts,
+ * [5] combine+download, [6] whole batch; then the multi-D kernels alone:
+ * [7] kNN tile kernels, [8] kNN deferred-query kernels, [9] count tile
+ * kernels, [10] count deferred-query kernels.  Returns the number written.
  */
 int egb_timings(const egb_ctx* ctx, double* ms, int32_t max);
 
@@ -170,8 +172,10 @@ int egb_last_transfer(const egb_ctx* ctx, int64_t* h2d_bytes, int64_t* d2h_bytes
 
 /* Work counters of the last batch: [0] kNN candidate-query pairs screened by
  * tile work items, [1] kNN pairs screened for deferred queries, [2] kNN
- * queries deferred, [3..5] the same for the multi-D counts.  Returns the
- * number written. */
+ * queries deferred, [3..5] the same for the multi-D counts, [6] / [7]
+ * algorithmic operations of the kNN / count tile kernels ((2d+1) per pair:
+ * d differences, d max-of-abs, one compare), [8] kernels launched.  Returns
+ * the number written. */
 int egb_last_stats(const egb_ctx* ctx, int64_t* out, int32_t max);
 
 /*
