@@ -30,6 +30,7 @@ TIMING = 1 << 2
 FORCE_BRUTE = 1 << 3
 KEEP_INTERNALS = 1 << 4
 FORCE_SLAB = 1 << 5
+FORCE_GRID = 1 << 6
 
 PHASES = ("upload", "prepare", "sort", "knn", "counts", "combine", "total",
           "knn_tile", "knn_defer", "count_tile", "count_defer")

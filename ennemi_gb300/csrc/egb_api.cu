@@ -214,6 +214,7 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   const int plain = (flags & EGB_PLAIN_FP64) ? 1 : 0;
   const bool force_brute = (flags & EGB_FORCE_BRUTE) != 0;
   const bool force_slab = (flags & EGB_FORCE_SLAB) != 0 && !force_brute;
+  const bool force_grid = (flags & EGB_FORCE_GRID) != 0 && !force_brute && !force_slab;
   const bool timing = (flags & EGB_TIMING) != 0;
   cudaStream_t st = ctx->stream;
   const long long launches0 = g_launches.load();
@@ -353,16 +354,25 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   };
 
   // kNN: 1-D sorted jobs, multi-D tile jobs, any-K select jobs
-  struct MJob { Space s; bool is_knn; int slab; int sort_seg; int sel; int sort_seg_b; };
+  // mode: 0 brute force, 1 slab, 2 grid (slab and grid jobs also carry the
+  // two sorted copies used by deferred queries)
+  struct MJob { Space s; bool is_knn; int slab; int sort_seg; int sel; int sort_seg_b; int mode; };
+  auto pick_mode = [&](int64_t len) {
+    if (force_brute) return 0;
+    if (force_slab) return 1;
+    if (force_grid) return 2;
+    return len >= SLAB_MIN ? 2 : 0;
+  };
   std::vector<std::pair<int, Space>> sorted_knn, sorted_cnt;  // (seg, space)
   std::vector<MJob> mjobs;
   for (const Space& s : knn) {
     if (s.sp.d == 1) {
       sorted_knn.push_back({seg_for(s.task, s.sp.cols[0], s.b, s.e), s});
     } else {
-      MJob m{s, true, 0, -1, 0, -1};
+      MJob m{s, true, 0, -1, 0, -1, 0};
       if (s.K > EGB_KREG_MAX) m.sel = 1;
-      else if (force_slab || (!force_brute && s.e - s.b >= SLAB_MIN)) m.slab = 1;
+      else m.mode = pick_mode(s.e - s.b);
+      m.slab = m.mode >= 1 ? 1 : 0;
       if (m.slab) {
         m.sort_seg = seg_for(s.task, s.sp.cols[0], s.b, s.e);
         m.sort_seg_b = seg_for(s.task, s.sp.cols[1], s.b, s.e);
@@ -374,8 +384,9 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
     if (s.sp.d == 1) {
       sorted_cnt.push_back({seg_for(s.task, s.sp.cols[0], s.b, s.e), s});
     } else {
-      MJob m{s, false, 0, -1, 0, -1};
-      if (force_slab || (!force_brute && s.e - s.b >= SLAB_MIN)) m.slab = 1;
+      MJob m{s, false, 0, -1, 0, -1, 0};
+      m.mode = pick_mode(s.e - s.b);
+      m.slab = m.mode >= 1 ? 1 : 0;
       if (m.slab) {
         m.sort_seg = seg_for(s.task, s.sp.cols[0], s.b, s.e);
         m.sort_seg_b = seg_for(s.task, s.sp.cols[1], s.b, s.e);
@@ -449,6 +460,10 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
 
   // multi-D job blocks
   std::vector<JobDev> jobs(mjobs.size());
+  std::vector<SortSeg> gsegs;        // strip-key sort, one segment per grid job
+  std::vector<int32_t> grid_jobs;    // job index of each grid job
+  int64_t gsort_total = 0, max_glen = 1;
+  int nblk_grid = 0;
   int64_t max_lds = 32;
   for (size_t j = 0; j < mjobs.size(); ++j) {
     const MJob& m = mjobs[j];
@@ -475,7 +490,35 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
       J.c32b = (float*)(uintptr_t)dl.take(sizeof(float) * (size_t)(d * J.lds));
       J.idxb = (int32_t*)(uintptr_t)dl.take(sizeof(int32_t) * (size_t)J.lds);
     }
+    if (m.mode == 2) {
+      J.c64g = (double*)(uintptr_t)dl.take(sizeof(double) * (size_t)(d * J.lds));
+      J.c32g = (float*)(uintptr_t)dl.take(sizeof(float) * (size_t)(d * J.lds));
+      J.idxg = (int32_t*)(uintptr_t)dl.take(sizeof(int32_t) * (size_t)J.lds);
+      J.posg = (int32_t*)(uintptr_t)dl.take(sizeof(int32_t) * (size_t)J.lds);
+      J.nstrips = (int32_t)std::max<int64_t>(1, std::min<int64_t>(256, len / GRID_MIN_STRIP));
+      J.gseg = (int32_t)gsegs.size();
+      SortSeg g{};
+      g.out_base = gsort_total;
+      g.len = (int32_t)len;
+      g.blk0 = nblk_grid;
+      g.nblk = (int32_t)((len + SORT_TILE - 1) / SORT_TILE);
+      g.task = m.s.task;
+      gsegs.push_back(g);
+      grid_jobs.push_back((int32_t)j);
+      gsort_total += len;
+      nblk_grid += g.nblk;
+      max_glen = std::max(max_glen, len);
+    }
   }
+
+  // strip-key sort of the grid jobs (one extra 8-bit radix pass)
+  const size_t off_gkeys_a = dl.take(sizeof(uint64_t) * (size_t)std::max<int64_t>(gsort_total, 1));
+  const size_t off_gkeys_b = dl.take(sizeof(uint64_t) * (size_t)std::max<int64_t>(gsort_total, 1));
+  const size_t off_gvals_a = dl.take(sizeof(int32_t) * (size_t)std::max<int64_t>(gsort_total, 1));
+  const size_t off_gvals_b = dl.take(sizeof(int32_t) * (size_t)std::max<int64_t>(gsort_total, 1));
+  const size_t off_ginv = dl.take(sizeof(int32_t) * (size_t)std::max<int64_t>(gsort_total, 1));
+  const size_t off_ghist = dl.take(sizeof(uint32_t) * 256 * (size_t)std::max(nblk_grid, 1));
+  const size_t off_gscan = dl.take(sizeof(uint32_t) * sort_scan_tmp_elems(std::max(nblk_grid, 1)));
 
   // sorted jobs
   std::vector<SortedJob> sj_knn, sj_cnt;
@@ -499,14 +542,14 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
 
   // tile launch groups
   struct Group {
-    int is_knn, sel, kclass, dclass, slab, dmax;
+    int is_knn, sel, kclass, dclass, slab, dmax, mode;
     std::vector<WorkItem> items;
     size_t tab_items = 0;
     int64_t defer_cap = 0;   // slab groups: every query may be deferred once
     size_t off_defer = 0;
   };
   std::vector<Group> groups;
-  std::map<std::tuple<int, int, int, int, int>, int> gidx;
+  std::map<std::tuple<int, int, int, int, int, int>, int> gidx;
   std::vector<size_t> order(mjobs.size());
   for (size_t j = 0; j < order.size(); ++j) order[j] = j;
   std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) { return jobs[a].len > jobs[b].len; });
@@ -517,7 +560,7 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
     const int dclass = (d >= 2 && d <= 4) ? d : 0;
     int kclass = 0;
     if (m.is_knn && !m.sel) kclass = m.s.K <= 4 ? 4 : m.s.K <= 8 ? 8 : m.s.K <= 16 ? 16 : 32;
-    const auto key = std::make_tuple(m.is_knn, m.sel, kclass, dclass, m.slab);
+    const auto key = std::make_tuple((int)m.is_knn, m.sel, kclass, dclass, m.slab, m.mode);
     auto it = gidx.find(key);
     int g;
     if (it == gidx.end()) {
@@ -525,6 +568,7 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
       gidx[key] = g;
       Group G;
       G.is_knn = m.is_knn; G.sel = m.sel; G.kclass = kclass; G.dclass = dclass; G.slab = m.slab; G.dmax = d;
+      G.mode = m.mode;
       groups.push_back(G);
     } else {
       g = it->second;
@@ -538,12 +582,23 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
     const int dclass = (d >= 2 && d <= 4) ? d : 0;
     int kclass = 0;
     if (m.is_knn && !m.sel) kclass = m.s.K <= 4 ? 4 : m.s.K <= 8 ? 8 : m.s.K <= 16 ? 16 : 32;
-    Group& G = groups[(size_t)gidx[std::make_tuple(m.is_knn, m.sel, kclass, dclass, m.slab)]];
+    Group& G = groups[(size_t)gidx[std::make_tuple((int)m.is_knn, m.sel, kclass, dclass, m.slab, m.mode)]];
+    if (G.mode == 2) {
+      const int S = jobs[j].nstrips;
+      const int64_t len = jobs[j].len;
+      for (int sidx = 0; sidx < S; ++sidx) {
+        const int32_t a = strip_start(sidx, len, S), b = strip_start(sidx + 1, len, S);
+        for (int32_t q0 = a; q0 < b; q0 += GRID_QB)
+          G.items.push_back({(int32_t)j, q0, std::min(q0 + GRID_QB, b), sidx});
+      }
+      G.defer_cap += len;
+      continue;
+    }
     int qb;
     if (G.sel) qb = SELECT_WARPS;
     else if (G.is_knn) qb = knn_shape(G.kclass, G.dclass, plain, G.slab, G.dmax).queries();
     else qb = count_shape(G.dclass, plain, G.slab, G.dmax).queries();
-    for (int64_t q0 = 0; q0 < jobs[j].len; q0 += qb) G.items.push_back({(int32_t)j, (int32_t)q0});
+    for (int64_t q0 = 0; q0 < jobs[j].len; q0 += qb) G.items.push_back({(int32_t)j, (int32_t)q0, 0, 0});
     if (G.slab) G.defer_cap += jobs[j].len;
   }
   for (Group& G : groups)
@@ -556,7 +611,7 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
     const int dclass = (d >= 2 && d <= 4) ? d : 0;
     int kclass = 0;
     if (m.is_knn && !m.sel) kclass = m.s.K <= 4 ? 4 : m.s.K <= 8 ? 8 : m.s.K <= 16 ? 16 : 32;
-    job_group[j] = gidx[std::make_tuple(m.is_knn, m.sel, kclass, dclass, m.slab)];
+    job_group[j] = gidx[std::make_tuple((int)m.is_knn, m.sel, kclass, dclass, m.slab, m.mode)];
   }
 
   // combine
@@ -587,6 +642,9 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   const size_t tab_sjk = tl.take(sizeof(SortedJob) * std::max<size_t>(sj_knn.size(), 1));
   const size_t tab_sjc = tl.take(sizeof(SortedJob) * std::max<size_t>(sj_cnt.size(), 1));
   const size_t tab_jobs = tl.take(sizeof(JobDev) * std::max<size_t>(jobs.size(), 1));
+  const size_t tab_gsegs = tl.take(sizeof(SortSeg) * std::max<size_t>(gsegs.size(), 1));
+  const size_t tab_blkgseg = tl.take(sizeof(int32_t) * (size_t)std::max(nblk_grid, 1));
+  const size_t tab_gridjobs = tl.take(sizeof(int32_t) * std::max<size_t>(grid_jobs.size(), 1));
   for (Group& G : groups) G.tab_items = tl.take(sizeof(WorkItem) * G.items.size());
   const size_t tab_cjobs = tl.take(sizeof(CombineJob) * std::max<size_t>(cjobs.size(), 1));
   const size_t tab_chunkjob = tl.take(sizeof(int32_t) * (size_t)std::max(nchunks, 1));
@@ -659,6 +717,14 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
     for (size_t s = 0; s < segs.size(); ++s)
       for (int b = 0; b < segs[s].nblk; ++b) bs[segs[s].blk0 + b] = (int32_t)s;
   }
+  if (!gsegs.empty()) std::memcpy(H + tab_gsegs, gsegs.data(), sizeof(SortSeg) * gsegs.size());
+  {
+    int32_t* bs = (int32_t*)(H + tab_blkgseg);
+    for (size_t g = 0; g < gsegs.size(); ++g)
+      for (int b = 0; b < gsegs[g].nblk; ++b) bs[gsegs[g].blk0 + b] = (int32_t)g;
+  }
+  if (!grid_jobs.empty())
+    std::memcpy(H + tab_gridjobs, grid_jobs.data(), sizeof(int32_t) * grid_jobs.size());
   if (!sj_knn.empty()) std::memcpy(H + tab_sjk, sj_knn.data(), sizeof(SortedJob) * sj_knn.size());
   if (!sj_cnt.empty()) std::memcpy(H + tab_sjc, sj_cnt.data(), sizeof(SortedJob) * sj_cnt.size());
   for (size_t j = 0; j < jobs.size(); ++j) {
@@ -672,6 +738,12 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
       J.c64b = (double*)(A + (uintptr_t)J.c64b);
       J.c32b = (float*)(A + (uintptr_t)J.c32b);
       J.idxb = (int32_t*)(A + (uintptr_t)J.idxb);
+    }
+    if (J.c64g) {
+      J.c64g = (double*)(A + (uintptr_t)J.c64g);
+      J.c32g = (float*)(A + (uintptr_t)J.c32g);
+      J.idxg = (int32_t*)(A + (uintptr_t)J.idxg);
+      J.posg = (int32_t*)(A + (uintptr_t)J.posg);
     }
     J.jflags = (uint32_t*)(A + off_zr + zr_jflags) + j;
     J.stats = (unsigned long long*)(A + off_zr + zr_stats) + 4 * job_group[j];
@@ -726,6 +798,20 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
               (uint32_t*)(A + off_hist), (uint32_t*)(A + off_scan), st);
   launch_materialize(tasks_d, (const JobDev*)dtab(tab_jobs), (int)jobs.size(), vals,
                      (const SortSeg*)dtab(tab_segs), max_lds, st);
+  if (!grid_jobs.empty()) {
+    launch_grid_keys((const JobDev*)dtab(tab_jobs), (const int32_t*)dtab(tab_gridjobs),
+                     (int)grid_jobs.size(), (const SortSeg*)dtab(tab_gsegs), vals,
+                     (const SortSeg*)dtab(tab_segs), (int32_t*)(A + off_ginv),
+                     (uint64_t*)(A + off_gkeys_a), (int32_t*)(A + off_gvals_a), max_glen, st);
+    launch_radix_pass((const SortSeg*)dtab(tab_gsegs), (const int32_t*)dtab(tab_blkgseg), nblk_grid,
+                      (const uint64_t*)(A + off_gkeys_a), (const int32_t*)(A + off_gvals_a),
+                      (uint64_t*)(A + off_gkeys_b), (int32_t*)(A + off_gvals_b), 0,
+                      (uint32_t*)(A + off_ghist), (uint32_t*)(A + off_gscan), st);
+    launch_materialize_grid(tasks_d, (const JobDev*)dtab(tab_jobs), (const int32_t*)dtab(tab_gridjobs),
+                            (int)grid_jobs.size(), vals, (const SortSeg*)dtab(tab_segs),
+                            (const int32_t*)(A + off_gvals_b), (const SortSeg*)dtab(tab_gsegs),
+                            max_lds, st);
+  }
   if (timing) EGB_CUDA(cudaEventRecord(ctx->ev[3], st));
 
   launch_sorted_jobs(tasks_d, (const SortedJob*)dtab(tab_sjk), (int)sj_knn.size(), blk_knn, keys, vals, st);
@@ -736,6 +822,10 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
     if (G.sel)
       launch_knn_select((const JobDev*)dtab(tab_jobs), (const WorkItem*)dtab(G.tab_items),
                         (int)G.items.size(), err_d, ctx->num_sms, st);
+    else if (G.mode == 2)
+      launch_knn_grid((const JobDev*)dtab(tab_jobs), (const WorkItem*)dtab(G.tab_items),
+                      (int)G.items.size(), G.kclass, G.dclass, plain, G.dmax, counters + 2 * g,
+                      err_d, (DeferEntry*)(A + G.off_defer), counters + 2 * g + 1, ctx->num_sms, st);
     else
       launch_knn_tile((const JobDev*)dtab(tab_jobs), (const WorkItem*)dtab(G.tab_items),
                       (int)G.items.size(), G.kclass, G.dclass, plain, G.slab, G.dmax,
@@ -760,6 +850,12 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   for (size_t g = 0; g < groups.size(); ++g) {
     Group& G = groups[g];
     if (G.is_knn || G.items.empty()) continue;
+    if (G.mode == 2) {
+      launch_count_grid((const JobDev*)dtab(tab_jobs), (const WorkItem*)dtab(G.tab_items),
+                        (int)G.items.size(), G.dclass, plain, G.dmax, counters + 2 * g, err_d,
+                        (DeferEntry*)(A + G.off_defer), counters + 2 * g + 1, ctx->num_sms, st);
+      continue;
+    }
     launch_count_tile((const JobDev*)dtab(tab_jobs), (const WorkItem*)dtab(G.tab_items),
                       (int)G.items.size(), G.dclass, plain, G.slab, G.dmax, counters + 2 * g,
                       err_d, (DeferEntry*)(A + G.off_defer), counters + 2 * g + 1, ctx->num_sms,

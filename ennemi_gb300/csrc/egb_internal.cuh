@@ -157,15 +157,35 @@ struct JobDev {
   double* c64b;
   float* c32b;
   int32_t* idxb;
+  // grid jobs: a third copy in strip order -- the points split into nstrips
+  // equal-count strips by their rank in column 1, each strip sorted by
+  // column 0 -- with, per position, its position in the column-0 order
+  double* c64g;
+  float* c32g;
+  int32_t* idxg;
+  int32_t* posg;
+  int32_t nstrips;
+  int32_t gseg;           // grid: its segment in the strip-key sort
   // work counters of this job's launch group: [0] pairs screened by tile
   // items, [1] pairs screened by deferred-query warps, [2] queries deferred
   unsigned long long* stats;
   SpaceCols sp;
 };
 
+// Strip s of a grid job of length len holds the column-1 ranks
+// [strip_start(s), strip_start(s + 1)).
+__host__ __device__ __forceinline__ int32_t strip_start(int64_t s, int64_t len, int32_t nstrips) {
+  return (int32_t)((s * len + nstrips - 1) / nstrips);
+}
+constexpr int GRID_QB = 128;     // queries per grid work item
+constexpr int GRID_TILE = 128;   // candidates per grid tile
+constexpr int GRID_MIN_STRIP = 64;
+
 struct WorkItem {         // one tile of queries of one job
   int32_t job;
   int32_t q0;
+  int32_t q1;             // grid items: end of the query range (exclusive)
+  int32_t strip;          // grid items: the strip holding the queries
 };
 
 // A slab query whose search a tile work item left unfinished (it needed a
@@ -234,6 +254,10 @@ void launch_prepare(const TaskDev* tasks_d, const int32_t* col_task_d, const int
 void launch_materialize(const TaskDev* tasks_d, const JobDev* jobs_d, int njobs,
                         const int32_t* sorted_vals, const SortSeg* segs_d, int64_t max_lds,
                         cudaStream_t st);
+void launch_materialize_grid(const TaskDev* tasks_d, const JobDev* jobs_d,
+                             const int32_t* grid_jobs_d, int ngrid, const int32_t* sorted_vals,
+                             const SortSeg* segs_d, const int32_t* gvals_sorted,
+                             const SortSeg* gsegs_d, int64_t max_lds, cudaStream_t st);
 void launch_radius(const TaskDev* tasks_d, int ntasks, int64_t max_ld, cudaStream_t st);
 void launch_combine(const TaskDev* tasks_d, const CombineJob* jobs_d, const int32_t* chunk_job_d,
                     int nchunks, const double* psi_tab, int64_t psi_len, double* partial,
@@ -241,6 +265,16 @@ void launch_combine(const TaskDev* tasks_d, const CombineJob* jobs_d, const int3
 
 // egb_sort.cu
 constexpr int SORT_TILE = 2048;
+// Strip keys of the grid jobs: keys[p] = strip of the point at column-0
+// position p (its column-1 rank * nstrips / len), vals[p] = p; then one
+// stable 8-bit radix pass orders each segment by (strip, column 0).
+void launch_grid_keys(const JobDev* jobs_d, const int32_t* grid_jobs_d, int ngrid,
+                      const SortSeg* gsegs_d, const int32_t* sorted_vals, const SortSeg* segs_d,
+                      int32_t* inv_scratch, uint64_t* gkeys, int32_t* gvals, int64_t max_len,
+                      cudaStream_t st);
+void launch_radix_pass(const SortSeg* segs_d, const int32_t* blk_seg_d, int nblk,
+                       const uint64_t* kin, const int32_t* vin, uint64_t* kout, int32_t* vout,
+                       int shift, uint32_t* hist, uint32_t* scan_tmp, cudaStream_t st);
 size_t sort_scan_tmp_elems(int nblk);
 void launch_sort(const TaskDev* tasks_d, const SortSeg* segs_d, const int32_t* blk_seg_d,
                  int nblk, uint64_t* keys_a, uint64_t* keys_b, int32_t* vals_a,
@@ -272,6 +306,16 @@ void launch_count_tile(const JobDev* jobs_d, const WorkItem* items_d, int nitems
                        DeferEntry* defer, int* defer_count, int num_sms, cudaStream_t st);
 void launch_count_defer(const JobDev* jobs_d, const DeferEntry* defer, const int* defer_count,
                         int defer_cap, int dclass, int plain, int num_sms, cudaStream_t st);
+
+// egb_grid.cu: grid (strip) tile kernels; deferred queries go to the same
+// warp-per-query kernels as the slab form.
+TileShape grid_shape(int dclass, int plain, int dmax);
+void launch_knn_grid(const JobDev* jobs_d, const WorkItem* items_d, int nitems, int kclass,
+                     int dclass, int plain, int dmax, int* counter, uint32_t* err,
+                     DeferEntry* defer, int* defer_count, int num_sms, cudaStream_t st);
+void launch_count_grid(const JobDev* jobs_d, const WorkItem* items_d, int nitems, int dclass,
+                       int plain, int dmax, int* counter, uint32_t* err, DeferEntry* defer,
+                       int* defer_count, int num_sms, cudaStream_t st);
 
 // egb_select.cu: any K (one warp per query, radix select on FP64 bits)
 constexpr int SELECT_WARPS = 8;

@@ -36,6 +36,37 @@ void launch_count_f64s(int, const JobDev*, const WorkItem*, int, int*, uint32_t*
 void count_defer_f32s(int, const JobDev*, const DeferEntry*, const int*, int, int, cudaStream_t);
 void count_defer_f64s(int, const JobDev*, const DeferEntry*, const int*, int, int, cudaStream_t);
 
+TileShape grid_shape_f32(int, int);
+TileShape grid_shape_f64(int, int);
+void launch_knn_grid_f32(int, int, const JobDev*, const WorkItem*, int, int*, uint32_t*, int,
+                         DeferEntry*, int*, int, cudaStream_t);
+void launch_knn_grid_f64(int, int, const JobDev*, const WorkItem*, int, int*, uint32_t*, int,
+                         DeferEntry*, int*, int, cudaStream_t);
+void launch_count_grid_f32(int, const JobDev*, const WorkItem*, int, int*, uint32_t*, int,
+                           DeferEntry*, int*, int, cudaStream_t);
+void launch_count_grid_f64(int, const JobDev*, const WorkItem*, int, int*, uint32_t*, int,
+                           DeferEntry*, int*, int, cudaStream_t);
+
+TileShape grid_shape(int dclass, int plain, int dmax) {
+  return plain ? grid_shape_f64(dclass, dmax) : grid_shape_f32(dclass, dmax);
+}
+
+void launch_knn_grid(const JobDev* jobs_d, const WorkItem* items_d, int nitems, int kclass,
+                     int dclass, int plain, int dmax, int* counter, uint32_t* err,
+                     DeferEntry* defer, int* defer_count, int num_sms, cudaStream_t st) {
+  if (nitems <= 0) return;
+  if (plain) launch_knn_grid_f64(kclass, dclass, jobs_d, items_d, nitems, counter, err, dmax, defer, defer_count, num_sms, st);
+  else launch_knn_grid_f32(kclass, dclass, jobs_d, items_d, nitems, counter, err, dmax, defer, defer_count, num_sms, st);
+}
+
+void launch_count_grid(const JobDev* jobs_d, const WorkItem* items_d, int nitems, int dclass,
+                       int plain, int dmax, int* counter, uint32_t* err, DeferEntry* defer,
+                       int* defer_count, int num_sms, cudaStream_t st) {
+  if (nitems <= 0) return;
+  if (plain) launch_count_grid_f64(dclass, jobs_d, items_d, nitems, counter, err, dmax, defer, defer_count, num_sms, st);
+  else launch_count_grid_f32(dclass, jobs_d, items_d, nitems, counter, err, dmax, defer, defer_count, num_sms, st);
+}
+
 TileShape knn_shape(int kclass, int dclass, int plain, int slab, int dmax) {
   if (plain) return slab ? knn_shape_v<true, true>(kclass, dclass, dmax)
                          : knn_shape_v<true, false>(kclass, dclass, dmax);

@@ -70,7 +70,7 @@ __global__ void noalloc_setup_kernel(unsigned char* scratch, Layout L, const dou
     unsigned char* cnt = scratch + L.counters;
     for (int i = threadIdx.x; i < 64; i += blockDim.x) cnt[i] = 0;
     egb::WorkItem* items = reinterpret_cast<egb::WorkItem*>(scratch + L.items);
-    for (int i = threadIdx.x; i < nitems; i += blockDim.x) items[i] = egb::WorkItem{0, i * qb};
+    for (int i = threadIdx.x; i < nitems; i += blockDim.x) items[i] = egb::WorkItem{0, i * qb, 0, 0};
     if (threadIdx.x == 0) {
       egb::JobDev J;
       memset(&J, 0, sizeof(J));

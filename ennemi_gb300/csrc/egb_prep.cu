@@ -139,6 +139,47 @@ __global__ void materialize_kernel(const TaskDev* __restrict__ tasks,
   }
 }
 
+// Grid copy: position p_G of the strip order takes the point at column-0
+// position p_A = gvals_sorted[p_G].
+__global__ void materialize_grid_kernel(const TaskDev* __restrict__ tasks,
+                                        const JobDev* __restrict__ jobs,
+                                        const int32_t* __restrict__ grid_jobs, int ngrid,
+                                        const int32_t* __restrict__ sorted_vals,
+                                        const SortSeg* __restrict__ segs,
+                                        const int32_t* __restrict__ gvals_sorted,
+                                        const SortSeg* __restrict__ gsegs) {
+  for (int g = blockIdx.y; g < ngrid; g += gridDim.y) {
+    const JobDev J = jobs[grid_jobs[g]];
+    const TaskDev t = tasks[J.task];
+    const int d = J.sp.d;
+    const int32_t* va = sorted_vals + segs[J.sort_seg].out_base;
+    const int32_t* gv = gvals_sorted + gsegs[J.gseg].out_base;
+    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < J.lds;
+         p += (int64_t)gridDim.x * blockDim.x) {
+      if (p < J.len) {
+        const int32_t pa = gv[p];
+        const int32_t w = va[pa];
+        J.posg[p] = pa;
+        J.idxg[p] = w;
+        for (int c = 0; c < d; ++c) {
+          const int tc = J.sp.cols[c];
+          const double v = t.x64[(int64_t)tc * t.ld + w];
+          J.c64g[(int64_t)c * J.lds + p] = v;
+          J.c32g[(int64_t)c * J.lds + p] =
+              __double2float_rn(fmin(fmax(v - t.center[tc], -1e37), 1e37));
+        }
+      } else {
+        J.posg[p] = 0;
+        J.idxg[p] = J.seg_begin;
+        for (int c = 0; c < d; ++c) {
+          J.c64g[(int64_t)c * J.lds + p] = 0.0;
+          J.c32g[(int64_t)c * J.lds + p] = 0.0f;
+        }
+      }
+    }
+  }
+}
+
 __global__ void radius_kernel(const TaskDev* __restrict__ tasks, int ntasks) {
   for (int ti = blockIdx.y; ti < ntasks; ti += gridDim.y) {
     const TaskDev t = tasks[ti];
@@ -256,6 +297,17 @@ void launch_materialize(const TaskDev* tasks_d, const JobDev* jobs_d, int njobs,
   if (njobs <= 0) return;
   dim3 grid(grid_x_for(max_lds), grid_y_for(njobs));
   materialize_kernel<<<grid, PREP_THREADS, 0, st>>>(tasks_d, jobs_d, njobs, sorted_vals, segs_d);
+  count_launch();
+}
+
+void launch_materialize_grid(const TaskDev* tasks_d, const JobDev* jobs_d,
+                             const int32_t* grid_jobs_d, int ngrid, const int32_t* sorted_vals,
+                             const SortSeg* segs_d, const int32_t* gvals_sorted,
+                             const SortSeg* gsegs_d, int64_t max_lds, cudaStream_t st) {
+  if (ngrid <= 0) return;
+  dim3 grid(grid_x_for(max_lds), grid_y_for(ngrid));
+  materialize_grid_kernel<<<grid, PREP_THREADS, 0, st>>>(tasks_d, jobs_d, grid_jobs_d, ngrid,
+                                                         sorted_vals, segs_d, gvals_sorted, gsegs_d);
   count_launch();
 }
 

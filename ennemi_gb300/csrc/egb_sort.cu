@@ -278,7 +278,63 @@ __global__ void sorted_jobs_kernel(const TaskDev* __restrict__ tasks,
   t.cnt[jb.slot][i] = count;
 }
 
+// ----------------------------------------------------------- grid keys ----
+// inv[out + (w_B - seg_begin)] = p_B for the column-1 order of each grid job.
+__global__ void grid_inv_kernel(const JobDev* __restrict__ jobs,
+                                const int32_t* __restrict__ grid_jobs, int ngrid,
+                                const SortSeg* __restrict__ gsegs,
+                                const int32_t* __restrict__ sorted_vals,
+                                const SortSeg* __restrict__ segs, int32_t* __restrict__ inv) {
+  for (int g = blockIdx.y; g < ngrid; g += gridDim.y) {
+    const JobDev& J = jobs[grid_jobs[g]];
+    const int64_t out = gsegs[J.gseg].out_base;
+    const int32_t* vb = sorted_vals + segs[J.sort_seg_b].out_base;
+    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < J.len;
+         p += (int64_t)gridDim.x * blockDim.x)
+      inv[out + (vb[p] - J.seg_begin)] = (int32_t)p;
+  }
+}
+
+// keys[out + p_A] = strip of the point at column-0 position p_A; vals = p_A.
+__global__ void grid_key_kernel(const JobDev* __restrict__ jobs,
+                                const int32_t* __restrict__ grid_jobs, int ngrid,
+                                const SortSeg* __restrict__ gsegs,
+                                const int32_t* __restrict__ sorted_vals,
+                                const SortSeg* __restrict__ segs,
+                                const int32_t* __restrict__ inv, uint64_t* __restrict__ keys,
+                                int32_t* __restrict__ vals) {
+  for (int g = blockIdx.y; g < ngrid; g += gridDim.y) {
+    const JobDev& J = jobs[grid_jobs[g]];
+    const int64_t out = gsegs[J.gseg].out_base;
+    const int32_t* va = sorted_vals + segs[J.sort_seg].out_base;
+    const int64_t len = J.len;
+    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < len;
+         p += (int64_t)gridDim.x * blockDim.x) {
+      const int64_t rank_b = inv[out + (va[p] - J.seg_begin)];
+      keys[out + p] = (uint64_t)(rank_b * J.nstrips / len);
+      vals[out + p] = (int32_t)p;
+    }
+  }
+}
+
 }  // namespace
+
+void launch_grid_keys(const JobDev* jobs_d, const int32_t* grid_jobs_d, int ngrid,
+                      const SortSeg* gsegs_d, const int32_t* sorted_vals, const SortSeg* segs_d,
+                      int32_t* inv_scratch, uint64_t* gkeys, int32_t* gvals, int64_t max_len,
+                      cudaStream_t st) {
+  if (ngrid <= 0) return;
+  int gx = (int)((max_len + 255) / 256);
+  if (gx > 1024) gx = 1024;
+  if (gx < 1) gx = 1;
+  dim3 grid(gx, ngrid > 65535 ? 65535 : ngrid);
+  grid_inv_kernel<<<grid, 256, 0, st>>>(jobs_d, grid_jobs_d, ngrid, gsegs_d, sorted_vals, segs_d,
+                                        inv_scratch);
+  count_launch();
+  grid_key_kernel<<<grid, 256, 0, st>>>(jobs_d, grid_jobs_d, ngrid, gsegs_d, sorted_vals, segs_d,
+                                        inv_scratch, gkeys, gvals);
+  count_launch();
+}
 
 size_t sort_scan_tmp_elems(int nblk) {
   const int64_t n = (int64_t)256 * nblk;
@@ -317,6 +373,18 @@ void launch_sort(const TaskDev* tasks_d, const SortSeg* segs_d, const int32_t* b
     int32_t* tv = vin; vin = vout; vout = tv;
   }
   // eight passes: the sorted keys and values are back in keys_a / vals_a
+}
+
+void launch_radix_pass(const SortSeg* segs_d, const int32_t* blk_seg_d, int nblk,
+                       const uint64_t* kin, const int32_t* vin, uint64_t* kout, int32_t* vout,
+                       int shift, uint32_t* hist, uint32_t* scan_tmp, cudaStream_t st) {
+  if (nblk <= 0) return;
+  sort_hist_kernel<<<nblk, SORT_THREADS, 0, st>>>(segs_d, blk_seg_d, kin, shift, hist);
+  count_launch();
+  excl_scan(hist, (int64_t)256 * nblk, scan_tmp, st);
+  sort_scatter_kernel<<<nblk, SORT_THREADS, 0, st>>>(segs_d, blk_seg_d, kin, vin, shift, hist,
+                                                     kout, vout);
+  count_launch();
 }
 
 void launch_sorted_jobs(const TaskDev* tasks_d, const SortedJob* jobs_d, int njobs,

@@ -68,11 +68,14 @@ enum egb_flags {
                                 comparator); default is FP32 distance tiles with
                                 an FP64 recheck of every borderline candidate   */
   EGB_TIMING = 1 << 2,       /* record per-phase CUDA-event timings             */
-  EGB_FORCE_BRUTE = 1 << 3,  /* never use the sorted-slab variant for multi-D
-                                spaces (plain brute force over the segment)     */
+  EGB_FORCE_BRUTE = 1 << 3,  /* never use the sorted (slab / grid) variants for
+                                multi-D spaces: brute force over the segment    */
   EGB_KEEP_INTERNALS = 1 << 4, /* keep eps / counts for egb_fetch()             */
-  EGB_FORCE_SLAB = 1 << 5      /* use the sorted-slab variant for every multi-D
+  EGB_FORCE_SLAB = 1 << 5,     /* use the sorted-slab variant for every multi-D
                                   space, whatever its size (tests)               */
+  EGB_FORCE_GRID = 1 << 6      /* use the strip (grid) variant for every multi-D
+                                  space, whatever its size (tests); the default
+                                  picks it for spaces of >= 4096 points          */
 };
 
 /* One float64 column: sample i at data[i * stride] (stride in elements). */

@@ -20,8 +20,10 @@ VARIANTS = {
     "fp32": 0,
     "fp32-brute": N.FORCE_BRUTE,
     "fp32-slab": N.FORCE_SLAB,
+    "fp32-grid": N.FORCE_GRID,
     "fp64-brute": N.PLAIN_FP64 | N.FORCE_BRUTE,
     "fp64-slab": N.PLAIN_FP64 | N.FORCE_SLAB,
+    "fp64-grid": N.PLAIN_FP64 | N.FORCE_GRID,
 }
 SLOTS = {"mi": ["nx", "ny"], "cmi": ["nxz", "nyz", "nz"], "semi": ["n"],
          "csemi": ["nxz", "nyz", "nz"], "ent": []}
@@ -70,7 +72,7 @@ def test_golden_estimators(case, variant):
     assert same_value(vals[0], float(case["value"])), (vals[0], float(case["value"]))
 
 
-@pytest.mark.parametrize("variant", ["fp32", "fp64-slab"])
+@pytest.mark.parametrize("variant", ["fp32", "fp64-slab", "fp32-grid"])
 def test_golden_all_in_one_batch(variant):
     tasks = [make_task(str(c["kind"]), int(c["k"]), inputs_of(c)) for c in CASES]
     vals = N.run_tasks(tasks, flags=VARIANTS[variant] | N.KEEP_INTERNALS)
@@ -121,7 +123,7 @@ def _medium_cases():
 MEDIUM = list(_medium_cases())
 
 
-@pytest.mark.parametrize("variant", ["fp32", "fp32-brute", "fp64-slab"])
+@pytest.mark.parametrize("variant", ["fp32", "fp32-brute", "fp32-slab", "fp64-grid"])
 @pytest.mark.parametrize("case", MEDIUM, ids=[c[0] for c in MEDIUM])
 def test_medium_against_oracle(oracle, case, variant):
     name, kind, k, inp = case
