@@ -31,6 +31,7 @@ FORCE_BRUTE = 1 << 3
 KEEP_INTERNALS = 1 << 4
 FORCE_SLAB = 1 << 5
 FORCE_GRID = 1 << 6
+FORCE_CTA_GRID = 1 << 7
 
 PHASES = ("upload", "prepare", "sort", "knn", "counts", "combine", "total",
           "knn_tile", "knn_defer", "count_tile", "count_defer")

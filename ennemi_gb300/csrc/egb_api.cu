@@ -215,6 +215,7 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   const bool force_brute = (flags & EGB_FORCE_BRUTE) != 0;
   const bool force_slab = (flags & EGB_FORCE_SLAB) != 0 && !force_brute;
   const bool force_grid = (flags & EGB_FORCE_GRID) != 0 && !force_brute && !force_slab;
+  const bool cta_grid = (flags & EGB_FORCE_CTA_GRID) != 0;  // grid without the warp form
   const bool timing = (flags & EGB_TIMING) != 0;
   cudaStream_t st = ctx->stream;
   const long long launches0 = g_launches.load();
@@ -354,8 +355,9 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   };
 
   // kNN: 1-D sorted jobs, multi-D tile jobs, any-K select jobs
-  // mode: 0 brute force, 1 slab, 2 grid (slab and grid jobs also carry the
-  // two sorted copies used by deferred queries)
+  // mode: 0 brute force, 1 slab, 2 grid (CTA items of 128 queries), 3 warp
+  // grid (warp items of 32 queries); modes 1-3 carry the two sorted copies
+  // (deferred queries, strip bounds), modes 2-3 the strip-ordered copy
   struct MJob { Space s; bool is_knn; int slab; int sort_seg; int sel; int sort_seg_b; int mode; };
   auto pick_mode = [&](int64_t len) {
     if (force_brute) return 0;
@@ -372,6 +374,7 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
       MJob m{s, true, 0, -1, 0, -1, 0};
       if (s.K > EGB_KREG_MAX) m.sel = 1;
       else m.mode = pick_mode(s.e - s.b);
+      if (m.mode == 2 && s.K <= 8 && !cta_grid) m.mode = 3;
       m.slab = m.mode >= 1 ? 1 : 0;
       if (m.slab) {
         m.sort_seg = seg_for(s.task, s.sp.cols[0], s.b, s.e);
@@ -386,6 +389,7 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
     } else {
       MJob m{s, false, 0, -1, 0, -1, 0};
       m.mode = pick_mode(s.e - s.b);
+      if (m.mode == 2 && !cta_grid) m.mode = 3;
       m.slab = m.mode >= 1 ? 1 : 0;
       if (m.slab) {
         m.sort_seg = seg_for(s.task, s.sp.cols[0], s.b, s.e);
@@ -490,12 +494,14 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
       J.c32b = (float*)(uintptr_t)dl.take(sizeof(float) * (size_t)(d * J.lds));
       J.idxb = (int32_t*)(uintptr_t)dl.take(sizeof(int32_t) * (size_t)J.lds);
     }
-    if (m.mode == 2) {
+    if (m.mode >= 2) {
       J.c64g = (double*)(uintptr_t)dl.take(sizeof(double) * (size_t)(d * J.lds));
       J.c32g = (float*)(uintptr_t)dl.take(sizeof(float) * (size_t)(d * J.lds));
       J.idxg = (int32_t*)(uintptr_t)dl.take(sizeof(int32_t) * (size_t)J.lds);
       J.posg = (int32_t*)(uintptr_t)dl.take(sizeof(int32_t) * (size_t)J.lds);
       J.nstrips = (int32_t)std::max<int64_t>(1, std::min<int64_t>(256, len / GRID_MIN_STRIP));
+      J.sylo = (double*)(uintptr_t)dl.take(sizeof(double) * (size_t)J.nstrips);
+      J.syhi = (double*)(uintptr_t)dl.take(sizeof(double) * (size_t)J.nstrips);
       J.gseg = (int32_t)gsegs.size();
       SortSeg g{};
       g.out_base = gsort_total;
@@ -583,15 +589,16 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
     int kclass = 0;
     if (m.is_knn && !m.sel) kclass = m.s.K <= 4 ? 4 : m.s.K <= 8 ? 8 : m.s.K <= 16 ? 16 : 32;
     Group& G = groups[(size_t)gidx[std::make_tuple((int)m.is_knn, m.sel, kclass, dclass, m.slab, m.mode)]];
-    if (G.mode == 2) {
+    if (G.mode >= 2) {
       const int S = jobs[j].nstrips;
       const int64_t len = jobs[j].len;
+      const int qb = G.mode == 3 ? WG_QB : GRID_QB;
       for (int sidx = 0; sidx < S; ++sidx) {
         const int32_t a = strip_start(sidx, len, S), b = strip_start(sidx + 1, len, S);
-        for (int32_t q0 = a; q0 < b; q0 += GRID_QB)
-          G.items.push_back({(int32_t)j, q0, std::min(q0 + GRID_QB, b), sidx});
+        for (int32_t q0 = a; q0 < b; q0 += qb)
+          G.items.push_back({(int32_t)j, q0, std::min(q0 + qb, b), sidx});
       }
-      G.defer_cap += len;
+      if (G.mode == 2) G.defer_cap += len;
       continue;
     }
     int qb;
@@ -645,6 +652,8 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   const size_t tab_gsegs = tl.take(sizeof(SortSeg) * std::max<size_t>(gsegs.size(), 1));
   const size_t tab_blkgseg = tl.take(sizeof(int32_t) * (size_t)std::max(nblk_grid, 1));
   const size_t tab_gridjobs = tl.take(sizeof(int32_t) * std::max<size_t>(grid_jobs.size(), 1));
+  std::vector<size_t> tab_sstart(jobs.size(), 0);
+  for (int32_t gj : grid_jobs) tab_sstart[(size_t)gj] = tl.take(sizeof(int32_t) * (size_t)(jobs[(size_t)gj].nstrips + 1));
   for (Group& G : groups) G.tab_items = tl.take(sizeof(WorkItem) * G.items.size());
   const size_t tab_cjobs = tl.take(sizeof(CombineJob) * std::max<size_t>(cjobs.size(), 1));
   const size_t tab_chunkjob = tl.take(sizeof(int32_t) * (size_t)std::max(nchunks, 1));
@@ -744,6 +753,11 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
       J.c32g = (float*)(A + (uintptr_t)J.c32g);
       J.idxg = (int32_t*)(A + (uintptr_t)J.idxg);
       J.posg = (int32_t*)(A + (uintptr_t)J.posg);
+      J.sylo = (double*)(A + (uintptr_t)J.sylo);
+      J.syhi = (double*)(A + (uintptr_t)J.syhi);
+      int32_t* st0 = (int32_t*)(H + tab_sstart[j]);
+      for (int s = 0; s <= J.nstrips; ++s) st0[s] = strip_start(s, J.len, J.nstrips);
+      J.sstart = (const int32_t*)(A + off_tab + tab_sstart[j]);
     }
     J.jflags = (uint32_t*)(A + off_zr + zr_jflags) + j;
     J.stats = (unsigned long long*)(A + off_zr + zr_stats) + 4 * job_group[j];
@@ -822,6 +836,10 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
     if (G.sel)
       launch_knn_select((const JobDev*)dtab(tab_jobs), (const WorkItem*)dtab(G.tab_items),
                         (int)G.items.size(), err_d, ctx->num_sms, st);
+    else if (G.mode == 3)
+      launch_knn_wgrid((const JobDev*)dtab(tab_jobs), (const WorkItem*)dtab(G.tab_items),
+                       (int)G.items.size(), G.kclass, G.dclass, plain, G.dmax, counters + 2 * g,
+                       ctx->num_sms, st);
     else if (G.mode == 2)
       launch_knn_grid((const JobDev*)dtab(tab_jobs), (const WorkItem*)dtab(G.tab_items),
                       (int)G.items.size(), G.kclass, G.dclass, plain, G.dmax, counters + 2 * g,
@@ -836,7 +854,7 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   if (timing) EGB_CUDA(cudaEventRecord(ctx->kev[2], st));
   for (size_t g = 0; g < groups.size(); ++g) {
     Group& G = groups[g];
-    if (!G.is_knn || G.sel || !G.slab || G.items.empty()) continue;
+    if (!G.is_knn || G.sel || !G.slab || G.mode == 3 || G.items.empty()) continue;
     launch_knn_defer((const JobDev*)dtab(tab_jobs), (const DeferEntry*)(A + G.off_defer),
                      counters + 2 * g + 1, (int)G.defer_cap, G.kclass, G.dclass, plain,
                      ctx->num_sms, st);
@@ -850,6 +868,12 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   for (size_t g = 0; g < groups.size(); ++g) {
     Group& G = groups[g];
     if (G.is_knn || G.items.empty()) continue;
+    if (G.mode == 3) {
+      launch_count_wgrid((const JobDev*)dtab(tab_jobs), (const WorkItem*)dtab(G.tab_items),
+                         (int)G.items.size(), G.dclass, plain, G.dmax, counters + 2 * g,
+                         ctx->num_sms, st);
+      continue;
+    }
     if (G.mode == 2) {
       launch_count_grid((const JobDev*)dtab(tab_jobs), (const WorkItem*)dtab(G.tab_items),
                         (int)G.items.size(), G.dclass, plain, G.dmax, counters + 2 * g, err_d,
@@ -865,7 +889,7 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   if (timing) EGB_CUDA(cudaEventRecord(ctx->kev[6], st));
   for (size_t g = 0; g < groups.size(); ++g) {
     Group& G = groups[g];
-    if (G.is_knn || !G.slab || G.items.empty()) continue;
+    if (G.is_knn || !G.slab || G.mode == 3 || G.items.empty()) continue;
     launch_count_defer((const JobDev*)dtab(tab_jobs), (const DeferEntry*)(A + G.off_defer),
                        counters + 2 * g + 1, (int)G.defer_cap, G.dclass, plain, ctx->num_sms, st);
   }

@@ -171,7 +171,9 @@ grid_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items,
     const int64_t lds = sj.lds;
     const double* __restrict__ c64 = sj.c64g;
     const T* gsrc = PLAIN ? reinterpret_cast<const T*>(sj.c64g) : reinterpret_cast<const T*>(sj.c32g);
-    const double* __restrict__ ycol = sj.c64b + lds;  // column 1, sorted
+    const int32_t* __restrict__ sst = sj.sstart;      // strip starts
+    const double* __restrict__ ylo_t = sj.sylo;       // strip column-1 bounds
+    const double* __restrict__ yhi_t = sj.syhi;
     const int S = sj.nstrips;
     const bool unsafe = !PLAIN && ((*sj.jflags & TF_UNSAFE32) != 0u);
 
@@ -254,8 +256,8 @@ grid_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items,
     sc.sq = wi.strip;
     sc.S = S;
     sc.len = len;
-    sc.s0 = strip_start(sc.sq, len, S);
-    sc.s1 = strip_start(sc.sq + 1, len, S);
+    sc.s0 = sst[sc.sq];
+    sc.s1 = sst[sc.sq + 1];
     sc.up = sc.sq + 1;
     sc.dn = sc.sq - 1;
     sc.up_open = sc.up < S;
@@ -276,8 +278,8 @@ grid_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items,
       if (!qok) return true;
       if (sc.stage < 3) return false;
       const double t = tq();
-      const bool u = !sc.up_open || sc.up >= S || (ycol[strip_start(sc.up, len, S)] - qy > t);
-      const bool l = !sc.dn_open || sc.dn < 0 || (qy - ycol[strip_start(sc.dn + 1, len, S) - 1] > t);
+      const bool u = !sc.up_open || sc.up >= S || (ylo_t[sc.up] - qy > t);
+      const bool l = !sc.dn_open || sc.dn < 0 || (qy - yhi_t[sc.dn] > t);
       return u && l;
     };
 
@@ -325,9 +327,9 @@ grid_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items,
         bool openu = false, opend = false;
         if (qok) {
           const double t = tq();
-          if (sc.up_open && sc.up < S) openu = !(ycol[strip_start(sc.up, len, S)] - qy > t);
+          if (sc.up_open && sc.up < S) openu = !(ylo_t[sc.up] - qy > t);
           if (sc.dn_open && sc.dn >= 0)
-            opend = !(qy - ycol[strip_start(sc.dn + 1, len, S) - 1] > t);
+            opend = !(qy - yhi_t[sc.dn] > t);
         }
         sc.up_open = sc.up_open && sc.up < S && __syncthreads_or(openu);
         sc.dn_open = sc.dn_open && sc.dn >= 0 && __syncthreads_or(opend);
@@ -353,7 +355,7 @@ grid_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items,
         }
         ++sc.strips_done;
         int wl, wh;
-        GridItem<THREADS, PLAIN>::window(c64, strip_start(s, len, S), strip_start(s + 1, len, S),
+        GridItem<THREADS, PLAIN>::window(c64, sst[s], sst[s + 1],
                                          xa - T, xb + T, wl, wh);
         sc.ra = wl;
         sc.rb = wh;

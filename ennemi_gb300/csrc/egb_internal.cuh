@@ -166,6 +166,9 @@ struct JobDev {
   int32_t* posg;
   int32_t nstrips;
   int32_t gseg;           // grid: its segment in the strip-key sort
+  const int32_t* sstart;  // grid: nstrips + 1 strip starts (strip_start table)
+  double* sylo;           // grid: smallest column-1 value of each strip
+  double* syhi;           // grid: largest column-1 value of each strip
   // work counters of this job's launch group: [0] pairs screened by tile
   // items, [1] pairs screened by deferred-query warps, [2] queries deferred
   unsigned long long* stats;
@@ -316,6 +319,14 @@ void launch_knn_grid(const JobDev* jobs_d, const WorkItem* items_d, int nitems, 
 void launch_count_grid(const JobDev* jobs_d, const WorkItem* items_d, int nitems, int dclass,
                        int plain, int dmax, int* counter, uint32_t* err, DeferEntry* defer,
                        int* defer_count, int num_sms, cudaStream_t st);
+
+// egb_wgrid.cu: warp-level grid kernels (items of WG_QB queries, outliers
+// finished in-warp, no deferred pass); kclass <= 8 for kNN.
+constexpr int WG_QB = 32;
+void launch_knn_wgrid(const JobDev* jobs_d, const WorkItem* items_d, int nitems, int kclass,
+                      int dclass, int plain, int dmax, int* counter, int num_sms, cudaStream_t st);
+void launch_count_wgrid(const JobDev* jobs_d, const WorkItem* items_d, int nitems, int dclass,
+                        int plain, int dmax, int* counter, int num_sms, cudaStream_t st);
 
 // egb_select.cu: any K (one warp per query, radix select on FP64 bits)
 constexpr int SELECT_WARPS = 8;

@@ -47,6 +47,25 @@ void launch_count_grid_f32(int, const JobDev*, const WorkItem*, int, int*, uint3
 void launch_count_grid_f64(int, const JobDev*, const WorkItem*, int, int*, uint32_t*, int,
                            DeferEntry*, int*, int, cudaStream_t);
 
+void launch_knn_wgrid_f32(int, int, const JobDev*, const WorkItem*, int, int*, int, int, cudaStream_t);
+void launch_knn_wgrid_f64(int, int, const JobDev*, const WorkItem*, int, int*, int, int, cudaStream_t);
+void launch_count_wgrid_f32(int, const JobDev*, const WorkItem*, int, int*, int, int, cudaStream_t);
+void launch_count_wgrid_f64(int, const JobDev*, const WorkItem*, int, int*, int, int, cudaStream_t);
+
+void launch_knn_wgrid(const JobDev* jobs_d, const WorkItem* items_d, int nitems, int kclass,
+                      int dclass, int plain, int dmax, int* counter, int num_sms, cudaStream_t st) {
+  if (nitems <= 0) return;
+  if (plain) launch_knn_wgrid_f64(kclass, dclass, jobs_d, items_d, nitems, counter, dmax, num_sms, st);
+  else launch_knn_wgrid_f32(kclass, dclass, jobs_d, items_d, nitems, counter, dmax, num_sms, st);
+}
+
+void launch_count_wgrid(const JobDev* jobs_d, const WorkItem* items_d, int nitems, int dclass,
+                        int plain, int dmax, int* counter, int num_sms, cudaStream_t st) {
+  if (nitems <= 0) return;
+  if (plain) launch_count_wgrid_f64(dclass, jobs_d, items_d, nitems, counter, dmax, num_sms, st);
+  else launch_count_wgrid_f32(dclass, jobs_d, items_d, nitems, counter, dmax, num_sms, st);
+}
+
 TileShape grid_shape(int dclass, int plain, int dmax) {
   return plain ? grid_shape_f64(dclass, dmax) : grid_shape_f32(dclass, dmax);
 }

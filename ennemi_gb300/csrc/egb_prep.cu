@@ -154,6 +154,11 @@ __global__ void materialize_grid_kernel(const TaskDev* __restrict__ tasks,
     const int d = J.sp.d;
     const int32_t* va = sorted_vals + segs[J.sort_seg].out_base;
     const int32_t* gv = gvals_sorted + gsegs[J.gseg].out_base;
+    // column-1 bounds of each strip, from the column-1 sorted copy
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < J.nstrips; s += gridDim.x * blockDim.x) {
+      J.sylo[s] = J.c64b[J.lds + J.sstart[s]];
+      J.syhi[s] = J.c64b[J.lds + J.sstart[s + 1] - 1];
+    }
     for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < J.lds;
          p += (int64_t)gridDim.x * blockDim.x) {
       if (p < J.len) {

@@ -1,0 +1,12 @@
+// Warp-level grid kernels, FP32 screen + FP64 decision (see egb_wgrid.cuh).
+#include "egb_wgrid.cuh"
+namespace egb {
+void launch_knn_wgrid_f32(int kclass, int dclass, const JobDev* jobs, const WorkItem* items,
+                           int nitems, int* ctr, int dmax, int sms, cudaStream_t st) {
+  wgrid_detail::WgridDispatch<false>::knn(kclass, dclass, jobs, items, nitems, ctr, dmax, sms, st);
+}
+void launch_count_wgrid_f32(int dclass, const JobDev* jobs, const WorkItem* items, int nitems,
+                             int* ctr, int dmax, int sms, cudaStream_t st) {
+  wgrid_detail::WgridDispatch<false>::count(dclass, jobs, items, nitems, ctr, dmax, sms, st);
+}
+}  // namespace egb

@@ -73,9 +73,11 @@ enum egb_flags {
   EGB_KEEP_INTERNALS = 1 << 4, /* keep eps / counts for egb_fetch()             */
   EGB_FORCE_SLAB = 1 << 5,     /* use the sorted-slab variant for every multi-D
                                   space, whatever its size (tests)               */
-  EGB_FORCE_GRID = 1 << 6      /* use the strip (grid) variant for every multi-D
+  EGB_FORCE_GRID = 1 << 6,     /* use the strip (grid) variant for every multi-D
                                   space, whatever its size (tests); the default
                                   picks it for spaces of >= 4096 points          */
+  EGB_FORCE_CTA_GRID = 1 << 7  /* grid spaces use the CTA-item kernels, never the
+                                  warp-item ones (tests, comparisons)            */
 };
 
 /* One float64 column: sample i at data[i * stride] (stride in elements). */

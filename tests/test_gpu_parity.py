@@ -21,6 +21,7 @@ VARIANTS = {
     "fp32-brute": N.FORCE_BRUTE,
     "fp32-slab": N.FORCE_SLAB,
     "fp32-grid": N.FORCE_GRID,
+    "fp32-ctagrid": N.FORCE_GRID | N.FORCE_CTA_GRID,
     "fp64-brute": N.PLAIN_FP64 | N.FORCE_BRUTE,
     "fp64-slab": N.PLAIN_FP64 | N.FORCE_SLAB,
     "fp64-grid": N.PLAIN_FP64 | N.FORCE_GRID,
@@ -123,7 +124,7 @@ def _medium_cases():
 MEDIUM = list(_medium_cases())
 
 
-@pytest.mark.parametrize("variant", ["fp32", "fp32-brute", "fp32-slab", "fp64-grid"])
+@pytest.mark.parametrize("variant", ["fp32", "fp32-brute", "fp32-slab", "fp32-ctagrid", "fp64-grid"])
 @pytest.mark.parametrize("case", MEDIUM, ids=[c[0] for c in MEDIUM])
 def test_medium_against_oracle(oracle, case, variant):
     name, kind, k, inp = case
