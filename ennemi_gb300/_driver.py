@@ -58,6 +58,12 @@ NOISE_SCALE = 1e-10
 
 # --------------------------------------------------------------- batching --
 
+# Extra egb_run_batch flags for every batch of the public API, e.g.
+# _native.PLAIN_FP64 for the all-FP64 comparator or _native.GRAPH to replay
+# repeated batches from a CUDA graph.  No flag changes a result.
+run_flags = 0
+
+
 class _Batch:
     """Collects estimator tasks and host-side values; evaluates all GPU work
     in one call and hands back the values in submission order."""
@@ -76,7 +82,7 @@ class _Batch:
         return len(self.slots) - 1
 
     def run(self) -> np.ndarray:
-        gpu = _native.run_tasks(self.tasks) if self.tasks else np.empty(0)
+        gpu = _native.run_tasks(self.tasks, flags=run_flags) if self.tasks else np.empty(0)
         out = np.empty(len(self.slots))
         for i, (kind, v) in enumerate(self.slots):
             out[i] = gpu[v] if kind == "gpu" else v

@@ -32,6 +32,21 @@ KEEP_INTERNALS = 1 << 4
 FORCE_SLAB = 1 << 5
 FORCE_GRID = 1 << 6
 FORCE_CTA_GRID = 1 << 7
+GRAPH = 1 << 8
+
+# layout policy (include/ennemi_gb.h)
+MODE_AUTO, MODE_BRUTE, MODE_SLAB, MODE_GRID, MODE_WARP_GRID = -1, 0, 1, 2, 3
+POLICY_SIZE_CLASSES = 32
+POLICY_ENTRIES = 2 * 4 * 4 * POLICY_SIZE_CLASSES
+
+
+def policy_index(search: int, d: int, K: int, length: int) -> int:
+    """egb_policy_index(): search 0 = kNN, 1 = ball count; K = k + 1."""
+    dc = 0 if d <= 2 else 1 if d == 3 else 2 if d == 4 else 3
+    kc = 0 if search else (0 if K <= 4 else 1 if K <= 8 else 2 if K <= 16 else 3)
+    sc = min(max(int(length).bit_length() - 1, 0), POLICY_SIZE_CLASSES - 1)
+    return ((search * 4 + dc) * 4 + kc) * POLICY_SIZE_CLASSES + sc
+
 
 PHASES = ("upload", "prepare", "sort", "knn", "counts", "combine", "total",
           "knn_tile", "knn_defer", "count_tile", "count_defer")
@@ -95,6 +110,12 @@ def load():
         lib.egb_last_transfer.restype = ctypes.c_int
         lib.egb_last_stats.argtypes = [vp, ctypes.POINTER(i64), i32]
         lib.egb_last_stats.restype = ctypes.c_int
+        lib.egb_set_policy.argtypes = [vp, ctypes.POINTER(ctypes.c_int8), i32]
+        lib.egb_set_policy.restype = ctypes.c_int
+        lib.egb_get_policy.argtypes = [vp, ctypes.POINTER(ctypes.c_int8), i32]
+        lib.egb_get_policy.restype = ctypes.c_int
+        lib.egb_device_info.argtypes = [vp, ctypes.c_char_p, i32, ctypes.POINTER(i32)]
+        lib.egb_device_info.restype = ctypes.c_int
         lib.egb_version.argtypes = []
         lib.egb_version.restype = ctypes.c_char_p
         _lib = lib
@@ -142,6 +163,28 @@ class Context:
         n = self.lib.egb_last_stats(self.h, buf, len(names))
         return {names[i]: int(buf[i]) for i in range(n)}
 
+    def device_name(self) -> str:
+        buf = ctypes.create_string_buffer(256)
+        sms = ctypes.c_int32()
+        self.check(self.lib.egb_device_info(self.h, buf, 256, ctypes.byref(sms)), "egb_device_info")
+        return f"{buf.value.decode()}_{sms.value}sm"
+
+    def set_policy(self, modes) -> None:
+        """Install a layout policy table (POLICY_ENTRIES modes); None resets it."""
+        if modes is None:
+            self.check(self.lib.egb_set_policy(self.h, None, 0), "egb_set_policy")
+            return
+        m = np.ascontiguousarray(modes, dtype=np.int8)
+        if m.shape != (POLICY_ENTRIES,):
+            raise ValueError(f"policy table must have {POLICY_ENTRIES} entries")
+        self.check(self.lib.egb_set_policy(
+            self.h, m.ctypes.data_as(ctypes.POINTER(ctypes.c_int8)), POLICY_ENTRIES), "egb_set_policy")
+
+    def get_policy(self) -> np.ndarray:
+        m = np.empty(POLICY_ENTRIES, dtype=np.int8)
+        self.lib.egb_get_policy(self.h, m.ctypes.data_as(ctypes.POINTER(ctypes.c_int8)), POLICY_ENTRIES)
+        return m
+
     def timings(self) -> dict:
         buf = (ctypes.c_double * len(PHASES))()
         n = self.lib.egb_timings(self.h, buf, len(PHASES))
@@ -152,6 +195,8 @@ def context(device: int = 0) -> Context:
     ctx = _ctx.get(device)
     if ctx is None:
         ctx = Context(device)
+        from . import autotune
+        autotune.load_cached(ctx)   # a saved layout policy for this device, if any
         _ctx[device] = ctx
     return ctx
 

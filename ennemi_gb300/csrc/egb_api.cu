@@ -127,6 +127,14 @@ struct egb_ctx {
   double timings[NPHASE + NKTIME] = {};
   int ntimings = 0;
   int64_t h2d_bytes = 0, d2h_bytes = 0;
+  // CUDA graph of the last batch run with EGB_GRAPH, replayed while the
+  // batch signature is unchanged
+  cudaGraphExec_t graph_exec = nullptr;
+  uint64_t graph_sig = 0;
+  long long graph_launches = 0;
+  // layout policy: mode per egb_policy_index() (EGB_MODE_AUTO = built-in rule)
+  int8_t policy[EGB_POLICY_ENTRIES];
+  egb_ctx() { std::memset(policy, EGB_MODE_AUTO, sizeof(policy)); }
   // kNN: tile pairs, deferred pairs, deferred queries; counts: the same;
   // [6] kNN tile ops, [7] count tile ops ((2d+1) per pair); [8] kernels launched
   int64_t stats[NSTATS] = {};
@@ -359,11 +367,20 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   // grid (warp items of 32 queries); modes 1-3 carry the two sorted copies
   // (deferred queries, strip bounds), modes 2-3 the strip-ordered copy
   struct MJob { Space s; bool is_knn; int slab; int sort_seg; int sel; int sort_seg_b; int mode; };
-  auto pick_mode = [&](int64_t len) {
-    if (force_brute) return 0;
-    if (force_slab) return 1;
-    if (force_grid) return 2;
-    return len >= SLAB_MIN ? 2 : 0;
+  // layout of a multi-D job: EGB_FORCE_* flags, else the context's policy
+  // table, else the built-in rule; warp grid kNN needs K <= 8
+  auto pick_mode = [&](bool is_knn, const Space& s) {
+    const int64_t len = s.e - s.b;
+    int mode;
+    if (force_brute) mode = 0;
+    else if (force_slab) mode = 1;
+    else if (force_grid) mode = 3;
+    else {
+      mode = ctx->policy[egb_policy_index(is_knn ? 0 : 1, s.sp.d, s.K, len)];
+      if (mode == EGB_MODE_AUTO) mode = len >= SLAB_MIN ? 3 : 0;
+    }
+    if (mode == 3 && (cta_grid || (is_knn && s.K > 8))) mode = 2;
+    return mode;
   };
   std::vector<std::pair<int, Space>> sorted_knn, sorted_cnt;  // (seg, space)
   std::vector<MJob> mjobs;
@@ -373,8 +390,7 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
     } else {
       MJob m{s, true, 0, -1, 0, -1, 0};
       if (s.K > EGB_KREG_MAX) m.sel = 1;
-      else m.mode = pick_mode(s.e - s.b);
-      if (m.mode == 2 && s.K <= 8 && !cta_grid) m.mode = 3;
+      else m.mode = pick_mode(true, s);
       m.slab = m.mode >= 1 ? 1 : 0;
       if (m.slab) {
         m.sort_seg = seg_for(s.task, s.sp.cols[0], s.b, s.e);
@@ -388,8 +404,7 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
       sorted_cnt.push_back({seg_for(s.task, s.sp.cols[0], s.b, s.e), s});
     } else {
       MJob m{s, false, 0, -1, 0, -1, 0};
-      m.mode = pick_mode(s.e - s.b);
-      if (m.mode == 2 && !cta_grid) m.mode = 3;
+      m.mode = pick_mode(false, s);
       m.slab = m.mode >= 1 ? 1 : 0;
       if (m.slab) {
         m.sort_seg = seg_for(s.task, s.sp.cols[0], s.b, s.e);
@@ -786,6 +801,10 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   if (!dev_in)
     for (const Range& r : ranges)
       EGB_CUDA(cudaMemcpyAsync(A + r.dev_off, (const void*)r.lo, r.hi - r.lo, cudaMemcpyHostToDevice, st));
+  const size_t pin_zr = pin_rb + sizeof(double) * (size_t)std::max(nchunks, 1);
+  // Everything from the descriptor upload to the read-back: issued directly,
+  // or captured once into a CUDA graph and replayed for identical batches.
+  auto enqueue = [&]() -> int {
   EGB_CUDA(cudaMemcpyAsync(A + off_tab, H, tab_bytes, cudaMemcpyHostToDevice, st));
   EGB_CUDA(cudaMemsetAsync(A + off_zr, 0, zr_bytes, st));
   if (dev_in)
@@ -902,8 +921,51 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   if (nchunks)
     EGB_CUDA(cudaMemcpyAsync(H + pin_rb, A + off_partial, sizeof(double) * (size_t)nchunks,
                              cudaMemcpyDeviceToHost, st));
-  const size_t pin_zr = pin_rb + sizeof(double) * (size_t)std::max(nchunks, 1);
   EGB_CUDA(cudaMemcpyAsync(H + pin_zr, A + off_zr, zr_bytes, cudaMemcpyDeviceToHost, st));
+  return EGB_OK;
+  };
+
+  const bool use_graph = (flags & EGB_GRAPH) != 0 && !timing;
+  if (use_graph) {
+    // signature of the batch: the descriptor blob (all device pointers,
+    // sizes, job tables) plus the arena, pinned buffer and flags
+    uint64_t sig = 1469598103934665603ull;
+    auto mix = [&](const void* p, size_t n) {
+      const unsigned char* b = (const unsigned char*)p;
+      for (size_t i = 0; i < n; ++i) sig = (sig ^ b[i]) * 1099511628211ull;
+    };
+    mix(H, tab_bytes);
+    const uintptr_t extra[8] = {(uintptr_t)A, (uintptr_t)H, (uintptr_t)flags, (uintptr_t)zr_bytes,
+                                (uintptr_t)nchunks, (uintptr_t)(void*)st, (uintptr_t)ctx->psi_d,
+                                (uintptr_t)ctx->psi_len};
+    mix(extra, sizeof(extra));
+    if (!(ctx->graph_exec && ctx->graph_sig == sig)) {
+      if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
+      ctx->graph_exec = nullptr;
+      const long long l0 = g_launches.load();
+      EGB_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+      const int rc_cap = enqueue();
+      cudaGraph_t graph = nullptr;
+      const cudaError_t ce = cudaStreamEndCapture(st, &graph);
+      if (rc_cap != EGB_OK) {
+        if (graph) cudaGraphDestroy(graph);
+        return rc_cap;
+      }
+      if (ce != cudaSuccess) return fail(ctx, EGB_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
+      const cudaError_t ie = cudaGraphInstantiate(&ctx->graph_exec, graph, 0);
+      cudaGraphDestroy(graph);
+      if (ie != cudaSuccess) {
+        ctx->graph_exec = nullptr;
+        return fail(ctx, EGB_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ie));
+      }
+      ctx->graph_sig = sig;
+      ctx->graph_launches = g_launches.load() - l0;
+    }
+    EGB_CUDA(cudaGraphLaunch(ctx->graph_exec, st));
+  } else {
+    const int rc_q = enqueue();
+    if (rc_q != EGB_OK) return rc_q;
+  }
   if (timing) EGB_CUDA(cudaEventRecord(ctx->ev[6], st));
   EGB_CUDA(cudaStreamSynchronize(st));
 
@@ -931,7 +993,7 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
       const int d = groups[g].dclass ? groups[g].dclass : groups[g].dmax;
       ctx->stats[groups[g].is_knn ? 6 : 7] += (int64_t)st4[4 * g] * (2 * d + 1);
     }
-    ctx->stats[8] = (int64_t)(g_launches.load() - launches0);
+    ctx->stats[8] = use_graph ? (int64_t)ctx->graph_launches : (int64_t)(g_launches.load() - launches0);
   }
   const uint32_t dev_err = *(const uint32_t*)(H + pin_zr + zr_err);
   if (dev_err) {
@@ -1028,6 +1090,7 @@ void egb_destroy(egb_ctx* ctx) {
   if (!ctx) return;
   cudaSetDevice(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
   if (ctx->arena) cudaFree(ctx->arena);
   if (ctx->pinned) cudaFreeHost(ctx->pinned);
   if (ctx->psi_d) cudaFree(ctx->psi_d);
@@ -1129,6 +1192,27 @@ int egb_ball_count(egb_ctx* ctx, const double* points, int64_t n, int32_t d, con
   return egb_fetch(ctx, 0, 1, count);
 }
 
+int egb_set_policy(egb_ctx* ctx, const int8_t* modes, int32_t n) {
+  if (!ctx) return EGB_ERR_ARG;
+  if (!modes) {
+    std::memset(ctx->policy, EGB_MODE_AUTO, sizeof(ctx->policy));
+    return EGB_OK;
+  }
+  if (n != EGB_POLICY_ENTRIES) return fail(ctx, EGB_ERR_ARG, "egb_set_policy: table size mismatch");
+  for (int i = 0; i < n; ++i)
+    if (modes[i] < EGB_MODE_AUTO || modes[i] > EGB_MODE_WARP_GRID)
+      return fail(ctx, EGB_ERR_ARG, "egb_set_policy: invalid mode at entry " + std::to_string(i));
+  std::memcpy(ctx->policy, modes, sizeof(ctx->policy));
+  return EGB_OK;
+}
+
+int egb_get_policy(const egb_ctx* ctx, int8_t* modes, int32_t n) {
+  if (!ctx || !modes) return 0;
+  const int m = std::min<int>(n, EGB_POLICY_ENTRIES);
+  std::memcpy(modes, ctx->policy, (size_t)m);
+  return m;
+}
+
 int egb_timings(const egb_ctx* ctx, double* ms, int32_t max) {
   if (!ctx || !ms) return 0;
   const int n = std::min<int>(max, ctx->ntimings);
@@ -1148,6 +1232,21 @@ int egb_last_stats(const egb_ctx* ctx, int64_t* out, int32_t max) {
   const int n = std::min<int>(max, NSTATS);
   for (int i = 0; i < n; ++i) out[i] = ctx->stats[i];
   return n;
+}
+
+int egb_device_info(const egb_ctx* ctx, char* name, int32_t len, int32_t* sms) {
+  if (!ctx) return EGB_ERR_ARG;
+  cudaDeviceProp prop{};
+  if (cudaGetDeviceProperties(&prop, ctx->device) != cudaSuccess) {
+    cudaGetLastError();
+    return EGB_ERR_CUDA;
+  }
+  if (name && len > 0) {
+    std::strncpy(name, prop.name, (size_t)len - 1);
+    name[len - 1] = 0;
+  }
+  if (sms) *sms = prop.multiProcessorCount;
+  return EGB_OK;
 }
 
 const char* egb_version(void) { return "ennemi_gb300 0.1.0 (sm_103a)"; }

@@ -1,0 +1,103 @@
+"""Seeded synthetic workloads with the shapes of the large-sample benchmark
+configurations (no dataset involved).  Used by bench.py and the tests.
+
+large_sample(n)      bivariate Gaussians rho in {0, .3, .6, .9} and a trivariate
+                     Gaussian (corr(x,y) = .5, corr(x,z) = corr(y,z) = .4)
+lagged_ar(length)    16 coupled AR(1) series (phi = .8, coupling .3 from the
+                     previous series with a 5-step delay), a mask with ~10 %
+                     false in runs of 1-50 samples; estimate_mi of series 0
+                     against all 16 at lags 0..48 (784 estimates)
+pairwise_mix(n)      64 columns: 16 correlated Gaussians, 16 sin(2x) + .3 noise,
+                     16 Student-t(3), 16 log-normal; plus a 2-D Gaussian
+                     condition (pairwise_mi: 2,016 pairs)
+semidiscrete_mix(n)  x of dimension 1-4 from 3-component Gaussian mixtures,
+                     discrete y with 2-50 classes of Dirichlet(.5) sizes; and
+                     a 3-D Gaussian mixture for entropy
+"""
+
+from __future__ import annotations
+
+import numpy as np
+from scipy.signal import lfilter
+
+RHOS = (0.0, 0.3, 0.6, 0.9)
+CMI_COV = [[1, 0.5, 0.4], [0.5, 1, 0.4], [0.4, 0.4, 1]]
+
+
+def large_sample(n: int = 1_000_000, seed: int = 0):
+    """[(kind, [columns])]: four 'mi' (x, y) tasks and one 'cmi' (x, y, z)."""
+    rng = np.random.default_rng(seed)
+    work = []
+    for rho in RHOS:
+        d = rng.multivariate_normal([0, 0], [[1, rho], [rho, 1]], size=n)
+        work.append(("mi", [np.ascontiguousarray(d[:, 0]), np.ascontiguousarray(d[:, 1])]))
+    d = rng.multivariate_normal([0, 0, 0], CMI_COV, size=n)
+    work.append(("cmi", [np.ascontiguousarray(d[:, c]) for c in range(3)]))
+    return work
+
+
+def lagged_ar(length: int = 200_000, nseries: int = 16, seed: int = 3):
+    """(y, x, lags, mask) for estimate_mi(y, x, lags, mask=mask).
+
+    x[:, i](t) = 0.8 x[:, i](t-1) + 0.3 x[:, i-1](t-5) + e_i(t) (series 0 has
+    no coupling term), so every series is stationary; y is series 0.
+    """
+    rng = np.random.default_rng(seed)
+    e = rng.normal(size=(length, nseries))
+    x = np.empty((length, nseries))
+    for i in range(nseries):
+        drive = e[:, i].copy()
+        if i > 0:
+            drive[5:] += 0.3 * x[:-5, i - 1]
+        x[:, i] = lfilter([1.0], [1.0, -0.8], drive)
+    mask = np.ones(length, dtype=bool)
+    target_false = int(0.1 * length)
+    while (~mask).sum() < target_false:
+        start = int(rng.integers(0, length))
+        run = int(rng.integers(1, 51))
+        mask[start:start + run] = False
+    return x[:, 0].copy(), x, np.arange(49), mask
+
+
+def _random_corr(k: int, rng) -> np.ndarray:
+    a = rng.normal(size=(k, k + 2))
+    c = a @ a.T
+    s = np.sqrt(np.diag(c))
+    return c / s[:, None] / s[None, :]
+
+
+def pairwise_mix(n: int = 50_000, seed: int = 4):
+    """(data (n x 64), cond (n x 2))."""
+    rng = np.random.default_rng(seed)
+    g = rng.multivariate_normal(np.zeros(16), _random_corr(16, rng), size=n)
+    base = rng.normal(size=(n, 16))
+    s = np.sin(2 * base) + 0.3 * rng.normal(size=(n, 16))
+    t = rng.standard_t(3, size=(n, 16))
+    ln = np.exp(rng.normal(size=(n, 16)))
+    data = np.column_stack((g, s, t, ln))
+    cond = rng.multivariate_normal([0, 0], [[1, 0.3], [0.3, 1]], size=n)
+    return data, cond
+
+
+def _mixture(n: int, dim: int, rng) -> np.ndarray:
+    comp = rng.integers(0, 3, size=n)
+    out = np.empty((n, dim))
+    for c in range(3):
+        sel = comp == c
+        mean = rng.normal(scale=2.0, size=dim)
+        cov = _random_corr(dim, rng) * rng.uniform(0.5, 2.0)
+        out[sel] = rng.multivariate_normal(mean, cov, size=int(sel.sum()))
+    return out
+
+
+def semidiscrete_mix(n: int = 500_000, seed: int = 5):
+    """([(x (n x d), labels)] for d = 1..4 with 2, 10, 25, 50 classes; entropy x (n x 3))."""
+    rng = np.random.default_rng(seed)
+    cases = []
+    for dim, ncls in zip((1, 2, 3, 4), (2, 10, 25, 50)):
+        p = rng.dirichlet(np.full(ncls, 0.5))
+        y = rng.choice(ncls, p=p, size=n)
+        x = _mixture(n, dim, rng) + 0.5 * y[:, None] / ncls
+        cases.append((x if dim > 1 else x[:, 0].copy(), y))
+    ent = _mixture(n, 3, rng)
+    return cases, ent

@@ -76,8 +76,13 @@ enum egb_flags {
   EGB_FORCE_GRID = 1 << 6,     /* use the strip (grid) variant for every multi-D
                                   space, whatever its size (tests); the default
                                   picks it for spaces of >= 4096 points          */
-  EGB_FORCE_CTA_GRID = 1 << 7  /* grid spaces use the CTA-item kernels, never the
+  EGB_FORCE_CTA_GRID = 1 << 7, /* grid spaces use the CTA-item kernels, never the
                                   warp-item ones (tests, comparisons)            */
+  EGB_GRAPH = 1 << 8           /* capture the batch's device work (descriptor
+                                  upload to read-back) in a CUDA graph and replay
+                                  it for later batches with the same signature
+                                  (same sizes, pointers and flags); ignored with
+                                  EGB_TIMING                                      */
 };
 
 /* One float64 column: sample i at data[i * stride] (stride in elements). */
@@ -184,6 +189,50 @@ int egb_last_transfer(const egb_ctx* ctx, int64_t* h2d_bytes, int64_t* d2h_bytes
 int egb_last_stats(const egb_ctx* ctx, int64_t* out, int32_t max);
 
 /*
+ * Layout policy (the table an autotuner fills; no counterpart in the
+ * reference, whose cKDTree has a single layout).  Every multi-dimensional
+ * search job of a batch -- a kNN search or a ball count over d >= 2 columns --
+ * runs in one of four layouts:
+ *   EGB_MODE_BRUTE      tiles of all points against all points
+ *   EGB_MODE_SLAB       points sorted by column 0, tiles from a window
+ *   EGB_MODE_GRID       equal-count strips, 128-query CTA work items
+ *   EGB_MODE_WARP_GRID  equal-count strips, 32-query warp work items
+ *                       (kNN only for K = k + 1 <= 8; otherwise GRID)
+ * Each layout gives the same results bit for bit; only speed differs.  The
+ * planner reads the context's table at egb_policy_index(search, d, K, len);
+ * EGB_MODE_AUTO (every entry of a new context) selects the built-in rule:
+ * brute force below 4096 points, otherwise the warp grid (CTA grid for kNN
+ * with 9 <= K <= 32).  K > 32 kNN always uses the select kernel, and the
+ * EGB_FORCE_* flags override the table.
+ */
+#define EGB_MODE_AUTO (-1)
+#define EGB_MODE_BRUTE 0
+#define EGB_MODE_SLAB 1
+#define EGB_MODE_GRID 2
+#define EGB_MODE_WARP_GRID 3
+#define EGB_POLICY_SIZE_CLASSES 32 /* floor(log2(len)) */
+#define EGB_POLICY_ENTRIES (2 * 4 * 4 * EGB_POLICY_SIZE_CLASSES)
+
+/* search: 0 = kNN, 1 = ball count; d: dimension (>= 2; 5 and up share a
+ * class); K: k + 1 for kNN (classes <= 4, <= 8, <= 16, above), ignored for
+ * counts; len: points in the job. */
+static inline int egb_policy_index(int search, int d, int K, int64_t len) {
+  int dc = d <= 2 ? 0 : d == 3 ? 1 : d == 4 ? 2 : 3;
+  int kc = search ? 0 : K <= 4 ? 0 : K <= 8 ? 1 : K <= 16 ? 2 : 3;
+  int sc = 0;
+  while (sc < EGB_POLICY_SIZE_CLASSES - 1 && (len >> (sc + 1)) > 0) ++sc;
+  return ((search * 4 + dc) * 4 + kc) * EGB_POLICY_SIZE_CLASSES + sc;
+}
+
+/* Replace the context's table with modes[0 .. n) (n == EGB_POLICY_ENTRIES;
+ * each entry EGB_MODE_AUTO .. EGB_MODE_WARP_GRID).  modes == NULL resets every
+ * entry to EGB_MODE_AUTO. */
+int egb_set_policy(egb_ctx* ctx, const int8_t* modes, int32_t n);
+
+/* Copy the context's table to modes[0 .. n); returns the number written. */
+int egb_get_policy(const egb_ctx* ctx, int8_t* modes, int32_t n);
+
+/*
  * egb_knn_eps_noalloc -- egb_knn_eps() for callers that may not allocate
  * device memory.  It has no counterpart in the reference; it exists for
  * callers such as a plugin inside a larger GPU application that owns a fixed,
@@ -215,6 +264,10 @@ int egb_last_stats(const egb_ctx* ctx, int64_t* out, int32_t max);
 #define EGB_NOALLOC_SCRATCH_BYTES (1152u * 1024u)
 int egb_knn_eps_noalloc(const double* points, int64_t n, int32_t d, int32_t k, double* eps,
                         void* stream);
+
+/* Name of the context's CUDA device (cudaDeviceProp::name) into name[0 ..
+ * len), NUL-terminated; *sms = its multiprocessor count.  Returns 0. */
+int egb_device_info(const egb_ctx* ctx, char* name, int32_t len, int32_t* sms);
 
 /* Library version string. */
 const char* egb_version(void);

@@ -20,6 +20,8 @@ def declared_functions():
     for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
         text = open(h).read()
         text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        # header-only helpers are not library symbols
+        text = re.sub(r"static inline[^{]*\{.*?\n\}", "", text, flags=re.S)
         for m in re.finditer(r"\b(egb_[a-z0-9_]+)\s*\(", text):
             names.add(m.group(1))
     return sorted(names)
@@ -65,3 +67,28 @@ def test_null_arguments_rejected_without_device(lib):
 
 def test_library_is_built_for_sm103a():
     assert "arch=compute_103a,code=sm_103a" in " ".join(_build.NVCC_FLAGS)
+
+
+def test_policy_index_matches_header(tmp_path):
+    """egb_policy_index() compiled from the header equals _native.policy_index."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    src = tmp_path / "pi.c"
+    src.write_text(
+        '#include <stdio.h>\n#include "ennemi_gb.h"\n'
+        "int main(void) { long long lens[] = {1, 2, 3, 255, 256, 4095, 4096, 1000000,"
+        " 1LL << 31, 1LL << 40};\n"
+        "  for (int s = 0; s < 2; ++s) for (int d = 1; d <= 9; ++d) for (int K = 2; K <= 40; K += 3)"
+        " for (int i = 0; i < 10; ++i) printf(\"%d\\n\", egb_policy_index(s, d, K, lens[i]));\n"
+        "  return 0; }\n")
+    exe = tmp_path / "pi"
+    subprocess.check_call([cc, "-std=c99", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)])
+    got = [int(v) for v in subprocess.check_output([str(exe)]).split()]
+    lens = [1, 2, 3, 255, 256, 4095, 4096, 1000000, 1 << 31, 1 << 40]
+    want = [_native.policy_index(s, d, K, n) for s in range(2) for d in range(1, 10)
+            for K in range(2, 41, 3) for n in lens]
+    assert got == want
+    assert max(want) < _native.POLICY_ENTRIES and min(want) >= 0

@@ -14,7 +14,7 @@ import pytest
 
 import ennemi_gb300 as eg
 from ennemi_gb300 import _driver, _native
-from conftest import driver_cases
+from conftest import driver_cases, oracle_run_tasks
 
 DCASES = driver_cases()
 
@@ -27,29 +27,7 @@ def _py(v):
 @pytest.fixture
 def on_oracle(oracle, monkeypatch):
     calls = []
-
-    def run(tasks, flags=0, device=0, results_out=None):
-        calls.append(len(tasks))
-        out = []
-        for t in tasks:
-            x = np.column_stack(t.x)
-            y = np.column_stack(t.y) if len(t.y) else None
-            z = np.column_stack(t.z) if len(t.z) else None
-            with np.errstate(all="ignore"):
-                if t.kind == _native.MI:
-                    v = oracle.ksg_mi(x, y, t.k)[0]
-                elif t.kind == _native.CMI:
-                    v = oracle.cmi(x, y, z, t.k)[0]
-                elif t.kind == _native.SEMI:
-                    v = oracle.semidiscrete_mi(x, t.labels, t.k)[0]
-                elif t.kind == _native.CSEMI:
-                    v = oracle.conditional_semidiscrete_mi(x, t.labels, z, t.k)[0]
-                else:
-                    v = oracle.entropy(x, t.k)[0]
-            out.append(v)
-        return np.array(out)
-
-    monkeypatch.setattr(_native, "run_tasks", run)
+    monkeypatch.setattr(_native, "run_tasks", oracle_run_tasks(oracle, calls))
     return calls
 
 

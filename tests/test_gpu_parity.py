@@ -169,3 +169,21 @@ def test_public_estimators_on_gpu():
     assert abs(mi - (-0.5 * np.log(1 - 0.36))) < 0.03
     h = E._estimate_single_entropy(d[:, 0])
     assert abs(h - 0.5 * np.log(2 * np.pi * np.e)) < 0.05
+
+
+def test_graph_replay_matches_direct_launch():
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(21)
+    n = 50000
+    cols = [torch.from_numpy(rng.normal(size=n)).cuda() for _ in range(3)]
+    tasks = [N.Task(N.MI, 3, [cols[0]], [cols[1]], n=n),
+             N.Task(N.CMI, 3, [cols[0]], [cols[1]], [cols[2]], n=n)]
+    direct = N.run_tasks(tasks, flags=N.INPUT_DEVICE)
+    first = N.run_tasks(tasks, flags=N.INPUT_DEVICE | N.GRAPH)   # captures
+    again = N.run_tasks(tasks, flags=N.INPUT_DEVICE | N.GRAPH)   # replays
+    assert np.array_equal(direct, first) and np.array_equal(direct, again)
+    # new data in the same buffers: the replayed graph reads them
+    cols[1].copy_(torch.from_numpy(0.7 * cols[0].cpu().numpy() + rng.normal(size=n)))
+    direct2 = N.run_tasks(tasks, flags=N.INPUT_DEVICE)
+    replay2 = N.run_tasks(tasks, flags=N.INPUT_DEVICE | N.GRAPH)
+    assert np.array_equal(direct2, replay2) and not np.array_equal(direct, direct2)
