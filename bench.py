@@ -42,20 +42,12 @@ sys.path.insert(0, ROOT)
 
 METRIC = "MI estimates/s, N=1e6 k=3: batched FP32+recheck vs plain GPU; counts bit-exact"
 UNIT = "MI estimates/s"
-RHOS = (0.0, 0.3, 0.6, 0.9)
-CMI_COV = [[1, 0.5, 0.4], [0.5, 1, 0.4], [0.4, 0.4, 1]]
 
 
 def make_workload(n: int, seed: int = 0):
     """[(kind, [columns])] -- kind 'mi' (x, y) or 'cmi' (x, y, z)."""
-    rng = np.random.default_rng(seed)
-    work = []
-    for rho in RHOS:
-        d = rng.multivariate_normal([0, 0], [[1, rho], [rho, 1]], size=n)
-        work.append(("mi", [np.ascontiguousarray(d[:, 0]), np.ascontiguousarray(d[:, 1])]))
-    d = rng.multivariate_normal([0, 0, 0], CMI_COV, size=n)
-    work.append(("cmi", [np.ascontiguousarray(d[:, c]) for c in range(3)]))
-    return work
+    from ennemi_gb300 import synthetic
+    return synthetic.large_sample(n, seed)
 
 
 def make_tasks(work, k, cols_of=lambda c: c):
@@ -194,6 +186,85 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def run_config(args, torch, N, ctx, dev):
+    """One JSON line for a batched workload: each step is the public-API
+    call(s) a user makes; `value` uses the device time of the batches
+    (EGB_TIMING), `e2e` the wall time of the calls (host preprocessing,
+    uploads and read-back included)."""
+    import ennemi_gb300 as eg
+    from ennemi_gb300 import _driver, synthetic
+    from ennemi_gb300 import _entropy_estimators as ee
+    if args.config == "lags":
+        y, x, lags, mask = synthetic.lagged_ar(seed=args.seed + 3)
+        calls = [lambda: eg.estimate_mi(y, x, lag=lags, mask=mask)]
+        ntask = len(lags) * x.shape[1]
+        desc = ("16 coupled AR(1) series, length 200,000, estimate_mi of series 0 vs all at lags "
+                "0..48 with a ~10 % mask in runs of 1-50 (one batch)")
+    elif args.config == "pairwise":
+        data, cond = synthetic.pairwise_mix(seed=args.seed + 4)
+        calls = [lambda: eg.pairwise_mi(data), lambda: eg.pairwise_mi(data, cond=cond)]
+        ntask = 2 * 64 * 63 // 2
+        desc = ("pairwise_mi of 64 mixed columns (Gaussian, sin, Student-t 3, log-normal), "
+                "N=50,000, plus the same conditional on a 2-D Gaussian (two batches)")
+    else:
+        cases, ent = synthetic.semidiscrete_mix(seed=args.seed + 5)
+        tasks = [ee.semidiscrete_task(xc, yc, args.k) for xc, yc in cases]
+        tasks.append(ee.entropy_task(ent, args.k))
+        calls = [lambda: N.run_tasks(tasks, device=dev)]
+        ntask = len(tasks)
+        desc = ("Ross MI of x (dim 1-4, 3-component Gaussian mixtures) vs y with 2/10/25/50 "
+                "Dirichlet(.5) classes + KL entropy of a 3-D mixture, N=500,000 (one batch)")
+
+    def step(flags):
+        _driver.run_flags = flags
+        dev_ms = 0.0
+        t0 = time.perf_counter()
+        for c in calls:
+            c()
+            dev_ms += ctx.timings().get("total", 0.0) if flags & N.TIMING else 0.0
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t0) * 1000.0, dev_ms
+
+    def run_steps(flags, steps):
+        step(flags)                                  # warm the arena
+        walls, devs = [], []
+        for _ in range(steps):
+            w, d = step(flags)
+            walls.append(w)
+            devs.append(d)
+        return walls, devs
+
+    old_flags = _driver.run_flags
+    try:
+        for _ in range(max(args.warmup - 1, 0)):
+            step(0)
+        with ClockSampler(dev) as clk:
+            walls, _ = run_steps(0, args.steps)
+        _, devs = run_steps(N.TIMING, args.steps)
+        plain = None
+        if not args.no_plain:
+            _, pdevs = run_steps(N.TIMING | N.PLAIN_FP64, 1)
+            plain = {"value": ntask / (pdevs[0] / 1000.0), "ms_per_step": pdevs[0],
+                     "form": "all-FP64 distances, same batches"}
+    finally:
+        _driver.run_flags = old_flags
+    ms_dev = statistics.median(devs)
+    ms_wall = statistics.median(walls)
+    line = {"metric": f"MI estimates/s, {args.config} workload", "value": ntask / (ms_dev / 1000.0),
+            "unit": "MI estimates/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms_dev, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32+f64", "data": "synthetic",
+            "config": {"workload": desc, "tasks_per_step": ntask, "k": args.k,
+                       "l2": "inputs re-uploaded by every call (host arrays)"},
+            "e2e": {"value": ntask / (ms_wall / 1000.0), "unit": "MI estimates/s", "ms_per_step": ms_wall,
+                    "host_ms_per_step": ms_wall - ms_dev},
+            "phases_ms_last_batch": ctx.timings(), "work_last_batch": ctx.stats(),
+            "plain": plain,
+            "speedup_vs_plain": (plain["ms_per_step"] / ms_dev) if plain else None,
+            "clocks": clk.summary()}
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -208,6 +279,9 @@ def main():
     ap.add_argument("--cpu-fraction", type=float, default=0.01)
     ap.add_argument("--ref-fraction", type=float, default=0.01)
     ap.add_argument("--profile", action="store_true", help="device-resident steps only (ncu)")
+    ap.add_argument("--config", default="large", choices=["large", "lags", "pairwise", "semidiscrete"],
+                    help="large: the headline workload; the others time one public-API call "
+                         "of the batched lag / pairwise / semidiscrete workloads")
     args = ap.parse_args()
 
     if args.impl == "reference":
@@ -229,6 +303,9 @@ def main():
     from ennemi_gb300 import _native as N
     ctx = N.context(dev)
     ctx.set_stream(torch.cuda.current_stream().cuda_stream)
+    if args.config != "large":
+        run_config(args, torch, N, ctx, dev)
+        return
 
     work = make_workload(args.n, args.seed + rank)
     dcols = [[torch.from_numpy(c).cuda() for c in cols] for _, cols in work]

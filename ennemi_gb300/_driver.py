@@ -6,16 +6,21 @@ or (i, j) task to a thread pool, each task building its own cKDTrees
 masking, validation and rescaling stay on the host in NumPy, so the inputs
 are bit-identical to the reference's -- and then evaluates all of them in one
 batched GPU launch sequence (``_native.run_tasks``).  Callbacks fire after
-that batch, once per task, in task order.  ``max_threads`` is accepted for
-compatibility and has no effect: there is no host thread pool.
+that batch, once per task, in task order.  ``max_threads`` bounds the host
+thread pool that prepares the tasks (slicing, masking, rescaling; default
+min(16, cpu_count)); the GPU work is one batch whatever its value.  Within a
+call, columns shared by several tasks (y, the condition, every column of
+pairwise_mi) are prepared once and uploaded once.
 
 Errors and warnings are those of the reference, raised at the same points.
 """
 
 from __future__ import annotations
 
+import os
 import sys
 import threading
+from concurrent.futures import ThreadPoolExecutor
 from typing import Callable, List, Optional, Sequence, Tuple, TypeVar, Union
 from warnings import warn
 
@@ -104,13 +109,16 @@ class _NoiseStream:
         self._lock = threading.Lock()
 
     def take(self, start: int, shape) -> np.ndarray:
+        """0 + NOISE_SCALE * z[start : start + prod(shape)] (a read-only view)."""
         count = int(np.prod(shape))
         with self._lock:
             if self._s.size < start + count:
                 size = max(start + count, 2 * self._s.size)
-                self._s = np.random.default_rng(NOISE_SEED).standard_normal(size)
+                s = 0.0 + NOISE_SCALE * np.random.default_rng(NOISE_SEED).standard_normal(size)
+                s.flags.writeable = False
+                self._s = s
             s = self._s
-        return (0.0 + NOISE_SCALE * s[start:start + count]).reshape(shape)
+        return s[start:start + count].reshape(shape)
 
 
 _noise = _NoiseStream()
@@ -262,7 +270,7 @@ def estimate_mi(y: ArrayLike, x: ArrayLike,
     estimators, `preprocess` the unit-variance rescaling with fixed-seed
     1e-10 noise, `normalize` the correlation scale.  Every (lag, variable)
     task of the call runs in one batched GPU launch; `callback(var, lag)`
-    fires once per task after it.  `max_threads` has no effect.
+    fires once per task after it.  `max_threads` bounds the host preparation threads.
     """
     x_arr = np.asarray(x)
     y_arr = np.asarray(y)
@@ -323,12 +331,15 @@ def _estimate_mi(y: FloatArray, x: FloatArray, lag: FloatArray, k: int,
 
     nvar = 1 if x.ndim == 1 else x.shape[1]
     indices = [(li, vi) for li in range(len(lag)) for vi in range(nvar)]
-    batch = _Batch()
-    slots = []
+    prep = _Prep(mask, min_lag, max_lag)
+    jobs = []
     for li, vi in indices:
         xv = x if x.ndim == 1 else x[:, vi]
-        slots.append(_lagged_mi_slot(batch, xv, y, lag[li], max_lag, min_lag, k, mask, cond,
-                                     cond_lag[li], discrete_x, discrete_y, preprocess, drop_nan))
+        jobs.append(_task_job(prep, ("x", vi), xv, ("y",), y, lag[li], max_lag, min_lag, k, mask,
+                              cond, cond_lag[li], discrete_x, discrete_y, preprocess, drop_nan,
+                              share_x=False))
+    batch = _Batch()
+    slots = [_add_prepared(batch, p) for p in _prepare_all(jobs, max_threads)]
     values = batch.run()
     result = np.empty((len(lag), nvar))
     for (li, vi), s in zip(indices, slots):
@@ -393,7 +404,7 @@ def pairwise_mi(data: ArrayLike,
 
     Same parameters and result as ennemi.pairwise_mi (_driver.py:540-623).
     All i < j pairs run in one batched GPU launch; `callback(i, j)` fires once
-    per pair after it.  `max_threads` has no effect.
+    per pair after it.  `max_threads` bounds the host preparation threads.
     """
     data_arr = np.asarray(data)
     cond_arr = None if cond is None else np.column_stack((np.asarray(cond),))
@@ -442,15 +453,17 @@ def _pairwise_mi(data: FloatArray, k: int, cond: Optional[FloatArray], preproces
     nvar = data.shape[1]
     cond_lag = np.full(cond.shape[1], 0) if cond is not None else np.asarray(0)
 
-    batch = _Batch()
+    prep = _Prep(mask, 0, 0)
     pairs = []
-    slots = []
+    jobs = []
     for i in range(nvar):
         for j in range(i + 1, nvar):
             pairs.append((i, j))
-            slots.append(_lagged_mi_slot(batch, data[:, i], data[:, j], 0, 0, 0, k, mask, cond,
-                                         cond_lag, discrete[i], discrete[j], preprocess,
-                                         drop_nan))
+            jobs.append(_task_job(prep, ("d", i), data[:, i], ("d", j), data[:, j], 0, 0, 0, k, mask,
+                                  cond, cond_lag, discrete[i], discrete[j], preprocess, drop_nan,
+                                  share_x=True))
+    batch = _Batch()
+    slots = [_add_prepared(batch, p) for p in _prepare_all(jobs, max_threads)]
     values = batch.run()
     result = np.full((nvar, nvar), np.nan)
     for (i, j), s in zip(pairs, slots):
@@ -463,12 +476,162 @@ def _pairwise_mi(data: FloatArray, k: int, cond: Optional[FloatArray], preproces
 
 # ------------------------------------------------------- per-task prep --
 
-def _lagged_mi_slot(batch: _Batch, x: FloatArray, y: FloatArray, lag: int, max_lag: int,
-                    min_lag: int, k: int, mask: Optional[FloatArray], cond: Optional[FloatArray],
-                    cond_lag: FloatArray, discrete_x: bool, discrete_y: bool, preprocess: bool,
-                    drop_nan: bool) -> int:
-    """One task of _lagged_mi (_driver.py:788-832): slice, mask, validate,
-    rescale, then queue the estimator (or evaluate a discrete one)."""
+class _Prep:
+    """Host preprocessing of one estimate_mi / pairwise_mi call, memoised per
+    column.
+
+    All tasks of a call slice their variables with the same mask, and y, the
+    condition and (in pairwise_mi) every data column recur in many tasks.
+    A column's sliced values depend only on (variable, offset), and its
+    rescaled values on (variable, offset, noise position), where the noise
+    position is fixed by the columns before it in the task (x, then y, then
+    z; a constant column draws none).  Computing each key once gives the same
+    arrays as the reference's per-task code (_driver.py:788-902), bit for bit
+    -- the same NumPy operations on the same values and memory layout -- and
+    lets the library upload every distinct array once.  With drop_nan the
+    rows a task keeps depend on all of its variables, so that case runs the
+    unshared per-task path.
+    """
+
+    def __init__(self, mask: Optional[FloatArray], min_lag: int, max_lag: int):
+        min_lag, max_lag = min(min_lag, 0), max(max_lag, 0)
+        self.idx = None if mask is None else np.flatnonzero(mask[max_lag: len(mask) + min_lag])
+        self._memo = {}
+        self._lock = threading.Lock()
+
+    def _get(self, key, make):
+        with self._lock:
+            hit = self._memo.get(key)
+        if hit is not None:
+            return hit
+        val = make()
+        with self._lock:
+            return self._memo.setdefault(key, val)
+
+    def base(self, key, var: FloatArray) -> FloatArray:
+        """The variable itself, or a contiguous copy of it when a mask gathers
+        from it (same values; gathering from a strided column is slow)."""
+        if self.idx is None or var.flags.c_contiguous:
+            return var
+        return self._get(("c", key), lambda: (np.ascontiguousarray(var),))[0]
+
+    def sliced(self, key, view, share: bool = True):
+        """The lagged, masked values of a variable (`view()` gives the lagged slice)."""
+        def make():
+            v = view()
+            return (v if self.idx is None else v[self.idx],)
+        return (make() if not share else self._get(("s",) + key, make))[0]
+
+    def has_nan(self, key, values, share: bool = True) -> bool:
+        make = lambda: (bool(np.isnan(values).any()),)
+        return (make() if not share else self._get(("n",) + key, make))[0]
+
+    def rescaled(self, key, values, pos: int, axis=None, share: bool = True):
+        """(values rescaled to zero mean, unit variance, plus noise at `pos`;
+        constant) -- a constant column comes back unchanged."""
+        def make():
+            std = values.std(axis=axis)
+            if np.any(np.abs(std) < 1e-20):
+                return values, True
+            out = (values - values.mean(axis=axis)) / std
+            out += _noise.take(pos, out.shape)
+            return out, False
+        return make() if not share else self._get(("r", pos) + key, make)
+
+
+def _prepared_task(prep: _Prep, xkey, x: FloatArray, ykey, y: FloatArray, lag: int,
+                   max_lag: int, min_lag: int, k: int, cond: Optional[FloatArray],
+                   cond_lag: FloatArray, discrete_x: bool, discrete_y: bool,
+                   preprocess: bool, share_x: bool):
+    """One task of _lagged_mi (_driver.py:788-832) without drop_nan, through
+    the per-call memo: ("task", Task) or ("value", float)."""
+    min_lag = min(min_lag, 0)
+    max_lag = max(max_lag, 0)
+    xk = (xkey, max_lag - lag)
+    yk = (ykey, max_lag)
+    xb, yb = prep.base(xkey, x), prep.base(ykey, y)
+    xs = prep.sliced(xk, lambda: xb[max_lag - lag: len(xb) - lag + min_lag], share_x)
+    ys = prep.sliced(yk, lambda: yb[max_lag: len(yb) + min_lag])
+    zs = None
+    if cond is not None:
+        zk = ("cond", tuple(int(c) for c in cond_lag))
+        zs = prep.sliced(zk, lambda: np.column_stack(
+            [cond[max_lag - cond_lag[i]: len(cond) - cond_lag[i] + min_lag, i]
+             for i in range(len(cond_lag))]))
+
+    # _validate_masked_data, in the reference's order
+    if len(ys) <= k:
+        raise ValueError(K_TOO_LARGE_MSG)
+    if (not discrete_x or xs.dtype.kind in "iufc") and prep.has_nan(xk, xs, share_x):
+        raise ValueError(NAN_MSG)
+    if (not discrete_y or ys.dtype.kind in "iufc") and prep.has_nan(yk, ys):
+        raise ValueError(NAN_MSG)
+    if not (discrete_x and discrete_y) and zs is not None and prep.has_nan(zk, zs):
+        raise ValueError(NAN_MSG)
+
+    if preprocess:
+        pos = 0
+        if not discrete_x:
+            xs, const = prep.rescaled(xk, xs, pos, share=share_x)
+            if const:
+                warn(PREPROCESS_CONSTANT_DATA_WARNING)
+            else:
+                pos += xs.size
+        if not discrete_y:
+            ys, const = prep.rescaled(yk, ys, pos)
+            if const:
+                warn(PREPROCESS_CONSTANT_DATA_WARNING)
+            else:
+                pos += ys.size
+        if zs is not None and not (discrete_x and discrete_y):
+            zs, const = prep.rescaled(zk, zs, pos, axis=0)
+            if const:
+                warn(PREPROCESS_CONSTANT_DATA_WARNING)
+    return _task_of(xs, ys, zs, k, discrete_x, discrete_y)
+
+
+def _task_of(xs, ys, zs, k: int, discrete_x: bool, discrete_y: bool):
+    """The estimator a prepared task calls (_driver.py:814-832)."""
+    if zs is None:
+        if discrete_x and discrete_y:
+            return ("value", _estimate_discrete_mi(xs, ys))
+        if discrete_x:
+            return ("task", semidiscrete_task(ys, xs, k))
+        if discrete_y:
+            return ("task", semidiscrete_task(xs, ys, k))
+        return ("task", mi_task(xs, ys, k))
+    if discrete_x and discrete_y:
+        return ("value", _estimate_conditional_discrete_mi(xs, ys, zs))
+    if discrete_x:
+        return ("task", conditional_semidiscrete_task(ys, xs, zs, k))
+    if discrete_y:
+        return ("task", conditional_semidiscrete_task(xs, ys, zs, k))
+    return ("task", cmi_task(xs, ys, zs, k))
+
+
+def _prepare_all(jobs: List[Callable[[], Tuple[str, object]]], max_threads: Optional[int]):
+    """Run the task preparations, on a thread pool when there are several
+    (NumPy releases the GIL in its array loops), and return them in order;
+    the first failing task in order raises, as in a sequential run."""
+    workers = max_threads if max_threads is not None else min(16, os.cpu_count() or 1)
+    if len(jobs) < 4 or workers <= 1:
+        return [j() for j in jobs]
+    with ThreadPoolExecutor(max_workers=min(workers, len(jobs))) as pool:
+        futures = [pool.submit(j) for j in jobs]
+        return [f.result() for f in futures]
+
+
+def _add_prepared(batch: _Batch, prepared) -> int:
+    kind, v = prepared
+    return batch.add_task(v) if kind == "task" else batch.add_value(v)
+
+
+
+def _unshared_task(x: FloatArray, y: FloatArray, lag: int, max_lag: int, min_lag: int, k: int,
+                   mask: Optional[FloatArray], cond: Optional[FloatArray], cond_lag: FloatArray,
+                   discrete_x: bool, discrete_y: bool, preprocess: bool, drop_nan: bool):
+    """One task of _lagged_mi (_driver.py:788-832) on its own: slice, mask,
+    validate, rescale; ("task", Task) or ("value", float)."""
     min_lag = min(min_lag, 0)
     max_lag = max(max_lag, 0)
     xs = x[max_lag - lag: len(x) - lag + min_lag]
@@ -483,22 +646,16 @@ def _lagged_mi_slot(batch: _Batch, x: FloatArray, y: FloatArray, lag: int, max_l
     _validate_masked_data(xs, ys, zs, k, discrete_x, discrete_y)
     if preprocess:
         xs, ys, zs = _rescale_data(xs, ys, zs, discrete_x, discrete_y)
+    return _task_of(xs, ys, zs, k, discrete_x, discrete_y)
 
-    if zs is None:
-        if discrete_x and discrete_y:
-            return batch.add_value(_estimate_discrete_mi(xs, ys))
-        if discrete_x:
-            return batch.add_task(semidiscrete_task(ys, xs, k))
-        if discrete_y:
-            return batch.add_task(semidiscrete_task(xs, ys, k))
-        return batch.add_task(mi_task(xs, ys, k))
-    if discrete_x and discrete_y:
-        return batch.add_value(_estimate_conditional_discrete_mi(xs, ys, zs))
-    if discrete_x:
-        return batch.add_task(conditional_semidiscrete_task(ys, xs, zs, k))
-    if discrete_y:
-        return batch.add_task(conditional_semidiscrete_task(xs, ys, zs, k))
-    return batch.add_task(cmi_task(xs, ys, zs, k))
+
+def _task_job(prep: _Prep, xkey, x, ykey, y, lag, max_lag, min_lag, k, mask, cond, cond_lag,
+              discrete_x, discrete_y, preprocess, drop_nan, share_x):
+    if drop_nan:
+        return lambda: _unshared_task(x, y, lag, max_lag, min_lag, k, mask, cond, cond_lag,
+                                      discrete_x, discrete_y, preprocess, drop_nan)
+    return lambda: _prepared_task(prep, xkey, x, ykey, y, lag, max_lag, min_lag, k, cond,
+                                  cond_lag, discrete_x, discrete_y, preprocess, share_x)
 
 
 def _apply_masks(xs: FloatArray, ys: FloatArray, zs: Optional[FloatArray],

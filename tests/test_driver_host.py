@@ -151,3 +151,58 @@ def test_fails_loudly_without_gpu():
     x = np.random.default_rng(0).normal(size=100)
     with pytest.raises(RuntimeError):
         eg.estimate_mi(x, x + 1)
+
+
+def _captured_inputs(monkeypatch, call, unshared):
+    """Columns of every task a public call hands to the GPU."""
+    seen = []
+
+    def run(tasks, flags=0, device=0, results_out=None):
+        for t in tasks:
+            seen.append([np.array(c, copy=True) for c in list(t.x) + list(t.y) + list(t.z)] +
+                        ([np.asarray(t.labels).copy()] if t.labels is not None else []))
+        return np.zeros(len(tasks))
+
+    with monkeypatch.context() as m:
+        m.setattr(_native, "run_tasks", run)
+        if unshared:
+            m.setattr(_driver, "_task_job",
+                      lambda prep, xkey, x, ykey, y, lag, max_lag, min_lag, k, mask, cond,
+                      cond_lag, dx, dy, pre, dn, share_x:
+                      (lambda: _driver._unshared_task(x, y, lag, max_lag, min_lag, k, mask, cond,
+                                                      cond_lag, dx, dy, pre, dn)))
+        with warnings.catch_warnings(record=True) as w:
+            warnings.simplefilter("always")
+            call()
+    return seen, len(w)
+
+
+@pytest.mark.parametrize("case", ["lags_mask", "lags_nomask", "lags_cond", "pairwise",
+                                  "pairwise_cond_mask", "pairwise_discrete", "constant"])
+def test_shared_preparation_is_bit_identical(monkeypatch, case):
+    """Columns prepared once per call equal the reference's per-task preparation."""
+    rng = np.random.default_rng(7)
+    n = 700
+    x = rng.normal(size=(n, 3))
+    y = x[:, 0] + rng.normal(size=n)
+    cond = rng.normal(size=(n, 2))
+    mask = rng.random(n) > 0.2
+    data = np.column_stack((x, y, rng.integers(0, 3, n)))
+    calls = {
+        "lags_mask": lambda: eg.estimate_mi(y, x, lag=[0, 1, 5, 1], mask=mask),
+        "lags_nomask": lambda: eg.estimate_mi(y, x, lag=[0, 2, -3]),
+        "lags_cond": lambda: eg.estimate_mi(y, x, lag=[0, 2], cond=cond, cond_lag=[[1, 0], [3, 2]],
+                                            mask=mask),
+        "pairwise": lambda: eg.pairwise_mi(data[:, :4]),
+        "pairwise_cond_mask": lambda: eg.pairwise_mi(data[:, :4], cond=cond, mask=mask),
+        "pairwise_discrete": lambda: eg.pairwise_mi(data, discrete=[False] * 4 + [True]),
+        "constant": lambda: eg.pairwise_mi(np.column_stack((x[:, :2], np.ones(n)))),
+    }
+    a, wa = _captured_inputs(monkeypatch, calls[case], unshared=False)
+    b, wb = _captured_inputs(monkeypatch, calls[case], unshared=True)
+    assert len(a) == len(b) and wa == wb
+    for ta, tb in zip(a, b):
+        assert len(ta) == len(tb)
+        for ca, cb in zip(ta, tb):
+            assert ca.dtype == cb.dtype and ca.shape == cb.shape
+            assert np.array_equal(ca.view(np.uint8), cb.view(np.uint8))
