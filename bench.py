@@ -210,7 +210,7 @@ def run_config(args, torch, N, ctx, dev):
         cases, ent = synthetic.semidiscrete_mix(seed=args.seed + 5)
         tasks = [ee.semidiscrete_task(xc, yc, args.k) for xc, yc in cases]
         tasks.append(ee.entropy_task(ent, args.k))
-        calls = [lambda: N.run_tasks(tasks, device=dev)]
+        calls = [lambda: N.run_tasks(tasks, flags=_driver.run_flags, device=dev)]
         ntask = len(tasks)
         desc = ("Ross MI of x (dim 1-4, 3-component Gaussian mixtures) vs y with 2/10/25/50 "
                 "Dirichlet(.5) classes + KL entropy of a 3-D mixture, N=500,000 (one batch)")

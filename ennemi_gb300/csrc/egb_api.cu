@@ -366,7 +366,11 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   // mode: 0 brute force, 1 slab, 2 grid (CTA items of 128 queries), 3 warp
   // grid (warp items of 32 queries); modes 1-3 carry the two sorted copies
   // (deferred queries, strip bounds), modes 2-3 the strip-ordered copy
-  struct MJob { Space s; bool is_knn; int slab; int sort_seg; int sel; int sort_seg_b; int mode; };
+  // warp-grid jobs of d >= 3 use nested cells and a third sorted column
+  struct MJob {
+    Space s; bool is_knn; int slab; int sort_seg; int sel; int sort_seg_b; int mode;
+    int sort_seg_c;
+  };
   // layout of a multi-D job: EGB_FORCE_* flags, else the context's policy
   // table, else the built-in rule; warp grid kNN needs K <= 8
   auto pick_mode = [&](bool is_knn, const Space& s) {
@@ -388,7 +392,7 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
     if (s.sp.d == 1) {
       sorted_knn.push_back({seg_for(s.task, s.sp.cols[0], s.b, s.e), s});
     } else {
-      MJob m{s, true, 0, -1, 0, -1, 0};
+      MJob m{s, true, 0, -1, 0, -1, 0, -1};
       if (s.K > EGB_KREG_MAX) m.sel = 1;
       else m.mode = pick_mode(true, s);
       m.slab = m.mode >= 1 ? 1 : 0;
@@ -396,6 +400,7 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
         m.sort_seg = seg_for(s.task, s.sp.cols[0], s.b, s.e);
         m.sort_seg_b = seg_for(s.task, s.sp.cols[1], s.b, s.e);
       }
+      if (m.mode == 3 && s.sp.d >= 3) m.sort_seg_c = seg_for(s.task, s.sp.cols[2], s.b, s.e);
       mjobs.push_back(m);
     }
   }
@@ -403,13 +408,14 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
     if (s.sp.d == 1) {
       sorted_cnt.push_back({seg_for(s.task, s.sp.cols[0], s.b, s.e), s});
     } else {
-      MJob m{s, false, 0, -1, 0, -1, 0};
+      MJob m{s, false, 0, -1, 0, -1, 0, -1};
       m.mode = pick_mode(false, s);
       m.slab = m.mode >= 1 ? 1 : 0;
       if (m.slab) {
         m.sort_seg = seg_for(s.task, s.sp.cols[0], s.b, s.e);
         m.sort_seg_b = seg_for(s.task, s.sp.cols[1], s.b, s.e);
       }
+      if (m.mode == 3 && s.sp.d >= 3) m.sort_seg_c = seg_for(s.task, s.sp.cols[2], s.b, s.e);
       mjobs.push_back(m);
     }
   }
@@ -482,6 +488,7 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   std::vector<SortSeg> gsegs;        // strip-key sort, one segment per grid job
   std::vector<int32_t> grid_jobs;    // job index of each grid job
   int64_t gsort_total = 0, max_glen = 1;
+  bool any_nested = false;
   int nblk_grid = 0;
   int64_t max_lds = 32;
   for (size_t j = 0; j < mjobs.size(); ++j) {
@@ -515,6 +522,19 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
       J.idxg = (int32_t*)(uintptr_t)dl.take(sizeof(int32_t) * (size_t)J.lds);
       J.posg = (int32_t*)(uintptr_t)dl.take(sizeof(int32_t) * (size_t)J.lds);
       J.nstrips = (int32_t)std::max<int64_t>(1, std::min<int64_t>(256, len / GRID_MIN_STRIP));
+      if (m.sort_seg_c >= 0) {
+        // nested: about NEST_CELL points per cell, as many strips as cells
+        // per strip, every cell at least GRID_MIN_STRIP / 2 points
+        int64_t side = (int64_t)std::lround(std::sqrt((double)len / NEST_CELL));
+        side = std::max<int64_t>(1, std::min<int64_t>(256, side));
+        while (side > 1 && len / (side * side) < GRID_MIN_STRIP / 2) --side;
+        J.nstrips = (int32_t)side;
+        J.nsub = (int32_t)side;
+        J.sort_seg_c = m.sort_seg_c;
+        any_nested = true;
+        J.czlo = (double*)(uintptr_t)dl.take(sizeof(double) * (size_t)(side * side));
+        J.czhi = (double*)(uintptr_t)dl.take(sizeof(double) * (size_t)(side * side));
+      }
       J.sylo = (double*)(uintptr_t)dl.take(sizeof(double) * (size_t)J.nstrips);
       J.syhi = (double*)(uintptr_t)dl.take(sizeof(double) * (size_t)J.nstrips);
       J.gseg = (int32_t)gsegs.size();
@@ -538,6 +558,7 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   const size_t off_gvals_a = dl.take(sizeof(int32_t) * (size_t)std::max<int64_t>(gsort_total, 1));
   const size_t off_gvals_b = dl.take(sizeof(int32_t) * (size_t)std::max<int64_t>(gsort_total, 1));
   const size_t off_ginv = dl.take(sizeof(int32_t) * (size_t)std::max<int64_t>(gsort_total, 1));
+  const size_t off_gsub = any_nested ? dl.take(sizeof(int32_t) * (size_t)std::max<int64_t>(gsort_total, 1)) : 0;
   const size_t off_ghist = dl.take(sizeof(uint32_t) * 256 * (size_t)std::max(nblk_grid, 1));
   const size_t off_gscan = dl.take(sizeof(uint32_t) * sort_scan_tmp_elems(std::max(nblk_grid, 1)));
 
@@ -606,10 +627,19 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
     Group& G = groups[(size_t)gidx[std::make_tuple((int)m.is_knn, m.sel, kclass, dclass, m.slab, m.mode)]];
     if (G.mode >= 2) {
       const int S = jobs[j].nstrips;
+      const int S2 = jobs[j].nsub;
       const int64_t len = jobs[j].len;
       const int qb = G.mode == 3 ? WG_QB : GRID_QB;
       for (int sidx = 0; sidx < S; ++sidx) {
         const int32_t a = strip_start(sidx, len, S), b = strip_start(sidx + 1, len, S);
+        if (S2 > 0) {  // nested: items never straddle a cell
+          for (int c2 = 0; c2 < S2; ++c2) {
+            const int32_t ca = cell_start(a, b - a, c2, S2), cb = cell_start(a, b - a, c2 + 1, S2);
+            for (int32_t q0 = ca; q0 < cb; q0 += qb)
+              G.items.push_back({(int32_t)j, q0, std::min(q0 + qb, cb), sidx | (c2 << 16)});
+          }
+          continue;
+        }
         for (int32_t q0 = a; q0 < b; q0 += qb)
           G.items.push_back({(int32_t)j, q0, std::min(q0 + qb, b), sidx});
       }
@@ -668,7 +698,12 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   const size_t tab_blkgseg = tl.take(sizeof(int32_t) * (size_t)std::max(nblk_grid, 1));
   const size_t tab_gridjobs = tl.take(sizeof(int32_t) * std::max<size_t>(grid_jobs.size(), 1));
   std::vector<size_t> tab_sstart(jobs.size(), 0);
-  for (int32_t gj : grid_jobs) tab_sstart[(size_t)gj] = tl.take(sizeof(int32_t) * (size_t)(jobs[(size_t)gj].nstrips + 1));
+  std::vector<size_t> tab_cstart(jobs.size(), 0);
+  for (int32_t gj : grid_jobs) {
+    const JobDev& J = jobs[(size_t)gj];
+    tab_sstart[(size_t)gj] = tl.take(sizeof(int32_t) * (size_t)(J.nstrips + 1));
+    if (J.nsub > 0) tab_cstart[(size_t)gj] = tl.take(sizeof(int32_t) * (size_t)(J.nstrips * J.nsub + 1));
+  }
   for (Group& G : groups) G.tab_items = tl.take(sizeof(WorkItem) * G.items.size());
   const size_t tab_cjobs = tl.take(sizeof(CombineJob) * std::max<size_t>(cjobs.size(), 1));
   const size_t tab_chunkjob = tl.take(sizeof(int32_t) * (size_t)std::max(nchunks, 1));
@@ -773,6 +808,16 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
       int32_t* st0 = (int32_t*)(H + tab_sstart[j]);
       for (int s = 0; s <= J.nstrips; ++s) st0[s] = strip_start(s, J.len, J.nstrips);
       J.sstart = (const int32_t*)(A + off_tab + tab_sstart[j]);
+      if (J.nsub > 0) {
+        J.czlo = (double*)(A + (uintptr_t)J.czlo);
+        J.czhi = (double*)(A + (uintptr_t)J.czhi);
+        int32_t* cs0 = (int32_t*)(H + tab_cstart[j]);
+        for (int s1 = 0; s1 < J.nstrips; ++s1)
+          for (int c2 = 0; c2 < J.nsub; ++c2)
+            cs0[s1 * J.nsub + c2] = cell_start(st0[s1], st0[s1 + 1] - st0[s1], c2, J.nsub);
+        cs0[J.nstrips * J.nsub] = J.len;
+        J.cstart = (const int32_t*)(A + off_tab + tab_cstart[j]);
+      }
     }
     J.jflags = (uint32_t*)(A + off_zr + zr_jflags) + j;
     J.stats = (unsigned long long*)(A + off_zr + zr_stats) + 4 * job_group[j];
@@ -832,17 +877,35 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   launch_materialize(tasks_d, (const JobDev*)dtab(tab_jobs), (int)jobs.size(), vals,
                      (const SortSeg*)dtab(tab_segs), max_lds, st);
   if (!grid_jobs.empty()) {
-    launch_grid_keys((const JobDev*)dtab(tab_jobs), (const int32_t*)dtab(tab_gridjobs),
-                     (int)grid_jobs.size(), (const SortSeg*)dtab(tab_gsegs), vals,
-                     (const SortSeg*)dtab(tab_segs), (int32_t*)(A + off_ginv),
-                     (uint64_t*)(A + off_gkeys_a), (int32_t*)(A + off_gvals_a), max_glen, st);
-    launch_radix_pass((const SortSeg*)dtab(tab_gsegs), (const int32_t*)dtab(tab_blkgseg), nblk_grid,
-                      (const uint64_t*)(A + off_gkeys_a), (const int32_t*)(A + off_gvals_a),
-                      (uint64_t*)(A + off_gkeys_b), (int32_t*)(A + off_gvals_b), 0,
-                      (uint32_t*)(A + off_ghist), (uint32_t*)(A + off_gscan), st);
+    const JobDev* jobs_d = (const JobDev*)dtab(tab_jobs);
+    const int32_t* gj_d = (const int32_t*)dtab(tab_gridjobs);
+    const int ngrid = (int)grid_jobs.size();
+    const SortSeg* gsegs_d = (const SortSeg*)dtab(tab_gsegs);
+    const int32_t* blkg_d = (const int32_t*)dtab(tab_blkgseg);
+    uint64_t* gka = (uint64_t*)(A + off_gkeys_a);
+    uint64_t* gkb = (uint64_t*)(A + off_gkeys_b);
+    int32_t* gva = (int32_t*)(A + off_gvals_a);
+    int32_t* gvb = (int32_t*)(A + off_gvals_b);
+    uint32_t* ghist = (uint32_t*)(A + off_ghist);
+    uint32_t* gscan = (uint32_t*)(A + off_gscan);
+    int32_t* ginv = (int32_t*)(A + off_ginv);
+    int32_t* gsub = any_nested ? (int32_t*)(A + off_gsub) : nullptr;
+    launch_grid_inv(jobs_d, gj_d, ngrid, gsegs_d, vals, (const SortSeg*)dtab(tab_segs), ginv, max_glen, st);
+    if (any_nested) {
+      // strips of the column-2 order -> cell of every point within its strip
+      launch_nest_key(jobs_d, gj_d, ngrid, gsegs_d, vals, (const SortSeg*)dtab(tab_segs), ginv, gka,
+                      gva, max_glen, st);
+      launch_radix_pass(gsegs_d, blkg_d, nblk_grid, gka, gva, gkb, gvb, 0, ghist, gscan, st);
+      launch_nest_sub(tasks_d, jobs_d, gj_d, ngrid, gsegs_d, gkb, gvb, gsub, max_glen, st);
+    }
+    launch_grid_key(jobs_d, gj_d, ngrid, gsegs_d, vals, (const SortSeg*)dtab(tab_segs), ginv, gsub, gka,
+                    gva, max_glen, st);
+    launch_radix_pass(gsegs_d, blkg_d, nblk_grid, gka, gva, gkb, gvb, 0, ghist, gscan, st);
+    if (any_nested)  // cell keys reach 16 bits: second digit
+      launch_radix_pass(gsegs_d, blkg_d, nblk_grid, gkb, gvb, gka, gva, 8, ghist, gscan, st);
     launch_materialize_grid(tasks_d, (const JobDev*)dtab(tab_jobs), (const int32_t*)dtab(tab_gridjobs),
                             (int)grid_jobs.size(), vals, (const SortSeg*)dtab(tab_segs),
-                            (const int32_t*)(A + off_gvals_b), (const SortSeg*)dtab(tab_gsegs),
+                            any_nested ? gva : gvb, (const SortSeg*)dtab(tab_gsegs),
                             max_lds, st);
   }
   if (timing) EGB_CUDA(cudaEventRecord(ctx->ev[3], st));

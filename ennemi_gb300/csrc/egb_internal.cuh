@@ -169,6 +169,14 @@ struct JobDev {
   const int32_t* sstart;  // grid: nstrips + 1 strip starts (strip_start table)
   double* sylo;           // grid: smallest column-1 value of each strip
   double* syhi;           // grid: largest column-1 value of each strip
+  // nested grid (warp-grid jobs of d >= 3): every strip split again into nsub
+  // equal-count cells by the rank of column 2 within the strip, each cell
+  // sorted by column 0; nsub == 0 for plain strips
+  int32_t nsub;
+  int32_t sort_seg_c;     // nested: sort segment of column 2
+  const int32_t* cstart;  // nstrips * nsub + 1 cell starts (cell_start table)
+  double* czlo;           // smallest column-2 value of each cell
+  double* czhi;           // largest column-2 value of each cell
   // work counters of this job's launch group: [0] pairs screened by tile
   // items, [1] pairs screened by deferred-query warps, [2] queries deferred
   unsigned long long* stats;
@@ -180,6 +188,13 @@ struct JobDev {
 __host__ __device__ __forceinline__ int32_t strip_start(int64_t s, int64_t len, int32_t nstrips) {
   return (int32_t)((s * len + nstrips - 1) / nstrips);
 }
+// Cell c2 of a strip starting at s0 with length L holds the within-strip
+// column-2 ranks [strip_start(c2, L, nsub), strip_start(c2 + 1, L, nsub)).
+__host__ __device__ __forceinline__ int32_t cell_start(int32_t s0, int32_t L, int32_t c2,
+                                                       int32_t nsub) {
+  return s0 + strip_start(c2, L, nsub);
+}
+constexpr int NEST_CELL = 768;   // target points per nested-grid cell
 constexpr int GRID_QB = 128;     // queries per grid work item
 constexpr int GRID_TILE = 128;   // candidates per grid tile
 constexpr int GRID_MIN_STRIP = 64;
@@ -188,7 +203,8 @@ struct WorkItem {         // one tile of queries of one job
   int32_t job;
   int32_t q0;
   int32_t q1;             // grid items: end of the query range (exclusive)
-  int32_t strip;          // grid items: the strip holding the queries
+  int32_t strip;          // grid items: the strip holding the queries (nested
+                          // grids: strip | cell << 16)
 };
 
 // A slab query whose search a tile work item left unfinished (it needed a
@@ -268,13 +284,31 @@ void launch_combine(const TaskDev* tasks_d, const CombineJob* jobs_d, const int3
 
 // egb_sort.cu
 constexpr int SORT_TILE = 2048;
-// Strip keys of the grid jobs: keys[p] = strip of the point at column-0
-// position p (its column-1 rank * nstrips / len), vals[p] = p; then one
-// stable 8-bit radix pass orders each segment by (strip, column 0).
-void launch_grid_keys(const JobDev* jobs_d, const int32_t* grid_jobs_d, int ngrid,
-                      const SortSeg* gsegs_d, const int32_t* sorted_vals, const SortSeg* segs_d,
-                      int32_t* inv_scratch, uint64_t* gkeys, int32_t* gvals, int64_t max_len,
-                      cudaStream_t st);
+// Strip keys of the grid jobs.  launch_grid_inv: inv[p_B] = column-1 rank
+// of each point (by working offset).  launch_grid_key: keys[p] = cell key of
+// the point at column-0 position p -- its strip (column-1 rank * nstrips /
+// len), times nsub plus its cell (nested grids, from sub[]) -- and vals[p] =
+// p; stable 8-bit radix passes then order each segment by (key, column 0).
+void launch_grid_inv(const JobDev* jobs_d, const int32_t* grid_jobs_d, int ngrid,
+                     const SortSeg* gsegs_d, const int32_t* sorted_vals, const SortSeg* segs_d,
+                     int32_t* inv_scratch, int64_t max_len, cudaStream_t st);
+void launch_grid_key(const JobDev* jobs_d, const int32_t* grid_jobs_d, int ngrid,
+                     const SortSeg* gsegs_d, const int32_t* sorted_vals, const SortSeg* segs_d,
+                     const int32_t* inv_scratch, const int32_t* sub, uint64_t* gkeys,
+                     int32_t* gvals, int64_t max_len, cudaStream_t st);
+// Nested grids.  launch_nest_key: over the column-2 order of each nested job,
+// keys[r] = strip of the point at column-2 position r, vals[r] = its working
+// offset (non-nested jobs: zeros).  After one stable radix pass (strips in
+// column-2 order), launch_nest_sub: sub[w] = cell of point w within its strip
+// (its within-strip column-2 rank * nsub / strip length), and the column-2
+// bounds czlo / czhi of every cell.
+void launch_nest_key(const JobDev* jobs_d, const int32_t* grid_jobs_d, int ngrid,
+                     const SortSeg* gsegs_d, const int32_t* sorted_vals, const SortSeg* segs_d,
+                     const int32_t* inv_scratch, uint64_t* keys, int32_t* vals, int64_t max_len,
+                     cudaStream_t st);
+void launch_nest_sub(const TaskDev* tasks_d, const JobDev* jobs_d, const int32_t* grid_jobs_d,
+                     int ngrid, const SortSeg* gsegs_d, const uint64_t* keys_sorted,
+                     const int32_t* vals_sorted, int32_t* sub, int64_t max_len, cudaStream_t st);
 void launch_radix_pass(const SortSeg* segs_d, const int32_t* blk_seg_d, int nblk,
                        const uint64_t* kin, const int32_t* vin, uint64_t* kout, int32_t* vout,
                        int shift, uint32_t* hist, uint32_t* scan_tmp, cudaStream_t st);

@@ -295,8 +295,32 @@ __global__ void grid_inv_kernel(const JobDev* __restrict__ jobs,
   }
 }
 
-// keys[out + p_A] = strip of the point at column-0 position p_A; vals = p_A.
+// keys[out + p_A] = cell key of the point at column-0 position p_A; vals = p_A.
 __global__ void grid_key_kernel(const JobDev* __restrict__ jobs,
+                                const int32_t* __restrict__ grid_jobs, int ngrid,
+                                const SortSeg* __restrict__ gsegs,
+                                const int32_t* __restrict__ sorted_vals,
+                                const SortSeg* __restrict__ segs,
+                                const int32_t* __restrict__ inv, const int32_t* __restrict__ sub,
+                                uint64_t* __restrict__ keys, int32_t* __restrict__ vals) {
+  for (int g = blockIdx.y; g < ngrid; g += gridDim.y) {
+    const JobDev& J = jobs[grid_jobs[g]];
+    const int64_t out = gsegs[J.gseg].out_base;
+    const int32_t* va = sorted_vals + segs[J.sort_seg].out_base;
+    const int64_t len = J.len;
+    const int nsub = J.nsub;
+    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < len;
+         p += (int64_t)gridDim.x * blockDim.x) {
+      const int64_t w = va[p] - J.seg_begin;
+      const int64_t strip = (int64_t)inv[out + w] * J.nstrips / len;
+      keys[out + p] = (uint64_t)(nsub > 0 ? strip * nsub + sub[out + w] : strip);
+      vals[out + p] = (int32_t)p;
+    }
+  }
+}
+
+// keys[out + r] = strip of the point at column-2 position r; vals = its offset.
+__global__ void nest_key_kernel(const JobDev* __restrict__ jobs,
                                 const int32_t* __restrict__ grid_jobs, int ngrid,
                                 const SortSeg* __restrict__ gsegs,
                                 const int32_t* __restrict__ sorted_vals,
@@ -306,33 +330,100 @@ __global__ void grid_key_kernel(const JobDev* __restrict__ jobs,
   for (int g = blockIdx.y; g < ngrid; g += gridDim.y) {
     const JobDev& J = jobs[grid_jobs[g]];
     const int64_t out = gsegs[J.gseg].out_base;
-    const int32_t* va = sorted_vals + segs[J.sort_seg].out_base;
     const int64_t len = J.len;
-    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < len;
-         p += (int64_t)gridDim.x * blockDim.x) {
-      const int64_t rank_b = inv[out + (va[p] - J.seg_begin)];
-      keys[out + p] = (uint64_t)(rank_b * J.nstrips / len);
-      vals[out + p] = (int32_t)p;
+    const bool nested = J.nsub > 0;
+    const int32_t* vc = nested ? sorted_vals + segs[J.sort_seg_c].out_base : nullptr;
+    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < len;
+         r += (int64_t)gridDim.x * blockDim.x) {
+      if (nested) {
+        const int32_t w = vc[r] - J.seg_begin;
+        keys[out + r] = (uint64_t)((int64_t)inv[out + w] * J.nstrips / len);
+        vals[out + r] = w;
+      } else {
+        keys[out + r] = 0;
+        vals[out + r] = (int32_t)r;
+      }
     }
   }
 }
 
-}  // namespace
+// After the strip pass over the column-2 order: position p2 of strip s1
+// holds within-strip column-2 rank p2 - sstart[s1].
+__global__ void nest_sub_kernel(const TaskDev* __restrict__ tasks,
+                                const JobDev* __restrict__ jobs,
+                                const int32_t* __restrict__ grid_jobs, int ngrid,
+                                const SortSeg* __restrict__ gsegs,
+                                const uint64_t* __restrict__ keys_sorted,
+                                const int32_t* __restrict__ vals_sorted,
+                                int32_t* __restrict__ sub) {
+  for (int g = blockIdx.y; g < ngrid; g += gridDim.y) {
+    const JobDev& J = jobs[grid_jobs[g]];
+    if (J.nsub <= 0) continue;
+    const TaskDev& t = tasks[J.task];
+    const int64_t out = gsegs[J.gseg].out_base;
+    const int nsub = J.nsub;
+    const double* z = t.x64 + (int64_t)J.sp.cols[2] * t.ld + J.seg_begin;
+    for (int64_t p2 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p2 < J.len;
+         p2 += (int64_t)gridDim.x * blockDim.x) {
+      const int s1 = (int)keys_sorted[out + p2];
+      const int32_t w = vals_sorted[out + p2];
+      const int32_t s0 = J.sstart[s1];
+      const int32_t L = J.sstart[s1 + 1] - s0;
+      const int c2 = (int)((p2 - s0) * nsub / L);
+      sub[out + w] = c2;
+      const int cell = s1 * nsub + c2;
+      if (p2 == J.cstart[cell]) J.czlo[cell] = z[w];
+      if (p2 == J.cstart[cell + 1] - 1) J.czhi[cell] = z[w];
+    }
+  }
+}
 
-void launch_grid_keys(const JobDev* jobs_d, const int32_t* grid_jobs_d, int ngrid,
-                      const SortSeg* gsegs_d, const int32_t* sorted_vals, const SortSeg* segs_d,
-                      int32_t* inv_scratch, uint64_t* gkeys, int32_t* gvals, int64_t max_len,
-                      cudaStream_t st) {
-  if (ngrid <= 0) return;
+dim3 grid_of(int ngrid, int64_t max_len) {
   int gx = (int)((max_len + 255) / 256);
   if (gx > 1024) gx = 1024;
   if (gx < 1) gx = 1;
-  dim3 grid(gx, ngrid > 65535 ? 65535 : ngrid);
-  grid_inv_kernel<<<grid, 256, 0, st>>>(jobs_d, grid_jobs_d, ngrid, gsegs_d, sorted_vals, segs_d,
-                                        inv_scratch);
+  return dim3(gx, ngrid > 65535 ? 65535 : ngrid);
+}
+
+}  // namespace
+
+void launch_grid_inv(const JobDev* jobs_d, const int32_t* grid_jobs_d, int ngrid,
+                     const SortSeg* gsegs_d, const int32_t* sorted_vals, const SortSeg* segs_d,
+                     int32_t* inv_scratch, int64_t max_len, cudaStream_t st) {
+  if (ngrid <= 0) return;
+  grid_inv_kernel<<<grid_of(ngrid, max_len), 256, 0, st>>>(jobs_d, grid_jobs_d, ngrid, gsegs_d,
+                                                           sorted_vals, segs_d, inv_scratch);
   count_launch();
-  grid_key_kernel<<<grid, 256, 0, st>>>(jobs_d, grid_jobs_d, ngrid, gsegs_d, sorted_vals, segs_d,
-                                        inv_scratch, gkeys, gvals);
+}
+
+void launch_grid_key(const JobDev* jobs_d, const int32_t* grid_jobs_d, int ngrid,
+                     const SortSeg* gsegs_d, const int32_t* sorted_vals, const SortSeg* segs_d,
+                     const int32_t* inv_scratch, const int32_t* sub, uint64_t* gkeys,
+                     int32_t* gvals, int64_t max_len, cudaStream_t st) {
+  if (ngrid <= 0) return;
+  grid_key_kernel<<<grid_of(ngrid, max_len), 256, 0, st>>>(jobs_d, grid_jobs_d, ngrid, gsegs_d,
+                                                           sorted_vals, segs_d, inv_scratch, sub,
+                                                           gkeys, gvals);
+  count_launch();
+}
+
+void launch_nest_key(const JobDev* jobs_d, const int32_t* grid_jobs_d, int ngrid,
+                     const SortSeg* gsegs_d, const int32_t* sorted_vals, const SortSeg* segs_d,
+                     const int32_t* inv_scratch, uint64_t* keys, int32_t* vals, int64_t max_len,
+                     cudaStream_t st) {
+  if (ngrid <= 0) return;
+  nest_key_kernel<<<grid_of(ngrid, max_len), 256, 0, st>>>(jobs_d, grid_jobs_d, ngrid, gsegs_d,
+                                                           sorted_vals, segs_d, inv_scratch, keys,
+                                                           vals);
+  count_launch();
+}
+
+void launch_nest_sub(const TaskDev* tasks_d, const JobDev* jobs_d, const int32_t* grid_jobs_d,
+                     int ngrid, const SortSeg* gsegs_d, const uint64_t* keys_sorted,
+                     const int32_t* vals_sorted, int32_t* sub, int64_t max_len, cudaStream_t st) {
+  if (ngrid <= 0) return;
+  nest_sub_kernel<<<grid_of(ngrid, max_len), 256, 0, st>>>(tasks_d, jobs_d, grid_jobs_d, ngrid,
+                                                           gsegs_d, keys_sorted, vals_sorted, sub);
   count_launch();
 }
 

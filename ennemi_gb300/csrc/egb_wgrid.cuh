@@ -153,7 +153,7 @@ __device__ __forceinline__ V warp_kth_of_lists(const V (&lst_in)[KMAX], int K, V
   return kth;
 }
 
-template <int D, int KMAX, bool PLAIN, bool COUNT>
+template <int D, int KMAX, bool PLAIN, bool COUNT, bool NEST>
 __global__ void __launch_bounds__(WG_WARPS * 32)
 wgrid_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items, int nitems,
              int* __restrict__ counter, int dmax) {
@@ -187,6 +187,11 @@ wgrid_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items
     const double* __restrict__ ylo_t = J->sylo;       // strip column-1 bounds
     const double* __restrict__ yhi_t = J->syhi;
     const int S = J->nstrips;
+    // nested grids: cells of strip s are s * S2 .. s * S2 + S2 - 1
+    const int S2 = NEST ? J->nsub : 1;
+    const int32_t* __restrict__ cst = J->cstart;
+    const double* __restrict__ czlo = J->czlo;
+    const double* __restrict__ czhi = J->czhi;
     const bool unsafe = !PLAIN && ((*J->jflags & TF_UNSAFE32) != 0u);
     const int K = COUNT ? 1 : J->K;
 
@@ -207,6 +212,7 @@ wgrid_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items
     const float mq = __double2float_ru(m);
     const double qx = exists ? c64[qp] : 0.0;
     const double qy = exists ? c64[lds + qp] : 0.0;
+    const double qz = (NEST && exists) ? c64[2 * lds + qp] : 0.0;
 
     // ---- per-lane state
     uint64_t top[COUNT ? 1 : KMAX];      // exact list (bit patterns)
@@ -389,10 +395,58 @@ wgrid_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items
       }
     };
 
-    const int sq = wi.strip;
-    const int hs0 = sst[sq], hs1 = sst[sq + 1];
+    const int sq = NEST ? (wi.strip & 0xffff) : wi.strip;
+    const int hc2 = NEST ? (wi.strip >> 16) : 0;  // home cell within the strip
+    const int hs0 = NEST ? cst[sq * S2 + hc2] : sst[sq];
+    const int hs1 = NEST ? cst[sq * S2 + hc2 + 1] : sst[sq + 1];
     const double xa = c64[wi.q0];
     const double xb = c64[wi.q1 - 1];
+    // column-2 centre of the item (nested grids: where other strips start)
+    const double zmid = NEST ? __shfl_sync(0xffffffffu, qz, (nq - 1) >> 1) : 0.0;
+
+    // Nested grids: first cell of strip s whose column-2 range reaches z.
+    auto start_cell = [&](int s, double z) -> int {
+      int c0 = 0;
+      for (int b = 0; b < S2; b += 32) {
+        const int c = b + lane;
+        c0 += __popc(__ballot_sync(0xffffffffu, c < S2 && czhi[s * S2 + c] < z));
+      }
+      return c0 < S2 ? c0 : S2 - 1;
+    };
+    // Nested grids: the cells of strip s that some lane still needs, outward
+    // in column 2 from cell c0 (cell `skip` already scanned).  A lane needs a
+    // cell while the strip's column-1 range and the cell's column-2 range are
+    // both within its threshold; cells are ordered by column 2, so each
+    // direction ends at the first cell that no lane reaches.
+    auto visit_cells = [&](int s, int c0, int skip) {
+      const int cb = s * S2;
+      int up2 = c0, dn2 = c0 - 1;
+      bool tu = true;
+      for (;;) {
+        const double t = tq();
+        const bool reach = qok && !(ylo_t[s] - qy > t) && !(qy - yhi_t[s] > t);
+        const bool ou = reach && up2 < S2 && !(czlo[cb + up2] - qz > t);
+        const bool od = reach && dn2 >= 0 && !(qz - czhi[cb + dn2] > t);
+        const bool any_u = __any_sync(0xffffffffu, ou);
+        const bool any_d = __any_sync(0xffffffffu, od);
+        if (!any_u && !any_d) break;
+        int c;
+        if ((tu && any_u) || !any_d) {
+          c = up2++;
+          tu = false;
+        } else {
+          c = dn2--;
+          tu = true;
+        }
+        if (c == skip) continue;
+        const bool nd = reach && !(czlo[cb + c] - qz > t) && !(qz - czhi[cb + c] > t);
+        if (!__any_sync(0xffffffffu, nd)) continue;
+        const double Tw = bits_to_double(warp_max_u64(nd ? tq_bits() : 0ull));
+        int wl, wh;
+        warp_window(c64, cst[cb + c], cst[cb + c + 1], xa - Tw, xb + Tw, wl, wh);
+        scan(wl, wh);
+      }
+    };
 
 #pragma unroll 1
     for (; pass < 2; ++pass) {
@@ -411,6 +465,7 @@ wgrid_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items
         scan(wl, min(wh, wi.q0));
         scan(max(wl, wi.q1), wh);
       }
+      if constexpr (NEST) visit_cells(sq, hc2, hc2);  // the rest of the home strip
 
       // ---- other strips
       int up = sq + 1, dn = sq - 1;
@@ -440,10 +495,14 @@ wgrid_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items
           s = dn--;
           turn_up = true;
         }
-        const double Tw = bits_to_double(warp_max_u64(unf ? tq_bits() : 0ull));
-        int wl, wh;
-        warp_window(c64, sst[s], sst[s + 1], xa - Tw, xb + Tw, wl, wh);
-        scan(wl, wh);
+        if constexpr (NEST) {
+          visit_cells(s, start_cell(s, zmid), -1);
+        } else {
+          const double Tw = bits_to_double(warp_max_u64(unf ? tq_bits() : 0ull));
+          int wl, wh;
+          warp_window(c64, sst[s], sst[s + 1], xa - Tw, xb + Tw, wl, wh);
+          scan(wl, wh);
+        }
       }
 
       // ---- remaining unfinished queries: one at a time, all lanes cooperating
@@ -453,6 +512,7 @@ wgrid_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items
         rest &= rest - 1u;
         const double oqx = __shfl_sync(0xffffffffu, qx, ol);
         const double oqy = __shfl_sync(0xffffffffu, qy, ol);
+        const double oqz = __shfl_sync(0xffffffffu, qz, ol);
         const float omq = __shfl_sync(0xffffffffu, mq, ol);
         T oqv[DQ];
 #pragma unroll
@@ -556,10 +616,24 @@ wgrid_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items
           if (!ou && !od) break;
           const int s = ou && (!od || (oup - sq) <= (sq - odn)) ? oup++ : odn--;
           int wl, wh;
-          warp_window(c64, sst[s], sst[s + 1], oqx - tb, oqx + tb,
-                      wl, wh);
-          pairs += (unsigned long long)(wh > wl ? wh - wl : 0);
-          oscan(wl, wh);
+          if constexpr (NEST) {
+            // cells with column-2 range meeting [oqz - tb, oqz + tb]: a run
+            int clo = 0, chi = 0;
+            for (int b = 0; b < S2; b += 32) {
+              const int c = b + lane;
+              clo += __popc(__ballot_sync(0xffffffffu, c < S2 && czhi[s * S2 + c] < oqz - tb));
+              chi += __popc(__ballot_sync(0xffffffffu, c < S2 && czlo[s * S2 + c] <= oqz + tb));
+            }
+            for (int c = clo; c < chi; ++c) {
+              warp_window(c64, cst[s * S2 + c], cst[s * S2 + c + 1], oqx - tb, oqx + tb, wl, wh);
+              pairs += (unsigned long long)(wh > wl ? wh - wl : 0);
+              oscan(wl, wh);
+            }
+          } else {
+            warp_window(c64, sst[s], sst[s + 1], oqx - tb, oqx + tb, wl, wh);
+            pairs += (unsigned long long)(wh > wl ? wh - wl : 0);
+            oscan(wl, wh);
+          }
         }
         if constexpr (COUNT) {
           const int add = __reduce_add_sync(0xffffffffu, cnt2);
@@ -599,10 +673,11 @@ wgrid_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items
   }
 }
 
+// d >= 3 (D != 2) runs on nested grids.
 template <int D, int KMAX, bool PLAIN, bool COUNT>
 void launch_wgrid_t(const JobDev* jobs, const WorkItem* items, int nitems, int* counter, int dmax,
                     int num_sms, cudaStream_t st) {
-  auto kern = wgrid_kernel<D, KMAX, PLAIN, COUNT>;
+  auto kern = wgrid_kernel<D, KMAX, PLAIN, COUNT, D != 2>;
   int per_sm = 1;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, WG_WARPS * 32, 0);
   if (per_sm < 1) per_sm = 1;

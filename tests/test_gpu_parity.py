@@ -119,6 +119,13 @@ def _medium_cases():
     yield "ent_9d_3k", "ent", 4, dict(x=rng.normal(size=(3000, 9)))
     big = rng.normal(size=(5000, 2))
     yield "mi_huge_unsafe32_5k", "mi", 3, dict(x=1e300 * big[:, 0], y=big[:, 1])
+    # nested-cell grids (d >= 3): generic d, heavy ties, K = 8, 4-D counts
+    yield "ent_5d_12k", "ent", 3, dict(x=rng.normal(size=(12000, 5)))
+    c3r = np.round(c3, 1)
+    yield "cmi_rounded3_20k", "cmi", 3, dict(x=c3r[:, 0], y=c3r[:, 1], z=c3r[:, 2:])
+    yield "ent_3d_k7_20k", "ent", 7, dict(x=rng.standard_t(4, size=(n, 3)))
+    c6 = rng.normal(size=(10000, 5))
+    yield "cmi_dz3_10k", "cmi", 3, dict(x=c6[:, 0], y=c6[:, 1] + 0.5 * c6[:, 2], z=c6[:, 2:])
 
 
 MEDIUM = list(_medium_cases())
