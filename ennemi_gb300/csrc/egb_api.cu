@@ -534,9 +534,13 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
         any_nested = true;
         J.czlo = (double*)(uintptr_t)dl.take(sizeof(double) * (size_t)(side * side));
         J.czhi = (double*)(uintptr_t)dl.take(sizeof(double) * (size_t)(side * side));
+        J.czlo32 = (float*)(uintptr_t)dl.take(sizeof(float) * (size_t)(side * side));
+        J.czhi32 = (float*)(uintptr_t)dl.take(sizeof(float) * (size_t)(side * side));
       }
       J.sylo = (double*)(uintptr_t)dl.take(sizeof(double) * (size_t)J.nstrips);
       J.syhi = (double*)(uintptr_t)dl.take(sizeof(double) * (size_t)J.nstrips);
+      J.sylo32 = (float*)(uintptr_t)dl.take(sizeof(float) * (size_t)J.nstrips);
+      J.syhi32 = (float*)(uintptr_t)dl.take(sizeof(float) * (size_t)J.nstrips);
       J.gseg = (int32_t)gsegs.size();
       SortSeg g{};
       g.out_base = gsort_total;
@@ -805,12 +809,16 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
       J.posg = (int32_t*)(A + (uintptr_t)J.posg);
       J.sylo = (double*)(A + (uintptr_t)J.sylo);
       J.syhi = (double*)(A + (uintptr_t)J.syhi);
+      J.sylo32 = (float*)(A + (uintptr_t)J.sylo32);
+      J.syhi32 = (float*)(A + (uintptr_t)J.syhi32);
       int32_t* st0 = (int32_t*)(H + tab_sstart[j]);
       for (int s = 0; s <= J.nstrips; ++s) st0[s] = strip_start(s, J.len, J.nstrips);
       J.sstart = (const int32_t*)(A + off_tab + tab_sstart[j]);
       if (J.nsub > 0) {
         J.czlo = (double*)(A + (uintptr_t)J.czlo);
         J.czhi = (double*)(A + (uintptr_t)J.czhi);
+        J.czlo32 = (float*)(A + (uintptr_t)J.czlo32);
+        J.czhi32 = (float*)(A + (uintptr_t)J.czhi32);
         int32_t* cs0 = (int32_t*)(H + tab_cstart[j]);
         for (int s1 = 0; s1 < J.nstrips; ++s1)
           for (int c2 = 0; c2 < J.nsub; ++c2)

@@ -177,6 +177,12 @@ struct JobDev {
   const int32_t* cstart;  // nstrips * nsub + 1 cell starts (cell_start table)
   double* czlo;           // smallest column-2 value of each cell
   double* czhi;           // largest column-2 value of each cell
+  // the strip and cell bounds centred and rounded outward to FP32
+  // (lower bounds down, upper bounds up): the FP32 kernels plan on these
+  float* sylo32;
+  float* syhi32;
+  float* czlo32;
+  float* czhi32;
   // work counters of this job's launch group: [0] pairs screened by tile
   // items, [1] pairs screened by deferred-query warps, [2] queries deferred
   unsigned long long* stats;

@@ -156,8 +156,12 @@ __global__ void materialize_grid_kernel(const TaskDev* __restrict__ tasks,
     const int32_t* gv = gvals_sorted + gsegs[J.gseg].out_base;
     // column-1 bounds of each strip, from the column-1 sorted copy
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < J.nstrips; s += gridDim.x * blockDim.x) {
-      J.sylo[s] = J.c64b[J.lds + J.sstart[s]];
-      J.syhi[s] = J.c64b[J.lds + J.sstart[s + 1] - 1];
+      const double lo = J.c64b[J.lds + J.sstart[s]];
+      const double hi = J.c64b[J.lds + J.sstart[s + 1] - 1];
+      J.sylo[s] = lo;
+      J.syhi[s] = hi;
+      J.sylo32[s] = __double2float_rd(__dsub_rd(lo, J.center[1]));
+      J.syhi32[s] = __double2float_ru(__dsub_ru(hi, J.center[1]));
     }
     for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < J.lds;
          p += (int64_t)gridDim.x * blockDim.x) {

@@ -372,8 +372,14 @@ __global__ void nest_sub_kernel(const TaskDev* __restrict__ tasks,
       const int c2 = (int)((p2 - s0) * nsub / L);
       sub[out + w] = c2;
       const int cell = s1 * nsub + c2;
-      if (p2 == J.cstart[cell]) J.czlo[cell] = z[w];
-      if (p2 == J.cstart[cell + 1] - 1) J.czhi[cell] = z[w];
+      if (p2 == J.cstart[cell]) {
+        J.czlo[cell] = z[w];
+        J.czlo32[cell] = __double2float_rd(__dsub_rd(z[w], J.center[2]));
+      }
+      if (p2 == J.cstart[cell + 1] - 1) {
+        J.czhi[cell] = z[w];
+        J.czhi32[cell] = __double2float_ru(__dsub_ru(z[w], J.center[2]));
+      }
     }
   }
 }

@@ -68,11 +68,25 @@ __device__ __forceinline__ uint64_t warp_min_u64(uint64_t v) {
   return v;
 }
 
+// Conservative FP32 planning values.  A grid copy holds, per coordinate,
+// f(v) = fl32(clamp(fl64(v - c), +-1e37)), monotone in v.  lo32_of / hi32_of
+// bound v - c from below / above; plan_margin(t) >= t (1 + 2^-20), so that a
+// candidate skipped because its coordinate gap exceeds plan_margin(t) has an
+// FP64 coordinate distance fl64(gap) >= gap (1 - 2^-53) > t.
+__device__ __forceinline__ float lo32_of(double v, double c) {
+  return __double2float_rd(__dsub_rd(v, c));
+}
+__device__ __forceinline__ float hi32_of(double v, double c) {
+  return __double2float_ru(__dsub_ru(v, c));
+}
+__device__ __forceinline__ float plan_margin(float t) { return __fmul_ru(t, 1.0f + 0x1p-20f); }
+
 // Exact window of strip [s0, s1) for column-0 values [xlo, xhi]: the lower
 // half-warp finds the first position with x >= xlo, the upper half the first
 // with x > xhi.
-__device__ __forceinline__ void warp_window(const double* x, int s0, int s1, double xlo,
-                                            double xhi, int& wlo, int& whi) {
+template <typename V>
+__device__ __forceinline__ void warp_window(const V* x, int s0, int s1, V xlo, V xhi, int& wlo,
+                                            int& whi) {
   const int lane = threadIdx.x & 31;
   const bool upper = lane >= 16;
   const int l16 = lane & 15;
@@ -85,7 +99,7 @@ __device__ __forceinline__ void warp_window(const double* x, int s0, int s1, dou
     int p = small ? lo + l16 : lo + (int)((int64_t)(l16 + 1) * n / 17);
     const bool inr = p < hi;
     p = inr ? p : s0;
-    const double v = x[p];
+    const V v = x[p];
     const bool t = inr && (upper ? (v <= xhi) : (v < xlo));
     const unsigned b = __ballot_sync(0xffffffffu, t) & m;
     const int c = __popc(b);
@@ -169,6 +183,11 @@ wgrid_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items
   constexpr float FINF = __builtin_huge_valf();
   const int lane = threadIdx.x & 31;
   (void)dmax;
+  // Planning -- window ends, strip and cell tests, thresholds -- is in type
+  // T: the FP64 comparator plans on the exact values; the FP32 path plans on
+  // centred FP32 values with outward-directed rounding and plan_margin(), so
+  // it visits a superset of the candidates exact planning would (GB300
+  // issues FP64 at a small fraction of the FP32 rate).
 
   for (;;) {
     int it = 0;
@@ -184,14 +203,16 @@ wgrid_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items
     const T* __restrict__ g = PLAIN ? reinterpret_cast<const T*>(J->c64g)
                                     : reinterpret_cast<const T*>(J->c32g);
     const int32_t* __restrict__ sst = J->sstart;      // strip starts
-    const double* __restrict__ ylo_t = J->sylo;       // strip column-1 bounds
-    const double* __restrict__ yhi_t = J->syhi;
+    const T* __restrict__ wx = g;                     // column 0: window searches
+    // strip column-1 bounds and (nested) cell column-2 bounds
+    const T* __restrict__ ylo_t = reinterpret_cast<const T*>(PLAIN ? (const void*)J->sylo : (const void*)J->sylo32);
+    const T* __restrict__ yhi_t = reinterpret_cast<const T*>(PLAIN ? (const void*)J->syhi : (const void*)J->syhi32);
     const int S = J->nstrips;
     // nested grids: cells of strip s are s * S2 .. s * S2 + S2 - 1
     const int S2 = NEST ? J->nsub : 1;
     const int32_t* __restrict__ cst = J->cstart;
-    const double* __restrict__ czlo = J->czlo;
-    const double* __restrict__ czhi = J->czhi;
+    const T* __restrict__ czlo = reinterpret_cast<const T*>(PLAIN ? (const void*)J->czlo : (const void*)J->czlo32);
+    const T* __restrict__ czhi = reinterpret_cast<const T*>(PLAIN ? (const void*)J->czhi : (const void*)J->czhi32);
     const bool unsafe = !PLAIN && ((*J->jflags & TF_UNSAFE32) != 0u);
     const int K = COUNT ? 1 : J->K;
 
@@ -213,12 +234,28 @@ wgrid_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items
     const double qx = exists ? c64[qp] : 0.0;
     const double qy = exists ? c64[lds + qp] : 0.0;
     const double qz = (NEST && exists) ? c64[2 * lds + qp] : 0.0;
+    // planning bounds of the query's coordinates 0..2
+    T qxl, qxh, qyl, qyh, qzl, qzh;
+    if constexpr (PLAIN) {
+      qxl = qxh = qx;
+      qyl = qyh = qy;
+      qzl = qzh = qz;
+    } else {
+      qxl = exists ? lo32_of(qx, J->center[0]) : 0.0f;
+      qxh = exists ? hi32_of(qx, J->center[0]) : 0.0f;
+      qyl = exists ? lo32_of(qy, J->center[1]) : 0.0f;
+      qyh = exists ? hi32_of(qy, J->center[1]) : 0.0f;
+      qzl = (NEST && exists) ? lo32_of(qz, J->center[2]) : 0.0f;
+      qzh = (NEST && exists) ? hi32_of(qz, J->center[2]) : 0.0f;
+    }
 
     // ---- per-lane state
     uint64_t top[COUNT ? 1 : KMAX];      // exact list (bit patterns)
     float l32[TWO_PASS ? KMAX : 1];      // FP32 list (pass 0)
     double ufix = 0.0;                    // pass 1: fixed bound of the k-th distance
+    float u32fix = 0.0f;                  // the same bound (a float)
     float sfix = 0.0f;                    // pass 1: FP32 screen threshold
+    float tcnt = -1.0f;                   // FP32 counts: planning threshold
     double qr = -1.0;
     uint64_t rbits = 0;
     float lo = -1.0f, hi = -1.0f;
@@ -229,6 +266,7 @@ wgrid_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items
       qr = exists ? J->rad[J->idxg[qp]] : -1.0;
       qok = exists && (qr >= 0.0);
       rbits = qok ? (uint64_t)__double_as_longlong(qr) : 0ull;
+      if (!PLAIN && qok) tcnt = plan_margin(__double2float_ru(qr));
       if (!PLAIN && qok) {
         if (isinf(qr)) {
           lo = hi = FINF;
@@ -260,9 +298,43 @@ wgrid_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items
         return bits_to_double(top[KMAX - 1]);
       }
     };
-    auto tq_bits = [&]() -> uint64_t {
-      const double t = tq();
-      return t >= 0.0 ? (uint64_t)__double_as_longlong(t) : 0ull;
+    // the same as a planning value (negative: nothing needed)
+    auto tqp = [&]() -> T {
+      if constexpr (PLAIN) {
+        return tq();
+      } else {
+        if (!qok) return -1.0f;
+        if constexpr (COUNT) return tcnt;
+        else return pass == 0 ? (unsafe ? FINF : plan_margin(up_band32(l32[KMAX - 1], mq)))
+                              : plan_margin(u32fix);
+      }
+    };
+    // largest planning threshold over the lanes (negative ones count as 0)
+    auto wmax = [&](T v) -> T {
+      if constexpr (PLAIN) {
+        return bits_to_double(warp_max_u64(v >= 0.0 ? (uint64_t)__double_as_longlong(v) : 0ull));
+      } else {
+        return __uint_as_float(__reduce_max_sync(0xffffffffu, v >= 0.0f ? __float_as_uint(v) : 0u));
+      }
+    };
+    // window ends around [a, b] for threshold t
+    auto wlo = [&](T a, T t) -> T {
+      if constexpr (PLAIN) return a - t;
+      else return fminf(__fsub_rd(a, t), 1e37f);
+    };
+    auto whi = [&](T b, T t) -> T {
+      if constexpr (PLAIN) return b + t;
+      else return fmaxf(__fadd_ru(b, t), -1e37f);
+    };
+    // a range with lower bound lb lies more than t above a query whose
+    // upper bound is qh / with upper bound hb more than t below ql
+    auto above = [&](T lb, T qh, T t) -> bool {
+      if constexpr (PLAIN) return lb - qh > t;
+      else return __fsub_rd(lb, qh) > t;
+    };
+    auto below = [&](T ql, T hb, T t) -> bool {
+      if constexpr (PLAIN) return ql - hb > t;
+      else return __fsub_rd(ql, hb) > t;
     };
     auto exact_dist = [&](int j, int q) -> uint64_t {
       uint64_t mm = 0;
@@ -399,13 +471,13 @@ wgrid_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items
     const int hc2 = NEST ? (wi.strip >> 16) : 0;  // home cell within the strip
     const int hs0 = NEST ? cst[sq * S2 + hc2] : sst[sq];
     const int hs1 = NEST ? cst[sq * S2 + hc2 + 1] : sst[sq + 1];
-    const double xa = c64[wi.q0];
-    const double xb = c64[wi.q1 - 1];
+    const T xal = __shfl_sync(0xffffffffu, qxl, 0);        // the item's column-0 range
+    const T xbh = __shfl_sync(0xffffffffu, qxh, nq - 1);
     // column-2 centre of the item (nested grids: where other strips start)
-    const double zmid = NEST ? __shfl_sync(0xffffffffu, qz, (nq - 1) >> 1) : 0.0;
+    const T zmid = NEST ? __shfl_sync(0xffffffffu, qzl, (nq - 1) >> 1) : T(0);
 
     // Nested grids: first cell of strip s whose column-2 range reaches z.
-    auto start_cell = [&](int s, double z) -> int {
+    auto start_cell = [&](int s, T z) -> int {
       int c0 = 0;
       for (int b = 0; b < S2; b += 32) {
         const int c = b + lane;
@@ -423,10 +495,10 @@ wgrid_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items
       int up2 = c0, dn2 = c0 - 1;
       bool tu = true;
       for (;;) {
-        const double t = tq();
-        const bool reach = qok && !(ylo_t[s] - qy > t) && !(qy - yhi_t[s] > t);
-        const bool ou = reach && up2 < S2 && !(czlo[cb + up2] - qz > t);
-        const bool od = reach && dn2 >= 0 && !(qz - czhi[cb + dn2] > t);
+        const T t = tqp();
+        const bool reach = qok && !above(ylo_t[s], qyh, t) && !below(qyl, yhi_t[s], t);
+        const bool ou = reach && up2 < S2 && !above(czlo[cb + up2], qzh, t);
+        const bool od = reach && dn2 >= 0 && !below(qzl, czhi[cb + dn2], t);
         const bool any_u = __any_sync(0xffffffffu, ou);
         const bool any_d = __any_sync(0xffffffffu, od);
         if (!any_u && !any_d) break;
@@ -439,11 +511,11 @@ wgrid_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items
           tu = true;
         }
         if (c == skip) continue;
-        const bool nd = reach && !(czlo[cb + c] - qz > t) && !(qz - czhi[cb + c] > t);
+        const bool nd = reach && !above(czlo[cb + c], qzh, t) && !below(qzl, czhi[cb + c], t);
         if (!__any_sync(0xffffffffu, nd)) continue;
-        const double Tw = bits_to_double(warp_max_u64(nd ? tq_bits() : 0ull));
+        const T Tw = wmax(nd ? t : T(-1));
         int wl, wh;
-        warp_window(c64, cst[cb + c], cst[cb + c + 1], xa - Tw, xb + Tw, wl, wh);
+        warp_window(wx, cst[cb + c], cst[cb + c + 1], wlo(xal, Tw), whi(xbh, Tw), wl, wh);
         scan(wl, wh);
       }
     };
@@ -454,14 +526,15 @@ wgrid_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items
         // fix the bound of pass 1 from the FP32 k-th distance of pass 0
         const float u32 = unsafe ? FINF : up_band32(l32[KMAX - 1], mq);
         ufix = qok ? (double)u32 : -1.0;
+        u32fix = qok ? u32 : -1.0f;
         sfix = unsafe ? FINF : up_band32(u32, mq);
       }
       // ---- own positions, then the home strip's window
       scan(wi.q0, wi.q1);
       {
-        const double Tw = bits_to_double(warp_max_u64(tq_bits()));
+        const T Tw = wmax(tqp());
         int wl, wh;
-        warp_window(c64, hs0, hs1, xa - Tw, xb + Tw, wl, wh);
+        warp_window(wx, hs0, hs1, wlo(xal, Tw), whi(xbh, Tw), wl, wh);
         scan(wl, min(wh, wi.q0));
         scan(max(wl, wi.q1), wh);
       }
@@ -472,18 +545,18 @@ wgrid_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items
       bool turn_up = true;
       auto unfinished = [&]() -> bool {
         if (!qok) return false;
-        const double t = tq();
-        const bool u = up >= S || (ylo_t[up] - qy > t);
-        const bool l = dn < 0 || (qy - yhi_t[dn] > t);
+        const T t = tqp();
+        const bool u = up >= S || above(ylo_t[up], qyh, t);
+        const bool l = dn < 0 || below(qyl, yhi_t[dn], t);
         return !(u && l);
       };
       for (;;) {
         const bool unf = unfinished();
         const unsigned ub = __ballot_sync(0xffffffffu, unf);
         if (ub == 0u || __popc(ub) <= OUTLIER_LANES) break;
-        const double t = tq();
-        const bool ou = unf && up < S && !(ylo_t[up] - qy > t);
-        const bool od = unf && dn >= 0 && !(qy - yhi_t[dn] > t);
+        const T t = tqp();
+        const bool ou = unf && up < S && !above(ylo_t[up], qyh, t);
+        const bool od = unf && dn >= 0 && !below(qyl, yhi_t[dn], t);
         const bool any_u = __any_sync(0xffffffffu, ou);
         const bool any_d = __any_sync(0xffffffffu, od);
         if (!any_u && !any_d) break;  // an unfinished query always needs a side
@@ -498,9 +571,9 @@ wgrid_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items
         if constexpr (NEST) {
           visit_cells(s, start_cell(s, zmid), -1);
         } else {
-          const double Tw = bits_to_double(warp_max_u64(unf ? tq_bits() : 0ull));
+          const T Tw = wmax(unf ? t : T(-1));
           int wl, wh;
-          warp_window(c64, sst[s], sst[s + 1], xa - Tw, xb + Tw, wl, wh);
+          warp_window(wx, sst[s], sst[s + 1], wlo(xal, Tw), whi(xbh, Tw), wl, wh);
           scan(wl, wh);
         }
       }
@@ -510,9 +583,9 @@ wgrid_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items
       while (rest) {
         const int ol = __ffs(rest) - 1;
         rest &= rest - 1u;
-        const double oqx = __shfl_sync(0xffffffffu, qx, ol);
-        const double oqy = __shfl_sync(0xffffffffu, qy, ol);
-        const double oqz = __shfl_sync(0xffffffffu, qz, ol);
+        const T oqxl = __shfl_sync(0xffffffffu, qxl, ol), oqxh = __shfl_sync(0xffffffffu, qxh, ol);
+        const T oqyl = __shfl_sync(0xffffffffu, qyl, ol), oqyh = __shfl_sync(0xffffffffu, qyh, ol);
+        const T oqzl = __shfl_sync(0xffffffffu, qzl, ol), oqzh = __shfl_sync(0xffffffffu, qzh, ol);
         const float omq = __shfl_sync(0xffffffffu, mq, ol);
         T oqv[DQ];
 #pragma unroll
@@ -527,9 +600,9 @@ wgrid_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items
         int cnt2 = 0;
         float olo = -1.0f, ohi = -1.0f, othr = FINF;
         uint64_t orbits = 0;
-        double tb = __shfl_sync(0xffffffffu, tq(), ol);  // bound of what the outlier needs
+        T tb = __shfl_sync(0xffffffffu, tqp(), ol);  // planning bound of what the outlier needs
         if constexpr (COUNT) {
-          orbits = (uint64_t)__double_as_longlong(tb);
+          orbits = __shfl_sync(0xffffffffu, rbits, ol);
           olo = __shfl_sync(0xffffffffu, lo, ol);
           ohi = __shfl_sync(0xffffffffu, hi, ol);
         } else {
@@ -604,15 +677,15 @@ wgrid_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items
 #pragma unroll
               for (int o = 16; o; o >>= 1) lk = fminf(lk, __shfl_xor_sync(0xffffffffu, lk, o));
               if (lk < othr) othr = lk;
-              const double nb = unsafe ? HUGE_VAL : (double)up_band32(othr, omq);
+              const T nb = unsafe ? T(FINF) : T(plan_margin(up_band32(othr, omq)));
               if (nb < tb) tb = nb;
             } else if constexpr (PLAIN) {
               const double lbd = bits_to_double(warp_min_u64(top2[KMAX - 1]));
               if (lbd < tb) tb = lbd;
             }
           }
-          const bool ou = oup < S && !(ylo_t[oup] - oqy > tb);
-          const bool od = odn >= 0 && !(oqy - yhi_t[odn] > tb);
+          const bool ou = oup < S && !above(ylo_t[oup], oqyh, tb);
+          const bool od = odn >= 0 && !below(oqyl, yhi_t[odn], tb);
           if (!ou && !od) break;
           const int s = ou && (!od || (oup - sq) <= (sq - odn)) ? oup++ : odn--;
           int wl, wh;
@@ -621,16 +694,16 @@ wgrid_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items
             int clo = 0, chi = 0;
             for (int b = 0; b < S2; b += 32) {
               const int c = b + lane;
-              clo += __popc(__ballot_sync(0xffffffffu, c < S2 && czhi[s * S2 + c] < oqz - tb));
-              chi += __popc(__ballot_sync(0xffffffffu, c < S2 && czlo[s * S2 + c] <= oqz + tb));
+              clo += __popc(__ballot_sync(0xffffffffu, c < S2 && below(oqzl, czhi[s * S2 + c], tb)));
+              chi += __popc(__ballot_sync(0xffffffffu, c < S2 && !above(czlo[s * S2 + c], oqzh, tb)));
             }
             for (int c = clo; c < chi; ++c) {
-              warp_window(c64, cst[s * S2 + c], cst[s * S2 + c + 1], oqx - tb, oqx + tb, wl, wh);
+              warp_window(wx, cst[s * S2 + c], cst[s * S2 + c + 1], wlo(oqxl, tb), whi(oqxh, tb), wl, wh);
               pairs += (unsigned long long)(wh > wl ? wh - wl : 0);
               oscan(wl, wh);
             }
           } else {
-            warp_window(c64, sst[s], sst[s + 1], oqx - tb, oqx + tb, wl, wh);
+            warp_window(wx, sst[s], sst[s + 1], wlo(oqxl, tb), whi(oqxh, tb), wl, wh);
             pairs += (unsigned long long)(wh > wl ? wh - wl : 0);
             oscan(wl, wh);
           }
