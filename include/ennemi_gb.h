@@ -82,7 +82,11 @@ enum egb_flags {
                                   upload to read-back) in a CUDA graph and replay
                                   it for later batches with the same signature
                                   (same sizes, pointers and flags); ignored with
-                                  EGB_TIMING                                      */
+                                  EGB_TIMING.  A batch of device-resident columns
+                                  without labels that repeats the previous batch
+                                  of the context exactly (shapes, column pointers
+                                  and strides, flags, stream; the data may have
+                                  changed) replays without being planned again  */
 };
 
 /* One float64 column: sample i at data[i * stride] (stride in elements). */

@@ -80,3 +80,24 @@ def test_saved_policy_loaded_by_new_context(tmp_path, monkeypatch):
         assert np.array_equal(ctx.get_policy(), table)
     finally:
         ctx.close()
+
+
+def test_policy_change_replans_a_replayed_batch():
+    torch = pytest.importorskip("torch")
+    ctx = N.context()
+    rng = np.random.default_rng(4)
+    n = 6000
+    cols = [torch.from_numpy(rng.normal(size=n)).cuda() for _ in range(2)]
+    tasks = [N.Task(N.MI, 3, [cols[0]], [cols[1]], n=n)]
+    flags = N.INPUT_DEVICE | N.GRAPH
+    try:
+        ctx.set_policy(None)
+        a = N.run_tasks(tasks, flags=flags)
+        b = N.run_tasks(tasks, flags=flags)          # replayed without planning
+        grid_pairs = ctx.stats()["knn_tile_pairs"]
+        ctx.set_policy(np.full(N.POLICY_ENTRIES, N.MODE_BRUTE, dtype=np.int8))
+        c = N.run_tasks(tasks, flags=flags)          # planned again: brute force
+        assert ctx.stats()["knn_tile_pairs"] >= n * n > grid_pairs
+        assert np.array_equal(a, b) and np.array_equal(a, c)
+    finally:
+        ctx.set_policy(None)
