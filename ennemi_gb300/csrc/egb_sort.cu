@@ -30,109 +30,6 @@ constexpr int SCAN_ITEMS = 16;
 constexpr int SCAN_CHUNK = SCAN_THREADS * SCAN_ITEMS;
 constexpr int SORTED_THREADS = SORTED_BLOCK;
 
-__global__ void sort_load_kernel(const TaskDev* __restrict__ tasks,
-                                 const SortSeg* __restrict__ segs,
-                                 const int32_t* __restrict__ blk_seg,
-                                 uint64_t* __restrict__ keys,
-                                 int32_t* __restrict__ vals) {
-  const int b = blockIdx.x;
-  const SortSeg s = segs[blk_seg[b]];
-  const TaskDev t = tasks[s.task];
-  const double* x = t.x64 + (int64_t)s.col * t.ld + s.src_begin;
-  const int i0 = (b - s.blk0) * SORT_TILE;
-  const int i1 = min(i0 + SORT_TILE, s.len);
-  for (int i = i0 + threadIdx.x; i < i1; i += SORT_THREADS) {
-    keys[s.out_base + i] = key_of(x[i]);
-    vals[s.out_base + i] = s.src_begin + i;
-  }
-}
-
-__global__ void sort_hist_kernel(const SortSeg* __restrict__ segs,
-                                 const int32_t* __restrict__ blk_seg,
-                                 const uint64_t* __restrict__ keys, int shift,
-                                 uint32_t* __restrict__ hist) {
-  __shared__ uint32_t h[256];
-  const int b = blockIdx.x;
-  const SortSeg s = segs[blk_seg[b]];
-  h[threadIdx.x] = 0;
-  __syncthreads();
-  const int i0 = (b - s.blk0) * SORT_TILE;
-  const int i1 = min(i0 + SORT_TILE, s.len);
-  for (int i = i0 + threadIdx.x; i < i1; i += SORT_THREADS) {
-    const uint32_t dgt = (uint32_t)(keys[s.out_base + i] >> shift) & 255u;
-    atomicAdd(&h[dgt], 1u);
-  }
-  __syncthreads();
-  const int lb = b - s.blk0;
-  hist[(int64_t)256 * s.blk0 + (int64_t)threadIdx.x * s.nblk + lb] = h[threadIdx.x];
-}
-
-// Stable scatter: the tile is consumed in rounds of 256 consecutive keys
-// (one per thread, in order).  Inside a round a key's rank is
-//   (earlier rounds, same digit) + (earlier warps, same digit)
-//   + (earlier lanes of its warp, same digit; via match_any).
-// offs[] already holds absolute positions in the concatenated buffer.
-__global__ void sort_scatter_kernel(const SortSeg* __restrict__ segs,
-                                    const int32_t* __restrict__ blk_seg,
-                                    const uint64_t* __restrict__ kin,
-                                    const int32_t* __restrict__ vin, int shift,
-                                    const uint32_t* __restrict__ offs,
-                                    uint64_t* __restrict__ kout,
-                                    int32_t* __restrict__ vout) {
-  constexpr int NW = SORT_THREADS / 32;
-  __shared__ uint32_t base[256];
-  __shared__ uint32_t wcnt[NW][256];
-  __shared__ uint32_t rtot[256];
-  const int b = blockIdx.x;
-  const SortSeg s = segs[blk_seg[b]];
-  const int lb = b - s.blk0;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  base[tid] = offs[(int64_t)256 * s.blk0 + (int64_t)tid * s.nblk + lb];
-  for (int w = 0; w < NW; ++w) wcnt[w][tid] = 0;
-  __syncthreads();
-  const int i0 = lb * SORT_TILE;
-  const int i1 = min(i0 + SORT_TILE, s.len);
-  const uint32_t lt_mask = (1u << lane) - 1u;
-  for (int r0 = i0; r0 < i1; r0 += SORT_THREADS) {
-    const int i = r0 + tid;
-    const bool valid = i < i1;
-    uint64_t key = 0;
-    int32_t val = 0;
-    uint32_t dgt = 256u + (uint32_t)lane;  // invalid lanes never match valid ones
-    if (valid) {
-      key = kin[s.out_base + i];
-      val = vin[s.out_base + i];
-      dgt = (uint32_t)(key >> shift) & 255u;
-    }
-    const uint32_t peers = __match_any_sync(0xffffffffu, dgt);
-    const uint32_t wrank = __popc(peers & lt_mask);
-    if (valid && wrank == 0) wcnt[warp][dgt] = __popc(peers);
-    __syncthreads();
-    {  // exclusive scan over warps for digit `tid`
-      uint32_t run = 0;
-#pragma unroll
-      for (int w = 0; w < NW; ++w) {
-        const uint32_t c = wcnt[w][tid];
-        wcnt[w][tid] = run;
-        run += c;
-      }
-      rtot[tid] = run;
-    }
-    __syncthreads();
-    if (valid) {
-      const uint32_t pos = base[dgt] + wcnt[warp][dgt] + wrank;
-      kout[pos] = key;
-      vout[pos] = val;
-    }
-    __syncthreads();
-    base[tid] += rtot[tid];
-#pragma unroll
-    for (int w = 0; w < NW; ++w) wcnt[w][tid] = 0;
-    __syncthreads();
-  }
-}
-
-// ------------------------------------------------------------------ scan --
 __device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* total) {
   __shared__ uint32_t ws[SCAN_THREADS / 32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -161,6 +58,128 @@ __device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* total)
   return r;
 }
 
+__global__ void sort_load_kernel(const TaskDev* __restrict__ tasks,
+                                 const SortSeg* __restrict__ segs,
+                                 const int32_t* __restrict__ blk_seg,
+                                 uint64_t* __restrict__ keys,
+                                 int32_t* __restrict__ vals) {
+  const int b = blockIdx.x;
+  const SortSeg s = segs[blk_seg[b]];
+  const TaskDev t = tasks[s.task];
+  const double* x = t.x64 + (int64_t)s.col * t.ld + s.src_begin;
+  const int i0 = (b - s.blk0) * SORT_TILE;
+  const int i1 = min(i0 + SORT_TILE, s.len);
+  for (int i = i0 + threadIdx.x; i < i1; i += SORT_THREADS) {
+    keys[s.out_base + i] = key_of(x[i]);
+    vals[s.out_base + i] = s.src_begin + i;
+  }
+}
+
+__global__ void sort_hist_kernel(const SortSeg* __restrict__ segs,
+                                 const int32_t* __restrict__ blk_seg,
+                                 const uint64_t* __restrict__ keys, int shift,
+                                 uint32_t* __restrict__ hist) {
+  __shared__ uint32_t h[256];
+  const int b = blockIdx.x;
+  const SortSeg s = segs[blk_seg[b]];
+  const int lane = threadIdx.x & 31;
+  h[threadIdx.x] = 0;
+  __syncthreads();
+  const int i0 = (b - s.blk0) * SORT_TILE;
+  const int i1 = min(i0 + SORT_TILE, s.len);
+  for (int r0 = i0; r0 < i1; r0 += SORT_THREADS) {  // one shared atomic per digit and warp
+    const int i = r0 + threadIdx.x;
+    const bool valid = i < i1;
+    const uint32_t dgt = valid ? (uint32_t)(keys[s.out_base + i] >> shift) & 255u : 256u + lane;
+    const uint32_t peers = __match_any_sync(0xffffffffu, dgt);
+    if (valid && (peers & ((1u << lane) - 1u)) == 0) atomicAdd(&h[dgt], (uint32_t)__popc(peers));
+  }
+  __syncthreads();
+  const int lb = b - s.blk0;
+  hist[(int64_t)256 * s.blk0 + (int64_t)threadIdx.x * s.nblk + lb] = h[threadIdx.x];
+}
+
+// Stable scatter of one tile.  Warp w ranks the keys [w * CH, (w + 1) * CH)
+// of the tile in rounds of 32: match_any gives a key's rank among the equal
+// digits of its round, per-warp counters carry the rank across rounds.  One
+// block scan then turns the per-warp digit counts into the tile's layout in
+// digit order, staged in shared memory and written out so that consecutive
+// threads store to consecutive addresses of each digit's output run.
+// offs[] holds absolute positions in the concatenated buffer.
+__global__ void __launch_bounds__(SORT_THREADS)
+sort_scatter_kernel(const SortSeg* __restrict__ segs, const int32_t* __restrict__ blk_seg,
+                    const uint64_t* __restrict__ kin, const int32_t* __restrict__ vin, int shift,
+                    const uint32_t* __restrict__ offs, uint64_t* __restrict__ kout,
+                    int32_t* __restrict__ vout) {
+  constexpr int NW = SORT_THREADS / 32;
+  constexpr int CH = SORT_TILE / NW;  // keys per warp
+  constexpr int R = CH / 32;          // rounds per warp
+  static_assert(SORT_THREADS == 256 && SCAN_THREADS == 256, "one thread per digit");
+  __shared__ uint32_t wcnt[NW][256];  // per-warp digit counts, then offsets
+  __shared__ uint32_t dstart[256];    // first tile slot of each digit
+  __shared__ uint32_t gbase[256];     // first output position of each digit
+  __shared__ uint64_t sk[SORT_TILE];
+  __shared__ int32_t sv[SORT_TILE];
+  const int b = blockIdx.x;
+  const SortSeg s = segs[blk_seg[b]];
+  const int lb = b - s.blk0;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  gbase[tid] = offs[(int64_t)256 * s.blk0 + (int64_t)tid * s.nblk + lb];
+#pragma unroll
+  for (int w = 0; w < NW; ++w) wcnt[w][tid] = 0;
+  __syncthreads();
+  const int i0 = lb * SORT_TILE;
+  const int n = min(SORT_TILE, s.len - i0);
+  const uint32_t lt = (1u << lane) - 1u;
+  uint64_t key[R];
+  int32_t val[R];
+  uint32_t dg[R], rk[R];
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const int t = warp * CH + r * 32 + lane;
+    const bool valid = t < n;
+    key[r] = valid ? kin[s.out_base + i0 + t] : 0ull;
+    val[r] = valid ? vin[s.out_base + i0 + t] : 0;
+    const uint32_t d = valid ? (uint32_t)(key[r] >> shift) & 255u : 256u + lane;
+    dg[r] = d;
+    const uint32_t peers = __match_any_sync(0xffffffffu, d);
+    const uint32_t before = valid ? wcnt[warp][d] : 0u;
+    __syncwarp();
+    if (valid && (peers & lt) == 0) wcnt[warp][d] = before + __popc(peers);
+    __syncwarp();
+    rk[r] = before + __popc(peers & lt);
+  }
+  __syncthreads();
+  uint32_t run = 0;  // digit tid: offsets of the warps, then of the digit
+#pragma unroll
+  for (int w = 0; w < NW; ++w) {
+    const uint32_t c = wcnt[w][tid];
+    wcnt[w][tid] = run;
+    run += c;
+  }
+  dstart[tid] = block_excl_scan(run, nullptr);
+  __syncthreads();
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const int t = warp * CH + r * 32 + lane;
+    if (t < n) {
+      const uint32_t d = dg[r];
+      const uint32_t slot = dstart[d] + wcnt[warp][d] + rk[r];
+      sk[slot] = key[r];
+      sv[slot] = val[r];
+    }
+  }
+  __syncthreads();
+  for (int t = tid; t < n; t += SORT_THREADS) {
+    const uint64_t k = sk[t];
+    const uint32_t d = (uint32_t)(k >> shift) & 255u;
+    const uint32_t pos = gbase[d] + ((uint32_t)t - dstart[d]);
+    kout[pos] = k;
+    vout[pos] = sv[t];
+  }
+}
+
+// ------------------------------------------------------------------ scan --
 __global__ void scan_reduce_kernel(const uint32_t* __restrict__ in, int64_t n,
                                    uint32_t* __restrict__ sums) {
   const int64_t c0 = (int64_t)blockIdx.x * SCAN_CHUNK;
