@@ -139,6 +139,27 @@ __device__ __forceinline__ void insert_sorted_f(float (&l)[KMAX], float v) {
   }
 }
 
+// Sorted insert of (v, j) into an FP32 list with candidate indices; returns
+// the value pushed out of the last slot.
+template <int KMAX>
+__device__ __forceinline__ float insert_sorted_fi(float (&l)[KMAX], int (&ix)[KMAX], float v,
+                                                  int j) {
+  const float out = l[KMAX - 1];
+  l[KMAX - 1] = v;
+  ix[KMAX - 1] = j;
+#pragma unroll
+  for (int s = KMAX - 1; s > 0; --s) {
+    const float a = l[s - 1], b = l[s];
+    const int ia = ix[s - 1], ib = ix[s];
+    const bool sw = b < a;
+    l[s - 1] = sw ? b : a;
+    l[s] = sw ? a : b;
+    ix[s - 1] = sw ? ib : ia;
+    ix[s] = sw ? ia : ib;
+  }
+  return out;
+}
+
 // K-th smallest of the union of per-lane sorted lists (the first KMAX - K
 // entries of each list are padding).  Warp-wide; result in every lane.
 template <int KMAX, typename V>
@@ -173,12 +194,17 @@ wgrid_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items
              int* __restrict__ counter, int dmax) {
   using T = CoordT<PLAIN>;
   constexpr int DQ = D ? D : EGB_DMAX;
-  // kNN with the FP32 screen runs the schedule twice: pass 0 finds each
-  // query's FP32 k-th distance t32 with an FP32 list (no FP64 at all);
-  // pass 1 re-runs it with the fixed bound U = t32 + band >= the exact k-th
-  // distance, so only the few candidates with FP32 distance <= U + band are
-  // decided in FP64 (instead of every improvement of a running list, each a
-  // divergent FP64 instruction on a 2-lane/clk/SM pipe).
+  // kNN with the FP32 screen: pass 0 finds each query's FP32 k-th distance
+  // t32 with an FP32 list of (distance, candidate) and the least FP32
+  // distance `rej` of every candidate left out of the list.  Every candidate
+  // with FP32 distance <= S = t32 + band + band (the screen bound of an
+  // exact pass) is then in the list when rej > S, and the exact k-th
+  // distance is the largest exact distance of the K listed candidates -- K
+  // FP64 evaluations per query.  Queries without that margin (near ties,
+  // unsafe jobs, fewer than K candidates) run pass 1: the schedule again with
+  // the fixed bound U = t32 + band >= the exact k-th distance, deciding every
+  // candidate with FP32 distance <= S in FP64.  FP64 stays off the hot loop
+  // (a 2-lane/clk/SM pipe on GB300).
   constexpr bool TWO_PASS = !PLAIN && !COUNT;
   constexpr float FINF = __builtin_huge_valf();
   const int lane = threadIdx.x & 31;
@@ -252,6 +278,8 @@ wgrid_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items
     // ---- per-lane state
     uint64_t top[COUNT ? 1 : KMAX];      // exact list (bit patterns)
     float l32[TWO_PASS ? KMAX : 1];      // FP32 list (pass 0)
+    int i32[TWO_PASS ? KMAX : 1];        // its candidates
+    float rej = FINF;                    // least FP32 distance left out of the list
     double ufix = 0.0;                    // pass 1: fixed bound of the k-th distance
     float u32fix = 0.0f;                  // the same bound (a float)
     float sfix = 0.0f;                    // pass 1: FP32 screen threshold
@@ -283,7 +311,10 @@ wgrid_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items
       for (int s = 0; s < KMAX; ++s) top[s] = (exists && s >= KMAX - K) ? INF_BITS : 0ull;
       if constexpr (TWO_PASS) {
 #pragma unroll
-        for (int s = 0; s < KMAX; ++s) l32[s] = (exists && s >= KMAX - K) ? FINF : 0.0f;
+        for (int s = 0; s < KMAX; ++s) {
+          l32[s] = (exists && s >= KMAX - K) ? FINF : 0.0f;
+          i32[s] = 0;
+        }
       }
     }
     // upper bound of what this lane's query still needs (planning threshold)
@@ -357,7 +388,8 @@ wgrid_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items
         if constexpr (TWO_PASS) {
           if (pass == 0) {
             const float dv = u == 0 ? dst[0] : u == 1 ? dst[1] : u == 2 ? dst[2] : dst[3];
-            if (dv < l32[KMAX - 1]) insert_sorted_f<KMAX>(l32, dv);
+            const float out = dv < l32[KMAX - 1] ? insert_sorted_fi<KMAX>(l32, i32, dv, j) : dv;
+            rej = fminf(rej, out);
             continue;
           }
         }
@@ -382,6 +414,21 @@ wgrid_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items
         }
       }
       if constexpr (COUNT) cntq += __popc(inside & vmask);
+      if constexpr (TWO_PASS) {
+        if (pass == 0) {
+          // the group's least distance, or the list bound when some is a hit
+          // (a hit that is left out after all updates rej in resolve)
+          float m4;
+          if (vmask == 0xFu) {
+            m4 = fminf(fminf(dst[0], dst[1]), fminf(dst[2], dst[3]));
+          } else {
+            m4 = FINF;
+#pragma unroll
+            for (int u = 0; u < 4; ++u) m4 = fminf(m4, ((vmask >> u) & 1u) ? dst[u] : FINF);
+          }
+          rej = fminf(rej, fmaxf(m4, l32[KMAX - 1]));
+        }
+      }
       hits &= vmask;
       if (__builtin_expect(hits != 0u, 0)) resolve(g0, hits, dst);
     };
@@ -522,12 +569,36 @@ wgrid_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items
 
 #pragma unroll 1
     for (; pass < 2; ++pass) {
-      if (TWO_PASS && pass == 1) {
-        // fix the bound of pass 1 from the FP32 k-th distance of pass 0
-        const float u32 = unsafe ? FINF : up_band32(l32[KMAX - 1], mq);
-        ufix = qok ? (double)u32 : -1.0;
-        u32fix = qok ? u32 : -1.0f;
-        sfix = unsafe ? FINF : up_band32(u32, mq);
+      if constexpr (TWO_PASS) {
+        if (pass == 1) {
+          // settle every query whose list holds all candidates within S
+          bool need = false;
+          const float u32 = unsafe ? FINF : up_band32(l32[KMAX - 1], mq);
+          const float s32 = unsafe ? FINF : up_band32(u32, mq);
+          if (qok) {
+            if (rej > s32) {
+              uint64_t mx = 0;
+#pragma unroll
+              for (int s = 0; s < KMAX; ++s) {
+                if (s >= KMAX - K) {
+                  const uint64_t e = exact_dist(i32[s], qp);
+                  mx = e > mx ? e : mx;
+                }
+              }
+              top[KMAX - 1] = mx;
+            } else {
+              need = true;
+            }
+          }
+          const unsigned fbm = __ballot_sync(0xffffffffu, need);
+          if (fbm == 0u) break;  // every query of the item is settled
+          if (lane == 0) atomicAdd(J->stats + 2, (unsigned long long)__popc(fbm));
+          // pass 1 for the rest, with the bound fixed from pass 0
+          qok = need;
+          ufix = need ? (double)u32 : -1.0;
+          u32fix = need ? u32 : -1.0f;
+          sfix = need ? s32 : -1.0f;
+        }
       }
       // ---- own positions, then the home strip's window
       scan(wi.q0, wi.q1);
@@ -597,6 +668,8 @@ wgrid_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items
         const bool op0 = TWO_PASS && pass == 0;
         uint64_t top2[COUNT ? 1 : KMAX];
         float l2[TWO_PASS ? KMAX : 1];
+        int ix2[TWO_PASS ? KMAX : 1];
+        float rej2 = FINF;
         int cnt2 = 0;
         float olo = -1.0f, ohi = -1.0f, othr = FINF;
         uint64_t orbits = 0;
@@ -610,7 +683,10 @@ wgrid_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items
           for (int s2 = 0; s2 < KMAX; ++s2) top2[s2] = s2 >= KMAX - K ? INF_BITS : 0ull;
           if constexpr (TWO_PASS) {
 #pragma unroll
-            for (int s2 = 0; s2 < KMAX; ++s2) l2[s2] = s2 >= KMAX - K ? FINF : 0.0f;
+            for (int s2 = 0; s2 < KMAX; ++s2) {
+              l2[s2] = s2 >= KMAX - K ? FINF : 0.0f;
+              ix2[s2] = 0;
+            }
             if (op0) l2[KMAX - 1] = FINF;
             othr = __shfl_sync(0xffffffffu, sfix, ol);
             if (op0) {
@@ -655,13 +731,13 @@ wgrid_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items
                 hit = dist <= othr;
               }
             }
-            if (hit) {
-              if constexpr (TWO_PASS) {
-                if (op0) {
-                  insert_sorted_f<KMAX>(l2, dist);
-                  continue;
-                }
+            if constexpr (TWO_PASS) {
+              if (op0) {
+                rej2 = fminf(rej2, hit ? insert_sorted_fi<KMAX>(l2, ix2, dist, j) : dist);
+                continue;
               }
+            }
+            if (hit) {
               const uint64_t mm = exact_dist(j, oqp);
               if constexpr (COUNT) cnt2 += mm <= orbits ? 1 : 0;
               else if (mm < top2[KMAX - 1]) insert_sorted<KMAX>(top2, mm);
@@ -715,13 +791,77 @@ wgrid_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items
           bool merged = false;
           if constexpr (TWO_PASS) {
             if (op0) {
-              if (lane == ol) {  // the owner's real entries join its lane list
+              if (lane == ol) {  // the owner's list and left-outs join its lane's
+                rej2 = fminf(rej2, rej);
+#pragma unroll
+                for (int s2 = 0; s2 < KMAX; ++s2) {
+                  if (s2 >= KMAX - K) {
+                    const float v = l32[s2];
+                    rej2 = fminf(rej2, v < l2[KMAX - 1] ? insert_sorted_fi<KMAX>(l2, ix2, v, i32[s2]) : v);
+                  }
+                }
+              }
+              // the K smallest of the union, in order, become the owner's list
+              float nl[KMAX];
+              int ni[KMAX];
+#pragma unroll
+              for (int s2 = 0; s2 < KMAX; ++s2) {
+                nl[s2] = 0.0f;
+                ni[s2] = 0;
+              }
+              int taken = 0;
+              for (int r = 0; r < K; ++r) {
+                const int hp = KMAX - K + taken;
+                float v = FINF;
+                int vi = 0;
+#pragma unroll
+                for (int s2 = 0; s2 < KMAX; ++s2) {
+                  if (s2 == hp) {
+                    v = l2[s2];
+                    vi = ix2[s2];
+                  }
+                }
+                int who = lane;
+#pragma unroll
+                for (int o = 16; o; o >>= 1) {
+                  const float ov = __shfl_xor_sync(0xffffffffu, v, o);
+                  const int ow = __shfl_xor_sync(0xffffffffu, who, o);
+                  if (ov < v || (ov == v && ow < who)) {
+                    v = ov;
+                    who = ow;
+                  }
+                }
+                const int bi = __shfl_sync(0xffffffffu, vi, who);
+                if (lane == who) ++taken;
+                if (lane == ol) {
+#pragma unroll
+                  for (int s2 = 0; s2 < KMAX - 1; ++s2) {
+                    nl[s2] = nl[s2 + 1];
+                    ni[s2] = ni[s2 + 1];
+                  }
+                  nl[KMAX - 1] = v;
+                  ni[KMAX - 1] = bi;
+                }
+              }
+              // left out: every lane's next entry and its rejections
+              {
+                const int hp = KMAX - K + taken;
+                float v = FINF;
 #pragma unroll
                 for (int s2 = 0; s2 < KMAX; ++s2)
-                  if (s2 >= KMAX - K && l32[s2] < l2[KMAX - 1]) insert_sorted_f<KMAX>(l2, l32[s2]);
+                  if (s2 == hp) v = l2[s2];
+                float lo2 = fminf(rej2, v);
+#pragma unroll
+                for (int o = 16; o; o >>= 1) lo2 = fminf(lo2, __shfl_xor_sync(0xffffffffu, lo2, o));
+                if (lane == ol) {
+#pragma unroll
+                  for (int s2 = 0; s2 < KMAX; ++s2) {
+                    l32[s2] = nl[s2];
+                    i32[s2] = ni[s2];
+                  }
+                  rej = lo2;
+                }
               }
-              const float kth = warp_kth_of_lists<KMAX, float>(l2, K, FINF);
-              if (lane == ol) l32[KMAX - 1] = kth;  // only the k-th is used by pass 1
               merged = true;
             }
           }
