@@ -1097,9 +1097,13 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
     Group& G = groups[g];
     if (G.is_knn || G.items.empty()) continue;
     if (G.mode == 3) {
-      launch_count_wgrid((const JobDev*)dtab(tab_jobs), (const WorkItem*)dtab(G.tab_items),
-                         (int)G.items.size(), G.dclass, plain, G.dmax, counters + 2 * g,
-                         ctx->num_sms, st);
+      if (!plain && count_keys_supported(G.dclass))
+        launch_count_keys((const JobDev*)dtab(tab_jobs), (const WorkItem*)dtab(G.tab_items),
+                          (int)G.items.size(), G.dclass, counters + 2 * g, ctx->num_sms, st);
+      else
+        launch_count_wgrid((const JobDev*)dtab(tab_jobs), (const WorkItem*)dtab(G.tab_items),
+                           (int)G.items.size(), G.dclass, plain, G.dmax, counters + 2 * g,
+                           ctx->num_sms, st);
       continue;
     }
     if (G.mode == 2) {

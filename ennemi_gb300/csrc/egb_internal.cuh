@@ -86,6 +86,96 @@ __device__ __forceinline__ double bits_to_double(uint64_t u) {
   return __longlong_as_double((long long)u);
 }
 
+// Order-preserving integer image of a double's bit pattern (raw: -0 sorts
+// just below +0) and its inverse.
+__device__ __forceinline__ uint64_t raw_key(uint64_t u) {
+  return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double raw_value(uint64_t k) {
+  return __longlong_as_double((long long)((k >> 63) ? (k & 0x7fffffffffffffffull) : ~k));
+}
+
+// Raw keys [kl, kr] of the doubles x with fl64(|x - q|) <= r, for q and r
+// finite, r >= 0.  x -> fl64(x - q) is monotone (rounding is), so the set
+// is one key range.  Its ends usually lie an ulp or two from fl64(q -+ r),
+// but where q -+ r is much smaller in magnitude than q many doubles share
+// one fl64 difference, so each end is found by galloping from there and
+// bisecting on the exact predicate (at most about 128 FP64 steps).
+__device__ __forceinline__ void ball_keys(double q, double r, uint64_t& kl, uint64_t& kr) {
+  // right end: largest k with value(k) - q <= r
+  {
+    uint64_t k = raw_key((uint64_t)__double_as_longlong(q + r));
+    auto P = [&](uint64_t x) { return raw_value(x) - q <= r; };
+    uint64_t good, bad;  // P(good), !P(bad), good < bad
+    if (P(k)) {
+      good = k;
+      uint64_t step = 1;
+      for (;;) {
+        const uint64_t nx = good + step;
+        if (nx < good || !P(nx)) {
+          bad = nx < good ? ~0ull : nx;
+          break;
+        }
+        good = nx;
+        step <<= 1;
+      }
+    } else {
+      bad = k;
+      uint64_t step = 1;
+      for (;;) {
+        const uint64_t nx = bad - step;
+        if (P(nx)) {  // value(key(q)) - q = 0 <= r bounds the walk
+          good = nx;
+          break;
+        }
+        bad = nx;
+        step <<= 1;
+      }
+    }
+    while (bad - good > 1) {
+      const uint64_t m = good + ((bad - good) >> 1);
+      if (P(m)) good = m; else bad = m;
+    }
+    kr = good;
+  }
+  // left end: smallest k with q - value(k) <= r
+  {
+    uint64_t k = raw_key((uint64_t)__double_as_longlong(q - r));
+    auto Q = [&](uint64_t x) { return q - raw_value(x) <= r; };
+    uint64_t good, bad;  // Q(good), !Q(bad), bad < good
+    if (Q(k)) {
+      good = k;
+      uint64_t step = 1;
+      for (;;) {
+        const uint64_t nx = good - step;
+        if (nx > good || !Q(nx)) {
+          bad = nx > good ? 0ull : nx;
+          break;
+        }
+        good = nx;
+        step <<= 1;
+      }
+    } else {
+      bad = k;
+      uint64_t step = 1;
+      for (;;) {
+        const uint64_t nx = bad + step;
+        if (Q(nx)) {
+          good = nx;
+          break;
+        }
+        bad = nx;
+        step <<= 1;
+      }
+    }
+    while (good - bad > 1) {
+      const uint64_t m = bad + ((good - bad) >> 1);
+      if (Q(m)) good = m; else bad = m;
+    }
+    kl = good;
+  }
+}
+
 // FP32 guard band.
 // Let c be a column centre (a double), q the query, p a candidate, and
 // D = max_c |p_c - q_c| the exact max-norm distance.  The filter works on
@@ -365,6 +455,11 @@ void launch_count_grid(const JobDev* jobs_d, const WorkItem* items_d, int nitems
 constexpr int WG_QB = 32;
 void launch_knn_wgrid(const JobDev* jobs_d, const WorkItem* items_d, int nitems, int kclass,
                       int dclass, int plain, int dmax, int* counter, int num_sms, cudaStream_t st);
+// egb_wcount.cu: exact key-range ball counts of d = 2 / nested d = 3
+// warp-grid jobs (FP32 path; the FP64 comparator keeps launch_count_wgrid)
+bool count_keys_supported(int dclass);
+void launch_count_keys(const JobDev* jobs_d, const WorkItem* items_d, int nitems, int dclass,
+                       int* counter, int num_sms, cudaStream_t st);
 void launch_count_wgrid(const JobDev* jobs_d, const WorkItem* items_d, int nitems, int dclass,
                         int plain, int dmax, int* counter, int num_sms, cudaStream_t st);
 

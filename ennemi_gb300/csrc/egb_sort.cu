@@ -268,85 +268,37 @@ __global__ void sorted_jobs_kernel(const TaskDev* __restrict__ tasks,
   } else if (r == INF) {
     count = (int32_t)len;
   } else {
-    // The ball is the key range [kL, kR]: kR the largest key with
-    // fl64(value - q) <= r, kL the smallest with fl64(q - value) <= r
-    // (s -> fl64(s - q) is monotone).  Both lie within an ulp or two of
-    // fl64(q +- r); a few FP64 steps per query find them, and the searches
-    // then compare integer keys (the FP64 pipe is a small fraction of the
-    // integer rate on GB300).
-    uint64_t kR = key_of(q + r), kL = key_of(q - r);
-    bool exact = true;
-    {
-      int i2 = 0;
-      for (; i2 < 8; ++i2) {  // up while the next value still qualifies
-        const double nv = value_of(kR + 1);
-        if (!(nv - q <= r)) break;
-        ++kR;
-      }
-      exact &= i2 < 8;
-      for (i2 = 0; i2 < 8 && !(value_of(kR) - q <= r); ++i2) --kR;
-      exact &= i2 < 8;
-      for (i2 = 0; i2 < 8; ++i2) {  // down while the previous value qualifies
-        const double pv = value_of(kL - 1);
-        if (!(q - pv <= r)) break;
-        --kL;
-      }
-      exact &= i2 < 8;
-      for (i2 = 0; i2 < 8 && !(q - value_of(kL) <= r); ++i2) ++kL;
-      exact &= i2 < 8;
+    // The ball is one key range (ball_keys); the searches compare integer
+    // keys (the FP64 pipe is a small fraction of the integer rate on GB300).
+    // The sorted keys fold -0 into +0, as the predicate does.
+    uint64_t kL, kR;
+    ball_keys(q, r, kL, kR);
+    kL = kL == 0x7fffffffffffffffull ? 0x8000000000000000ull : kL;  // raw -0 -> +0
+    // right end: last j >= p with keys[j] <= kR   (true at j = p)
+    int64_t a = p, step = 1;
+    while (a + step < len && keys[a + step] <= kR) {
+      a += step;
+      step <<= 1;
     }
-    if (exact) {
-      // right end: last j >= p with keys[j] <= kR   (true at j = p)
-      int64_t a = p, step = 1;
-      while (a + step < len && keys[a + step] <= kR) {
-        a += step;
-        step <<= 1;
-      }
-      int64_t b = a + step < len ? a + step : len;
-      while (b - a > 1) {
-        const int64_t m = a + ((b - a) >> 1);
-        if (keys[m] <= kR) a = m; else b = m;
-      }
-      const int64_t R = a;
-      // left end: first j <= p with keys[j] >= kL   (true at j = p)
-      a = p;
-      step = 1;
-      while (a - step >= 0 && keys[a - step] >= kL) {
-        a -= step;
-        step <<= 1;
-      }
-      b = a - step >= 0 ? a - step : -1;
-      while (a - b > 1) {
-        const int64_t m = b + ((a - b) >> 1);
-        if (keys[m] >= kL) a = m; else b = m;
-      }
-      count = (int32_t)(R - a + 1);
-    } else {
-      // (never expected) the same searches on FP64 distances
-      int64_t a = p, step = 1;
-      while (a + step < len && value_of(keys[a + step]) - q <= r) {
-        a += step;
-        step <<= 1;
-      }
-      int64_t b = a + step < len ? a + step : len;
-      while (b - a > 1) {
-        const int64_t m = a + ((b - a) >> 1);
-        if (value_of(keys[m]) - q <= r) a = m; else b = m;
-      }
-      const int64_t R = a;
-      a = p;
-      step = 1;
-      while (a - step >= 0 && q - value_of(keys[a - step]) <= r) {
-        a -= step;
-        step <<= 1;
-      }
-      b = a - step >= 0 ? a - step : -1;
-      while (a - b > 1) {
-        const int64_t m = b + ((a - b) >> 1);
-        if (q - value_of(keys[m]) <= r) a = m; else b = m;
-      }
-      count = (int32_t)(R - a + 1);
+    int64_t b = a + step < len ? a + step : len;
+    while (b - a > 1) {
+      const int64_t m = a + ((b - a) >> 1);
+      if (keys[m] <= kR) a = m; else b = m;
     }
+    const int64_t R = a;
+    // left end: first j <= p with keys[j] >= kL   (true at j = p)
+    a = p;
+    step = 1;
+    while (a - step >= 0 && keys[a - step] >= kL) {
+      a -= step;
+      step <<= 1;
+    }
+    b = a - step >= 0 ? a - step : -1;
+    while (a - b > 1) {
+      const int64_t m = b + ((a - b) >> 1);
+      if (keys[m] >= kL) a = m; else b = m;
+    }
+    count = (int32_t)(R - a + 1);
   }
   t.cnt[jb.slot][i] = count;
 }

@@ -1,0 +1,255 @@
+// egb_wcount.cu -- ball counts of d = 2 and d = 3 warp-grid jobs by key
+// ranges: integer comparisons only, no distance arithmetic.
+//
+// The count of query q is #{j : max_c fl64(|p_jc - q_c|) <= r}, r =
+// fl64(eps_q - 1e-12) (query_ball_point with p=inf and return_length=True,
+// ennemi/_entropy_estimators.py:109-110, :152-154).  Per coordinate,
+// x -> fl64(x - q_c) is monotone, so {x : fl64(|x - q_c|) <= r} is one range
+// of doubles, and -- mapping doubles to order-preserving integer keys -- one
+// key range [kl_c, kr_c] whose ends ball_keys() finds with a few exact FP64
+// steps per query.  The ball is then the box of those key ranges, exactly.
+//
+// Layout: the job's grid copy (strips by column 1, nested cells by column 2
+// for d = 3, column-0 order inside).  A warp takes an item of up to 32
+// queries of one strip (cell) and visits the strips outward from its own
+// while some lane's column-1 key range reaches them; in a nested grid, the
+// cells of each strip whose column-2 range meets some lane's.  In each strip
+// (cell) the warp finds the union column-0 window of its lanes with a 16-ary
+// warp search, then every lane binary-searches its own column-0 key range
+// inside the window.  A strip (cell) whose column-1 (and column-2) bounds
+// lie inside the lane's ball adds the length of that range; otherwise the
+// lane checks the column-1 (column-2) keys of the candidates in its range.
+#include "egb_internal.cuh"
+
+namespace egb {
+namespace {
+
+constexpr int WC_WARPS = 4;
+
+__device__ __forceinline__ uint64_t rkey(uint64_t u) { return raw_key(u); }
+
+__device__ __forceinline__ uint64_t wmin64(uint64_t v) {
+#pragma unroll
+  for (int o = 16; o; o >>= 1) {
+    const uint64_t w = __shfl_xor_sync(0xffffffffu, v, o);
+    v = w < v ? w : v;
+  }
+  return v;
+}
+__device__ __forceinline__ uint64_t wmax64(uint64_t v) {
+#pragma unroll
+  for (int o = 16; o; o >>= 1) {
+    const uint64_t w = __shfl_xor_sync(0xffffffffu, v, o);
+    v = w > v ? w : v;
+  }
+  return v;
+}
+
+// Positions [wlo, whi) of [s0, s1) whose column-0 key lies in [lo, hi]
+// (x sorted): the lower half-warp finds the first key >= lo, the upper half
+// the first key > hi, 16-ary.
+__device__ __forceinline__ void warp_window_keys(const unsigned long long* __restrict__ x, int s0,
+                                                 int s1, uint64_t lo, uint64_t hi, int& wlo,
+                                                 int& whi) {
+  const int lane = threadIdx.x & 31;
+  const bool upper = lane >= 16;
+  const int l16 = lane & 15;
+  const unsigned m = upper ? 0xffff0000u : 0x0000ffffu;
+  int a = s0, b = s1;
+  for (int round = 0; round < 40; ++round) {
+    const int n = b - a;
+    const bool small = n <= 16;
+    int p = small ? a + l16 : a + (int)((int64_t)(l16 + 1) * n / 17);
+    const bool inr = p < b;
+    p = inr ? p : s0;
+    const uint64_t k = rkey(x[p]);
+    const bool t = inr && (upper ? (k <= hi) : (k < lo));
+    const int c = __popc(__ballot_sync(0xffffffffu, t) & m);
+    if (small) {
+      a = a + c;
+      b = a;
+    } else {
+      const int na = c == 0 ? a : a + (int)((int64_t)c * n / 17) + 1;
+      const int nb = c == 16 ? b : a + (int)((int64_t)(c + 1) * n / 17);
+      a = na;
+      b = nb;
+    }
+    if (__all_sync(0xffffffffu, b - a <= 0)) break;
+  }
+  wlo = __shfl_sync(0xffffffffu, a, 0);
+  whi = __shfl_sync(0xffffffffu, a, 16);
+  if (whi < wlo) whi = wlo;
+}
+
+// First position of [a, b) with key >= k (x sorted).
+__device__ __forceinline__ int lower_key(const unsigned long long* __restrict__ x, int a, int b,
+                                         uint64_t k) {
+  int n = b - a;
+  while (n > 0) {
+    const int h = n >> 1;
+    if (rkey(x[a + h]) < k) {
+      a += h + 1;
+      n -= h + 1;
+    } else {
+      n = h;
+    }
+  }
+  return a;
+}
+// First position of [a, b) with key > k.
+__device__ __forceinline__ int upper_key(const unsigned long long* __restrict__ x, int a, int b,
+                                         uint64_t k) {
+  int n = b - a;
+  while (n > 0) {
+    const int h = n >> 1;
+    if (rkey(x[a + h]) <= k) {
+      a += h + 1;
+      n -= h + 1;
+    } else {
+      n = h;
+    }
+  }
+  return a;
+}
+
+template <int D>
+__global__ void __launch_bounds__(WC_WARPS * 32)
+wcount_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items, int nitems,
+              int* __restrict__ counter) {
+  static_assert(D == 2 || D == 3, "d = 2 strips or d = 3 nested cells");
+  const int lane = threadIdx.x & 31;
+  for (;;) {
+    int it = 0;
+    if (lane == 0) it = atomicAdd(counter, 1);
+    it = __shfl_sync(0xffffffffu, it, 0);
+    if (it >= nitems) break;
+    const WorkItem wi = items[it];
+    const JobDev* __restrict__ J = jobs + wi.job;
+    const int len = J->len;
+    const int64_t lds = J->lds;
+    const unsigned long long* __restrict__ xb = reinterpret_cast<const unsigned long long*>(J->c64g);
+    const unsigned long long* __restrict__ yb = xb + lds;
+    const unsigned long long* __restrict__ zb = xb + 2 * lds;
+    const int32_t* __restrict__ sst = J->sstart;
+    const unsigned long long* __restrict__ sylo = reinterpret_cast<const unsigned long long*>(J->sylo);
+    const unsigned long long* __restrict__ syhi = reinterpret_cast<const unsigned long long*>(J->syhi);
+    const int S = J->nstrips;
+    const int S2 = D == 3 ? J->nsub : 1;
+    const int32_t* __restrict__ cst = J->cstart;
+    const unsigned long long* __restrict__ czlo = reinterpret_cast<const unsigned long long*>(J->czlo);
+    const unsigned long long* __restrict__ czhi = reinterpret_cast<const unsigned long long*>(J->czhi);
+
+    const int qp = wi.q0 + lane;
+    const bool exists = qp < wi.q1;
+    const double qr = exists ? J->rad[J->idxg[qp]] : -1.0;
+    const bool qok = exists && qr >= 0.0;
+    const bool every = qok && isinf(qr);  // an infinite radius holds every point
+    uint64_t kxl = 1, kxr = 0, kyl = 1, kyr = 0, kzl = 1, kzr = 0;  // empty ranges
+    const bool act = qok && !every;
+    if (act) {
+      ball_keys(__longlong_as_double((long long)xb[qp]), qr, kxl, kxr);
+      ball_keys(__longlong_as_double((long long)yb[qp]), qr, kyl, kyr);
+      if (D == 3) ball_keys(__longlong_as_double((long long)zb[qp]), qr, kzl, kzr);
+    }
+    int cnt = every ? len : 0;
+    unsigned long long checked = 0;
+
+    // Count this lane's ball in the positions [a, b) of one strip or cell.
+    auto count_range = [&](int a, int b, bool inner, bool reach) {
+      // union column-0 window of the lanes that reach this range
+      const uint64_t ul = wmin64(reach ? kxl : ~0ull);
+      const uint64_t uh = wmax64(reach ? kxr : 0ull);
+      int wl, wh;
+      warp_window_keys(xb, a, b, ul, uh, wl, wh);
+      if (!reach) return;
+      const int pl = lower_key(xb, wl, wh, kxl);
+      const int ph = upper_key(xb, pl, wh, kxr);
+      if (inner) {
+        cnt += ph - pl;
+        return;
+      }
+      checked += (unsigned long long)(ph - pl);
+      for (int p = pl; p < ph; ++p) {
+        const uint64_t ky = rkey(yb[p]);
+        bool in = ky >= kyl && ky <= kyr;
+        if (D == 3) {
+          const uint64_t kz = rkey(zb[p]);
+          in = in && kz >= kzl && kz <= kzr;
+        }
+        cnt += in ? 1 : 0;
+      }
+    };
+    // Strip s: its cells (nested) or the strip itself.
+    auto visit = [&](int s) {
+      const uint64_t lo1 = rkey(sylo[s]), hi1 = rkey(syhi[s]);
+      const bool reach = act && hi1 >= kyl && lo1 <= kyr;
+      if (!__any_sync(0xffffffffu, reach)) return;
+      const bool in1 = reach && lo1 >= kyl && hi1 <= kyr;
+      if (D == 2) {
+        count_range(sst[s], sst[s + 1], in1, reach);
+        return;
+      }
+      // cells whose column-2 range meets a reaching lane's: a contiguous run
+      const uint64_t zl = wmin64(reach ? kzl : ~0ull);
+      const uint64_t zh = wmax64(reach ? kzr : 0ull);
+      int c0 = 0, c1 = 0;
+      for (int b = 0; b < S2; b += 32) {
+        const int c = b + lane;
+        c0 += __popc(__ballot_sync(0xffffffffu, c < S2 && rkey(czhi[s * S2 + c]) < zl));
+        c1 += __popc(__ballot_sync(0xffffffffu, c < S2 && rkey(czlo[s * S2 + c]) <= zh));
+      }
+      for (int c = c0; c < c1; ++c) {
+        const uint64_t lo2 = rkey(czlo[s * S2 + c]), hi2 = rkey(czhi[s * S2 + c]);
+        const bool rc = reach && hi2 >= kzl && lo2 <= kzr;
+        if (!__any_sync(0xffffffffu, rc)) continue;
+        const bool in2 = rc && in1 && lo2 >= kzl && hi2 <= kzr;
+        count_range(cst[s * S2 + c], cst[s * S2 + c + 1], in2, rc);
+      }
+    };
+
+    const int sq = D == 3 ? (wi.strip & 0xffff) : wi.strip;
+    visit(sq);
+    // strips above: their lower bounds grow, so the first one that no lane
+    // reaches ends the direction (every lane's ball starts below its own
+    // strip's upper bound); the same below
+    for (int s = sq + 1; s < S; ++s) {
+      if (!__any_sync(0xffffffffu, act && rkey(sylo[s]) <= kyr)) break;
+      visit(s);
+    }
+    for (int s = sq - 1; s >= 0; --s) {
+      if (!__any_sync(0xffffffffu, act && rkey(syhi[s]) >= kyl)) break;
+      visit(s);
+    }
+
+    if (exists) J->cnt[J->idxg[qp]] = qok ? cnt : 0;
+    const unsigned long long tot = __reduce_add_sync(0xffffffffu, (unsigned)checked);
+    if (lane == 0) atomicAdd(J->stats + 0, tot);
+  }
+}
+
+template <int D>
+void launch_t(const JobDev* jobs, const WorkItem* items, int nitems, int* counter, int num_sms,
+              cudaStream_t st) {
+  auto kern = wcount_kernel<D>;
+  int per_sm = 1;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, WC_WARPS * 32, 0);
+  if (per_sm < 1) per_sm = 1;
+  int grid = num_sms * per_sm;
+  const int need = (nitems + WC_WARPS - 1) / WC_WARPS;
+  if (grid > need) grid = need;
+  if (grid < 1) return;
+  kern<<<grid, WC_WARPS * 32, 0, st>>>(jobs, items, nitems, counter);
+  count_launch();
+}
+
+}  // namespace
+
+bool count_keys_supported(int dclass) { return dclass == 2 || dclass == 3; }
+
+void launch_count_keys(const JobDev* jobs_d, const WorkItem* items_d, int nitems, int dclass,
+                       int* counter, int num_sms, cudaStream_t st) {
+  if (dclass == 2) launch_t<2>(jobs_d, items_d, nitems, counter, num_sms, st);
+  else launch_t<3>(jobs_d, items_d, nitems, counter, num_sms, st);
+}
+
+}  // namespace egb

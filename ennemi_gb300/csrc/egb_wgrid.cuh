@@ -284,6 +284,13 @@ wgrid_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items
     float u32fix = 0.0f;                  // the same bound (a float)
     float sfix = 0.0f;                    // pass 1: FP32 screen threshold
     float tcnt = -1.0f;                   // FP32 counts: planning threshold
+    // FP32 counts of d = 2 (strips) and d = 3 (cells): a strip or cell whose
+    // other coordinates lie inside the ball for every lane is counted by key
+    // ranges of column 0 instead of scanned
+    constexpr bool INNER = COUNT && !PLAIN && (D == 2 || (NEST && D == 3));
+    uint64_t kxl = 0, kxr = 0;            // column-0 key range of the ball
+    float r32lo = -1.0f;                  // FP32 lower bound of the radius
+    bool kx_ok = false;
     double qr = -1.0;
     uint64_t rbits = 0;
     float lo = -1.0f, hi = -1.0f;
@@ -295,6 +302,13 @@ wgrid_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items
       qok = exists && (qr >= 0.0);
       rbits = qok ? (uint64_t)__double_as_longlong(qr) : 0ull;
       if (!PLAIN && qok) tcnt = plan_margin(__double2float_ru(qr));
+      if constexpr (INNER) {
+        if (qok && !isinf(qr) && !unsafe) {
+          ball_keys(qx, qr, kxl, kxr);
+          kx_ok = true;
+          r32lo = __double2float_rd(qr);
+        }
+      }
       if (!PLAIN && qok) {
         if (isinf(qr)) {
           lo = hi = FINF;
@@ -532,6 +546,39 @@ wgrid_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items
       }
       return c0 < S2 ? c0 : S2 - 1;
     };
+    // INNER: does the ball of this lane contain the column-1 range [lb, hb]
+    // (and column-2 range [lc, hc] for cells)?  Conservative in FP32.
+    auto inside = [&](T lb, T hb, T q_lo, T q_hi) -> bool {
+      if constexpr (INNER) return kx_ok && __fsub_ru(q_hi, lb) <= r32lo && __fsub_ru(hb, q_lo) <= r32lo;
+      else return false;
+    };
+    // INNER: points of [a, b) whose column-0 key lies in [kxl, kxr]
+    auto count_keys = [&](int a, int b) -> int {
+      const unsigned long long* xb = reinterpret_cast<const unsigned long long*>(c64);
+      int lo = a, n = b - a;
+      while (n > 0) {  // first key >= kxl
+        const int h = n >> 1;
+        if (raw_key(xb[lo + h]) < kxl) {
+          lo += h + 1;
+          n -= h + 1;
+        } else {
+          n = h;
+        }
+      }
+      int hi = lo;
+      n = b - lo;
+      while (n > 0) {  // first key > kxr
+        const int h = n >> 1;
+        if (raw_key(xb[hi + h]) <= kxr) {
+          hi += h + 1;
+          n -= h + 1;
+        } else {
+          n = h;
+        }
+      }
+      return hi - lo;
+    };
+
     // Nested grids: the cells of strip s that some lane still needs, outward
     // in column 2 from cell c0 (cell `skip` already scanned).  A lane needs a
     // cell while the strip's column-1 range and the cell's column-2 range are
@@ -563,6 +610,13 @@ wgrid_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items
         const T Tw = wmax(nd ? t : T(-1));
         int wl, wh;
         warp_window(wx, cst[cb + c], cst[cb + c + 1], wlo(xal, Tw), whi(xbh, Tw), wl, wh);
+        if constexpr (INNER) {
+          const bool in = inside(ylo_t[s], yhi_t[s], qyl, qyh) && inside(czlo[cb + c], czhi[cb + c], qzl, qzh);
+          if (__all_sync(0xffffffffu, in || !nd)) {
+            if (in) cntq += count_keys(wl, wh);
+            continue;
+          }
+        }
         scan(wl, wh);
       }
     };
@@ -601,13 +655,25 @@ wgrid_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items
         }
       }
       // ---- own positions, then the home strip's window
-      scan(wi.q0, wi.q1);
       {
+        if constexpr (!INNER) scan(wi.q0, wi.q1);  // kNN: seeds the thresholds
         const T Tw = wmax(tqp());
         int wl, wh;
         warp_window(wx, hs0, hs1, wlo(xal, Tw), whi(xbh, Tw), wl, wh);
-        scan(wl, min(wh, wi.q0));
-        scan(max(wl, wi.q1), wh);
+        bool keyed = false;
+        if constexpr (INNER) {
+          const bool in = inside(ylo_t[sq], yhi_t[sq], qyl, qyh) &&
+                          (!NEST || inside(czlo[sq * S2 + hc2], czhi[sq * S2 + hc2], qzl, qzh));
+          if (__all_sync(0xffffffffu, in || !qok)) {
+            if (in) cntq += count_keys(wl, wh);  // the window holds the own positions
+            keyed = true;
+          }
+        }
+        if (!keyed) {
+          if constexpr (INNER) scan(wi.q0, wi.q1);
+          scan(wl, min(wh, wi.q0));
+          scan(max(wl, wi.q1), wh);
+        }
       }
       if constexpr (NEST) visit_cells(sq, hc2, hc2);  // the rest of the home strip
 
@@ -645,6 +711,14 @@ wgrid_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items
           const T Tw = wmax(unf ? t : T(-1));
           int wl, wh;
           warp_window(wx, sst[s], sst[s + 1], wlo(xal, Tw), whi(xbh, Tw), wl, wh);
+          if constexpr (INNER) {
+            const bool rs = unf && !above(ylo_t[s], qyh, t) && !below(qyl, yhi_t[s], t);
+            const bool in = inside(ylo_t[s], yhi_t[s], qyl, qyh);
+            if (__all_sync(0xffffffffu, in || !rs)) {
+              if (in) cntq += count_keys(wl, wh);
+              continue;
+            }
+          }
           scan(wl, wh);
         }
       }
