@@ -215,13 +215,24 @@ def run_config(args, torch, N, ctx, dev):
         desc = ("Ross MI of x (dim 1-4, 3-component Gaussian mixtures) vs y with 2/10/25/50 "
                 "Dirichlet(.5) classes + KL entropy of a 3-D mixture, N=500,000 (one batch)")
 
+    phase_sum = {}
+    work_sum = {}
+
     def step(flags):
         _driver.run_flags = flags
         dev_ms = 0.0
         t0 = time.perf_counter()
+        phase_sum.clear()
+        work_sum.clear()
         for c in calls:
             c()
-            dev_ms += ctx.timings().get("total", 0.0) if flags & N.TIMING else 0.0
+            if flags & N.TIMING:
+                ph = ctx.timings()
+                dev_ms += ph.get("total", 0.0)
+                for key, v in ph.items():
+                    phase_sum[key] = phase_sum.get(key, 0.0) + v
+                for key, v in ctx.stats().items():
+                    work_sum[key] = work_sum.get(key, 0) + v
         torch.cuda.synchronize()
         return (time.perf_counter() - t0) * 1000.0, dev_ms
 
@@ -241,6 +252,7 @@ def run_config(args, torch, N, ctx, dev):
         with ClockSampler(dev) as clk:
             walls, _ = run_steps(0, args.steps)
         _, devs = run_steps(N.TIMING, args.steps)
+        fast_phases, fast_work = dict(phase_sum), dict(work_sum)
         plain = None
         if not args.no_plain:
             _, pdevs = run_steps(N.TIMING | N.PLAIN_FP64, 1)
@@ -258,7 +270,7 @@ def run_config(args, torch, N, ctx, dev):
                        "l2": "inputs re-uploaded by every call (host arrays)"},
             "e2e": {"value": ntask / (ms_wall / 1000.0), "unit": "MI estimates/s", "ms_per_step": ms_wall,
                     "host_ms_per_step": ms_wall - ms_dev},
-            "phases_ms_last_batch": ctx.timings(), "work_last_batch": ctx.stats(),
+            "phases_ms": fast_phases, "work": fast_work,
             "plain": plain,
             "speedup_vs_plain": (plain["ms_per_step"] / ms_dev) if plain else None,
             "clocks": clk.summary()}

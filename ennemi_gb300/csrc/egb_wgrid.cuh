@@ -188,8 +188,16 @@ __device__ __forceinline__ V warp_kth_of_lists(const V (&lst_in)[KMAX], int K, V
   return kth;
 }
 
+// Blocks per SM the register budget of a variant targets: the K <= 4 kNN
+// kernels are latency-bound and gain from occupancy more than they lose to
+// a few spilled registers outside the candidate loop.
+template <int D, int KMAX, bool COUNT>
+constexpr int wgrid_min_blocks() {
+  return (!COUNT && KMAX == 4) ? (D == 2 ? 5 : 4) : 1;
+}
+
 template <int D, int KMAX, bool PLAIN, bool COUNT, bool NEST>
-__global__ void __launch_bounds__(WG_WARPS * 32)
+__global__ void __launch_bounds__(WG_WARPS * 32, (wgrid_min_blocks<D, KMAX, COUNT>()))
 wgrid_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items, int nitems,
              int* __restrict__ counter, int dmax) {
   using T = CoordT<PLAIN>;
@@ -284,13 +292,6 @@ wgrid_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items
     float u32fix = 0.0f;                  // the same bound (a float)
     float sfix = 0.0f;                    // pass 1: FP32 screen threshold
     float tcnt = -1.0f;                   // FP32 counts: planning threshold
-    // FP32 counts of d = 2 (strips) and d = 3 (cells): a strip or cell whose
-    // other coordinates lie inside the ball for every lane is counted by key
-    // ranges of column 0 instead of scanned
-    constexpr bool INNER = COUNT && !PLAIN && (D == 2 || (NEST && D == 3));
-    uint64_t kxl = 0, kxr = 0;            // column-0 key range of the ball
-    float r32lo = -1.0f;                  // FP32 lower bound of the radius
-    bool kx_ok = false;
     double qr = -1.0;
     uint64_t rbits = 0;
     float lo = -1.0f, hi = -1.0f;
@@ -302,13 +303,6 @@ wgrid_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items
       qok = exists && (qr >= 0.0);
       rbits = qok ? (uint64_t)__double_as_longlong(qr) : 0ull;
       if (!PLAIN && qok) tcnt = plan_margin(__double2float_ru(qr));
-      if constexpr (INNER) {
-        if (qok && !isinf(qr) && !unsafe) {
-          ball_keys(qx, qr, kxl, kxr);
-          kx_ok = true;
-          r32lo = __double2float_rd(qr);
-        }
-      }
       if (!PLAIN && qok) {
         if (isinf(qr)) {
           lo = hi = FINF;
@@ -446,18 +440,24 @@ wgrid_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items
       hits &= vmask;
       if (__builtin_expect(hits != 0u, 0)) resolve(g0, hits, dst);
     };
-    auto group_mask = [](int g0, int ra, int rb) -> uint32_t {
+    // candidates of the group at g0 inside [ra, rb) and outside [ea, eb)
+    auto group_mask = [](int g0, int ra, int rb, int ea, int eb) -> uint32_t {
       uint32_t vmask = 0xFu;
       if (g0 < ra) vmask &= ~((1u << (ra - g0)) - 1u);
       if (g0 + 4 > rb) vmask &= (1u << (rb - g0)) - 1u;
+      if (g0 + 4 > ea && g0 < eb) {
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+          if (g0 + u >= ea && g0 + u < eb) vmask &= ~(1u << u);
+      }
       return vmask;
     };
 
     unsigned long long pairs = 0;  // candidate-query pairs screened by this item
-    // Screen the candidates [ra, rb) against this lane's query.
-    auto scan = [&](int ra, int rb) {
+    // Screen the candidates [ra, rb) minus [ea, eb) against this lane's query.
+    auto scan = [&](int ra, int rb, int ea, int eb) {
       if (rb <= ra) return;
-      pairs += (unsigned long long)(rb - ra) * (unsigned long long)nq;
+      pairs += (unsigned long long)(rb - ra - max(0, min(rb, eb) - max(ra, ea))) * (unsigned long long)nq;
       if constexpr (D != 0 && !PLAIN) {
         // two groups of 4 per step: both groups' loads are in flight together
         for (int g0 = ra & ~3; g0 < rb; g0 += 8) {
@@ -486,12 +486,12 @@ wgrid_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items
           EGB_WG_LANE(2)
           EGB_WG_LANE(3)
 #undef EGB_WG_LANE
-          decide(g0, group_mask(g0, ra, rb), da);
-          if (hasb) decide(g0 + 4, group_mask(g0 + 4, ra, rb), db);
+          decide(g0, group_mask(g0, ra, rb, ea, eb), da);
+          if (hasb) decide(g0 + 4, group_mask(g0 + 4, ra, rb, ea, eb), db);
         }
       } else {
         for (int g0 = ra & ~3; g0 < rb; g0 += 4) {
-          const uint32_t vmask = group_mask(g0, ra, rb);
+          const uint32_t vmask = group_mask(g0, ra, rb, ea, eb);
           float dst[4];
           uint32_t hits = 0;
 #pragma unroll
@@ -546,39 +546,6 @@ wgrid_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items
       }
       return c0 < S2 ? c0 : S2 - 1;
     };
-    // INNER: does the ball of this lane contain the column-1 range [lb, hb]
-    // (and column-2 range [lc, hc] for cells)?  Conservative in FP32.
-    auto inside = [&](T lb, T hb, T q_lo, T q_hi) -> bool {
-      if constexpr (INNER) return kx_ok && __fsub_ru(q_hi, lb) <= r32lo && __fsub_ru(hb, q_lo) <= r32lo;
-      else return false;
-    };
-    // INNER: points of [a, b) whose column-0 key lies in [kxl, kxr]
-    auto count_keys = [&](int a, int b) -> int {
-      const unsigned long long* xb = reinterpret_cast<const unsigned long long*>(c64);
-      int lo = a, n = b - a;
-      while (n > 0) {  // first key >= kxl
-        const int h = n >> 1;
-        if (raw_key(xb[lo + h]) < kxl) {
-          lo += h + 1;
-          n -= h + 1;
-        } else {
-          n = h;
-        }
-      }
-      int hi = lo;
-      n = b - lo;
-      while (n > 0) {  // first key > kxr
-        const int h = n >> 1;
-        if (raw_key(xb[hi + h]) <= kxr) {
-          hi += h + 1;
-          n -= h + 1;
-        } else {
-          n = h;
-        }
-      }
-      return hi - lo;
-    };
-
     // Nested grids: the cells of strip s that some lane still needs, outward
     // in column 2 from cell c0 (cell `skip` already scanned).  A lane needs a
     // cell while the strip's column-1 range and the cell's column-2 range are
@@ -610,14 +577,7 @@ wgrid_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items
         const T Tw = wmax(nd ? t : T(-1));
         int wl, wh;
         warp_window(wx, cst[cb + c], cst[cb + c + 1], wlo(xal, Tw), whi(xbh, Tw), wl, wh);
-        if constexpr (INNER) {
-          const bool in = inside(ylo_t[s], yhi_t[s], qyl, qyh) && inside(czlo[cb + c], czhi[cb + c], qzl, qzh);
-          if (__all_sync(0xffffffffu, in || !nd)) {
-            if (in) cntq += count_keys(wl, wh);
-            continue;
-          }
-        }
-        scan(wl, wh);
+        scan(wl, wh, 0, 0);
       }
     };
 
@@ -654,32 +614,20 @@ wgrid_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items
           sfix = need ? s32 : -1.0f;
         }
       }
-      // ---- own positions, then the home strip's window
+      // ---- own positions (they seed the kNN thresholds), then the rest of
+      // the home strip's (cell's) window
+      scan(wi.q0, wi.q1, 0, 0);
       {
-        if constexpr (!INNER) scan(wi.q0, wi.q1);  // kNN: seeds the thresholds
         const T Tw = wmax(tqp());
         int wl, wh;
         warp_window(wx, hs0, hs1, wlo(xal, Tw), whi(xbh, Tw), wl, wh);
-        bool keyed = false;
-        if constexpr (INNER) {
-          const bool in = inside(ylo_t[sq], yhi_t[sq], qyl, qyh) &&
-                          (!NEST || inside(czlo[sq * S2 + hc2], czhi[sq * S2 + hc2], qzl, qzh));
-          if (__all_sync(0xffffffffu, in || !qok)) {
-            if (in) cntq += count_keys(wl, wh);  // the window holds the own positions
-            keyed = true;
-          }
-        }
-        if (!keyed) {
-          if constexpr (INNER) scan(wi.q0, wi.q1);
-          scan(wl, min(wh, wi.q0));
-          scan(max(wl, wi.q1), wh);
-        }
+        scan(wl, wh, wi.q0, wi.q1);
       }
-      if constexpr (NEST) visit_cells(sq, hc2, hc2);  // the rest of the home strip
 
-      // ---- other strips
+      // ---- other strips (nested grids: first the other cells of the home strip)
       int up = sq + 1, dn = sq - 1;
       bool turn_up = true;
+      bool home_cells = NEST;
       auto unfinished = [&]() -> bool {
         if (!qok) return false;
         const T t = tqp();
@@ -688,6 +636,11 @@ wgrid_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items
         return !(u && l);
       };
       for (;;) {
+        if (NEST && home_cells) {
+          home_cells = false;
+          visit_cells(sq, hc2, hc2);
+          continue;
+        }
         const bool unf = unfinished();
         const unsigned ub = __ballot_sync(0xffffffffu, unf);
         if (ub == 0u || __popc(ub) <= OUTLIER_LANES) break;
@@ -711,15 +664,7 @@ wgrid_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items
           const T Tw = wmax(unf ? t : T(-1));
           int wl, wh;
           warp_window(wx, sst[s], sst[s + 1], wlo(xal, Tw), whi(xbh, Tw), wl, wh);
-          if constexpr (INNER) {
-            const bool rs = unf && !above(ylo_t[s], qyh, t) && !below(qyl, yhi_t[s], t);
-            const bool in = inside(ylo_t[s], yhi_t[s], qyl, qyh);
-            if (__all_sync(0xffffffffu, in || !rs)) {
-              if (in) cntq += count_keys(wl, wh);
-              continue;
-            }
-          }
-          scan(wl, wh);
+          scan(wl, wh, 0, 0);
         }
       }
 
