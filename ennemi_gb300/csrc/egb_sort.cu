@@ -82,18 +82,12 @@ __global__ void sort_hist_kernel(const SortSeg* __restrict__ segs,
   __shared__ uint32_t h[256];
   const int b = blockIdx.x;
   const SortSeg s = segs[blk_seg[b]];
-  const int lane = threadIdx.x & 31;
   h[threadIdx.x] = 0;
   __syncthreads();
   const int i0 = (b - s.blk0) * SORT_TILE;
   const int i1 = min(i0 + SORT_TILE, s.len);
-  for (int r0 = i0; r0 < i1; r0 += SORT_THREADS) {  // one shared atomic per digit and warp
-    const int i = r0 + threadIdx.x;
-    const bool valid = i < i1;
-    const uint32_t dgt = valid ? (uint32_t)(keys[s.out_base + i] >> shift) & 255u : 256u + lane;
-    const uint32_t peers = __match_any_sync(0xffffffffu, dgt);
-    if (valid && (peers & ((1u << lane) - 1u)) == 0) atomicAdd(&h[dgt], (uint32_t)__popc(peers));
-  }
+  for (int i = i0 + threadIdx.x; i < i1; i += SORT_THREADS)
+    atomicAdd(&h[(uint32_t)(keys[s.out_base + i] >> shift) & 255u], 1u);
   __syncthreads();
   const int lb = b - s.blk0;
   hist[(int64_t)256 * s.blk0 + (int64_t)threadIdx.x * s.nblk + lb] = h[threadIdx.x];
