@@ -640,6 +640,8 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
     J.seg_begin = (int32_t)m.s.b;
     J.len = (int32_t)len;
     J.K = m.is_knn ? m.s.K : 0;
+    // FP32-path warp-grid counts of d = 2, 3 run on keys (egb_wcount.cu)
+    J.kform = (m.mode == 3 && !m.is_knn && !plain && count_keys_supported(m.s.sp.d)) ? 1 : 0;
     J.slab = m.slab;
     J.sort_seg = m.sort_seg;
     J.sp = m.s.sp;

@@ -241,7 +241,9 @@ struct JobDev {
   int32_t slab;           // 1: sorted by the first column
   int32_t sort_seg;       // slab: index of the sort segment of column 0
   int32_t sort_seg_b;     // slab: sort segment of column 1 (second order)
-  int32_t pad_;
+  int32_t kform;          // grid copy holds order-preserving keys, not values:
+                          // column c's high words at (uint32*)c64g + 2c*lds,
+                          // low words at + (2c+1)*lds (key-range count jobs)
   // slab jobs: a second copy sorted by column 1, scanned by deferred queries
   // whose column-1 slab is narrower than their column-0 slab
   double* c64b;

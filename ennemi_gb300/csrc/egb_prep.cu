@@ -173,16 +173,29 @@ __global__ void materialize_grid_kernel(const TaskDev* __restrict__ tasks,
         for (int c = 0; c < d; ++c) {
           const int tc = J.sp.cols[c];
           const double v = t.x64[(int64_t)tc * t.ld + w];
-          J.c64g[(int64_t)c * J.lds + p] = v;
-          J.c32g[(int64_t)c * J.lds + p] =
-              __double2float_rn(fmin(fmax(v - t.center[tc], -1e37), 1e37));
+          if (J.kform) {
+            const uint64_t k = raw_key((uint64_t)__double_as_longlong(v));
+            uint32_t* kw = reinterpret_cast<uint32_t*>(J.c64g);
+            kw[(int64_t)(2 * c) * J.lds + p] = (uint32_t)(k >> 32);
+            kw[(int64_t)(2 * c + 1) * J.lds + p] = (uint32_t)k;
+          } else {
+            J.c64g[(int64_t)c * J.lds + p] = v;
+            J.c32g[(int64_t)c * J.lds + p] =
+                __double2float_rn(fmin(fmax(v - t.center[tc], -1e37), 1e37));
+          }
         }
       } else {
         J.posg[p] = 0;
         J.idxg[p] = J.seg_begin;
         for (int c = 0; c < d; ++c) {
-          J.c64g[(int64_t)c * J.lds + p] = 0.0;
-          J.c32g[(int64_t)c * J.lds + p] = 0.0f;
+          if (J.kform) {
+            uint32_t* kw = reinterpret_cast<uint32_t*>(J.c64g);
+            kw[(int64_t)(2 * c) * J.lds + p] = 0u;
+            kw[(int64_t)(2 * c + 1) * J.lds + p] = 0u;
+          } else {
+            J.c64g[(int64_t)c * J.lds + p] = 0.0;
+            J.c32g[(int64_t)c * J.lds + p] = 0.0f;
+          }
         }
       }
     }

@@ -10,7 +10,9 @@
 // steps per query.  The ball is then the box of those key ranges, exactly.
 //
 // Layout: the job's grid copy (strips by column 1, nested cells by column 2
-// for d = 3, column-0 order inside).  A warp takes an item of up to 32
+// for d = 3, column-0 order inside), holding the keys themselves as high and
+// low 32-bit words (JobDev::kform): most comparisons are settled by the high
+// words, and the low word is read only on a tie.  A warp takes an item of up to 32
 // queries of one strip (cell) and visits the strips outward from its own
 // while some lane's column-1 key range reaches them; in a nested grid, the
 // cells of each strip whose column-2 range meets some lane's.  In each strip
@@ -25,6 +27,31 @@ namespace egb {
 namespace {
 
 constexpr int WC_WARPS = 4;
+
+// One key column of the grid copy: high words, then low words.
+struct KeyCol {
+  const uint32_t* __restrict__ hi;
+  const uint32_t* __restrict__ lo;
+  __device__ __forceinline__ uint64_t key(int p) const {
+    return ((uint64_t)hi[p] << 32) | lo[p];
+  }
+  __device__ __forceinline__ bool lt(int p, uint64_t k) const {  // key(p) < k
+    const uint32_t h = hi[p], kh = (uint32_t)(k >> 32);
+    return h < kh || (h == kh && lo[p] < (uint32_t)k);
+  }
+  __device__ __forceinline__ bool le(int p, uint64_t k) const {  // key(p) <= k
+    const uint32_t h = hi[p], kh = (uint32_t)(k >> 32);
+    return h < kh || (h == kh && lo[p] <= (uint32_t)k);
+  }
+  // key(p) in [a, b]
+  __device__ __forceinline__ bool in(int p, uint64_t a, uint64_t b) const {
+    const uint32_t h = hi[p], ah = (uint32_t)(a >> 32), bh = (uint32_t)(b >> 32);
+    if (h > ah && h < bh) return true;
+    if (h < ah || h > bh) return false;
+    const uint64_t k = ((uint64_t)h << 32) | lo[p];
+    return k >= a && k <= b;
+  }
+};
 
 __device__ __forceinline__ uint64_t rkey(uint64_t u) { return raw_key(u); }
 
@@ -46,11 +73,10 @@ __device__ __forceinline__ uint64_t wmax64(uint64_t v) {
 }
 
 // Positions [wlo, whi) of [s0, s1) whose column-0 key lies in [lo, hi]
-// (x sorted): the lower half-warp finds the first key >= lo, the upper half
-// the first key > hi, 16-ary.
-__device__ __forceinline__ void warp_window_keys(const unsigned long long* __restrict__ x, int s0,
-                                                 int s1, uint64_t lo, uint64_t hi, int& wlo,
-                                                 int& whi) {
+// (keys sorted): the lower half-warp finds the first key >= lo, the upper
+// half the first key > hi, 16-ary.
+__device__ __forceinline__ void warp_window_keys(const KeyCol& x, int s0, int s1, uint64_t lo,
+                                                 uint64_t hi, int& wlo, int& whi) {
   const int lane = threadIdx.x & 31;
   const bool upper = lane >= 16;
   const int l16 = lane & 15;
@@ -62,8 +88,7 @@ __device__ __forceinline__ void warp_window_keys(const unsigned long long* __res
     int p = small ? a + l16 : a + (int)((int64_t)(l16 + 1) * n / 17);
     const bool inr = p < b;
     p = inr ? p : s0;
-    const uint64_t k = rkey(x[p]);
-    const bool t = inr && (upper ? (k <= hi) : (k < lo));
+    const bool t = inr && (upper ? x.le(p, hi) : x.lt(p, lo));
     const int c = __popc(__ballot_sync(0xffffffffu, t) & m);
     if (small) {
       a = a + c;
@@ -81,13 +106,12 @@ __device__ __forceinline__ void warp_window_keys(const unsigned long long* __res
   if (whi < wlo) whi = wlo;
 }
 
-// First position of [a, b) with key >= k (x sorted).
-__device__ __forceinline__ int lower_key(const unsigned long long* __restrict__ x, int a, int b,
-                                         uint64_t k) {
+// First position of [a, b) with key >= k (keys sorted).
+__device__ __forceinline__ int lower_key(const KeyCol& x, int a, int b, uint64_t k) {
   int n = b - a;
   while (n > 0) {
     const int h = n >> 1;
-    if (rkey(x[a + h]) < k) {
+    if (x.lt(a + h, k)) {
       a += h + 1;
       n -= h + 1;
     } else {
@@ -97,12 +121,11 @@ __device__ __forceinline__ int lower_key(const unsigned long long* __restrict__ 
   return a;
 }
 // First position of [a, b) with key > k.
-__device__ __forceinline__ int upper_key(const unsigned long long* __restrict__ x, int a, int b,
-                                         uint64_t k) {
+__device__ __forceinline__ int upper_key(const KeyCol& x, int a, int b, uint64_t k) {
   int n = b - a;
   while (n > 0) {
     const int h = n >> 1;
-    if (rkey(x[a + h]) <= k) {
+    if (x.le(a + h, k)) {
       a += h + 1;
       n -= h + 1;
     } else {
@@ -127,9 +150,9 @@ wcount_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ item
     const JobDev* __restrict__ J = jobs + wi.job;
     const int len = J->len;
     const int64_t lds = J->lds;
-    const unsigned long long* __restrict__ xb = reinterpret_cast<const unsigned long long*>(J->c64g);
-    const unsigned long long* __restrict__ yb = xb + lds;
-    const unsigned long long* __restrict__ zb = xb + 2 * lds;
+    const uint32_t* kw = reinterpret_cast<const uint32_t*>(J->c64g);
+    const KeyCol xk{kw, kw + lds}, yk{kw + 2 * lds, kw + 3 * lds};
+    const KeyCol zk{kw + 4 * lds, kw + 5 * lds};  // d = 3 only
     const int32_t* __restrict__ sst = J->sstart;
     const unsigned long long* __restrict__ sylo = reinterpret_cast<const unsigned long long*>(J->sylo);
     const unsigned long long* __restrict__ syhi = reinterpret_cast<const unsigned long long*>(J->syhi);
@@ -147,9 +170,9 @@ wcount_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ item
     uint64_t kxl = 1, kxr = 0, kyl = 1, kyr = 0, kzl = 1, kzr = 0;  // empty ranges
     const bool act = qok && !every;
     if (act) {
-      ball_keys(__longlong_as_double((long long)xb[qp]), qr, kxl, kxr);
-      ball_keys(__longlong_as_double((long long)yb[qp]), qr, kyl, kyr);
-      if (D == 3) ball_keys(__longlong_as_double((long long)zb[qp]), qr, kzl, kzr);
+      ball_keys(raw_value(xk.key(qp)), qr, kxl, kxr);
+      ball_keys(raw_value(yk.key(qp)), qr, kyl, kyr);
+      if (D == 3) ball_keys(raw_value(zk.key(qp)), qr, kzl, kzr);
     }
     int cnt = every ? len : 0;
     unsigned long long checked = 0;
@@ -160,22 +183,18 @@ wcount_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ item
       const uint64_t ul = wmin64(reach ? kxl : ~0ull);
       const uint64_t uh = wmax64(reach ? kxr : 0ull);
       int wl, wh;
-      warp_window_keys(xb, a, b, ul, uh, wl, wh);
+      warp_window_keys(xk, a, b, ul, uh, wl, wh);
       if (!reach) return;
-      const int pl = lower_key(xb, wl, wh, kxl);
-      const int ph = upper_key(xb, pl, wh, kxr);
+      const int pl = lower_key(xk, wl, wh, kxl);
+      const int ph = upper_key(xk, pl, wh, kxr);
       if (inner) {
         cnt += ph - pl;
         return;
       }
       checked += (unsigned long long)(ph - pl);
       for (int p = pl; p < ph; ++p) {
-        const uint64_t ky = rkey(yb[p]);
-        bool in = ky >= kyl && ky <= kyr;
-        if (D == 3) {
-          const uint64_t kz = rkey(zb[p]);
-          in = in && kz >= kzl && kz <= kzr;
-        }
+        bool in = yk.in(p, kyl, kyr);
+        if (D == 3) in = in && zk.in(p, kzl, kzr);
         cnt += in ? 1 : 0;
       }
     };
