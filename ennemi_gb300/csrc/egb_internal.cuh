@@ -457,6 +457,9 @@ void launch_count_grid(const JobDev* jobs_d, const WorkItem* items_d, int nitems
 constexpr int WG_QB = 32;
 void launch_knn_wgrid(const JobDev* jobs_d, const WorkItem* items_d, int nitems, int kclass,
                       int dclass, int plain, int dmax, int* counter, int num_sms, cudaStream_t st);
+// egb_wwalk.cu: FP32-path kNN of warp-grid jobs (K <= 8) by per-lane walks
+void launch_knn_walk(const JobDev* jobs_d, const WorkItem* items_d, int nitems, int kclass,
+                     int dclass, int* counter, int num_sms, cudaStream_t st);
 // egb_wcount.cu: exact key-range ball counts of d = 2 / nested d = 3
 // warp-grid jobs (FP32 path; the FP64 comparator keeps launch_count_wgrid)
 bool count_keys_supported(int dclass);

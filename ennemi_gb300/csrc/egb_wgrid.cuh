@@ -670,6 +670,7 @@ wgrid_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items
 
       // ---- remaining unfinished queries: one at a time, all lanes cooperating
       unsigned rest = __ballot_sync(0xffffffffu, unfinished());
+      if (lane == 0 && rest) atomicAdd(J->stats + 1, (unsigned long long)__popc(rest));
       while (rest) {
         const int ol = __ffs(rest) - 1;
         rest &= rest - 1u;

@@ -1,0 +1,323 @@
+// egb_wwalk.cu -- kNN distances of warp-grid jobs by per-lane walks.
+//
+// (k+1)-th smallest max-norm distance per point, self included, over the
+// job's grid copy (strips by column 1; nested cells by column 2 for d >= 3;
+// column-0 order inside): cKDTree.query(k=[k+1], p=inf)
+// (ennemi/_entropy_estimators.py:39, :108, :142, :194, :240).
+//
+// A warp takes an item of up to 32 consecutive positions of one strip
+// (cell), one query per lane, and every lane then works alone: it walks
+// outward in column 0 from its own position -- always to the nearer of the
+// next point on the left and on the right -- while that point's column-0 gap
+// is within the lane's current screen bound; then the other cells of its
+// strip outward in column 2, then the other strips outward in column 1, each
+// while its column-1 (column-2) gap is within the lane's planning bound,
+// starting each walk at the binary-searched position of the query's column 0.
+// A lane thus screens only the points of its own neighbourhood, instead of
+// the union window of 32 queries.
+//
+// Exactness as in egb_wgrid.cuh.  Pass 0 keeps the K smallest FP32 distances
+// with their candidates and `rej`, the least FP32 distance of every visited
+// candidate left out of the list.  With t32 the FP32 K-th, U = t32 + band
+// and S = U + band (band proven in egb_internal.cuh):
+//   * a walk stops a direction when the column-0 FP32 gap exceeds S, so every
+//     unvisited point of a walked range has FP32 distance > S;
+//   * a strip or cell is skipped when its column-1 / column-2 gap exceeds
+//     plan_margin(U) on bounds rounded outward, so its points are farther
+//     than U in FP64;
+//   * if rej > S, every candidate outside the list is farther than U >= the
+//     exact K-th, and the exact K-th is the largest exact distance of the K
+//     listed candidates.
+// Lanes without that margin (near ties, fewer than K candidates, jobs whose
+// centred values reach 1e37) walk again with U fixed, deciding in FP64 every
+// candidate with FP32 distance <= S.
+#include "egb_wgrid.cuh"
+
+namespace egb {
+namespace {
+
+using wgrid_detail::insert_sorted;
+using wgrid_detail::insert_sorted_fi;
+using wgrid_detail::hi32_of;
+using wgrid_detail::lo32_of;
+using wgrid_detail::plan_margin;
+using wgrid_detail::up_band32;
+
+constexpr int WW_WARPS = 4;
+
+// First position of [a, b) with x[p] >= v (x ascending).
+__device__ __forceinline__ int lower_bound_f(const float* __restrict__ x, int a, int b, float v) {
+  int n = b - a;
+  while (n > 0) {
+    const int h = n >> 1;
+    if (x[a + h] < v) {
+      a += h + 1;
+      n -= h + 1;
+    } else {
+      n = h;
+    }
+  }
+  return a;
+}
+
+template <int D, int KMAX, bool NEST>
+__global__ void __launch_bounds__(WW_WARPS * 32)
+wwalk_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items, int nitems,
+             int* __restrict__ counter) {
+  constexpr int DQ = D ? D : EGB_DMAX;
+  constexpr float FINF = __builtin_huge_valf();
+  const int lane = threadIdx.x & 31;
+
+  for (;;) {
+    int it = 0;
+    if (lane == 0) it = atomicAdd(counter, 1);
+    it = __shfl_sync(0xffffffffu, it, 0);
+    if (it >= nitems) break;
+    const WorkItem wi = items[it];
+    const JobDev* __restrict__ J = jobs + wi.job;
+    const int qp = wi.q0 + lane;
+    const bool exists = qp < wi.q1;
+    unsigned long long visited = 0;
+    bool again = false;
+
+    if (exists) {
+      const int d = D ? D : J->sp.d;
+      const int64_t lds = J->lds;
+      const double* __restrict__ c64 = J->c64g;
+      const float* __restrict__ g = J->c32g;
+      const int32_t* __restrict__ sst = J->sstart;
+      const float* __restrict__ ylo = J->sylo32;
+      const float* __restrict__ yhi = J->syhi32;
+      const int S = J->nstrips;
+      const int S2 = NEST ? J->nsub : 1;
+      const int32_t* __restrict__ cst = J->cstart;
+      const float* __restrict__ zlo = J->czlo32;
+      const float* __restrict__ zhi = J->czhi32;
+      const bool unsafe = (*J->jflags & TF_UNSAFE32) != 0u;
+      const int K = J->K;
+      const int sq = NEST ? (wi.strip & 0xffff) : wi.strip;
+      const int hc2 = NEST ? (wi.strip >> 16) : 0;
+
+      float qv[DQ];
+      double m = 0.0;
+#pragma unroll
+      for (int c = 0; c < DQ; ++c) {
+        if (D == 0 && c >= d) break;
+        qv[c] = g[(int64_t)c * lds + qp];
+        const double v = fabs(c64[(int64_t)c * lds + qp] - J->center[c]);
+        m = v > m ? v : m;
+      }
+      const float mq = __double2float_ru(m);
+      const double qy = c64[lds + qp];
+      const float qyl = lo32_of(qy, J->center[1]), qyh = hi32_of(qy, J->center[1]);
+      float qzl = 0.0f, qzh = 0.0f;
+      if (NEST) {
+        const double qz = c64[2 * lds + qp];
+        qzl = lo32_of(qz, J->center[2]);
+        qzh = hi32_of(qz, J->center[2]);
+      }
+
+      float l32[KMAX];   // pass 0: K smallest FP32 distances (padding first)
+      int i32[KMAX];     // their candidates
+      uint64_t top[KMAX];  // pass 1: K smallest exact distances (bit patterns)
+#pragma unroll
+      for (int s = 0; s < KMAX; ++s) {
+        l32[s] = s >= KMAX - K ? FINF : 0.0f;
+        i32[s] = 0;
+        top[s] = s >= KMAX - K ? INF_BITS : 0ull;
+      }
+      float rej = FINF;          // least FP32 distance left out of the list
+      bool pass1 = unsafe;       // unsafe jobs decide everything in FP64
+      float ufix = FINF, sfix = FINF;
+
+      auto exact_dist = [&](int j) -> uint64_t {
+        uint64_t mm = 0;
+#pragma unroll
+        for (int c = 0; c < DQ; ++c) {
+          if (D == 0 && c >= d) break;
+          const int64_t off = (int64_t)c * lds;
+          const uint64_t v = absdiff_bits(c64[off + j], c64[off + qp]);
+          mm = v > mm ? v : mm;
+        }
+        return mm;
+      };
+      // screen bound S and planning bound plan_margin(U)
+      auto sbound = [&]() -> float {
+        if (pass1) return sfix;
+        return up_band32(up_band32(l32[KMAX - 1], mq), mq);
+      };
+      auto pbound = [&]() -> float {
+        if (pass1) return plan_margin(ufix);
+        return plan_margin(up_band32(l32[KMAX - 1], mq));
+      };
+      auto visit = [&](int j, float dd) {
+        ++visited;
+        if (!pass1) {
+          rej = fminf(rej, dd < l32[KMAX - 1] ? insert_sorted_fi<KMAX>(l32, i32, dd, j) : dd);
+        } else if (dd <= sfix) {
+          const uint64_t mm = exact_dist(j);
+          if (mm < top[KMAX - 1]) insert_sorted<KMAX>(top, mm);
+        }
+      };
+      // Walk [a, b) outward from p0 (the first position whose column 0 is
+      // >= the query's): nearer side first, until both sides pass S.
+      auto walk = [&](int a, int b, int p0) {
+        int L = p0 - 1, R = p0;
+        float dl = L >= a ? qv[0] - g[L] : FINF;
+        float dr = R < b ? g[R] - qv[0] : FINF;
+        for (;;) {
+          const bool go_l = dl <= dr;
+          const float dx = go_l ? dl : dr;
+          // both sides exhausted (real gaps are finite: values are clamped
+          // to +-1e37), or the nearer side is beyond the screen bound
+          if (!(dx < FINF) || !(dx <= sbound())) break;
+          const int j = go_l ? L : R;
+          float dd = dx;
+#pragma unroll
+          for (int c = 1; c < DQ; ++c) {
+            if (D == 0 && c >= d) break;
+            dd = fmaxf(dd, fabsf(g[(int64_t)c * lds + j] - qv[c]));
+          }
+          visit(j, dd);
+          if (go_l) {
+            --L;
+            dl = L >= a ? qv[0] - g[L] : FINF;
+          } else {
+            ++R;
+            dr = R < b ? g[R] - qv[0] : FINF;
+          }
+        }
+      };
+      // Nested grids: the cells of strip s outward in column 2 from c0
+      // (cell `skip` already walked).
+      auto cells = [&](int s, int c0, int skip) {
+        const int cb = s * S2;
+        int up = c0, dn = c0 - 1;
+        for (;;) {
+          const float t = pbound();
+          const bool ou = up < S2 && !(__fsub_rd(zlo[cb + up], qzh) > t);
+          const bool od = dn >= 0 && !(__fsub_rd(qzl, zhi[cb + dn]) > t);
+          if (!ou && !od) break;
+          int c;
+          if (ou && (!od || __fsub_rd(zlo[cb + up], qzh) <= __fsub_rd(qzl, zhi[cb + dn]))) c = up++;
+          else c = dn--;
+          if (c == skip) continue;
+          const int a = cst[cb + c], b = cst[cb + c + 1];
+          walk(a, b, lower_bound_f(g, a, b, qv[0]));
+        }
+      };
+      // the whole search: home strip (cell), then strips outward in column 1
+      auto search = [&]() {
+        if (NEST) {
+          const int cb = sq * S2;
+          walk(cst[cb + hc2], cst[cb + hc2 + 1], qp);
+          cells(sq, hc2, hc2);
+        } else {
+          walk(sst[sq], sst[sq + 1], qp);
+        }
+        int up = sq + 1, dn = sq - 1;
+        for (;;) {
+          const float t = pbound();
+          const bool ou = up < S && !(__fsub_rd(ylo[up], qyh) > t);
+          const bool od = dn >= 0 && !(__fsub_rd(qyl, yhi[dn]) > t);
+          if (!ou && !od) break;
+          int s;
+          if (ou && (!od || __fsub_rd(ylo[up], qyh) <= __fsub_rd(qyl, yhi[dn]))) s = up++;
+          else s = dn--;
+          if (NEST) {
+            // first cell of the strip whose column-2 range reaches the query
+            int lo = 0, n = S2;
+            while (n > 0) {
+              const int h = n >> 1;
+              if (zhi[s * S2 + lo + h] < qzl) {
+                lo += h + 1;
+                n -= h + 1;
+              } else {
+                n = h;
+              }
+            }
+            cells(s, lo < S2 ? lo : S2 - 1, -1);
+          } else {
+            const int a = sst[s], b = sst[s + 1];
+            walk(a, b, lower_bound_f(g, a, b, qv[0]));
+          }
+        }
+      };
+
+      uint64_t kth;
+      if (!pass1) {
+        search();
+        const float u32 = up_band32(l32[KMAX - 1], mq);
+        const float s32 = up_band32(u32, mq);
+        if (rej > s32) {
+          // every left-out candidate is farther than U >= the exact K-th
+          uint64_t mx = 0;
+#pragma unroll
+          for (int s = 0; s < KMAX; ++s) {
+            if (s >= KMAX - K) {
+              const uint64_t e = exact_dist(i32[s]);
+              mx = e > mx ? e : mx;
+            }
+          }
+          kth = mx;
+        } else {
+          again = true;
+          pass1 = true;
+          ufix = u32;
+          sfix = s32;
+          search();
+          kth = top[KMAX - 1];
+        }
+      } else {
+        again = true;
+        search();
+        kth = top[KMAX - 1];
+      }
+      J->eps[J->idxg[qp]] = bits_to_double(kth);
+    }
+
+    const unsigned long long tot = __reduce_add_sync(0xffffffffu, (unsigned)visited);
+    const unsigned agm = __ballot_sync(0xffffffffu, again);
+    if (lane == 0) {
+      atomicAdd(J->stats + 0, tot);
+      if (agm) atomicAdd(J->stats + 2, (unsigned long long)__popc(agm));
+    }
+  }
+}
+
+template <int D, int KMAX, bool NEST>
+void launch_t(const JobDev* jobs, const WorkItem* items, int nitems, int* counter, int num_sms,
+              cudaStream_t st) {
+  auto kern = wwalk_kernel<D, KMAX, NEST>;
+  int per_sm = 1;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, WW_WARPS * 32, 0);
+  if (per_sm < 1) per_sm = 1;
+  int grid = num_sms * per_sm;
+  const int need = (nitems + WW_WARPS - 1) / WW_WARPS;
+  if (grid > need) grid = need;
+  if (grid < 1) return;
+  kern<<<grid, WW_WARPS * 32, 0, st>>>(jobs, items, nitems, counter);
+  count_launch();
+}
+
+template <int KMAX>
+void launch_k(int dclass, const JobDev* jobs, const WorkItem* items, int nitems, int* counter,
+              int num_sms, cudaStream_t st) {
+  switch (dclass) {
+    case 2: launch_t<2, KMAX, false>(jobs, items, nitems, counter, num_sms, st); break;
+    case 3: launch_t<3, KMAX, true>(jobs, items, nitems, counter, num_sms, st); break;
+    case 4: launch_t<4, KMAX, true>(jobs, items, nitems, counter, num_sms, st); break;
+    default: launch_t<0, KMAX, true>(jobs, items, nitems, counter, num_sms, st); break;
+  }
+}
+
+}  // namespace
+
+void launch_knn_walk(const JobDev* jobs_d, const WorkItem* items_d, int nitems, int kclass,
+                     int dclass, int* counter, int num_sms, cudaStream_t st) {
+  if (nitems <= 0) return;
+  if (kclass <= 4) launch_k<4>(dclass, jobs_d, items_d, nitems, counter, num_sms, st);
+  else launch_k<8>(dclass, jobs_d, items_d, nitems, counter, num_sms, st);
+}
+
+}  // namespace egb
