@@ -6,15 +6,16 @@
 // (ennemi/_entropy_estimators.py:39, :108, :142, :194, :240).
 //
 // A warp takes an item of up to 32 consecutive positions of one strip
-// (cell), one query per lane, and every lane then works alone: it walks
-// outward in column 0 from its own position -- always to the nearer of the
-// next point on the left and on the right -- while that point's column-0 gap
-// is within the lane's current screen bound; then the other cells of its
-// strip outward in column 2, then the other strips outward in column 1, each
-// while its column-1 (column-2) gap is within the lane's planning bound,
-// starting each walk at the binary-searched position of the query's column 0.
-// A lane thus screens only the points of its own neighbourhood, instead of
-// the union window of 32 queries.
+// (cell), one query per lane.  Every lane walks outward in column 0 from its
+// own position -- always to the nearer of the next point on the left and on
+// the right -- while that point's column-0 gap is within the lane's current
+// screen bound.  Then the warp visits, together, the other cells of the
+// strip outward in column 2 and the other strips outward in column 1, while
+// some lane's planning bound reaches them; in each one, every lane that it
+// reaches walks again from the binary-searched position of its query's
+// column 0.  A lane thus screens only the points of its own neighbourhood,
+// not the union window of 32 queries, while the control flow of the warp
+// stays uniform outside the walks.
 //
 // Exactness as in egb_wgrid.cuh.  Pass 0 keeps the K smallest FP32 distances
 // with their candidates and `rej`, the least FP32 distance of every visited
@@ -38,8 +39,6 @@ namespace {
 
 using wgrid_detail::insert_sorted;
 using wgrid_detail::insert_sorted_fi;
-using wgrid_detail::hi32_of;
-using wgrid_detail::lo32_of;
 using wgrid_detail::plan_margin;
 using wgrid_detail::up_band32;
 
@@ -75,178 +74,207 @@ wwalk_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items
     if (it >= nitems) break;
     const WorkItem wi = items[it];
     const JobDev* __restrict__ J = jobs + wi.job;
+    const int d = D ? D : J->sp.d;
+    const int64_t lds = J->lds;
+    const double* __restrict__ c64 = J->c64g;
+    const float* __restrict__ g = J->c32g;
+    const int32_t* __restrict__ sst = J->sstart;
+    const float* __restrict__ ylo = J->sylo32;
+    const float* __restrict__ yhi = J->syhi32;
+    const int S = J->nstrips;
+    const int S2 = NEST ? J->nsub : 1;
+    const int32_t* __restrict__ cst = J->cstart;
+    const float* __restrict__ zlo = J->czlo32;
+    const float* __restrict__ zhi = J->czhi32;
+    const bool unsafe = (*J->jflags & TF_UNSAFE32) != 0u;
+    const int K = J->K;
+    const int sq = NEST ? (wi.strip & 0xffff) : wi.strip;
+    const int hc2 = NEST ? (wi.strip >> 16) : 0;
+    const int nq = wi.q1 - wi.q0;
     const int qp = wi.q0 + lane;
     const bool exists = qp < wi.q1;
+
+    // qv = fl32(fl64(q - c)); for a job without clamped values
+    // |fl32(fl64(v)) - v| <= 2^-22 |fl32(..)| + 2^-148 bounds v = q - c,
+    // which gives M = max_c |q_c - c| and the planning bounds of columns 1
+    // and 2 without FP64 instructions (jobs with clamped values run the FP64
+    // pass, whose bounds are infinite)
+    float qv[DQ];
+    float am = 0.0f;
+#pragma unroll
+    for (int c = 0; c < DQ; ++c) {
+      if (D == 0 && c >= d) break;
+      qv[c] = exists ? g[(int64_t)c * lds + qp] : 0.0f;
+      am = fmaxf(am, fabsf(qv[c]));
+    }
+    const float mq = __fmaf_ru(am, 1.0f + 0x1p-22f, 0x1p-148f);
+    const float ey = __fmaf_ru(fabsf(qv[1]), 0x1p-22f, 0x1p-148f);
+    const float qyl = __fsub_rd(qv[1], ey), qyh = __fadd_ru(qv[1], ey);
+    float qzl = 0.0f, qzh = 0.0f;
+    if (NEST) {
+      const float ez = __fmaf_ru(fabsf(qv[2]), 0x1p-22f, 0x1p-148f);
+      qzl = __fsub_rd(qv[2], ez);
+      qzh = __fadd_ru(qv[2], ez);
+    }
+    // column-2 centre of the item: where the cells of other strips start
+    const float zmid = NEST ? __shfl_sync(0xffffffffu, qv[NEST ? 2 : 0], (nq - 1) >> 1) : 0.0f;
+
+    float l32[KMAX];     // pass 0: K smallest FP32 distances (padding first)
+    int i32[KMAX];       // their candidates
+    uint64_t top[KMAX];  // pass 1: K smallest exact distances (bit patterns)
+#pragma unroll
+    for (int s = 0; s < KMAX; ++s) {
+      l32[s] = s >= KMAX - K ? FINF : 0.0f;
+      i32[s] = 0;
+      top[s] = s >= KMAX - K ? INF_BITS : 0ull;
+    }
+    float rej = FINF;      // least FP32 distance left out of the list
+    bool pass1 = unsafe;   // jobs with clamped values decide everything in FP64
+    float ufix = FINF, sfix = FINF;
+    bool act = exists;     // this lane searches in the current pass
     unsigned long long visited = 0;
-    bool again = false;
 
-    if (exists) {
-      const int d = D ? D : J->sp.d;
-      const int64_t lds = J->lds;
-      const double* __restrict__ c64 = J->c64g;
-      const float* __restrict__ g = J->c32g;
-      const int32_t* __restrict__ sst = J->sstart;
-      const float* __restrict__ ylo = J->sylo32;
-      const float* __restrict__ yhi = J->syhi32;
-      const int S = J->nstrips;
-      const int S2 = NEST ? J->nsub : 1;
-      const int32_t* __restrict__ cst = J->cstart;
-      const float* __restrict__ zlo = J->czlo32;
-      const float* __restrict__ zhi = J->czhi32;
-      const bool unsafe = (*J->jflags & TF_UNSAFE32) != 0u;
-      const int K = J->K;
-      const int sq = NEST ? (wi.strip & 0xffff) : wi.strip;
-      const int hc2 = NEST ? (wi.strip >> 16) : 0;
-
-      float qv[DQ];
-      double m = 0.0;
+    auto exact_dist = [&](int j) -> uint64_t {
+      uint64_t mm = 0;
 #pragma unroll
       for (int c = 0; c < DQ; ++c) {
         if (D == 0 && c >= d) break;
-        qv[c] = g[(int64_t)c * lds + qp];
-        const double v = fabs(c64[(int64_t)c * lds + qp] - J->center[c]);
-        m = v > m ? v : m;
+        const int64_t off = (int64_t)c * lds;
+        const uint64_t v = absdiff_bits(c64[off + j], c64[off + qp]);
+        mm = v > mm ? v : mm;
       }
-      const float mq = __double2float_ru(m);
-      const double qy = c64[lds + qp];
-      const float qyl = lo32_of(qy, J->center[1]), qyh = hi32_of(qy, J->center[1]);
-      float qzl = 0.0f, qzh = 0.0f;
-      if (NEST) {
-        const double qz = c64[2 * lds + qp];
-        qzl = lo32_of(qz, J->center[2]);
-        qzh = hi32_of(qz, J->center[2]);
-      }
-
-      float l32[KMAX];   // pass 0: K smallest FP32 distances (padding first)
-      int i32[KMAX];     // their candidates
-      uint64_t top[KMAX];  // pass 1: K smallest exact distances (bit patterns)
-#pragma unroll
-      for (int s = 0; s < KMAX; ++s) {
-        l32[s] = s >= KMAX - K ? FINF : 0.0f;
-        i32[s] = 0;
-        top[s] = s >= KMAX - K ? INF_BITS : 0ull;
-      }
-      float rej = FINF;          // least FP32 distance left out of the list
-      bool pass1 = unsafe;       // unsafe jobs decide everything in FP64
-      float ufix = FINF, sfix = FINF;
-
-      auto exact_dist = [&](int j) -> uint64_t {
-        uint64_t mm = 0;
-#pragma unroll
-        for (int c = 0; c < DQ; ++c) {
-          if (D == 0 && c >= d) break;
-          const int64_t off = (int64_t)c * lds;
-          const uint64_t v = absdiff_bits(c64[off + j], c64[off + qp]);
-          mm = v > mm ? v : mm;
-        }
-        return mm;
-      };
-      // screen bound S and planning bound plan_margin(U)
-      auto sbound = [&]() -> float {
-        if (pass1) return sfix;
-        return up_band32(up_band32(l32[KMAX - 1], mq), mq);
-      };
-      auto pbound = [&]() -> float {
-        if (pass1) return plan_margin(ufix);
-        return plan_margin(up_band32(l32[KMAX - 1], mq));
-      };
-      auto visit = [&](int j, float dd) {
-        ++visited;
-        if (!pass1) {
-          rej = fminf(rej, dd < l32[KMAX - 1] ? insert_sorted_fi<KMAX>(l32, i32, dd, j) : dd);
-        } else if (dd <= sfix) {
-          const uint64_t mm = exact_dist(j);
-          if (mm < top[KMAX - 1]) insert_sorted<KMAX>(top, mm);
-        }
-      };
-      // Walk [a, b) outward from p0 (the first position whose column 0 is
-      // >= the query's): nearer side first, until both sides pass S.
-      auto walk = [&](int a, int b, int p0) {
-        int L = p0 - 1, R = p0;
-        float dl = L >= a ? qv[0] - g[L] : FINF;
-        float dr = R < b ? g[R] - qv[0] : FINF;
-        for (;;) {
-          const bool go_l = dl <= dr;
-          const float dx = go_l ? dl : dr;
-          // both sides exhausted (real gaps are finite: values are clamped
-          // to +-1e37), or the nearer side is beyond the screen bound
-          if (!(dx < FINF) || !(dx <= sbound())) break;
-          const int j = go_l ? L : R;
-          float dd = dx;
-#pragma unroll
-          for (int c = 1; c < DQ; ++c) {
-            if (D == 0 && c >= d) break;
-            dd = fmaxf(dd, fabsf(g[(int64_t)c * lds + j] - qv[c]));
-          }
-          visit(j, dd);
-          if (go_l) {
-            --L;
-            dl = L >= a ? qv[0] - g[L] : FINF;
-          } else {
-            ++R;
-            dr = R < b ? g[R] - qv[0] : FINF;
-          }
-        }
-      };
-      // Nested grids: the cells of strip s outward in column 2 from c0
-      // (cell `skip` already walked).
-      auto cells = [&](int s, int c0, int skip) {
-        const int cb = s * S2;
-        int up = c0, dn = c0 - 1;
-        for (;;) {
-          const float t = pbound();
-          const bool ou = up < S2 && !(__fsub_rd(zlo[cb + up], qzh) > t);
-          const bool od = dn >= 0 && !(__fsub_rd(qzl, zhi[cb + dn]) > t);
-          if (!ou && !od) break;
-          int c;
-          if (ou && (!od || __fsub_rd(zlo[cb + up], qzh) <= __fsub_rd(qzl, zhi[cb + dn]))) c = up++;
-          else c = dn--;
-          if (c == skip) continue;
-          const int a = cst[cb + c], b = cst[cb + c + 1];
-          walk(a, b, lower_bound_f(g, a, b, qv[0]));
-        }
-      };
-      // the whole search: home strip (cell), then strips outward in column 1
-      auto search = [&]() {
-        if (NEST) {
-          const int cb = sq * S2;
-          walk(cst[cb + hc2], cst[cb + hc2 + 1], qp);
-          cells(sq, hc2, hc2);
-        } else {
-          walk(sst[sq], sst[sq + 1], qp);
-        }
-        int up = sq + 1, dn = sq - 1;
-        for (;;) {
-          const float t = pbound();
-          const bool ou = up < S && !(__fsub_rd(ylo[up], qyh) > t);
-          const bool od = dn >= 0 && !(__fsub_rd(qyl, yhi[dn]) > t);
-          if (!ou && !od) break;
-          int s;
-          if (ou && (!od || __fsub_rd(ylo[up], qyh) <= __fsub_rd(qyl, yhi[dn]))) s = up++;
-          else s = dn--;
-          if (NEST) {
-            // first cell of the strip whose column-2 range reaches the query
-            int lo = 0, n = S2;
-            while (n > 0) {
-              const int h = n >> 1;
-              if (zhi[s * S2 + lo + h] < qzl) {
-                lo += h + 1;
-                n -= h + 1;
-              } else {
-                n = h;
-              }
-            }
-            cells(s, lo < S2 ? lo : S2 - 1, -1);
-          } else {
-            const int a = sst[s], b = sst[s + 1];
-            walk(a, b, lower_bound_f(g, a, b, qv[0]));
-          }
-        }
-      };
-
-      uint64_t kth;
+      return mm;
+    };
+    // screen bound S and planning bound plan_margin(U); -1 when inactive
+    auto sbound = [&]() -> float {
+      if (pass1) return sfix;
+      return up_band32(up_band32(l32[KMAX - 1], mq), mq);
+    };
+    auto pbound = [&]() -> float {
+      if (!act) return -1.0f;
+      if (pass1) return plan_margin(ufix);
+      return plan_margin(up_band32(l32[KMAX - 1], mq));
+    };
+    auto visit = [&](int j, float dd) {
+      ++visited;
       if (!pass1) {
-        search();
+        rej = fminf(rej, dd < l32[KMAX - 1] ? insert_sorted_fi<KMAX>(l32, i32, dd, j) : dd);
+      } else if (dd <= sfix) {
+        const uint64_t mm = exact_dist(j);
+        if (mm < top[KMAX - 1]) insert_sorted<KMAX>(top, mm);
+      }
+    };
+    // This lane's walk of [a, b) outward from p0 (the first position whose
+    // column 0 is >= the query's): nearer side first, until both sides pass
+    // S or end.
+    auto walk = [&](int a, int b, int p0) {
+      int L = p0 - 1, R = p0;
+      float dl = L >= a ? qv[0] - g[L] : FINF;
+      float dr = R < b ? g[R] - qv[0] : FINF;
+      for (;;) {
+        const bool go_l = dl <= dr;
+        const float dx = go_l ? dl : dr;
+        // both sides exhausted (real gaps are finite: values are clamped to
+        // +-1e37), or the nearer side is beyond the screen bound
+        if (!(dx < FINF) || !(dx <= sbound())) break;
+        const int j = go_l ? L : R;
+        float dd = dx;
+#pragma unroll
+        for (int c = 1; c < DQ; ++c) {
+          if (D == 0 && c >= d) break;
+          dd = fmaxf(dd, fabsf(g[(int64_t)c * lds + j] - qv[c]));
+        }
+        visit(j, dd);
+        if (go_l) {
+          --L;
+          dl = L >= a ? qv[0] - g[L] : FINF;
+        } else {
+          ++R;
+          dr = R < b ? g[R] - qv[0] : FINF;
+        }
+      }
+    };
+    auto walk_range = [&](int a, int b) { walk(a, b, lower_bound_f(g, a, b, qv[0])); };
+    // The warp visits strips and cells together; a lane walks the ones its
+    // planning bound reaches.
+    auto strip_reach = [&](int s, float t) {
+      return act && !(__fsub_rd(ylo[s], qyh) > t) && !(__fsub_rd(qyl, yhi[s]) > t);
+    };
+    // Nested grids: the cells of strip s outward in column 2 from c0 (cell
+    // `skip` already walked); each direction ends at the first cell no lane
+    // reaches (cells are ordered by column 2).
+    auto cells = [&](int s, int c0, int skip) {
+      const int cb = s * S2;
+      int up = c0, dn = c0 - 1;
+      bool tu = true;
+      for (;;) {
+        const float t = pbound();
+        const bool r = strip_reach(s, t);
+        const bool ou = r && up < S2 && !(__fsub_rd(zlo[cb + up], qzh) > t);
+        const bool od = r && dn >= 0 && !(__fsub_rd(qzl, zhi[cb + dn]) > t);
+        const bool any_u = __any_sync(0xffffffffu, ou);
+        const bool any_d = __any_sync(0xffffffffu, od);
+        if (!any_u && !any_d) break;
+        int c;
+        if ((tu && any_u) || !any_d) {
+          c = up++;
+          tu = false;
+        } else {
+          c = dn--;
+          tu = true;
+        }
+        if (c == skip) continue;
+        const bool need = r && !(__fsub_rd(zlo[cb + c], qzh) > t) && !(__fsub_rd(qzl, zhi[cb + c]) > t);
+        if (need) walk_range(cst[cb + c], cst[cb + c + 1]);
+      }
+    };
+    auto start_cell = [&](int s) -> int {
+      int c0 = 0;
+      for (int b = 0; b < S2; b += 32) {
+        const int c = b + lane;
+        c0 += __popc(__ballot_sync(0xffffffffu, c < S2 && zhi[s * S2 + c] < zmid));
+      }
+      return c0 < S2 ? c0 : S2 - 1;
+    };
+    // the whole search of the current pass (warp-uniform)
+    auto search = [&]() {
+      if (NEST) {
+        const int cb = sq * S2;
+        if (act) walk(cst[cb + hc2], cst[cb + hc2 + 1], qp);
+        cells(sq, hc2, hc2);
+      } else {
+        if (act) walk(sst[sq], sst[sq + 1], qp);
+      }
+      int up = sq + 1, dn = sq - 1;
+      bool tu = true;
+      for (;;) {
+        const float t = pbound();
+        const bool ou = act && up < S && !(__fsub_rd(ylo[up], qyh) > t);
+        const bool od = act && dn >= 0 && !(__fsub_rd(qyl, yhi[dn]) > t);
+        const bool any_u = __any_sync(0xffffffffu, ou);
+        const bool any_d = __any_sync(0xffffffffu, od);
+        if (!any_u && !any_d) break;
+        int s;
+        if ((tu && any_u) || !any_d) {
+          s = up++;
+          tu = false;
+        } else {
+          s = dn--;
+          tu = true;
+        }
+        if (NEST) {
+          cells(s, start_cell(s), -1);
+        } else if (strip_reach(s, t)) {
+          walk_range(sst[s], sst[s + 1]);
+        }
+      }
+    };
+
+    uint64_t kth = INF_BITS;
+    bool again = false;
+    if (!unsafe) {
+      search();
+      if (exists) {
         const float u32 = up_band32(l32[KMAX - 1], mq);
         const float s32 = up_band32(u32, mq);
         if (rej > s32) {
@@ -262,19 +290,21 @@ wwalk_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items
           kth = mx;
         } else {
           again = true;
-          pass1 = true;
           ufix = u32;
           sfix = s32;
-          search();
-          kth = top[KMAX - 1];
         }
-      } else {
-        again = true;
-        search();
-        kth = top[KMAX - 1];
       }
-      J->eps[J->idxg[qp]] = bits_to_double(kth);
+      act = again;
+      pass1 = true;
+    } else {
+      again = exists;
+      act = exists;
     }
+    if (__any_sync(0xffffffffu, act)) {
+      search();  // pass 1 for the lanes without the margin
+      if (again) kth = top[KMAX - 1];
+    }
+    if (exists) J->eps[J->idxg[qp]] = bits_to_double(kth);
 
     const unsigned long long tot = __reduce_add_sync(0xffffffffu, (unsigned)visited);
     const unsigned agm = __ballot_sync(0xffffffffu, again);
