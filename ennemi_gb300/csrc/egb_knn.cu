@@ -55,12 +55,10 @@ void launch_count_wgrid_f64(int, const JobDev*, const WorkItem*, int, int*, int,
 void launch_knn_wgrid(const JobDev* jobs_d, const WorkItem* items_d, int nitems, int kclass,
                       int dclass, int plain, int dmax, int* counter, int num_sms, cudaStream_t st) {
   if (nitems <= 0) return;
-  // the FP32 path of 2-D jobs walks per lane (egb_wwalk.cu); nested grids
-  // (d >= 3) keep the warp-window kernel, whose cooperative finishing of
-  // far-out queries matters there; so does the FP64 comparator
+  // the FP32 path walks per lane (egb_wwalk.cu); the FP64 comparator keeps
+  // the warp-window kernel
   if (plain) launch_knn_wgrid_f64(kclass, dclass, jobs_d, items_d, nitems, counter, dmax, num_sms, st);
-  else if (dclass == 2) launch_knn_walk(jobs_d, items_d, nitems, kclass, dclass, counter, num_sms, st);
-  else launch_knn_wgrid_f32(kclass, dclass, jobs_d, items_d, nitems, counter, dmax, num_sms, st);
+  else launch_knn_walk(jobs_d, items_d, nitems, kclass, dclass, counter, num_sms, st);
 }
 
 void launch_count_wgrid(const JobDev* jobs_d, const WorkItem* items_d, int nitems, int dclass,

@@ -43,6 +43,9 @@ using wgrid_detail::plan_margin;
 using wgrid_detail::up_band32;
 
 constexpr int WW_WARPS = 4;
+// A lane whose walks screen more candidates than this in pass 0 leaves its
+// query to the cooperative phase (far-out queries of sparse regions).
+constexpr int WALK_BUDGET = 384;
 
 // First position of [a, b) with x[p] >= v (x ascending).
 __device__ __forceinline__ int lower_bound_f(const float* __restrict__ x, int a, int b, float v) {
@@ -132,6 +135,7 @@ wwalk_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items
     bool pass1 = unsafe;   // jobs with clamped values decide everything in FP64
     float ufix = FINF, sfix = FINF;
     bool act = exists;     // this lane searches in the current pass
+    bool heavy = false;    // pass 0 gave up: the warp finishes the query together
     unsigned long long visited = 0;
 
     auto exact_dist = [&](int j) -> uint64_t {
@@ -177,6 +181,11 @@ wwalk_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items
         // both sides exhausted (real gaps are finite: values are clamped to
         // +-1e37), or the nearer side is beyond the screen bound
         if (!(dx < FINF) || !(dx <= sbound())) break;
+        if (!pass1 && visited >= (unsigned long long)WALK_BUDGET) {
+          heavy = true;  // leave it to the cooperative phase
+          act = false;
+          break;
+        }
         const int j = go_l ? L : R;
         float dd = dx;
 #pragma unroll
@@ -274,6 +283,148 @@ wwalk_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items
     bool again = false;
     if (!unsafe) {
       search();
+      // Far-out queries, one at a time with all 32 lanes: a fresh search of
+      // every strip and cell within the owner's current planning bound, each
+      // lane screening every 32nd candidate of the column-0 windows into its
+      // own list; the K smallest of the lists, with their candidates, become
+      // the owner's list, and every entry not taken counts as left out.
+      unsigned hm = __ballot_sync(0xffffffffu, heavy);
+      while (hm) {
+        const int ol = __ffs(hm) - 1;
+        hm &= hm - 1u;
+        float oq[DQ];
+#pragma unroll
+        for (int c = 0; c < DQ; ++c) {
+          if (D == 0 && c >= d) break;
+          oq[c] = __shfl_sync(0xffffffffu, qv[c], ol);
+        }
+        const float omq = __shfl_sync(0xffffffffu, mq, ol);
+        const float oyl = __shfl_sync(0xffffffffu, qyl, ol), oyh = __shfl_sync(0xffffffffu, qyh, ol);
+        const float ozl = __shfl_sync(0xffffffffu, qzl, ol), ozh = __shfl_sync(0xffffffffu, qzh, ol);
+        const float ek = __fmaf_ru(fabsf(oq[0]), 0x1p-22f, 0x1p-148f);
+        const float oxl = __fsub_rd(oq[0], ek), oxh = __fadd_ru(oq[0], ek);
+        float othr = __shfl_sync(0xffffffffu, l32[KMAX - 1], ol);  // caps every lane's list
+        float tb = plan_margin(up_band32(othr, omq));
+        float l2[KMAX];
+        int ix2[KMAX];
+#pragma unroll
+        for (int s2 = 0; s2 < KMAX; ++s2) {
+          l2[s2] = s2 >= KMAX - K ? FINF : 0.0f;
+          ix2[s2] = 0;
+        }
+        float rej2 = FINF;
+        unsigned long long cvis = 0;
+        auto crange = [&](int a, int b) {
+          int wl, wh;
+          wgrid_detail::warp_window<float>(g, a, b, fminf(__fsub_rd(oxl, tb), 1e37f),
+                                           fmaxf(__fadd_ru(oxh, tb), -1e37f), wl, wh);
+          for (int j0 = wl; j0 < wh; j0 += 32) {
+            const int j = j0 + lane;
+            if (j < wh) {
+              float dd = 0.0f;
+#pragma unroll
+              for (int c = 0; c < DQ; ++c) {
+                if (D == 0 && c >= d) break;
+                dd = fmaxf(dd, fabsf(g[(int64_t)c * lds + j] - oq[c]));
+              }
+              ++cvis;
+              // <= : the owner's own K-th candidate lies exactly at the cap
+              const bool hit = dd < l2[KMAX - 1] && dd <= othr;
+              rej2 = fminf(rej2, hit ? insert_sorted_fi<KMAX>(l2, ix2, dd, j) : dd);
+            }
+          }
+          // any lane holding K entries bounds the union's K-th
+          float lk = l2[KMAX - 1];
+#pragma unroll
+          for (int o = 16; o; o >>= 1) lk = fminf(lk, __shfl_xor_sync(0xffffffffu, lk, o));
+          if (lk < othr) othr = lk;
+          const float nb = plan_margin(up_band32(othr, omq));
+          if (nb < tb) tb = nb;
+        };
+        auto ccells = [&](int s) {  // nested: the cells of strip s within tb
+          int c0 = 0, c1 = 0;
+          for (int b = 0; b < S2; b += 32) {
+            const int c = b + lane;
+            c0 += __popc(__ballot_sync(0xffffffffu, c < S2 && __fsub_rd(ozl, zhi[s * S2 + c]) > tb));
+            c1 += __popc(__ballot_sync(0xffffffffu, c < S2 && !(__fsub_rd(zlo[s * S2 + c], ozh) > tb)));
+          }
+          for (int c = c0; c < c1; ++c) crange(cst[s * S2 + c], cst[s * S2 + c + 1]);
+        };
+        auto cstrip = [&](int s) {
+          if (NEST) ccells(s);
+          else crange(sst[s], sst[s + 1]);
+        };
+        cstrip(sq);
+        for (int up = sq + 1, dn = sq - 1;;) {
+          const bool ou = up < S && !(__fsub_rd(ylo[up], oyh) > tb);
+          const bool od = dn >= 0 && !(__fsub_rd(oyl, yhi[dn]) > tb);
+          if (!ou && !od) break;
+          const int s = ou && (!od || (up - sq) <= (sq - dn)) ? up++ : dn--;
+          cstrip(s);
+        }
+        // the K smallest of the union, in order, become the owner's list
+        float nl[KMAX];
+        int ni[KMAX];
+#pragma unroll
+        for (int s2 = 0; s2 < KMAX; ++s2) {
+          nl[s2] = 0.0f;
+          ni[s2] = 0;
+        }
+        int taken = 0;
+        for (int r = 0; r < K; ++r) {
+          const int hp = KMAX - K + taken;
+          float v = FINF;
+          int vi = 0;
+#pragma unroll
+          for (int s2 = 0; s2 < KMAX; ++s2) {
+            if (s2 == hp) {
+              v = l2[s2];
+              vi = ix2[s2];
+            }
+          }
+          int who = lane;
+#pragma unroll
+          for (int o = 16; o; o >>= 1) {
+            const float ov = __shfl_xor_sync(0xffffffffu, v, o);
+            const int ow = __shfl_xor_sync(0xffffffffu, who, o);
+            if (ov < v || (ov == v && ow < who)) {
+              v = ov;
+              who = ow;
+            }
+          }
+          const int bi = __shfl_sync(0xffffffffu, vi, who);
+          if (lane == who) ++taken;
+          if (lane == ol) {
+#pragma unroll
+            for (int s2 = 0; s2 < KMAX - 1; ++s2) {
+              nl[s2] = nl[s2 + 1];
+              ni[s2] = ni[s2 + 1];
+            }
+            nl[KMAX - 1] = v;
+            ni[KMAX - 1] = bi;
+          }
+        }
+        {
+          const int hp = KMAX - K + taken;
+          float v = FINF;
+#pragma unroll
+          for (int s2 = 0; s2 < KMAX; ++s2)
+            if (s2 == hp) v = l2[s2];
+          float lo2 = fminf(rej2, v);
+#pragma unroll
+          for (int o = 16; o; o >>= 1) lo2 = fminf(lo2, __shfl_xor_sync(0xffffffffu, lo2, o));
+          const unsigned long long cv = __reduce_add_sync(0xffffffffu, (unsigned)cvis);
+          if (lane == ol) {
+#pragma unroll
+            for (int s2 = 0; s2 < KMAX; ++s2) {
+              l32[s2] = nl[s2];
+              i32[s2] = ni[s2];
+            }
+            rej = lo2;
+            visited += cv;
+          }
+        }
+      }
       if (exists) {
         const float u32 = up_band32(l32[KMAX - 1], mq);
         const float s32 = up_band32(u32, mq);
