@@ -647,11 +647,16 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
     J.sp = m.s.sp;
     const int d = m.s.sp.d;
     J.sort_seg_b = m.sort_seg_b;
-    J.c64 = (double*)(uintptr_t)dl.take(sizeof(double) * (size_t)(d * J.lds));
-    J.c32 = (float*)(uintptr_t)dl.take(sizeof(float) * (size_t)(d * J.lds));
-    J.idx = (int32_t*)(uintptr_t)dl.take(sizeof(int32_t) * (size_t)J.lds);
+    // warp-grid jobs read only their grid copy: no working-order or sorted
+    // copies
+    const bool gonly = m.mode == 3;
+    if (!gonly) {
+      J.c64 = (double*)(uintptr_t)dl.take(sizeof(double) * (size_t)(d * J.lds));
+      J.c32 = (float*)(uintptr_t)dl.take(sizeof(float) * (size_t)(d * J.lds));
+      J.idx = (int32_t*)(uintptr_t)dl.take(sizeof(int32_t) * (size_t)J.lds);
+    }
     J.center = (double*)(uintptr_t)dl.take(sizeof(double) * (size_t)d);
-    if (m.slab) {
+    if (m.slab && !gonly) {
       J.c64b = (double*)(uintptr_t)dl.take(sizeof(double) * (size_t)(d * J.lds));
       J.c32b = (float*)(uintptr_t)dl.take(sizeof(float) * (size_t)(d * J.lds));
       J.idxb = (int32_t*)(uintptr_t)dl.take(sizeof(int32_t) * (size_t)J.lds);
@@ -933,9 +938,11 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   for (size_t j = 0; j < jobs.size(); ++j) {
     JobDev J = jobs[j];
     const TaskDev& D = tdev[(size_t)J.task];
-    J.c64 = (double*)(A + (uintptr_t)J.c64);
-    J.c32 = (float*)(A + (uintptr_t)J.c32);
-    J.idx = (int32_t*)(A + (uintptr_t)J.idx);
+    if (J.c64) {
+      J.c64 = (double*)(A + (uintptr_t)J.c64);
+      J.c32 = (float*)(A + (uintptr_t)J.c32);
+      J.idx = (int32_t*)(A + (uintptr_t)J.idx);
+    }
     J.center = (double*)(A + (uintptr_t)J.center);
     if (J.c64b) {
       J.c64b = (double*)(A + (uintptr_t)J.c64b);

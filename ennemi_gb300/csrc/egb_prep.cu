@@ -131,6 +131,7 @@ __global__ void materialize_kernel(const TaskDev* __restrict__ tasks,
     const TaskDev t = tasks[J.task];
     const int d = J.sp.d;
     if (blockIdx.x == 0 && threadIdx.x < d) J.center[threadIdx.x] = t.center[J.sp.cols[threadIdx.x]];
+    if (J.c64 == nullptr) continue;  // grid copy only (materialize_grid_kernel)
     const int32_t* sv = J.slab ? sorted_vals + segs[J.sort_seg].out_base : nullptr;
     bool bad = materialize_copy(t, J, d, J.c64, J.c32, J.idx, sv);
     if (J.c64b != nullptr)  // second copy, sorted by column 1 (same values)
@@ -154,15 +155,18 @@ __global__ void materialize_grid_kernel(const TaskDev* __restrict__ tasks,
     const int d = J.sp.d;
     const int32_t* va = sorted_vals + segs[J.sort_seg].out_base;
     const int32_t* gv = gvals_sorted + gsegs[J.gseg].out_base;
-    // column-1 bounds of each strip, from the column-1 sorted copy
+    // column-1 bounds of each strip, from the column-1 sort
+    const int32_t* vb = sorted_vals + segs[J.sort_seg_b].out_base;
+    const double* x1 = t.x64 + (int64_t)J.sp.cols[1] * t.ld;
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < J.nstrips; s += gridDim.x * blockDim.x) {
-      const double lo = J.c64b[J.lds + J.sstart[s]];
-      const double hi = J.c64b[J.lds + J.sstart[s + 1] - 1];
+      const double lo = x1[vb[J.sstart[s]]];
+      const double hi = x1[vb[J.sstart[s + 1] - 1]];
       J.sylo[s] = lo;
       J.syhi[s] = hi;
       J.sylo32[s] = __double2float_rd(__dsub_rd(lo, J.center[1]));
       J.syhi32[s] = __double2float_ru(__dsub_ru(hi, J.center[1]));
     }
+    bool bad = false;  // a centred value too large for the FP32 copy
     for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < J.lds;
          p += (int64_t)gridDim.x * blockDim.x) {
       if (p < J.len) {
@@ -179,9 +183,10 @@ __global__ void materialize_grid_kernel(const TaskDev* __restrict__ tasks,
             kw[(int64_t)(2 * c) * J.lds + p] = (uint32_t)(k >> 32);
             kw[(int64_t)(2 * c + 1) * J.lds + p] = (uint32_t)k;
           } else {
+            const double cv = v - t.center[tc];
+            bad |= !(fabs(cv) < 1e37);
             J.c64g[(int64_t)c * J.lds + p] = v;
-            J.c32g[(int64_t)c * J.lds + p] =
-                __double2float_rn(fmin(fmax(v - t.center[tc], -1e37), 1e37));
+            J.c32g[(int64_t)c * J.lds + p] = __double2float_rn(fmin(fmax(cv, -1e37), 1e37));
           }
         }
       } else {
@@ -199,6 +204,7 @@ __global__ void materialize_grid_kernel(const TaskDev* __restrict__ tasks,
         }
       }
     }
+    if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(J.jflags, (uint32_t)TF_UNSAFE32);
   }
 }
 

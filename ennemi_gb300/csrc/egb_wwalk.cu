@@ -45,7 +45,7 @@ using wgrid_detail::up_band32;
 constexpr int WW_WARPS = 4;
 // A lane whose walks screen more candidates than this in pass 0 leaves its
 // query to the cooperative phase (far-out queries of sparse regions).
-constexpr int WALK_BUDGET = 384;
+constexpr int WALK_BUDGET = 192;
 
 // First position of [a, b) with x[p] >= v (x ascending).
 __device__ __forceinline__ int lower_bound_f(const float* __restrict__ x, int a, int b, float v) {
@@ -63,7 +63,7 @@ __device__ __forceinline__ int lower_bound_f(const float* __restrict__ x, int a,
 }
 
 template <int D, int KMAX, bool NEST>
-__global__ void __launch_bounds__(WW_WARPS * 32)
+__global__ void __launch_bounds__(WW_WARPS * 32, (D == 2 ? 6 : 1))
 wwalk_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items, int nitems,
              int* __restrict__ counter) {
   constexpr int DQ = D ? D : EGB_DMAX;
