@@ -627,6 +627,7 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   std::vector<int32_t> grid_jobs;    // job index of each grid job
   int64_t gsort_total = 0, max_glen = 1;
   bool any_nested = false;
+  int64_t max_gkey = 1;  // largest strip / cell key of the grid jobs
   int nblk_grid = 0;
   int64_t max_lds = 32;
   for (size_t j = 0; j < mjobs.size(); ++j) {
@@ -666,7 +667,10 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
       J.c32g = (float*)(uintptr_t)dl.take(sizeof(float) * (size_t)(d * J.lds));
       J.idxg = (int32_t*)(uintptr_t)dl.take(sizeof(int32_t) * (size_t)J.lds);
       J.posg = (int32_t*)(uintptr_t)dl.take(sizeof(int32_t) * (size_t)J.lds);
-      J.nstrips = (int32_t)std::max<int64_t>(1, std::min<int64_t>(256, len / GRID_MIN_STRIP));
+      // strips of at least GRID_MIN_STRIP points, at most GRID_STRIPS_KNN /
+      // GRID_STRIPS_COUNT of them (warp-grid jobs; 256 for the CTA grid)
+      const int64_t cap = m.mode == 3 ? (m.is_knn ? GRID_STRIPS_KNN : GRID_STRIPS_COUNT) : 256;
+      J.nstrips = (int32_t)std::max<int64_t>(1, std::min<int64_t>(cap, len / GRID_MIN_STRIP));
       if (m.sort_seg_c >= 0) {
         // nested: about NEST_CELL points per cell, as many strips as cells
         // per strip, every cell at least GRID_MIN_STRIP / 2 points
@@ -682,6 +686,7 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
         J.czlo32 = (float*)(uintptr_t)dl.take(sizeof(float) * (size_t)(side * side));
         J.czhi32 = (float*)(uintptr_t)dl.take(sizeof(float) * (size_t)(side * side));
       }
+      max_gkey = std::max<int64_t>(max_gkey, (int64_t)J.nstrips * std::max<int32_t>(1, J.nsub));
       J.sylo = (double*)(uintptr_t)dl.take(sizeof(double) * (size_t)J.nstrips);
       J.syhi = (double*)(uintptr_t)dl.take(sizeof(double) * (size_t)J.nstrips);
       J.sylo32 = (float*)(uintptr_t)dl.take(sizeof(float) * (size_t)J.nstrips);
@@ -1056,11 +1061,11 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
     launch_grid_key(jobs_d, gj_d, ngrid, gsegs_d, vals, (const SortSeg*)dtab(tab_segs), ginv, gsub, gka,
                     gva, max_glen, st);
     launch_radix_pass(gsegs_d, blkg_d, nblk_grid, gka, gva, gkb, gvb, 0, ghist, gscan, st);
-    if (any_nested)  // cell keys reach 16 bits: second digit
+    if (max_gkey > 256)  // strip / cell keys above 8 bits: second digit
       launch_radix_pass(gsegs_d, blkg_d, nblk_grid, gkb, gvb, gka, gva, 8, ghist, gscan, st);
     launch_materialize_grid(tasks_d, (const JobDev*)dtab(tab_jobs), (const int32_t*)dtab(tab_gridjobs),
                             (int)grid_jobs.size(), vals, (const SortSeg*)dtab(tab_segs),
-                            any_nested ? gva : gvb, (const SortSeg*)dtab(tab_gsegs),
+                            max_gkey > 256 ? gva : gvb, (const SortSeg*)dtab(tab_gsegs),
                             max_lds, st);
   }
   if (timing) EGB_CUDA(cudaEventRecord(ctx->ev[3], st));

@@ -296,6 +296,8 @@ constexpr int NEST_CELL = 768;   // target points per nested-grid cell
 constexpr int GRID_QB = 128;     // queries per grid work item
 constexpr int GRID_TILE = 128;   // candidates per grid tile
 constexpr int GRID_MIN_STRIP = 64;
+constexpr int GRID_STRIPS_KNN = 256;    // most strips of a 2-D warp-grid kNN job
+constexpr int GRID_STRIPS_COUNT = 256;  // most strips of a 2-D warp-grid count job
 
 struct WorkItem {         // one tile of queries of one job
   int32_t job;
