@@ -674,7 +674,7 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
       if (m.sort_seg_c >= 0) {
         // nested: about NEST_CELL points per cell, as many strips as cells
         // per strip, every cell at least GRID_MIN_STRIP / 2 points
-        int64_t side = (int64_t)std::lround(std::sqrt((double)len / NEST_CELL));
+        int64_t side = (int64_t)std::lround(std::sqrt((double)len / (m.is_knn ? NEST_CELL : NEST_CELL_COUNT)));
         side = std::max<int64_t>(1, std::min<int64_t>(256, side));
         while (side > 1 && len / (side * side) < GRID_MIN_STRIP / 2) --side;
         J.nstrips = (int32_t)side;

@@ -292,7 +292,8 @@ __host__ __device__ __forceinline__ int32_t cell_start(int32_t s0, int32_t L, in
                                                        int32_t nsub) {
   return s0 + strip_start(c2, L, nsub);
 }
-constexpr int NEST_CELL = 768;   // target points per nested-grid cell
+constexpr int NEST_CELL = 768;        // target points per nested-grid cell (kNN jobs)
+constexpr int NEST_CELL_COUNT = 768;  // the same for key-range count jobs
 constexpr int GRID_QB = 128;     // queries per grid work item
 constexpr int GRID_TILE = 128;   // candidates per grid tile
 constexpr int GRID_MIN_STRIP = 64;
@@ -462,7 +463,7 @@ void launch_knn_wgrid(const JobDev* jobs_d, const WorkItem* items_d, int nitems,
 // egb_wwalk.cu: FP32-path kNN of warp-grid jobs (K <= 8) by per-lane walks
 void launch_knn_walk(const JobDev* jobs_d, const WorkItem* items_d, int nitems, int kclass,
                      int dclass, int* counter, int num_sms, cudaStream_t st);
-// egb_wcount.cu: exact key-range ball counts of d = 2 / nested d = 3
+// egb_wcount.cu: exact key-range ball counts of d = 2 / nested d = 3, 4
 // warp-grid jobs (FP32 path; the FP64 comparator keeps launch_count_wgrid)
 bool count_keys_supported(int dclass);
 void launch_count_keys(const JobDev* jobs_d, const WorkItem* items_d, int nitems, int dclass,

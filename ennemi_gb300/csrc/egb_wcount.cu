@@ -1,4 +1,4 @@
-// egb_wcount.cu -- ball counts of d = 2 and d = 3 warp-grid jobs by key
+// egb_wcount.cu -- ball counts of d = 2, 3 and 4 warp-grid jobs by key
 // ranges: integer comparisons only, no distance arithmetic.
 //
 // The count of query q is #{j : max_c fl64(|p_jc - q_c|) <= r}, r =
@@ -10,7 +10,7 @@
 // steps per query.  The ball is then the box of those key ranges, exactly.
 //
 // Layout: the job's grid copy (strips by column 1, nested cells by column 2
-// for d = 3, column-0 order inside), holding the keys themselves as high and
+// for d >= 3, column-0 order inside), holding the keys themselves as high and
 // low 32-bit words (JobDev::kform): most comparisons are settled by the high
 // words, and the low word is read only on a tie.  A warp takes an item of up to 32
 // queries of one strip (cell) and visits the strips outward from its own
@@ -139,7 +139,8 @@ template <int D>
 __global__ void __launch_bounds__(WC_WARPS * 32)
 wcount_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items, int nitems,
               int* __restrict__ counter) {
-  static_assert(D == 2 || D == 3, "d = 2 strips or d = 3 nested cells");
+  static_assert(D >= 2 && D <= 4, "d = 2 strips, d = 3 and 4 nested cells");
+  constexpr bool NEST = D >= 3;
   const int lane = threadIdx.x & 31;
   for (;;) {
     int it = 0;
@@ -152,12 +153,13 @@ wcount_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ item
     const int64_t lds = J->lds;
     const uint32_t* kw = reinterpret_cast<const uint32_t*>(J->c64g);
     const KeyCol xk{kw, kw + lds}, yk{kw + 2 * lds, kw + 3 * lds};
-    const KeyCol zk{kw + 4 * lds, kw + 5 * lds};  // d = 3 only
+    const KeyCol zk{kw + 4 * lds, kw + 5 * lds};  // d >= 3
+    const KeyCol wk{kw + 6 * lds, kw + 7 * lds};  // d = 4
     const int32_t* __restrict__ sst = J->sstart;
     const unsigned long long* __restrict__ sylo = reinterpret_cast<const unsigned long long*>(J->sylo);
     const unsigned long long* __restrict__ syhi = reinterpret_cast<const unsigned long long*>(J->syhi);
     const int S = J->nstrips;
-    const int S2 = D == 3 ? J->nsub : 1;
+    const int S2 = NEST ? J->nsub : 1;
     const int32_t* __restrict__ cst = J->cstart;
     const unsigned long long* __restrict__ czlo = reinterpret_cast<const unsigned long long*>(J->czlo);
     const unsigned long long* __restrict__ czhi = reinterpret_cast<const unsigned long long*>(J->czhi);
@@ -167,12 +169,13 @@ wcount_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ item
     const double qr = exists ? J->rad[J->idxg[qp]] : -1.0;
     const bool qok = exists && qr >= 0.0;
     const bool every = qok && isinf(qr);  // an infinite radius holds every point
-    uint64_t kxl = 1, kxr = 0, kyl = 1, kyr = 0, kzl = 1, kzr = 0;  // empty ranges
+    uint64_t kxl = 1, kxr = 0, kyl = 1, kyr = 0, kzl = 1, kzr = 0, kwl = 1, kwr = 0;  // empty
     const bool act = qok && !every;
     if (act) {
       ball_keys(raw_value(xk.key(qp)), qr, kxl, kxr);
       ball_keys(raw_value(yk.key(qp)), qr, kyl, kyr);
-      if (D == 3) ball_keys(raw_value(zk.key(qp)), qr, kzl, kzr);
+      if (D >= 3) ball_keys(raw_value(zk.key(qp)), qr, kzl, kzr);
+      if (D == 4) ball_keys(raw_value(wk.key(qp)), qr, kwl, kwr);
     }
     int cnt = every ? len : 0;
     unsigned long long checked = 0;
@@ -194,7 +197,8 @@ wcount_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ item
       checked += (unsigned long long)(ph - pl);
       for (int p = pl; p < ph; ++p) {
         bool in = yk.in(p, kyl, kyr);
-        if (D == 3) in = in && zk.in(p, kzl, kzr);
+        if (D >= 3) in = in && zk.in(p, kzl, kzr);
+        if (D == 4) in = in && wk.in(p, kwl, kwr);
         cnt += in ? 1 : 0;
       }
     };
@@ -221,12 +225,13 @@ wcount_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ item
         const uint64_t lo2 = rkey(czlo[s * S2 + c]), hi2 = rkey(czhi[s * S2 + c]);
         const bool rc = reach && hi2 >= kzl && lo2 <= kzr;
         if (!__any_sync(0xffffffffu, rc)) continue;
-        const bool in2 = rc && in1 && lo2 >= kzl && hi2 <= kzr;
+        // d = 4: column 3 has no cell bounds, so every candidate is checked
+        const bool in2 = D == 3 && rc && in1 && lo2 >= kzl && hi2 <= kzr;
         count_range(cst[s * S2 + c], cst[s * S2 + c + 1], in2, rc);
       }
     };
 
-    const int sq = D == 3 ? (wi.strip & 0xffff) : wi.strip;
+    const int sq = NEST ? (wi.strip & 0xffff) : wi.strip;
     visit(sq);
     // strips above: their lower bounds grow, so the first one that no lane
     // reaches ends the direction (every lane's ball starts below its own
@@ -263,12 +268,16 @@ void launch_t(const JobDev* jobs, const WorkItem* items, int nitems, int* counte
 
 }  // namespace
 
-bool count_keys_supported(int dclass) { return dclass == 2 || dclass == 3; }
+// d = 2: measured faster than the FP32 union-window counts on every workload
+// here; for d = 3 and 4 the radii of those workloads are large and few cells
+// lie wholly inside a ball, so the FP32 kernel (egb_wgrid.cuh) is kept there
+bool count_keys_supported(int dclass) { return dclass == 2; }
 
 void launch_count_keys(const JobDev* jobs_d, const WorkItem* items_d, int nitems, int dclass,
                        int* counter, int num_sms, cudaStream_t st) {
   if (dclass == 2) launch_t<2>(jobs_d, items_d, nitems, counter, num_sms, st);
-  else launch_t<3>(jobs_d, items_d, nitems, counter, num_sms, st);
+  else if (dclass == 3) launch_t<3>(jobs_d, items_d, nitems, counter, num_sms, st);
+  else launch_t<4>(jobs_d, items_d, nitems, counter, num_sms, st);
 }
 
 }  // namespace egb
