@@ -739,8 +739,11 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   // tile launch groups
   struct Group {
     int is_knn, sel, kclass, dclass, slab, dmax, mode;
-    std::vector<WorkItem> items;
-    size_t tab_items = 0;
+    std::vector<WorkItem> items;  // tile groups: items built here
+    std::vector<ItemRun> runs;    // grid groups: items built on the device
+    std::vector<int32_t> cum;
+    int64_t nitems = 0, ncells = 0;
+    size_t tab_items = 0, tab_runs = 0, tab_cum = 0, off_items = 0;
     int64_t defer_cap = 0;   // slab groups: every query may be deferred once
     size_t off_defer = 0;
   };
@@ -780,23 +783,30 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
     if (m.is_knn && !m.sel) kclass = m.s.K <= 4 ? 4 : m.s.K <= 8 ? 8 : m.s.K <= 16 ? 16 : 32;
     Group& G = groups[(size_t)gidx[std::make_tuple((int)m.is_knn, m.sel, kclass, dclass, m.slab, m.mode)]];
     if (G.mode >= 2) {
+      // items never straddle a strip (cell); the device writes them
+      // (launch_emit_items) from these per-cell offsets
       const int S = jobs[j].nstrips;
       const int S2 = jobs[j].nsub;
       const int64_t len = jobs[j].len;
       const int qb = G.mode == 3 ? WG_QB : GRID_QB;
+      ItemRun r{};
+      r.job = (int32_t)j;
+      r.ncell = S * std::max(S2, 1);
+      r.cum0 = (int32_t)G.cum.size();
+      r.qb = qb;
+      r.cell0 = G.ncells;
       for (int sidx = 0; sidx < S; ++sidx) {
         const int32_t a = strip_start(sidx, len, S), b = strip_start(sidx + 1, len, S);
-        if (S2 > 0) {  // nested: items never straddle a cell
-          for (int c2 = 0; c2 < S2; ++c2) {
-            const int32_t ca = cell_start(a, b - a, c2, S2), cb = cell_start(a, b - a, c2 + 1, S2);
-            for (int32_t q0 = ca; q0 < cb; q0 += qb)
-              G.items.push_back({(int32_t)j, q0, std::min(q0 + qb, cb), sidx | (c2 << 16)});
-          }
-          continue;
+        for (int c2 = 0; c2 < std::max(S2, 1); ++c2) {
+          const int32_t ca = S2 > 0 ? cell_start(a, b - a, c2, S2) : a;
+          const int32_t cb = S2 > 0 ? cell_start(a, b - a, c2 + 1, S2) : b;
+          G.cum.push_back((int32_t)G.nitems);
+          G.nitems += (cb - ca + qb - 1) / qb;
         }
-        for (int32_t q0 = a; q0 < b; q0 += qb)
-          G.items.push_back({(int32_t)j, q0, std::min(q0 + qb, b), sidx});
       }
+      G.cum.push_back((int32_t)G.nitems);
+      G.ncells += r.ncell;
+      G.runs.push_back(r);
       if (G.mode == 2) G.defer_cap += len;
       continue;
     }
@@ -805,8 +815,11 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
     else if (G.is_knn) qb = knn_shape(G.kclass, G.dclass, plain, G.slab, G.dmax).queries();
     else qb = count_shape(G.dclass, plain, G.slab, G.dmax).queries();
     for (int64_t q0 = 0; q0 < jobs[j].len; q0 += qb) G.items.push_back({(int32_t)j, (int32_t)q0, 0, 0});
+    G.nitems = (int64_t)G.items.size();
     if (G.slab) G.defer_cap += jobs[j].len;
   }
+  for (Group& G : groups)
+    if (!G.runs.empty()) G.off_items = dl.take(sizeof(WorkItem) * (size_t)std::max<int64_t>(G.nitems, 1));
   for (Group& G : groups)
     if (G.defer_cap > 0) G.off_defer = dl.take(sizeof(DeferEntry) * (size_t)G.defer_cap);
 
@@ -858,7 +871,11 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
     tab_sstart[(size_t)gj] = tl.take(sizeof(int32_t) * (size_t)(J.nstrips + 1));
     if (J.nsub > 0) tab_cstart[(size_t)gj] = tl.take(sizeof(int32_t) * (size_t)(J.nstrips * J.nsub + 1));
   }
-  for (Group& G : groups) G.tab_items = tl.take(sizeof(WorkItem) * G.items.size());
+  for (Group& G : groups) {
+    G.tab_items = tl.take(sizeof(WorkItem) * G.items.size());
+    G.tab_runs = tl.take(sizeof(ItemRun) * G.runs.size());
+    G.tab_cum = tl.take(sizeof(int32_t) * G.cum.size());
+  }
   const size_t tab_cjobs = tl.take(sizeof(CombineJob) * std::max<size_t>(cjobs.size(), 1));
   const size_t tab_chunkjob = tl.take(sizeof(int32_t) * (size_t)std::max(nchunks, 1));
   const size_t tab_bytes = align_up(tl.off, 256);
@@ -986,12 +1003,18 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
     J.cnt = mjobs[j].is_knn ? nullptr : D.cnt[mjobs[j].s.slot];
     std::memcpy(H + tab_jobs + sizeof(JobDev) * j, &J, sizeof(JobDev));
   }
-  for (Group& G : groups)
+  for (Group& G : groups) {
     if (!G.items.empty()) std::memcpy(H + G.tab_items, G.items.data(), sizeof(WorkItem) * G.items.size());
+    if (!G.runs.empty()) std::memcpy(H + G.tab_runs, G.runs.data(), sizeof(ItemRun) * G.runs.size());
+    if (!G.cum.empty()) std::memcpy(H + G.tab_cum, G.cum.data(), sizeof(int32_t) * G.cum.size());
+  }
   if (!cjobs.empty()) std::memcpy(H + tab_cjobs, cjobs.data(), sizeof(CombineJob) * cjobs.size());
   if (nchunks) std::memcpy(H + tab_chunkjob, chunk_job.data(), sizeof(int32_t) * (size_t)nchunks);
 
   auto dtab = [&](size_t off) { return (void*)(A + off_tab + off); };
+  auto items_of = [&](const Group& G) -> const WorkItem* {
+    return G.runs.empty() ? (const WorkItem*)dtab(G.tab_items) : (const WorkItem*)(A + G.off_items);
+  };
   const TaskDev* tasks_d = (const TaskDev*)dtab(tab_tasks);
   int* counters = (int*)(A + off_zr + zr_counters);
   uint32_t* zero_d = (uint32_t*)(A + off_zr + zr_zero);
@@ -1024,6 +1047,11 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
                                  sizeof(double) * (size_t)P[(size_t)t].n, cudaMemcpyDeviceToDevice, st));
   if (timing) EGB_CUDA(cudaEventRecord(ctx->ev[1], st));
 
+  for (const Group& G : groups)  // grid work items, written on the device
+    if (!G.runs.empty())
+      launch_emit_items((const JobDev*)dtab(tab_jobs), (const ItemRun*)dtab(G.tab_runs),
+                        (int)G.runs.size(), (const int32_t*)dtab(G.tab_cum), G.nitems,
+                        (WorkItem*)(A + G.off_items), st);
   launch_gather(tasks_d, (const GatherCol*)dtab(tab_gcols), ncols_total, max_ld, st);
   launch_prepare(tasks_d, (const int32_t*)dtab(tab_coltask), (const int32_t*)dtab(tab_colidx),
                  ncols_total, (unsigned long long*)(A + off_minmax), (double*)(A + off_centers), st);
@@ -1074,21 +1102,21 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   if (timing) EGB_CUDA(cudaEventRecord(ctx->kev[0], st));
   for (size_t g = 0; g < groups.size(); ++g) {
     Group& G = groups[g];
-    if (!G.is_knn || G.items.empty()) continue;
+    if (!G.is_knn || G.nitems == 0) continue;
     if (G.sel)
-      launch_knn_select((const JobDev*)dtab(tab_jobs), (const WorkItem*)dtab(G.tab_items),
-                        (int)G.items.size(), err_d, ctx->num_sms, st);
+      launch_knn_select((const JobDev*)dtab(tab_jobs), items_of(G),
+                        (int)G.nitems, err_d, ctx->num_sms, st);
     else if (G.mode == 3)
-      launch_knn_wgrid((const JobDev*)dtab(tab_jobs), (const WorkItem*)dtab(G.tab_items),
-                       (int)G.items.size(), G.kclass, G.dclass, plain, G.dmax, counters + 2 * g,
+      launch_knn_wgrid((const JobDev*)dtab(tab_jobs), items_of(G),
+                       (int)G.nitems, G.kclass, G.dclass, plain, G.dmax, counters + 2 * g,
                        ctx->num_sms, st);
     else if (G.mode == 2)
-      launch_knn_grid((const JobDev*)dtab(tab_jobs), (const WorkItem*)dtab(G.tab_items),
-                      (int)G.items.size(), G.kclass, G.dclass, plain, G.dmax, counters + 2 * g,
+      launch_knn_grid((const JobDev*)dtab(tab_jobs), items_of(G),
+                      (int)G.nitems, G.kclass, G.dclass, plain, G.dmax, counters + 2 * g,
                       err_d, (DeferEntry*)(A + G.off_defer), counters + 2 * g + 1, ctx->num_sms, st);
     else
-      launch_knn_tile((const JobDev*)dtab(tab_jobs), (const WorkItem*)dtab(G.tab_items),
-                      (int)G.items.size(), G.kclass, G.dclass, plain, G.slab, G.dmax,
+      launch_knn_tile((const JobDev*)dtab(tab_jobs), items_of(G),
+                      (int)G.nitems, G.kclass, G.dclass, plain, G.slab, G.dmax,
                       counters + 2 * g, err_d, (DeferEntry*)(A + G.off_defer),
                       counters + 2 * g + 1, ctx->num_sms, st);
   }
@@ -1096,7 +1124,7 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   if (timing) EGB_CUDA(cudaEventRecord(ctx->kev[2], st));
   for (size_t g = 0; g < groups.size(); ++g) {
     Group& G = groups[g];
-    if (!G.is_knn || G.sel || !G.slab || G.mode == 3 || G.items.empty()) continue;
+    if (!G.is_knn || G.sel || !G.slab || G.mode == 3 || G.nitems == 0) continue;
     launch_knn_defer((const JobDev*)dtab(tab_jobs), (const DeferEntry*)(A + G.off_defer),
                      counters + 2 * g + 1, (int)G.defer_cap, G.kclass, G.dclass, plain,
                      ctx->num_sms, st);
@@ -1109,25 +1137,25 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   if (timing) EGB_CUDA(cudaEventRecord(ctx->kev[4], st));
   for (size_t g = 0; g < groups.size(); ++g) {
     Group& G = groups[g];
-    if (G.is_knn || G.items.empty()) continue;
+    if (G.is_knn || G.nitems == 0) continue;
     if (G.mode == 3) {
       if (!plain && count_keys_supported(G.dclass))
-        launch_count_keys((const JobDev*)dtab(tab_jobs), (const WorkItem*)dtab(G.tab_items),
-                          (int)G.items.size(), G.dclass, counters + 2 * g, ctx->num_sms, st);
+        launch_count_keys((const JobDev*)dtab(tab_jobs), items_of(G),
+                          (int)G.nitems, G.dclass, counters + 2 * g, ctx->num_sms, st);
       else
-        launch_count_wgrid((const JobDev*)dtab(tab_jobs), (const WorkItem*)dtab(G.tab_items),
-                           (int)G.items.size(), G.dclass, plain, G.dmax, counters + 2 * g,
+        launch_count_wgrid((const JobDev*)dtab(tab_jobs), items_of(G),
+                           (int)G.nitems, G.dclass, plain, G.dmax, counters + 2 * g,
                            ctx->num_sms, st);
       continue;
     }
     if (G.mode == 2) {
-      launch_count_grid((const JobDev*)dtab(tab_jobs), (const WorkItem*)dtab(G.tab_items),
-                        (int)G.items.size(), G.dclass, plain, G.dmax, counters + 2 * g, err_d,
+      launch_count_grid((const JobDev*)dtab(tab_jobs), items_of(G),
+                        (int)G.nitems, G.dclass, plain, G.dmax, counters + 2 * g, err_d,
                         (DeferEntry*)(A + G.off_defer), counters + 2 * g + 1, ctx->num_sms, st);
       continue;
     }
-    launch_count_tile((const JobDev*)dtab(tab_jobs), (const WorkItem*)dtab(G.tab_items),
-                      (int)G.items.size(), G.dclass, plain, G.slab, G.dmax, counters + 2 * g,
+    launch_count_tile((const JobDev*)dtab(tab_jobs), items_of(G),
+                      (int)G.nitems, G.dclass, plain, G.slab, G.dmax, counters + 2 * g,
                       err_d, (DeferEntry*)(A + G.off_defer), counters + 2 * g + 1, ctx->num_sms,
                       st);
   }
@@ -1135,7 +1163,7 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   if (timing) EGB_CUDA(cudaEventRecord(ctx->kev[6], st));
   for (size_t g = 0; g < groups.size(); ++g) {
     Group& G = groups[g];
-    if (G.is_knn || !G.slab || G.mode == 3 || G.items.empty()) continue;
+    if (G.is_knn || !G.slab || G.mode == 3 || G.nitems == 0) continue;
     launch_count_defer((const JobDev*)dtab(tab_jobs), (const DeferEntry*)(A + G.off_defer),
                        counters + 2 * g + 1, (int)G.defer_cap, G.dclass, plain, ctx->num_sms, st);
   }

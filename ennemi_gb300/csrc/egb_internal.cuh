@@ -308,6 +308,18 @@ struct WorkItem {         // one tile of queries of one job
                           // grids: strip | cell << 16)
 };
 
+// Grid work items built on the device (launch_emit_items): per grid job of a
+// launch group, its cells -- strips, or strips x cells when nested -- in
+// order; cell c of the run holds the group's items [cum[cum0 + c],
+// cum[cum0 + c + 1]), each of up to qb consecutive positions.
+struct ItemRun {
+  int32_t job;
+  int32_t ncell;
+  int32_t cum0;   // offset of the run's ncell + 1 item offsets in cum[]
+  int32_t qb;     // queries per item
+  int64_t cell0;  // index of the run's first cell among the group's cells
+};
+
 // A slab query whose search a tile work item left unfinished (it needed a
 // much wider window than the rest of its item); finished one warp per query.
 struct DeferEntry {
@@ -379,6 +391,8 @@ void launch_materialize_grid(const TaskDev* tasks_d, const JobDev* jobs_d,
                              const SortSeg* segs_d, const int32_t* gvals_sorted,
                              const SortSeg* gsegs_d, int64_t max_lds, cudaStream_t st);
 void launch_radius(const TaskDev* tasks_d, int ntasks, int64_t max_ld, cudaStream_t st);
+void launch_emit_items(const JobDev* jobs_d, const ItemRun* runs_d, int nruns, const int32_t* cum_d,
+                       int64_t nitems, WorkItem* items_d, cudaStream_t st);
 void launch_combine(const TaskDev* tasks_d, const CombineJob* jobs_d, const int32_t* chunk_job_d,
                     int nchunks, const double* psi_tab, int64_t psi_len, double* partial,
                     uint32_t* zero_flags, uint32_t* err, cudaStream_t st);

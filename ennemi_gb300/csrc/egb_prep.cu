@@ -328,6 +328,51 @@ void launch_materialize(const TaskDev* tasks_d, const JobDev* jobs_d, int njobs,
   count_launch();
 }
 
+namespace {
+// One thread per item: its run (the last whose first item is <= it), then
+// its cell within the run, both by binary search over the item offsets.
+__global__ void emit_items_kernel(const JobDev* __restrict__ jobs, const ItemRun* __restrict__ runs,
+                                  int nruns, const int32_t* __restrict__ cum, int64_t nitems,
+                                  WorkItem* __restrict__ items) {
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < nitems;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    int lo = 0, hi = nruns;
+    while (hi - lo > 1) {
+      const int m = (lo + hi) >> 1;
+      if (cum[runs[m].cum0] <= t) lo = m; else hi = m;
+    }
+    const ItemRun r = runs[lo];
+    int c0 = 0, c1 = r.ncell;  // the last cell whose first item is <= t
+    while (c1 - c0 > 1) {
+      const int m = (c0 + c1) >> 1;
+      if (cum[r.cum0 + m] <= t) c0 = m; else c1 = m;
+    }
+    const JobDev& J = jobs[r.job];
+    int a, b, code;
+    if (J.nsub > 0) {
+      a = J.cstart[c0];
+      b = J.cstart[c0 + 1];
+      code = (c0 / J.nsub) | ((c0 % J.nsub) << 16);
+    } else {
+      a = J.sstart[c0];
+      b = J.sstart[c0 + 1];
+      code = c0;
+    }
+    const int q0 = a + (int)(t - cum[r.cum0 + c0]) * r.qb;
+    items[t] = WorkItem{r.job, q0, min(q0 + r.qb, b), code};
+  }
+}
+}  // namespace
+
+void launch_emit_items(const JobDev* jobs_d, const ItemRun* runs_d, int nruns, const int32_t* cum_d,
+                       int64_t nitems, WorkItem* items_d, cudaStream_t st) {
+  if (nruns <= 0 || nitems <= 0) return;
+  int grid = (int)((nitems + 255) / 256);
+  if (grid > 8192) grid = 8192;
+  emit_items_kernel<<<grid, 256, 0, st>>>(jobs_d, runs_d, nruns, cum_d, nitems, items_d);
+  count_launch();
+}
+
 void launch_materialize_grid(const TaskDev* tasks_d, const JobDev* jobs_d,
                              const int32_t* grid_jobs_d, int ngrid, const int32_t* sorted_vals,
                              const SortSeg* segs_d, const int32_t* gvals_sorted,
