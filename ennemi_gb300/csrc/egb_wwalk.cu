@@ -149,20 +149,31 @@ wwalk_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items
       }
       return mm;
     };
-    // screen bound S and planning bound plan_margin(U); -1 when inactive
-    auto sbound = [&]() -> float {
-      if (pass1) return sfix;
-      return up_band32(up_band32(l32[KMAX - 1], mq), mq);
+    // screen bound S and planning bound plan_margin(U), kept current as the
+    // list changes (refresh); the planning bound is -1 when inactive
+    float sb_c = FINF, pb_c = FINF;
+    auto refresh = [&]() {
+      if (pass1) {
+        sb_c = sfix;
+        pb_c = plan_margin(ufix);
+      } else {
+        const float u = up_band32(l32[KMAX - 1], mq);
+        sb_c = up_band32(u, mq);
+        pb_c = plan_margin(u);
+      }
     };
-    auto pbound = [&]() -> float {
-      if (!act) return -1.0f;
-      if (pass1) return plan_margin(ufix);
-      return plan_margin(up_band32(l32[KMAX - 1], mq));
-    };
+    refresh();
+    auto sbound = [&]() -> float { return sb_c; };
+    auto pbound = [&]() -> float { return act ? pb_c : -1.0f; };
     auto visit = [&](int j, float dd) {
       ++visited;
       if (!pass1) {
-        rej = fminf(rej, dd < l32[KMAX - 1] ? insert_sorted_fi<KMAX>(l32, i32, dd, j) : dd);
+        if (dd < l32[KMAX - 1]) {
+          rej = fminf(rej, insert_sorted_fi<KMAX>(l32, i32, dd, j));
+          refresh();
+        } else {
+          rej = fminf(rej, dd);
+        }
       } else if (dd <= sfix) {
         const uint64_t mm = exact_dist(j);
         if (mm < top[KMAX - 1]) insert_sorted<KMAX>(top, mm);
@@ -422,6 +433,7 @@ wwalk_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items
             }
             rej = lo2;
             visited += cv;
+            refresh();
           }
         }
       }
@@ -447,6 +459,7 @@ wwalk_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items
       }
       act = again;
       pass1 = true;
+      refresh();
     } else {
       again = exists;
       act = exists;
