@@ -94,8 +94,8 @@ __global__ void sort_hist_kernel(const SortSeg* __restrict__ segs,
 }
 
 // Stable scatter of one tile.  Warp w ranks the keys [w * CH, (w + 1) * CH)
-// of the tile in rounds of 32: match_any gives a key's rank among the equal
-// digits of its round, per-warp counters carry the rank across rounds.  One
+// of the tile in rounds of 32: per-bit ballots give a key's rank among the
+// equal digits of its round, per-warp counters carry the rank across rounds.  One
 // block scan then turns the per-warp digit counts into the tile's layout in
 // digit order, staged in shared memory and written out so that consecutive
 // threads store to consecutive addresses of each digit's output run.
@@ -136,7 +136,14 @@ sort_scatter_kernel(const SortSeg* __restrict__ segs, const int32_t* __restrict_
     val[r] = valid ? vin[s.out_base + i0 + t] : 0;
     const uint32_t d = valid ? (uint32_t)(key[r] >> shift) & 255u : 256u + lane;
     dg[r] = d;
-    const uint32_t peers = __match_any_sync(0xffffffffu, d);
+    // lanes with the same digit (9 bits: invalid lanes carry 256 + lane),
+    // from one ballot per bit (measured faster than match_any here)
+    uint32_t peers = 0xffffffffu;
+#pragma unroll
+    for (int bit = 0; bit < 9; ++bit) {
+      const uint32_t bb = __ballot_sync(0xffffffffu, (d >> bit) & 1u);
+      peers &= ((d >> bit) & 1u) ? bb : ~bb;
+    }
     const uint32_t before = valid ? wcnt[warp][d] : 0u;
     __syncwarp();
     if (valid && (peers & lt) == 0) wcnt[warp][d] = before + __popc(peers);
