@@ -62,6 +62,37 @@ __device__ __forceinline__ int lower_bound_f(const float* __restrict__ x, int a,
   return a;
 }
 
+// The same from a guessed position g in [a, b): gallop towards the answer,
+// then bisect (exact for any g; a few steps when g is close).
+__device__ __forceinline__ int lower_bound_from(const float* __restrict__ x, int a, int b, float v,
+                                                int g) {
+  if (b <= a) return a;
+  g = g < a ? a : (g >= b ? b - 1 : g);
+  int lo, hi;  // x[lo - 1] < v <= x[hi] (lo = a, hi = b when absent)
+  if (x[g] < v) {
+    lo = g + 1;
+    int step = 1;
+    for (;;) {
+      const int t = g + step;
+      if (t >= b) { hi = b; break; }
+      if (!(x[t] < v)) { hi = t; break; }
+      lo = t + 1;
+      step <<= 1;
+    }
+  } else {
+    hi = g;
+    int step = 1;
+    for (;;) {
+      const int t = g - step;
+      if (t < a) { lo = a; break; }
+      if (x[t] < v) { lo = t + 1; break; }
+      hi = t;
+      step <<= 1;
+    }
+  }
+  return lower_bound_f(x, lo, hi, v);
+}
+
 template <int D, int KMAX, bool NEST>
 __global__ void __launch_bounds__(WW_WARPS * 32, (D == 2 ? 6 : 1))
 wwalk_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items, int nitems,
@@ -214,7 +245,14 @@ wwalk_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items
         }
       }
     };
-    auto walk_range = [&](int a, int b) { walk(a, b, lower_bound_f(g, a, b, qv[0])); };
+    // the query's relative position in its own strip (cell): where to guess
+    // its column 0 in another
+    const int ha = NEST ? cst[sq * S2 + hc2] : sst[sq];
+    const int hb = NEST ? cst[sq * S2 + hc2 + 1] : sst[sq + 1];
+    const float frel = hb > ha ? (float)(qp - ha) / (float)(hb - ha) : 0.0f;
+    auto walk_range = [&](int a, int b) {
+      walk(a, b, lower_bound_from(g, a, b, qv[0], a + (int)(frel * (float)(b - a))));
+    };
     // The warp visits strips and cells together; a lane walks the ones its
     // planning bound reaches.
     auto strip_reach = [&](int s, float t) {
