@@ -16,9 +16,9 @@
 // queries of one strip (cell) and visits the strips outward from its own
 // while some lane's column-1 key range reaches them; in a nested grid, the
 // cells of each strip whose column-2 range meets some lane's.  In each strip
-// (cell) the warp finds the union column-0 window of its lanes with a 16-ary
-// warp search, then every lane binary-searches its own column-0 key range
-// inside the window.  A strip (cell) whose column-1 (and column-2) bounds
+// (cell) every lane finds its own column-0 key range by galloping from a
+// guess -- its own position at home, the same relative positions elsewhere --
+// and bisecting.  A strip (cell) whose column-1 (and column-2) bounds
 // lie inside the lane's ball adds the length of that range; otherwise the
 // lane checks the column-1 (column-2) keys of the candidates in its range.
 #include "egb_internal.cuh"
@@ -72,40 +72,6 @@ __device__ __forceinline__ uint64_t wmax64(uint64_t v) {
   return v;
 }
 
-// Positions [wlo, whi) of [s0, s1) whose column-0 key lies in [lo, hi]
-// (keys sorted): the lower half-warp finds the first key >= lo, the upper
-// half the first key > hi, 16-ary.
-__device__ __forceinline__ void warp_window_keys(const KeyCol& x, int s0, int s1, uint64_t lo,
-                                                 uint64_t hi, int& wlo, int& whi) {
-  const int lane = threadIdx.x & 31;
-  const bool upper = lane >= 16;
-  const int l16 = lane & 15;
-  const unsigned m = upper ? 0xffff0000u : 0x0000ffffu;
-  int a = s0, b = s1;
-  for (int round = 0; round < 40; ++round) {
-    const int n = b - a;
-    const bool small = n <= 16;
-    int p = small ? a + l16 : a + (int)((int64_t)(l16 + 1) * n / 17);
-    const bool inr = p < b;
-    p = inr ? p : s0;
-    const bool t = inr && (upper ? x.le(p, hi) : x.lt(p, lo));
-    const int c = __popc(__ballot_sync(0xffffffffu, t) & m);
-    if (small) {
-      a = a + c;
-      b = a;
-    } else {
-      const int na = c == 0 ? a : a + (int)((int64_t)c * n / 17) + 1;
-      const int nb = c == 16 ? b : a + (int)((int64_t)(c + 1) * n / 17);
-      a = na;
-      b = nb;
-    }
-    if (__all_sync(0xffffffffu, b - a <= 0)) break;
-  }
-  wlo = __shfl_sync(0xffffffffu, a, 0);
-  whi = __shfl_sync(0xffffffffu, a, 16);
-  if (whi < wlo) whi = wlo;
-}
-
 // First position of [a, b) with key >= k (keys sorted).
 __device__ __forceinline__ int lower_key(const KeyCol& x, int a, int b, uint64_t k) {
   int n = b - a;
@@ -133,6 +99,39 @@ __device__ __forceinline__ int upper_key(const KeyCol& x, int a, int b, uint64_t
     }
   }
   return a;
+}
+
+// First position of [a, b) with key >= k (lt = false) or > k (lt = true:
+// first key not <= k), from a guessed position g: gallop towards the
+// answer, then bisect (exact for any g).
+__device__ __forceinline__ int bound_from(const KeyCol& x, int a, int b, uint64_t k, bool upper,
+                                          int g) {
+  if (b <= a) return a;
+  g = g < a ? a : (g >= b ? b - 1 : g);
+  auto before = [&](int p) { return upper ? x.le(p, k) : x.lt(p, k); };  // p precedes the bound
+  int lo, hi;
+  if (before(g)) {
+    lo = g + 1;
+    int step = 1;
+    for (;;) {
+      const int t = g + step;
+      if (t >= b) { hi = b; break; }
+      if (!before(t)) { hi = t; break; }
+      lo = t + 1;
+      step <<= 1;
+    }
+  } else {
+    hi = g;
+    int step = 1;
+    for (;;) {
+      const int t = g - step;
+      if (t < a) { lo = a; break; }
+      if (before(t)) { lo = t + 1; break; }
+      hi = t;
+      step <<= 1;
+    }
+  }
+  return upper ? upper_key(x, lo, hi, k) : lower_key(x, lo, hi, k);
 }
 
 template <int D>
@@ -181,15 +180,24 @@ wcount_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ item
     unsigned long long checked = 0;
 
     // Count this lane's ball in the positions [a, b) of one strip or cell.
-    auto count_range = [&](int a, int b, bool inner, bool reach) {
-      // union column-0 window of the lanes that reach this range
-      const uint64_t ul = wmin64(reach ? kxl : ~0ull);
-      const uint64_t uh = wmax64(reach ? kxr : 0ull);
-      int wl, wh;
-      warp_window_keys(xk, a, b, ul, uh, wl, wh);
+    // In its own strip (cell) the lane searches its column-0 range from its
+    // own position; elsewhere from the same relative positions, which the
+    // equal-count layout makes close guesses.
+    const int sq = NEST ? (wi.strip & 0xffff) : wi.strip;
+    const int hc2 = NEST ? (wi.strip >> 16) : 0;
+    float frl = 0.0f, frh = 0.0f;
+    auto count_range = [&](int a, int b, bool inner, bool reach, bool home) {
       if (!reach) return;
-      const int pl = lower_key(xk, wl, wh, kxl);
-      const int ph = upper_key(xk, pl, wh, kxr);
+      int pl, ph;
+      if (home) {
+        pl = bound_from(xk, a, b, kxl, false, qp);
+        ph = bound_from(xk, pl, b, kxr, true, qp);
+        frl = b > a ? (float)(pl - a) / (float)(b - a) : 0.0f;
+        frh = b > a ? (float)(ph - a) / (float)(b - a) : 0.0f;
+      } else {
+        pl = bound_from(xk, a, b, kxl, false, a + (int)(frl * (float)(b - a)));
+        ph = bound_from(xk, pl, b, kxr, true, a + (int)(frh * (float)(b - a)));
+      }
       if (inner) {
         cnt += ph - pl;
         return;
@@ -209,7 +217,7 @@ wcount_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ item
       if (!__any_sync(0xffffffffu, reach)) return;
       const bool in1 = reach && lo1 >= kyl && hi1 <= kyr;
       if (D == 2) {
-        count_range(sst[s], sst[s + 1], in1, reach);
+        count_range(sst[s], sst[s + 1], in1, reach, s == sq);
         return;
       }
       // cells whose column-2 range meets a reaching lane's: a contiguous run
@@ -227,11 +235,10 @@ wcount_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ item
         if (!__any_sync(0xffffffffu, rc)) continue;
         // d = 4: column 3 has no cell bounds, so every candidate is checked
         const bool in2 = D == 3 && rc && in1 && lo2 >= kzl && hi2 <= kzr;
-        count_range(cst[s * S2 + c], cst[s * S2 + c + 1], in2, rc);
+        count_range(cst[s * S2 + c], cst[s * S2 + c + 1], in2, rc, s == sq && c == hc2);
       }
     };
 
-    const int sq = NEST ? (wi.strip & 0xffff) : wi.strip;
     visit(sq);
     // strips above: their lower bounds grow, so the first one that no lane
     // reaches ends the direction (every lane's ball starts below its own

@@ -126,6 +126,14 @@ def _medium_cases():
     yield "ent_3d_k7_20k", "ent", 7, dict(x=rng.standard_t(4, size=(n, 3)))
     c6 = rng.normal(size=(10000, 5))
     yield "cmi_dz3_10k", "cmi", 3, dict(x=c6[:, 0], y=c6[:, 1] + 0.5 * c6[:, 2], z=c6[:, 2:])
+    # walk kNN / key-range counts: exact duplicates (K-th distance 0, counts
+    # with negative radius), K = 8 in 2-D, a job just above the grid size
+    dup = rng.integers(0, 40, size=(20000, 2)).astype(np.float64)
+    yield "mi_duplicates_20k", "mi", 3, dict(x=dup[:, 0], y=dup[:, 1])
+    yield "mi_k7_20k", "mi", 7, dict(x=g[:, 0], y=g[:, 1] ** 3)
+    yield "mi_4100", "mi", 3, dict(x=g[:4100, 0], y=g[:4100, 1])
+    yield "cmi_dup_z_15k", "cmi", 3, dict(x=c3[:15000, 0], y=c3[:15000, 1],
+                                           z=np.round(c3[:15000, 2:], 0))
 
 
 MEDIUM = list(_medium_cases())
