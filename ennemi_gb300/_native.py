@@ -33,6 +33,7 @@ FORCE_SLAB = 1 << 5
 FORCE_GRID = 1 << 6
 FORCE_CTA_GRID = 1 << 7
 GRAPH = 1 << 8
+STAGE_HOST = 1 << 9
 
 # layout policy (include/ennemi_gb.h)
 MODE_AUTO, MODE_BRUTE, MODE_SLAB, MODE_GRID, MODE_WARP_GRID = -1, 0, 1, 2, 3

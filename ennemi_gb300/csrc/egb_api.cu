@@ -143,6 +143,9 @@ struct egb_ctx {
   double timings[NPHASE + NKTIME] = {};
   int ntimings = 0;
   int64_t h2d_bytes = 0, d2h_bytes = 0;
+  // the device reads pageable host memory through the host's page tables
+  // (address translation services over a coherent CPU-GPU link)
+  bool host_direct = false;
   // CUDA graph of the last batch run with EGB_GRAPH, replayed while the
   // batch signature is unchanged
   cudaGraphExec_t graph_exec = nullptr;
@@ -571,27 +574,40 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   // ------------------------------------------------------------- layout --
   Layout dl;  // device arena
   Layout tl;  // table blob (pinned host, copied to the device as one block)
-  // caller data ranges (host input): dedupe by address range
-  struct Range { uintptr_t lo, hi; size_t dev_off; };
+  // caller data ranges (host input), deduplicated by address range.  Where
+  // the device reads pageable host memory directly, the gather kernel reads a
+  // range in place when every column in it is contiguous and read in order
+  // (one pass over the link, no staging copy); strided columns (re-read once
+  // per column) and class-permuted ones (scattered reads) are staged in the
+  // arena with one copy per range.
+  struct Range { uintptr_t lo, hi; size_t dev_off; bool stage; };
   std::vector<Range> ranges;
+  const bool direct_ok = !dev_in && ctx->host_direct && !(flags & EGB_STAGE_HOST);
   if (!dev_in) {
-    std::vector<std::pair<uintptr_t, uintptr_t>> rs;
+    struct Span { uintptr_t lo, hi; bool stage; };
+    std::vector<Span> rs;
     for (int t = 0; t < ntasks; ++t)
       for (int c = 0; c < P[(size_t)t].ncol; ++c) {
         const egb_column& col = tasks[t].cols[c];
         const uintptr_t lo = (uintptr_t)col.data;
         const uintptr_t hi = lo + (uintptr_t)(((tasks[t].n - 1) * col.stride + 1) * sizeof(double));
-        rs.push_back({lo, hi});
+        rs.push_back({lo, hi, !direct_ok || col.stride != 1 || !P[(size_t)t].perm.empty()});
       }
-    std::sort(rs.begin(), rs.end());
-    for (auto& r : rs) {
-      if (!ranges.empty() && r.first <= ranges.back().hi) ranges.back().hi = std::max(ranges.back().hi, r.second);
-      else ranges.push_back({r.first, r.second, 0});
+    std::sort(rs.begin(), rs.end(), [](const Span& a, const Span& b) {
+      return a.lo < b.lo || (a.lo == b.lo && a.hi < b.hi);
+    });
+    for (const Span& r : rs) {
+      if (!ranges.empty() && r.lo <= ranges.back().hi) {
+        ranges.back().hi = std::max(ranges.back().hi, r.hi);
+        ranges.back().stage = ranges.back().stage || r.stage;
+      } else {
+        ranges.push_back({r.lo, r.hi, 0, r.stage});
+      }
     }
     for (auto& r : ranges) {
       // keep the element alignment of the source within the 256-byte block
       const size_t mis = r.lo & 255u;
-      r.dev_off = dl.take(r.hi - r.lo + mis) + mis;
+      if (r.stage) r.dev_off = dl.take(r.hi - r.lo + mis) + mis;
     }
   }
   auto dev_col = [&](int t, int c) -> const double* {
@@ -599,7 +615,8 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
     if (dev_in) return col.data;
     const uintptr_t a = (uintptr_t)col.data;
     for (const Range& r : ranges)
-      if (a >= r.lo && a < r.hi) return (const double*)((char*)ctx->arena + r.dev_off + (a - r.lo));
+      if (a >= r.lo && a < r.hi)
+        return r.stage ? (const double*)((char*)ctx->arena + r.dev_off + (a - r.lo)) : col.data;
     return nullptr;
   };
 
@@ -1028,7 +1045,8 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   if (timing) EGB_CUDA(cudaEventRecord(ctx->ev[0], st));
   if (!dev_in)
     for (const Range& r : ranges)
-      EGB_CUDA(cudaMemcpyAsync(A + r.dev_off, (const void*)r.lo, r.hi - r.lo, cudaMemcpyHostToDevice, st));
+      if (r.stage)
+        EGB_CUDA(cudaMemcpyAsync(A + r.dev_off, (const void*)r.lo, r.hi - r.lo, cudaMemcpyHostToDevice, st));
   const size_t pin_zr = pin_rb + sizeof(double) * (size_t)std::max(nchunks, 1);
   // Everything from the descriptor upload to the read-back: issued directly,
   // or captured once into a CUDA graph and replayed for identical batches.
@@ -1284,6 +1302,10 @@ int egb_create(int device, egb_ctx** out) {
   ctx->stream = ctx->own_stream;
   cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
   if (ctx->num_sms < 1) ctx->num_sms = 1;
+  int pageable = 0, host_tables = 0;
+  cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, device);
+  cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, device);
+  ctx->host_direct = pageable && host_tables;
   for (auto& e : ctx->ev) cudaEventCreate(&e);
   for (auto& e : ctx->kev) cudaEventCreate(&e);
   *out = ctx;

@@ -78,7 +78,7 @@ enum egb_flags {
                                   picks it for spaces of >= 4096 points          */
   EGB_FORCE_CTA_GRID = 1 << 7, /* grid spaces use the CTA-item kernels, never the
                                   warp-item ones (tests, comparisons)            */
-  EGB_GRAPH = 1 << 8           /* capture the batch's device work (descriptor
+  EGB_GRAPH = 1 << 8,          /* capture the batch's device work (descriptor
                                   upload to read-back) in a CUDA graph and replay
                                   it for later batches with the same signature
                                   (same sizes, pointers and flags); ignored with
@@ -87,6 +87,10 @@ enum egb_flags {
                                   of the context exactly (shapes, column pointers
                                   and strides, flags, stream; the data may have
                                   changed) replays without being planned again  */
+  EGB_STAGE_HOST = 1 << 9      /* copy host columns into device memory before the
+                                  gather even where the device reads pageable
+                                  host memory directly (by default contiguous
+                                  host columns are then read in place)           */
 };
 
 /* One float64 column: sample i at data[i * stride] (stride in elements). */

@@ -176,6 +176,35 @@ def test_device_input_matches_host_input():
     assert host[0] == dev[0]
 
 
+def test_host_columns_read_in_place_match_staged_copies():
+    """Contiguous host columns may be read by the gather kernel in place
+    (devices that read pageable memory); strided, shared and class-permuted
+    columns are staged.  Every route gives the same bits."""
+    rng = np.random.default_rng(23)
+    n = 40000
+    a = rng.normal(size=n)
+    b = 0.6 * a + rng.normal(size=n)
+    m = rng.normal(size=(n, 3))                     # strided column views
+    m[:, 1] += 0.5 * m[:, 0]
+    lab = rng.integers(0, 4, size=n).astype(np.int32)
+    s = a + 0.3 * lab
+    tasks = [E.mi_task(a, b, 3),
+             N.Task(N.MI, 3, [m[:, 0]], [m[:, 1]], n=n),
+             N.Task(N.CMI, 3, [a], [m[:, 1]], [b], n=n),
+             N.Task(N.CMI, 4, [m[:, 0], m[:, 2]], [b], [a], n=n),
+             N.Task(N.SEMI, 3, [s], labels=lab, nclass=4, n=n),
+             N.Task(N.ENTROPY, 3, [b, a], n=n)]
+    for extra in (0, N.GRAPH):
+        staged = N.run_tasks(tasks, flags=N.STAGE_HOST | extra)
+        default = N.run_tasks(tasks, flags=extra)
+        assert np.array_equal(staged, default), extra
+    pts = np.ascontiguousarray(m[:, :2])
+    r = N.knn_eps(pts, 3)
+    assert np.array_equal(r, N.knn_eps(pts, 3, flags=N.STAGE_HOST))
+    assert np.array_equal(N.ball_count(pts, r - 1e-12),
+                          N.ball_count(pts, r - 1e-12, flags=N.STAGE_HOST))
+
+
 def test_public_estimators_on_gpu():
     rng = np.random.default_rng(0)
     cov = [[1, 0.6], [0.6, 1]]
