@@ -379,15 +379,17 @@ def main():
     sms = torch.cuda.get_device_properties(dev).multi_processor_count
     max_mhz = clocks.get("sm_max_mhz") or peaks.get("sm_max_mhz") or 2070.0
     peak_ops = sms * 128 * max_mhz * 1e6
-    cand = [("count_tile_kernel", phases.get("count_tile", 0.0), work_stats.get("count_tile_ops", 0),
+    # multi-D kernels of the workload: the kNN walk (2-D MI and 3-D CMI joint
+    # spaces) and the exact key-range counts (2-D CMI marginals)
+    cand = [("wcount_kernel", phases.get("count_tile", 0.0), work_stats.get("count_tile_ops", 0),
              work_stats.get("count_tile_pairs", 0)),
-            ("knn_tile_kernel", phases.get("knn_tile", 0.0), work_stats.get("knn_tile_ops", 0),
+            ("wwalk_kernel", phases.get("knn_tile", 0.0), work_stats.get("knn_tile_ops", 0),
              work_stats.get("knn_tile_pairs", 0))]
     kname, kms, kops, kpairs = max(cand, key=lambda c: c[1])
     achieved = kops / (kms / 1000.0) if kms > 0 else 0.0
-    # the brute-force work the same kernel replaces (SURVEY-style N_q*N_c*(2d+1)
-    # per job: every query against every point of its space)
-    if kname == "knn_tile_kernel":
+    # the brute-force work the same kernel replaces (N_q * N_c * (2d+1) per
+    # job: every query against every point of its space)
+    if kname == "wwalk_kernel":
         bf_ops = sum(float(args.n) ** 2 * (2 * (2 if kind == "mi" else 3) + 1) for kind, _ in work)
     else:
         bf_ops = sum(2 * float(args.n) ** 2 * 5 for kind, _ in work if kind == "cmi")

@@ -53,6 +53,35 @@ struct KeyCol {
   }
 };
 
+// 1 if position p, whose high word w equals that of a or b, has its key in [a, b]
+__device__ __forceinline__ int tied_in(const KeyCol& c, uint32_t w, int p, uint64_t a, uint64_t b) {
+  if (w != (uint32_t)(a >> 32) && w != (uint32_t)(b >> 32)) return 0;
+  const uint64_t k = ((uint64_t)w << 32) | c.lo[p];
+  return (k >= a && k <= b) ? 1 : 0;
+}
+
+// #{p in [pl, ph) : key(p) in [a, b]}, four high words per 16-byte load
+// (the key columns start 128-byte aligned: lds is a multiple of 32); a
+// high word strictly between those of a and b settles the point, one equal
+// to either is settled by the full key.
+__device__ __forceinline__ int count_in(const KeyCol& c, int pl, int ph, uint64_t a, uint64_t b) {
+  const uint32_t ah = (uint32_t)(a >> 32), bh = (uint32_t)(b >> 32);
+  int cnt = 0;
+  int p = pl;
+  for (; p < ph && (p & 3); ++p) cnt += c.in(p, a, b) ? 1 : 0;
+  for (; p + 4 <= ph; p += 4) {
+    const uint4 h = *reinterpret_cast<const uint4*>(c.hi + p);
+    cnt += (h.x > ah && h.x < bh) + (h.y > ah && h.y < bh) + (h.z > ah && h.z < bh) +
+           (h.w > ah && h.w < bh);
+    const bool tie = h.x == ah || h.x == bh || h.y == ah || h.y == bh || h.z == ah ||
+                     h.z == bh || h.w == ah || h.w == bh;
+    if (tie) cnt += tied_in(c, h.x, p, a, b) + tied_in(c, h.y, p + 1, a, b) +
+                    tied_in(c, h.z, p + 2, a, b) + tied_in(c, h.w, p + 3, a, b);
+  }
+  for (; p < ph; ++p) cnt += c.in(p, a, b) ? 1 : 0;
+  return cnt;
+}
+
 __device__ __forceinline__ uint64_t rkey(uint64_t u) { return raw_key(u); }
 
 __device__ __forceinline__ uint64_t wmin64(uint64_t v) {
@@ -203,6 +232,10 @@ wcount_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ item
         return;
       }
       checked += (unsigned long long)(ph - pl);
+      if (D == 2) {
+        cnt += count_in(yk, pl, ph, kyl, kyr);
+        return;
+      }
       for (int p = pl; p < ph; ++p) {
         bool in = yk.in(p, kyl, kyr);
         if (D >= 3) in = in && zk.in(p, kzl, kzr);
