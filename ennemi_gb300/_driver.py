@@ -338,12 +338,23 @@ def _estimate_mi(y: FloatArray, x: FloatArray, lag: FloatArray, k: int,
         jobs.append(_task_job(prep, ("x", vi), xv, ("y",), y, lag[li], max_lag, min_lag, k, mask,
                               cond, cond_lag[li], discrete_x, discrete_y, preprocess, drop_nan,
                               share_x=False))
-    batch = _Batch()
-    slots = [_add_prepared(batch, p) for p in _prepare_all(jobs, max_threads)]
-    values = batch.run()
+    if _device_prep_ok((x, y) + (() if cond is None else (cond,)), cond, preprocess, drop_nan,
+                       discrete_x or discrete_y):
+        lo, hi = min(min_lag, 0), max(max_lag, 0)
+        n = len(y) - hi + lo if prep.idx is None else len(prep.idx)
+        specs = []
+        for li, vi in indices:
+            xv = x if x.ndim == 1 else x[:, vi]
+            zv = None if cond is None else cond[hi - cond_lag[li][0]:, 0]
+            specs.append((xv[hi - lag[li]:], y[hi:], zv))
+        values = _run_device_prep(specs, n, k, prep.idx, jobs, max_threads)
+    else:
+        batch = _Batch()
+        slots = [_add_prepared(batch, p) for p in _prepare_all(jobs, max_threads)]
+        values = batch.run()[slots]
     result = np.empty((len(lag), nvar))
-    for (li, vi), s in zip(indices, slots):
-        result[li, vi] = values[s]
+    for (li, vi), v in zip(indices, values):
+        result[li, vi] = v
         if callback is not None:
             callback(vi, lag[li])
     return result
@@ -462,16 +473,119 @@ def _pairwise_mi(data: FloatArray, k: int, cond: Optional[FloatArray], preproces
             jobs.append(_task_job(prep, ("d", i), data[:, i], ("d", j), data[:, j], 0, 0, 0, k, mask,
                                   cond, cond_lag, discrete[i], discrete[j], preprocess, drop_nan,
                                   share_x=True))
-    batch = _Batch()
-    slots = [_add_prepared(batch, p) for p in _prepare_all(jobs, max_threads)]
-    values = batch.run()
+    if pairs and _device_prep_ok((data,) + (() if cond is None else (cond,)), cond, preprocess,
+                                 drop_nan, bool(np.any(discrete))):
+        n = len(data) if prep.idx is None else len(prep.idx)
+        specs = [(data[:, i], data[:, j], None if cond is None else cond[:, 0]) for i, j in pairs]
+        values = _run_device_prep(specs, n, k, prep.idx, jobs, max_threads)
+    else:
+        batch = _Batch()
+        slots = [_add_prepared(batch, p) for p in _prepare_all(jobs, max_threads)]
+        values = batch.run()[slots] if slots else np.empty(0)
     result = np.full((nvar, nvar), np.nan)
-    for (i, j), s in zip(pairs, slots):
-        result[i, j] = values[s]
-        result[j, i] = values[s]
+    for (i, j), v in zip(pairs, values):
+        result[i, j] = v
+        result[j, i] = v
         if callback is not None:
             callback(i, j)
     return result
+
+
+# ------------------------------------------------- device preprocessing --
+
+# Tasks whose variables are all continuous float64 arrays free of NaNs, with
+# at most one condition column, are sliced, masked and rescaled on the device
+# (EGB_RESCALE): the library sums in NumPy's pairwise order, and
+# _numpy_sums_pairwise() confirms once per process that this NumPy sums that
+# way, so the preprocessed columns equal the reference's bit for bit.  Any
+# other task, and a task with a constant column (which the reference leaves
+# unscaled, with a warning), goes through the host preparation below.
+device_prep = True   # False: always prepare on the host
+
+_pairwise_checked: Optional[bool] = None
+
+
+def _pairwise_sum(a) -> float:
+    """NumPy's pairwise summation (numpy/_core/src/umath/loops_utils.h.src,
+    pairwise_sum) in plain Python, for the run-time check."""
+    n = len(a)
+    if n < 8:
+        r = 0.0
+        for v in a:
+            r += v
+        return r
+    if n <= 128:
+        r = [float(v) for v in a[:8]]
+        i = 8
+        while i < n - (n % 8):
+            for j in range(8):
+                r[j] += a[i + j]
+            i += 8
+        res = ((r[0] + r[1]) + (r[2] + r[3])) + ((r[4] + r[5]) + (r[6] + r[7]))
+        while i < n:
+            res += a[i]
+            i += 1
+        return res
+    n2 = n // 2
+    n2 -= n2 % 8
+    return _pairwise_sum(a[:n2]) + _pairwise_sum(a[n2:])
+
+
+def _numpy_sums_pairwise() -> bool:
+    """True when this NumPy's sum, mean and std of 1-D float64 arrays follow
+    _pairwise_sum (sizes around every branch and beyond one 8192-value block)."""
+    global _pairwise_checked
+    if _pairwise_checked is None:
+        rng = np.random.default_rng(12345)
+        ok = True
+        for n in (1, 5, 8, 9, 100, 128, 129, 136, 1000, 8191, 8193, 20011):
+            a = rng.standard_normal(n) * 3.0 + 1.0
+            vals = a.tolist()
+            s = _pairwise_sum(vals)
+            m = s / n
+            d = [(v - m) * (v - m) for v in vals]
+            sd = float(np.sqrt(_pairwise_sum(d) / n))
+            ok = ok and float(np.add.reduce(a)) == s and float(a.mean()) == m and float(a.std()) == sd
+        _pairwise_checked = ok
+    return _pairwise_checked
+
+
+def _device_prep_ok(arrays, cond, preprocess: bool, drop_nan: bool, any_discrete: bool) -> bool:
+    if not (device_prep and preprocess) or drop_nan or any_discrete:
+        return False
+    if cond is not None and cond.shape[1] != 1:
+        return False
+    for a in arrays:
+        if a.dtype != np.float64 or np.isnan(a).any():
+            return False
+    return _numpy_sums_pairwise()
+
+
+def _run_device_prep(specs, n: int, k: int, idx, jobs, max_threads) -> np.ndarray:
+    """Estimates of the tasks (x, y, z or None): the columns are lagged views
+    of the caller's arrays, sample w at view[idx[w]] (idx None: the first n),
+    rescaled on the device.  Tasks with a constant column are prepared on the
+    host (`jobs`, same order) and run in a second batch."""
+    if n <= k:
+        raise ValueError(K_TOO_LARGE_MSG)
+    index = None if idx is None else np.ascontiguousarray(idx, dtype=np.int32)
+    tasks = []
+    for xv, yv, zv in specs:
+        if zv is None:
+            tasks.append(_native.Task(_native.MI, k, [xv], [yv], n=n, index=index))
+        else:
+            tasks.append(_native.Task(_native.CMI, k, [xv], [yv], [zv], n=n, index=index))
+    res = []
+    values = _native.run_tasks(tasks, flags=run_flags | _native.RESCALE, results_out=res,
+                               noise=lambda m: _noise.take(0, (m,)))
+    redo = [i for i, r in enumerate(res) if r.status == _native.TASK_CONSTANT]
+    if redo:
+        batch = _Batch()
+        slots = [_add_prepared(batch, p) for p in _prepare_all([jobs[i] for i in redo], max_threads)]
+        again = batch.run()
+        for i, s in zip(redo, slots):
+            values[i] = again[s]
+    return values
 
 
 # ------------------------------------------------------- per-task prep --

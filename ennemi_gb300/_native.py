@@ -34,6 +34,8 @@ FORCE_GRID = 1 << 6
 FORCE_CTA_GRID = 1 << 7
 GRAPH = 1 << 8
 STAGE_HOST = 1 << 9
+RESCALE = 1 << 10
+TASK_CONSTANT = 1        # egb_result.status: constant column under RESCALE
 
 # layout policy (include/ennemi_gb.h)
 MODE_AUTO, MODE_BRUTE, MODE_SLAB, MODE_GRID, MODE_WARP_GRID = -1, 0, 1, 2, 3
@@ -61,7 +63,8 @@ class EgbTask(ctypes.Structure):
     _fields_ = [("kind", ctypes.c_int32), ("k", ctypes.c_int32), ("n", ctypes.c_int64),
                 ("dx", ctypes.c_int32), ("dy", ctypes.c_int32), ("dz", ctypes.c_int32),
                 ("nclass", ctypes.c_int32), ("cols", ctypes.POINTER(EgbColumn)),
-                ("labels", ctypes.POINTER(ctypes.c_int32))]
+                ("labels", ctypes.POINTER(ctypes.c_int32)),
+                ("index", ctypes.POINTER(ctypes.c_int32))]
 
 
 class EgbResult(ctypes.Structure):
@@ -113,6 +116,8 @@ def load():
         lib.egb_last_stats.restype = ctypes.c_int
         lib.egb_set_policy.argtypes = [vp, ctypes.POINTER(ctypes.c_int8), i32]
         lib.egb_set_policy.restype = ctypes.c_int
+        lib.egb_set_noise.argtypes = [vp, ctypes.POINTER(ctypes.c_double), ctypes.c_int64]
+        lib.egb_set_noise.restype = ctypes.c_int
         lib.egb_get_policy.argtypes = [vp, ctypes.POINTER(ctypes.c_int8), i32]
         lib.egb_get_policy.restype = ctypes.c_int
         lib.egb_device_info.argtypes = [vp, ctypes.c_char_p, i32, ctypes.POINTER(i32)]
@@ -135,6 +140,7 @@ class Context:
             raise RuntimeError(f"egb_create(device={device}) failed ({rc}): no usable CUDA device")
         self.h = h
         self.lock = threading.Lock()
+        self.noise_len = 0      # values of the RESCALE noise stream on the device
 
     def close(self):
         if self.h:
@@ -181,6 +187,15 @@ class Context:
         self.check(self.lib.egb_set_policy(
             self.h, m.ctypes.data_as(ctypes.POINTER(ctypes.c_int8)), POLICY_ENTRIES), "egb_set_policy")
 
+    def set_noise(self, values) -> None:
+        """The RESCALE noise stream: values[p] = p-th draw of the reference's
+        default_rng(2_718281828).normal(0.0, 1e-10, ...)."""
+        v = np.ascontiguousarray(values, dtype=np.float64)
+        with self.lock:
+            self.check(self.lib.egb_set_noise(
+                self.h, v.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), len(v)), "egb_set_noise")
+            self.noise_len = len(v)
+
     def get_policy(self) -> np.ndarray:
         m = np.empty(POLICY_ENTRIES, dtype=np.int8)
         self.lib.egb_get_policy(self.h, m.ctypes.data_as(ctypes.POINTER(ctypes.c_int8)), POLICY_ENTRIES)
@@ -212,6 +227,7 @@ class Task:
     z: Sequence = ()
     labels: Optional[np.ndarray] = None   # int32 class index per sample (SEMI/CSEMI)
     nclass: int = 0
+    index: Optional[np.ndarray] = None    # int32 sample positions in the columns (shareable)
     n: int = 0
     keep: List = field(default_factory=list)
 
@@ -239,14 +255,25 @@ def _col_struct(col, device: bool):
 
 
 def run_tasks(tasks: List[Task], flags: int = 0, device: int = 0,
-              results_out: Optional[list] = None) -> np.ndarray:
-    """Evaluate the tasks in one batched call; returns the estimates."""
+              results_out: Optional[list] = None, noise=None) -> np.ndarray:
+    """Evaluate the tasks in one batched call; returns the estimates.
+
+    With RESCALE, `noise(m)` returns the first m values (at least) of the
+    preprocessing noise stream; the device copy is extended when a batch needs
+    more values than it holds."""
     if not tasks:
         return np.empty(0)
     ctx = context(device)
+    if flags & RESCALE:
+        need = max((t.n or len(t.x[0])) * (len(t.x) + len(t.y) + len(t.z)) for t in tasks)
+        if ctx.noise_len < need:
+            if noise is None:
+                raise ValueError("RESCALE needs the noise stream")
+            ctx.set_noise(noise(max(need, 2 * ctx.noise_len)))
     is_dev = bool(flags & INPUT_DEVICE)
     ctasks = (EgbTask * len(tasks))()
     keep = []
+    index_ptr = {}   # one int32 copy per index array shared by tasks
     for i, t in enumerate(tasks):
         cols = list(t.x) + list(t.y) + list(t.z)
         arr = (EgbColumn * len(cols))()
@@ -264,6 +291,13 @@ def run_tasks(tasks: List[Task], flags: int = 0, device: int = 0,
             keep.append(lab)
             ct.labels = lab.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
             ct.nclass = int(t.nclass)
+        if t.index is not None:
+            ptr = index_ptr.get(id(t.index))
+            if ptr is None:
+                ix = np.ascontiguousarray(t.index, dtype=np.int32)
+                keep.append(ix)
+                ptr = index_ptr[id(t.index)] = ix.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+            ct.index = ptr
     res = (EgbResult * len(tasks))()
     with ctx.lock:
         rc = ctx.lib.egb_run_batch(ctx.h, ctasks, len(tasks), flags, res)
@@ -274,9 +308,10 @@ def run_tasks(tasks: List[Task], flags: int = 0, device: int = 0,
 
 
 def fetch(task_index: int, which: int, n: int, device: int = 0) -> np.ndarray:
-    """eps (which=0) or count slot which-1 of the last batch run with KEEP_INTERNALS."""
+    """eps (which=0), count slot which-1, or working column which-16 of the
+    last batch run with KEEP_INTERNALS."""
     ctx = context(device)
-    out = np.empty(n, dtype=np.float64 if which == 0 else np.int64)
+    out = np.empty(n, dtype=np.float64 if which == 0 or which >= 16 else np.int64)
     with ctx.lock:
         ctx.check(ctx.lib.egb_fetch(ctx.h, task_index, which, out.ctypes.data), "egb_fetch")
     return out

@@ -84,7 +84,11 @@ struct TaskPlan {
   int kind = 0, k = 0, K = 0;
   int64_t n = 0, ld = 0;
   int dx = 0, dy = 0, dz = 0, ncol = 0, nclass = 0, nslot = 0;
-  std::vector<int32_t> perm;      // working -> caller index; empty = identity
+  std::vector<int32_t> perm;      // working -> sample index; empty = identity
+  std::vector<int32_t> gperm;     // working -> caller position (perm through index), if both
+  const int32_t* index = nullptr; // caller's shared sample index (no labels)
+  int64_t src_len = 0;            // samples the caller's columns must hold
+  size_t tab_index = 0;           // offset of the shared index in the table blob
   std::vector<int64_t> cls_off;   // class segment starts (nclass + 1)
   size_t off_x64 = 0, off_eps = 0, off_rad = 0, off_cnt[3] = {0, 0, 0};
   size_t tab_perm = 0;            // offset of perm inside the table blob
@@ -138,6 +142,8 @@ struct egb_ctx {
   size_t pinned_cap = 0;
   double* psi_d = nullptr;
   int64_t psi_len = 0;
+  double* noise_d = nullptr;      // preprocessing noise stream (egb_set_noise)
+  int64_t noise_len = 0;
   cudaEvent_t ev[NPHASE + 1] = {};
   cudaEvent_t kev[2 * NKTIME] = {};
   double timings[NPHASE + NKTIME] = {};
@@ -271,7 +277,13 @@ int finish_batch(egb_ctx* ctx, const ReplayState& R, const char* H, int64_t laun
     const CombineJob& c = R.cjobs[(size_t)ci++];
     double S = 0.0;
     for (int i = 0; i < c.nchunk; ++i) S += partial[c.chunk0 + i];
-    const uint32_t z = zf[t];
+    const uint32_t z = zf[t] & ~RESCALE_CONSTANT;
+    if (zf[t] & RESCALE_CONSTANT) {  // the caller preprocesses this task itself
+      r.value = NAN;
+      r.status = EGB_TASK_CONSTANT;
+      if (results) results[t] = r;
+      continue;
+    }
     const double N = (double)p.n;
     const double mean = S / N;
     double v = 0.0;
@@ -310,6 +322,82 @@ int finish_batch(egb_ctx* ctx, const ReplayState& R, const char* H, int64_t laun
   return EGB_OK;
 }
 
+// NumPy's pairwise summation of n doubles (pairwise_sum,
+// numpy/_core/src/umath/loops_utils.h.src, the order np.add.reduce, mean()
+// and std() of a contiguous 1-D array use): n <= 128 values are summed
+// directly with eight accumulators, larger n split at n2 = n / 2 rounded
+// down to a multiple of 8.  Stored leaves first (offset, length), then the
+// inner nodes (left, right child) by height, so that the nodes of one height
+// depend only on lower ones; returns the tree's index.
+int32_t pw_build(int64_t n, std::vector<PwTree>& trees, std::vector<int2>& nodes,
+                 std::vector<int32_t>& levels) {
+  struct Ref { bool leaf; int32_t i; };
+  struct Inner { Ref l, r; int h; };
+  std::vector<int2> leaves;
+  std::vector<Inner> inner;
+  std::vector<int> hts;
+  // explicit recursion (depth about log2(n / 64))
+  struct Frame { int64_t off, m; int stage; Ref l; int hl; };
+  std::vector<Frame> stack{{0, n, 0, {true, 0}, 0}};
+  Ref ret{true, 0};
+  int ret_h = 0;
+  while (!stack.empty()) {
+    Frame& f = stack.back();
+    if (f.m <= 128) {
+      leaves.push_back(make_int2((int)f.off, (int)f.m));
+      ret = {true, (int32_t)leaves.size() - 1};
+      ret_h = 0;
+      stack.pop_back();
+      continue;
+    }
+    int64_t m2 = f.m / 2;
+    m2 -= m2 % 8;
+    if (f.stage == 0) {
+      f.stage = 1;
+      stack.push_back({f.off, m2, 0, {true, 0}, 0});
+    } else if (f.stage == 1) {
+      f.stage = 2;
+      f.l = ret;
+      f.hl = ret_h;
+      const int64_t off = f.off + m2, m = f.m - m2;
+      stack.push_back({off, m, 0, {true, 0}, 0});
+    } else {
+      const int h = 1 + std::max(f.hl, ret_h);
+      inner.push_back({f.l, ret, h});
+      ret = {false, (int32_t)inner.size() - 1};
+      ret_h = h;
+      stack.pop_back();
+    }
+  }
+  std::vector<int32_t> order(inner.size());
+  for (size_t i = 0; i < order.size(); ++i) order[i] = (int32_t)i;
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int32_t a, int32_t b) { return inner[(size_t)a].h < inner[(size_t)b].h; });
+  const int32_t L = (int32_t)leaves.size();
+  std::vector<int32_t> pos(inner.size());
+  for (size_t k = 0; k < order.size(); ++k) pos[(size_t)order[k]] = L + (int32_t)k;
+  auto idx = [&](Ref r) { return r.leaf ? r.i : pos[(size_t)r.i]; };
+  PwTree T{};
+  T.node0 = (int32_t)nodes.size();
+  T.nleaf = L;
+  T.nnode = L + (int32_t)inner.size();
+  T.lvl0 = (int32_t)levels.size();
+  nodes.insert(nodes.end(), leaves.begin(), leaves.end());
+  int H = 0;
+  for (size_t k = 0; k < order.size(); ++k) {
+    const Inner& in = inner[(size_t)order[k]];
+    nodes.push_back(make_int2(idx(in.l), idx(in.r)));
+    if (in.h > H) {  // first node of height in.h
+      levels.push_back(L + (int32_t)k);
+      H = in.h;
+    }
+  }
+  T.nlvl = H;
+  levels.push_back(T.nnode);
+  trees.push_back(T);
+  return (int32_t)trees.size() - 1;
+}
+
 // Key of a batch for replay: everything the plan depends on when the inputs
 // are device-resident and carry no host labels -- task shapes, column
 // pointers and strides, flags, stream.  0 = not replayable.
@@ -327,7 +415,7 @@ uint64_t replay_key(const egb_ctx* ctx, const egb_task* tasks, int ntasks, int f
   mix((uint64_t)(uintptr_t)ctx->stream);
   for (int t = 0; t < ntasks; ++t) {
     const egb_task& T = tasks[t];
-    if (T.labels || T.kind < EGB_MI || T.kind > EGB_ENTROPY || !T.cols) return 0;
+    if (T.labels || T.index || T.kind < EGB_MI || T.kind > EGB_ENTROPY || !T.cols) return 0;
     mix((uint64_t)(uint32_t)T.kind | ((uint64_t)(uint32_t)T.k << 32));
     mix((uint64_t)T.n);
     mix((uint64_t)(uint32_t)T.dx | ((uint64_t)(uint32_t)T.dy << 16) | ((uint64_t)(uint32_t)T.dz << 32));
@@ -375,6 +463,9 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   std::vector<TaskPlan> P((size_t)ntasks);
   int64_t max_n = 1, max_ld = 32;
   int ncols_total = 0;
+  const bool rescale = (flags & EGB_RESCALE) != 0;
+  // shared sample indices, checked once per (array, n): largest entry
+  std::map<std::pair<const int32_t*, int64_t>, int64_t> index_max;
   for (int t = 0; t < ntasks; ++t) {
     const egb_task& T = tasks[t];
     TaskPlan& p = P[(size_t)t];
@@ -401,6 +492,30 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
     for (int c = 0; c < p.ncol; ++c)
       if (!T.cols[c].data || T.cols[c].stride < 1)
         return fail(ctx, EGB_ERR_ARG, who + "invalid column " + std::to_string(c));
+    p.src_len = T.n;
+    if (T.index) {
+      if (internal) return fail(ctx, EGB_ERR_ARG, who + "index not supported for this kind");
+      auto it = index_max.find({T.index, T.n});
+      if (it == index_max.end()) {
+        int64_t mx = -1;
+        for (int64_t i = 0; i < T.n; ++i) {
+          if (T.index[i] < 0) return fail(ctx, EGB_ERR_ARG, who + "negative sample index");
+          mx = std::max<int64_t>(mx, T.index[i]);
+        }
+        it = index_max.emplace(std::make_pair(T.index, T.n), mx).first;
+      }
+      p.src_len = it->second + 1;
+      p.index = T.index;
+    }
+    if (rescale && T.kind != EGB_ENTROPY) {
+      if (internal) return fail(ctx, EGB_ERR_ARG, who + "EGB_RESCALE applies to estimator tasks only");
+      if (T.dx != 1 || T.dy > 1 || T.dz > 1)
+        return fail(ctx, EGB_ERR_ARG, who + "EGB_RESCALE needs one column per variable");
+      const int64_t draws = T.n * (int64_t)(T.dx + T.dy + T.dz);
+      if (!ctx->noise_d || draws > ctx->noise_len)
+        return fail(ctx, EGB_ERR_ARG, who + "EGB_RESCALE needs " + std::to_string(draws) +
+                                          " noise values (egb_set_noise)");
+    }
     p.K = T.k + 1;
     p.ld = round32(T.n);
     p.center0 = ncols_total;
@@ -423,6 +538,11 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
       std::vector<int64_t> pos(p.cls_off.begin(), p.cls_off.end() - 1);
       p.perm.resize((size_t)T.n);
       for (int64_t i = 0; i < T.n; ++i) p.perm[(size_t)pos[(size_t)T.labels[i]]++] = (int32_t)i;
+      if (p.index) {  // class order, then the caller's sample index
+        p.gperm.resize(p.perm.size());
+        for (size_t w = 0; w < p.perm.size(); ++w) p.gperm[w] = p.index[p.perm[w]];
+        p.index = nullptr;
+      }
     } else {
       p.nclass = 1;
       p.cls_off = {0, T.n};
@@ -590,7 +710,8 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
       for (int c = 0; c < P[(size_t)t].ncol; ++c) {
         const egb_column& col = tasks[t].cols[c];
         const uintptr_t lo = (uintptr_t)col.data;
-        const uintptr_t hi = lo + (uintptr_t)(((tasks[t].n - 1) * col.stride + 1) * sizeof(double));
+        const uintptr_t hi =
+            lo + (uintptr_t)(((P[(size_t)t].src_len - 1) * col.stride + 1) * sizeof(double));
         rs.push_back({lo, hi, !direct_ok || col.stride != 1 || !P[(size_t)t].perm.empty()});
       }
     std::sort(rs.begin(), rs.end(), [](const Span& a, const Span& b) {
@@ -626,7 +747,8 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
     p.off_eps = dl.take(sizeof(double) * (size_t)p.ld);
     p.off_rad = dl.take(sizeof(double) * (size_t)p.ld);
     for (int s = 0; s < p.nslot; ++s) p.off_cnt[s] = dl.take(sizeof(int32_t) * (size_t)p.ld);
-    if (!p.perm.empty()) p.tab_perm = tl.take(sizeof(int32_t) * p.perm.size());
+    const std::vector<int32_t>& gp = p.gperm.empty() ? p.perm : p.gperm;
+    if (!gp.empty()) p.tab_perm = tl.take(sizeof(int32_t) * gp.size());
     if (p.kind == KIND_COUNT_ONLY && !dev_in) p.tab_rad = tl.take(sizeof(double) * (size_t)p.n);
   }
   const size_t off_centers = dl.take(sizeof(double) * (size_t)ncols_total);
@@ -866,6 +988,46 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   }
   const int nchunks = (int)chunk_job.size();
 
+  // device rescale (EGB_RESCALE): one summation tree per distinct n, every
+  // column of MI / CMI / SEMI / CSEMI tasks; noise positions follow the
+  // reference's draws (x from 0, then y, then z, n values each)
+  std::vector<PwTree> pw_trees;
+  std::vector<int2> pw_nodes;
+  std::vector<int32_t> pw_levels;
+  std::vector<RescaleCol> rcols;
+  std::vector<int32_t> rinv;              // inverse class orders, concatenated
+  std::vector<size_t> rinv_task;          // per task: offset in rinv, or SIZE_MAX
+  size_t off_pw_scratch = 0;
+  if (rescale) {
+    std::map<int64_t, int32_t> tree_of;
+    size_t scratch_elems = 0;
+    for (int t = 0; t < ntasks; ++t) {
+      const TaskPlan& p = P[(size_t)t];
+      if (p.kind != EGB_MI && p.kind != EGB_CMI && p.kind != EGB_SEMI && p.kind != EGB_CSEMI) continue;
+      auto it = tree_of.find(p.n);
+      if (it == tree_of.end()) it = tree_of.emplace(p.n, pw_build(p.n, pw_trees, pw_nodes, pw_levels)).first;
+      // class-ordered tasks sum in sample order through the inverse order
+      if (rinv_task.empty()) rinv_task.assign((size_t)ntasks, SIZE_MAX);
+      if (!p.perm.empty()) {
+        rinv_task[(size_t)t] = rinv.size();
+        rinv.resize(rinv.size() + p.perm.size());
+        int32_t* inv = rinv.data() + rinv_task[(size_t)t];
+        for (size_t w = 0; w < p.perm.size(); ++w) inv[p.perm[w]] = (int32_t)w;
+      }
+      for (int c = 0; c < p.ncol; ++c) {
+        RescaleCol rc{};
+        rc.task = t;
+        rc.col = c;
+        rc.tree = it->second;
+        rc.noise_pos = (int64_t)c * p.n;
+        rc.scratch = (int64_t)scratch_elems;
+        scratch_elems += (size_t)pw_trees[(size_t)it->second].nnode;
+        rcols.push_back(rc);
+      }
+    }
+    off_pw_scratch = dl.take(sizeof(double) * std::max<size_t>(scratch_elems, 1));
+  }
+
   // tables (pinned blob -> device)
   std::vector<GatherCol> gcols;
   std::vector<int32_t> col_task, col_idx;
@@ -881,6 +1043,20 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   const size_t tab_gsegs = tl.take(sizeof(SortSeg) * std::max<size_t>(gsegs.size(), 1));
   const size_t tab_blkgseg = tl.take(sizeof(int32_t) * (size_t)std::max(nblk_grid, 1));
   const size_t tab_gridjobs = tl.take(sizeof(int32_t) * std::max<size_t>(grid_jobs.size(), 1));
+  const size_t tab_pwtrees = tl.take(sizeof(PwTree) * std::max<size_t>(pw_trees.size(), 1));
+  const size_t tab_pwnodes = tl.take(sizeof(int2) * std::max<size_t>(pw_nodes.size(), 1));
+  const size_t tab_pwlevels = tl.take(sizeof(int32_t) * std::max<size_t>(pw_levels.size(), 1));
+  const size_t tab_rcols = tl.take(sizeof(RescaleCol) * std::max<size_t>(rcols.size(), 1));
+  const size_t tab_rinv = tl.take(sizeof(int32_t) * std::max<size_t>(rinv.size(), 1));
+  // shared sample indices: one copy per (array, n)
+  std::map<std::pair<const int32_t*, int64_t>, size_t> index_tab;
+  for (TaskPlan& p : P) {
+    if (!p.index) continue;
+    auto it = index_tab.find({p.index, p.n});
+    if (it == index_tab.end())
+      it = index_tab.emplace(std::make_pair(p.index, p.n), tl.take(sizeof(int32_t) * (size_t)p.n)).first;
+    p.tab_index = it->second;
+  }
   std::vector<size_t> tab_sstart(jobs.size(), 0);
   std::vector<size_t> tab_cstart(jobs.size(), 0);
   for (int32_t gj : grid_jobs) {
@@ -938,8 +1114,10 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
     D.n = (int32_t)p.n;
     D.ncol = p.ncol;
     D.rad_given = p.kind == KIND_COUNT_ONLY ? 1 : 0;
-    const int32_t* perm_dev = p.perm.empty() ? nullptr : (const int32_t*)(A + off_tab + p.tab_perm);
-    if (!p.perm.empty()) std::memcpy(H + p.tab_perm, p.perm.data(), sizeof(int32_t) * p.perm.size());
+    const std::vector<int32_t>& gp = p.gperm.empty() ? p.perm : p.gperm;
+    const int32_t* perm_dev = p.index ? (const int32_t*)(A + off_tab + p.tab_index)
+                              : gp.empty() ? nullptr : (const int32_t*)(A + off_tab + p.tab_perm);
+    if (!gp.empty()) std::memcpy(H + p.tab_perm, gp.data(), sizeof(int32_t) * gp.size());
     if (p.kind == KIND_COUNT_ONLY && !dev_in)
       std::memcpy(H + p.tab_rad, count_radius, sizeof(double) * (size_t)p.n);
     for (int c = 0; c < p.ncol; ++c) {
@@ -956,6 +1134,19 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   }
   std::memcpy(H + tab_tasks, tdev.data(), sizeof(TaskDev) * tdev.size());
   std::memcpy(H + tab_gcols, gcols.data(), sizeof(GatherCol) * gcols.size());
+  for (const auto& e : index_tab)
+    std::memcpy(H + e.second, e.first.first, sizeof(int32_t) * (size_t)e.first.second);
+  if (!rcols.empty()) {
+    std::memcpy(H + tab_pwtrees, pw_trees.data(), sizeof(PwTree) * pw_trees.size());
+    std::memcpy(H + tab_pwnodes, pw_nodes.data(), sizeof(int2) * pw_nodes.size());
+    std::memcpy(H + tab_pwlevels, pw_levels.data(), sizeof(int32_t) * pw_levels.size());
+    for (RescaleCol& rc : rcols) {
+      const size_t o = rinv_task[(size_t)rc.task];
+      rc.inv = o == SIZE_MAX ? nullptr : (const int32_t*)(A + off_tab + tab_rinv) + o;
+    }
+    std::memcpy(H + tab_rcols, rcols.data(), sizeof(RescaleCol) * rcols.size());
+    if (!rinv.empty()) std::memcpy(H + tab_rinv, rinv.data(), sizeof(int32_t) * rinv.size());
+  }
   std::memcpy(H + tab_coltask, col_task.data(), sizeof(int32_t) * col_task.size());
   std::memcpy(H + tab_colidx, col_idx.data(), sizeof(int32_t) * col_idx.size());
   if (!segs.empty()) std::memcpy(H + tab_segs, segs.data(), sizeof(SortSeg) * segs.size());
@@ -1071,6 +1262,11 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
                         (int)G.runs.size(), (const int32_t*)dtab(G.tab_cum), G.nitems,
                         (WorkItem*)(A + G.off_items), st);
   launch_gather(tasks_d, (const GatherCol*)dtab(tab_gcols), ncols_total, max_ld, st);
+  if (!rcols.empty())
+    launch_rescale(tasks_d, (const RescaleCol*)dtab(tab_rcols), (int)rcols.size(),
+                   (const PwTree*)dtab(tab_pwtrees), (const int2*)dtab(tab_pwnodes),
+                   (const int32_t*)dtab(tab_pwlevels), (double*)(A + off_pw_scratch), ctx->noise_d,
+                   zero_d, st);
   launch_prepare(tasks_d, (const int32_t*)dtab(tab_coltask), (const int32_t*)dtab(tab_colidx),
                  ncols_total, (unsigned long long*)(A + off_minmax), (double*)(A + off_centers), st);
   if (timing) EGB_CUDA(cudaEventRecord(ctx->ev[2], st));
@@ -1208,9 +1404,9 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
       for (size_t i = 0; i < n; ++i) sig = (sig ^ b[i]) * 1099511628211ull;
     };
     mix(H, tab_bytes);
-    const uintptr_t extra[8] = {(uintptr_t)A, (uintptr_t)H, (uintptr_t)flags, (uintptr_t)zr_bytes,
+    const uintptr_t extra[9] = {(uintptr_t)A, (uintptr_t)H, (uintptr_t)flags, (uintptr_t)zr_bytes,
                                 (uintptr_t)nchunks, (uintptr_t)(void*)st, (uintptr_t)ctx->psi_d,
-                                (uintptr_t)ctx->psi_len};
+                                (uintptr_t)ctx->psi_len, (uintptr_t)ctx->noise_d};
     mix(extra, sizeof(extra));
     if (!(ctx->graph_exec && ctx->graph_sig == sig)) {
       if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
@@ -1320,6 +1516,7 @@ void egb_destroy(egb_ctx* ctx) {
   if (ctx->arena) cudaFree(ctx->arena);
   if (ctx->pinned) cudaFreeHost(ctx->pinned);
   if (ctx->psi_d) cudaFree(ctx->psi_d);
+  if (ctx->noise_d) cudaFree(ctx->noise_d);
   for (auto& e : ctx->ev)
     if (e) cudaEventDestroy(e);
   for (auto& e : ctx->kev)
@@ -1351,17 +1548,20 @@ int egb_fetch(egb_ctx* ctx, int32_t task, int32_t which, void* host_out) {
   if (!ctx->kept) return fail(ctx, EGB_ERR_STATE, "no batch internals kept (run with EGB_KEEP_INTERNALS)");
   if (task < 0 || task >= (int)ctx->keep.size()) return fail(ctx, EGB_ERR_ARG, "task index out of range");
   const TaskPlan& p = ctx->keep[(size_t)task];
-  if (which < 0 || which > p.nslot) return fail(ctx, EGB_ERR_ARG, "no such internal array");
+  const bool column = which >= 16 && which < 16 + p.ncol;
+  if (!column && (which < 0 || which > p.nslot)) return fail(ctx, EGB_ERR_ARG, "no such internal array");
   cudaSetDevice(ctx->device);
   const size_t n = (size_t)p.n;
   std::vector<char> buf(n * 8);
-  const char* src = (const char*)ctx->arena + (which == 0 ? p.off_eps : p.off_cnt[which - 1]);
-  const size_t esz = which == 0 ? 8 : 4;
+  const char* src = (const char*)ctx->arena +
+                    (column ? p.off_x64 + sizeof(double) * (size_t)((which - 16) * p.ld)
+                            : which == 0 ? p.off_eps : p.off_cnt[which - 1]);
+  const size_t esz = (which == 0 || column) ? 8 : 4;
   EGB_CUDA(cudaMemcpyAsync(buf.data(), src, n * esz, cudaMemcpyDeviceToHost, ctx->stream));
   EGB_CUDA(cudaStreamSynchronize(ctx->stream));
   for (size_t w = 0; w < n; ++w) {
     const size_t i = p.perm.empty() ? w : (size_t)p.perm[w];
-    if (which == 0) ((double*)host_out)[i] = ((const double*)buf.data())[w];
+    if (esz == 8) ((double*)host_out)[i] = ((const double*)buf.data())[w];
     else ((int64_t*)host_out)[i] = ((const int32_t*)buf.data())[w];
   }
   return EGB_OK;
@@ -1431,6 +1631,29 @@ int egb_set_policy(egb_ctx* ctx, const int8_t* modes, int32_t n) {
       return fail(ctx, EGB_ERR_ARG, "egb_set_policy: invalid mode at entry " + std::to_string(i));
   std::memcpy(ctx->policy, modes, sizeof(ctx->policy));
   ctx->replay.valid = false;  // the plan of a replayed batch may change
+  return EGB_OK;
+}
+
+int egb_set_noise(egb_ctx* ctx, const double* noise, int64_t len) {
+  if (!ctx) return EGB_ERR_ARG;
+  if (len < 0 || (len > 0 && !noise)) return fail(ctx, EGB_ERR_ARG, "invalid noise stream");
+  cudaSetDevice(ctx->device);
+  EGB_CUDA(cudaStreamSynchronize(ctx->stream));
+  // captured graphs hold the stream's address: capture again
+  ctx->graph_sig = 0;
+  ctx->replay.valid = false;
+  if (len > ctx->noise_len || !ctx->noise_d) {
+    if (ctx->noise_d) cudaFree(ctx->noise_d);
+    ctx->noise_d = nullptr;
+    ctx->noise_len = 0;
+    if (cudaMalloc(&ctx->noise_d, sizeof(double) * (size_t)std::max<int64_t>(len, 1)) != cudaSuccess) {
+      cudaGetLastError();
+      ctx->noise_d = nullptr;
+      return fail(ctx, EGB_ERR_NOMEM, "noise stream allocation failed");
+    }
+  }
+  if (len > 0) EGB_CUDA(cudaMemcpy(ctx->noise_d, noise, sizeof(double) * (size_t)len, cudaMemcpyHostToDevice));
+  ctx->noise_len = len;
   return EGB_OK;
 }
 

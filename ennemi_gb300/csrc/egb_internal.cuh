@@ -361,6 +361,28 @@ struct GatherCol {        // working column <- caller column (strided, permuted)
   int32_t col;
 };
 
+// Device rescale (EGB_RESCALE).  A column's sum in NumPy's pairwise order
+// is a tree: leaves of at most 128 samples summed with eight accumulators,
+// inner nodes the sum of their two children.  Nodes of one tree are stored
+// leaves first ((offset, length) in .x/.y), then inner nodes by height
+// ((left, right) child), heights 1 .. nlvl starting at levels[lvl0 + h - 1]
+// (local node indices; levels[lvl0 + nlvl] = nnode).  The root is the last.
+struct PwTree {
+  int32_t node0, nleaf, nnode, lvl0, nlvl;
+};
+struct RescaleCol {       // one column to rescale in place
+  int32_t task, col, tree, pad_;
+  int64_t noise_pos;      // first noise value of the column
+  int64_t scratch;        // first node-sum slot (tree.nnode doubles)
+  const int32_t* inv;     // sample -> working position (class-ordered tasks), or null
+};
+// zero_flags bit of a task with a column whose standard deviation was below
+// 1e-20: left as given, the task is reported EGB_TASK_CONSTANT
+constexpr uint32_t RESCALE_CONSTANT = 1u << 31;
+void launch_rescale(const TaskDev* tasks_d, const RescaleCol* cols_d, int ncols,
+                    const PwTree* trees_d, const int2* nodes_d, const int32_t* levels_d,
+                    double* scratch, const double* noise, uint32_t* zero_flags, cudaStream_t st);
+
 struct CombineJob {       // per-task reduction of per-sample terms
   int32_t task;
   int32_t kind;           // egb_kind

@@ -55,6 +55,98 @@ __global__ void gather_kernel(const TaskDev* __restrict__ tasks,
   }
 }
 
+// ----------------------------------------------------------- rescale --
+// The reference's _rescale_data (_driver.py:871-902) per column, bit for bit:
+// mean = pairwise_sum(x) / n, std = sqrt(pairwise_sum((x - mean)^2) / n),
+// x = (x - mean) / std + noise -- every operation one IEEE double rounding
+// (explicit _rn intrinsics: no contraction), the sums in NumPy's order.
+
+// Sample i of the column: x[i], or x[inv[i]] for a class-ordered task.
+__device__ __forceinline__ double pw_value(const double* a, const int32_t* inv, int i, bool sq,
+                                           double m) {
+  const double v = inv ? a[inv[i]] : a[i];
+  if (!sq) return v;
+  const double d = __dsub_rn(v, m);
+  return __dmul_rn(d, d);
+}
+
+// One leaf of pairwise_sum: fewer than 8 values in order from 0.0; else eight
+// running sums over strides of 8, combined ((r0+r1)+(r2+r3))+((r4+r5)+(r6+r7)),
+// then the remaining (len % 8) values in order.
+// (a, inv: the column with the leaf's first sample at index 0)
+__device__ double pw_leaf(const double* a, const int32_t* inv, int len, bool sq, double m) {
+  if (len < 8) {
+    double r = 0.0;
+    for (int i = 0; i < len; ++i) r = __dadd_rn(r, pw_value(a, inv, i, sq, m));
+    return r;
+  }
+  double r0 = pw_value(a, inv, 0, sq, m), r1 = pw_value(a, inv, 1, sq, m), r2 = pw_value(a, inv, 2, sq, m),
+         r3 = pw_value(a, inv, 3, sq, m), r4 = pw_value(a, inv, 4, sq, m), r5 = pw_value(a, inv, 5, sq, m),
+         r6 = pw_value(a, inv, 6, sq, m), r7 = pw_value(a, inv, 7, sq, m);
+  const int end = len - (len % 8);
+  int i = 8;
+  for (; i < end; i += 8) {
+    r0 = __dadd_rn(r0, pw_value(a, inv, i + 0, sq, m));
+    r1 = __dadd_rn(r1, pw_value(a, inv, i + 1, sq, m));
+    r2 = __dadd_rn(r2, pw_value(a, inv, i + 2, sq, m));
+    r3 = __dadd_rn(r3, pw_value(a, inv, i + 3, sq, m));
+    r4 = __dadd_rn(r4, pw_value(a, inv, i + 4, sq, m));
+    r5 = __dadd_rn(r5, pw_value(a, inv, i + 5, sq, m));
+    r6 = __dadd_rn(r6, pw_value(a, inv, i + 6, sq, m));
+    r7 = __dadd_rn(r7, pw_value(a, inv, i + 7, sq, m));
+  }
+  double res = __dadd_rn(__dadd_rn(__dadd_rn(r0, r1), __dadd_rn(r2, r3)),
+                         __dadd_rn(__dadd_rn(r4, r5), __dadd_rn(r6, r7)));
+  for (; i < len; ++i) res = __dadd_rn(res, pw_value(a, inv, i, sq, m));
+  return res;
+}
+
+// The block's pairwise sum of x[0, n) (sq: of (x - m)^2): leaves in parallel,
+// then one height at a time; node sums in ns (global, read back through L2).
+__device__ double pw_sum(const double* x, const int32_t* inv, const PwTree& tr,
+                         const int2* __restrict__ nodes, const int32_t* __restrict__ levels,
+                         double* ns, bool sq, double m) {
+  for (int i = threadIdx.x; i < tr.nleaf; i += blockDim.x) {
+    const int2 L = nodes[tr.node0 + i];
+    ns[i] = inv ? pw_leaf(x, inv + L.x, L.y, sq, m) : pw_leaf(x + L.x, nullptr, L.y, sq, m);
+  }
+  __syncthreads();
+  for (int h = 0; h < tr.nlvl; ++h) {
+    const int a = levels[tr.lvl0 + h], b = levels[tr.lvl0 + h + 1];
+    for (int i = a + threadIdx.x; i < b; i += blockDim.x) {
+      const int2 c = nodes[tr.node0 + i];
+      ns[i] = __dadd_rn(__ldcg(ns + c.x), __ldcg(ns + c.y));
+    }
+    __syncthreads();
+  }
+  return __ldcg(ns + tr.nnode - 1);
+}
+
+__global__ void __launch_bounds__(PREP_THREADS)
+rescale_kernel(const TaskDev* __restrict__ tasks, const RescaleCol* __restrict__ cols,
+               const PwTree* __restrict__ trees, const int2* __restrict__ nodes,
+               const int32_t* __restrict__ levels, double* __restrict__ scratch,
+               const double* __restrict__ noise, uint32_t* __restrict__ zero_flags) {
+  const RescaleCol rc = cols[blockIdx.x];
+  const TaskDev t = tasks[rc.task];
+  double* x = const_cast<double*>(t.x64) + (int64_t)rc.col * t.ld;
+  const PwTree tr = trees[rc.tree];
+  double* ns = scratch + rc.scratch;
+  const double n = (double)t.n;
+  const double mean = __ddiv_rn(pw_sum(x, rc.inv, tr, nodes, levels, ns, false, 0.0), n);
+  __syncthreads();  // every thread has read the root before the slots are reused
+  const double sd = __dsqrt_rn(__ddiv_rn(pw_sum(x, rc.inv, tr, nodes, levels, ns, true, mean), n));
+  if (fabs(sd) < 1e-20) {  // np.abs(std) < 1e-20: the reference warns and keeps x
+    if (threadIdx.x == 0) atomicOr(zero_flags + rc.task, RESCALE_CONSTANT);
+    return;
+  }
+  const double* nz = noise + rc.noise_pos;
+  for (int i = threadIdx.x; i < t.n; i += blockDim.x) {  // sample i
+    const int w = rc.inv ? rc.inv[i] : i;
+    x[w] = __dadd_rn(__ddiv_rn(__dsub_rn(x[w], mean), sd), nz[i]);
+  }
+}
+
 __global__ void minmax_kernel(const TaskDev* __restrict__ tasks,
                               const int32_t* __restrict__ col_task,
                               const int32_t* __restrict__ col_idx, int ncols,
@@ -299,6 +391,15 @@ void launch_gather(const TaskDev* tasks_d, const GatherCol* cols_d, int ncols, i
   if (ncols <= 0) return;
   dim3 grid(grid_x_for(max_ld), grid_y_for(ncols));
   gather_kernel<<<grid, PREP_THREADS, 0, st>>>(tasks_d, cols_d, ncols);
+  count_launch();
+}
+
+void launch_rescale(const TaskDev* tasks_d, const RescaleCol* cols_d, int ncols,
+                    const PwTree* trees_d, const int2* nodes_d, const int32_t* levels_d,
+                    double* scratch, const double* noise, uint32_t* zero_flags, cudaStream_t st) {
+  if (ncols <= 0) return;
+  rescale_kernel<<<ncols, PREP_THREADS, 0, st>>>(tasks_d, cols_d, trees_d, nodes_d, levels_d, scratch,
+                                                 noise, zero_flags);
   count_launch();
 }
 

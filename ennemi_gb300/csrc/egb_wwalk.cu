@@ -93,8 +93,12 @@ __device__ __forceinline__ int lower_bound_from(const float* __restrict__ x, int
   return lower_bound_f(x, lo, hi, v);
 }
 
+// Resident blocks per SM the register budget is cut for (measured: 2-D at
+// six, 3-D with K <= 4 at five; the others keep what they need)
+constexpr int walk_min_blocks(int D, int KMAX) { return D == 2 ? 6 : (D == 3 && KMAX == 4 ? 5 : 1); }
+
 template <int D, int KMAX, bool NEST>
-__global__ void __launch_bounds__(WW_WARPS * 32, (D == 2 ? 6 : 1))
+__global__ void __launch_bounds__(WW_WARPS * 32, walk_min_blocks(D, KMAX))
 wwalk_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items, int nitems,
              int* __restrict__ counter) {
   constexpr int DQ = D ? D : EGB_DMAX;

@@ -58,6 +58,12 @@ enum egb_status {
   EGB_ERR_DEVICE = -3,   /* a kernel reported an error (bounded wait gave up,
                             index guard tripped)                               */
   EGB_ERR_NOMEM = -4,    /* device or pinned host allocation failed           */
+  EGB_TASK_CONSTANT = 1, /* egb_result.status only: under EGB_RESCALE a column
+                            of the task had standard deviation below 1e-20,
+                            which the reference rescales differently (no
+                            rescale, no noise, a warning); value is NaN and
+                            the caller computes the task with its own
+                            preprocessing                                     */
   EGB_ERR_STATE = -5     /* call out of order (e.g. fetch before a batch)     */
 };
 
@@ -87,10 +93,19 @@ enum egb_flags {
                                   of the context exactly (shapes, column pointers
                                   and strides, flags, stream; the data may have
                                   changed) replays without being planned again  */
-  EGB_STAGE_HOST = 1 << 9      /* copy host columns into device memory before the
+  EGB_STAGE_HOST = 1 << 9,     /* copy host columns into device memory before the
                                   gather even where the device reads pageable
                                   host memory directly (by default contiguous
                                   host columns are then read in place)           */
+  EGB_RESCALE = 1 << 10        /* preprocess on the device as the reference's
+                                  _rescale_data (_driver.py:871-902) does: every
+                                  column of MI, CMI, SEMI and CSEMI tasks becomes
+                                  (x - mean) / std + noise, mean and std by
+                                  NumPy's pairwise summation (bit-identical), the
+                                  noise from the stream set by egb_set_noise at
+                                  the reference's positions (x from 0, then y,
+                                  then z).  Requires one column per variable;
+                                  ENTROPY tasks are left as given             */
 };
 
 /* One float64 column: sample i at data[i * stride] (stride in elements). */
@@ -118,6 +133,10 @@ typedef struct egb_task {
   int32_t nclass;
   const egb_column* cols;  /* dx + dy + dz entries */
   const int32_t* labels;   /* SEMI / CSEMI: n entries, host memory */
+  const int32_t* index;    /* optional (host memory): sample w of every column
+                              is data[index[w] * stride] -- the reference's mask
+                              subset (_driver.py:834-842) without a copy; NULL =
+                              samples 0 .. n-1.  Tasks may share one array.   */
 } egb_task;
 
 /*
@@ -156,7 +175,9 @@ int egb_run_batch(egb_ctx* ctx, const egb_task* tasks, int32_t ntasks, int32_t f
 /*
  * Internals of the last batch run with EGB_KEEP_INTERNALS, in the caller's
  * sample order: which = 0 -> eps (double[n]); which = 1 + s -> count slot s
- * (int64[n]).  Slots: MI nx, ny; CMI nxz, nyz, nz; SEMI n; CSEMI nxz, nyz, nz.
+ * (int64[n]); which = 16 + c -> the task's column c as the estimator used it
+ * (double[n]: after the index and EGB_RESCALE).  Slots: MI nx, ny; CMI nxz,
+ * nyz, nz; SEMI n; CSEMI nxz, nyz, nz.
  */
 int egb_fetch(egb_ctx* ctx, int32_t task, int32_t which, void* host_out);
 
@@ -239,6 +260,13 @@ int egb_set_policy(egb_ctx* ctx, const int8_t* modes, int32_t n);
 
 /* Copy the context's table to modes[0 .. n); returns the number written. */
 int egb_get_policy(const egb_ctx* ctx, int8_t* modes, int32_t n);
+
+/* The preprocessing noise stream of EGB_RESCALE batches: noise[p] is the p-th
+ * draw of the reference's np.random.default_rng(2_718281828).normal(0.0,
+ * 1e-10, ...) (_driver.py:874, :882).  Copied to the device (host memory,
+ * len values); kept until replaced.  A batch needs as many values as its
+ * largest task draws: n per rescaled column. */
+int egb_set_noise(egb_ctx* ctx, const double* noise, int64_t len);
 
 /*
  * egb_knn_eps_noalloc -- egb_knn_eps() for callers that may not allocate

@@ -53,14 +53,32 @@ def oracle_run_tasks(O, calls=None):
     oracle O (tests only).  Appends the batch size to `calls` if given."""
     from ennemi_gb300 import _native
 
-    def run(tasks, flags=0, device=0, results_out=None):
+    class Result:
+        def __init__(self, value, status):
+            self.value, self.status = value, status
+
+    def run(tasks, flags=0, device=0, results_out=None, noise=None):
         if calls is not None:
             calls.append(len(tasks))
         out = []
         for t in tasks:
-            x = np.column_stack(t.x)
-            y = np.column_stack(t.y) if len(t.y) else None
-            z = np.column_stack(t.z) if len(t.z) else None
+            n = t.n or len(t.x[0])
+            ix = np.arange(n) if t.index is None else np.asarray(t.index)
+            cols = [np.asarray(c)[ix] for c in list(t.x) + list(t.y) + list(t.z)]
+            if flags & _native.RESCALE and t.kind != _native.ENTROPY:
+                # the library's EGB_RESCALE, as the reference's _rescale_data
+                # computes it (x from noise position 0, then y, then z)
+                nz = noise(n * len(cols))
+                if any(np.abs(c.std()) < 1e-20 for c in cols):
+                    out.append(np.nan)
+                    if results_out is not None:
+                        results_out.append(Result(np.nan, _native.TASK_CONSTANT))
+                    continue
+                cols = [(c - c.mean()) / c.std() + nz[i * n:(i + 1) * n] for i, c in enumerate(cols)]
+            dx, dy = len(t.x), len(t.y)
+            x = np.column_stack(cols[:dx])
+            y = np.column_stack(cols[dx:dx + dy]) if dy else None
+            z = np.column_stack(cols[dx + dy:]) if len(t.z) else None
             with np.errstate(all="ignore"):
                 if t.kind == _native.MI:
                     v = O.ksg_mi(x, y, t.k)[0]
@@ -73,6 +91,8 @@ def oracle_run_tasks(O, calls=None):
                 else:
                     v = O.entropy(x, t.k)[0]
             out.append(v)
+            if results_out is not None:
+                results_out.append(Result(v, 0))
         return np.array(out)
 
     return run

@@ -50,12 +50,32 @@ def test_version_string(lib):
     assert b"sm_103a" in lib.egb_version()
 
 
-def test_struct_layouts_match_header():
-    # egb_column {ptr, i64}; egb_task {i32,i32,i64,4*i32,ptr,ptr}; egb_result {f64,f64,u32,i32}
-    assert ctypes.sizeof(_native.EgbColumn) == 16
-    assert ctypes.sizeof(_native.EgbTask) == 48
-    assert _native.EgbTask.cols.offset == 32
-    assert ctypes.sizeof(_native.EgbResult) == 24
+def test_struct_layouts_match_header(tmp_path):
+    """sizeof / offsetof of the header's structs, compiled with gcc, equal the
+    ctypes binding's."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    fields = {"egb_column": (_native.EgbColumn, ["data", "stride"]),
+              "egb_task": (_native.EgbTask, [f for f, _ in _native.EgbTask._fields_]),
+              "egb_result": (_native.EgbResult, [f for f, _ in _native.EgbResult._fields_])}
+    lines = []
+    for st, (_, names) in fields.items():
+        lines.append(f'printf("%zu\\n", sizeof({st}));')
+        lines += [f'printf("%zu\\n", offsetof({st}, {f}));' for f in names]
+    src = tmp_path / "lay.c"
+    src.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "ennemi_gb.h"\n'
+                   "int main(void) {\n" + "\n".join(lines) + "\nreturn 0; }\n")
+    exe = tmp_path / "lay"
+    subprocess.check_call([cc, "-std=c99", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)])
+    got = [int(v) for v in subprocess.check_output([str(exe)]).split()]
+    want = []
+    for st, (cls, names) in fields.items():
+        want.append(ctypes.sizeof(cls))
+        want += [getattr(cls, f).offset for f in names]
+    assert got == want
 
 
 def test_null_arguments_rejected_without_device(lib):

@@ -165,6 +165,7 @@ def _captured_inputs(monkeypatch, call, unshared):
 
     with monkeypatch.context() as m:
         m.setattr(_native, "run_tasks", run)
+        m.setattr(_driver, "device_prep", False)   # the host preparation itself
         if unshared:
             m.setattr(_driver, "_task_job",
                       lambda prep, xkey, x, ykey, y, lag, max_lag, min_lag, k, mask, cond,
@@ -206,3 +207,58 @@ def test_shared_preparation_is_bit_identical(monkeypatch, case):
         for ca, cb in zip(ta, tb):
             assert ca.dtype == cb.dtype and ca.shape == cb.shape
             assert np.array_equal(ca.view(np.uint8), cb.view(np.uint8))
+
+
+@pytest.mark.parametrize("case", ["lags_mask", "lags_nomask", "lags_cond1", "lags_cond2",
+                                  "pairwise", "pairwise_cond_mask", "constant", "nan_elsewhere"])
+def test_device_preprocessing_matches_host_preparation(oracle, monkeypatch, case):
+    """The EGB_RESCALE path (lagged views + shared sample index, rescaled in the
+    library) gives what the host preparation gives; the library is stood in for
+    by the oracle applying the reference's _rescale_data to the indexed columns."""
+    rng = np.random.default_rng(11)
+    n = 600
+    x = rng.normal(size=(n, 3))
+    y = x[:, 0] + rng.normal(size=n)
+    cond = rng.normal(size=(n, 2))
+    mask = rng.random(n) > 0.2
+    xn = x.copy()
+    xn[-3:, 1] = np.nan                     # after every lagged slice below (lags 5, 6)
+    calls = {
+        "lags_mask": lambda: eg.estimate_mi(y, x, lag=[0, 1, 5, -2], mask=mask),
+        "lags_nomask": lambda: eg.estimate_mi(y, x, lag=[0, 2, -3]),
+        "lags_cond1": lambda: eg.estimate_mi(y, x, lag=[0, 2], cond=cond[:, 0], cond_lag=[1, 3],
+                                             mask=mask),
+        "lags_cond2": lambda: eg.estimate_mi(y, x, lag=[0, 2], cond=cond, mask=mask),
+        "pairwise": lambda: eg.pairwise_mi(np.column_stack((x, y))),
+        "pairwise_cond_mask": lambda: eg.pairwise_mi(x, cond=cond[:, 1], mask=mask),
+        "constant": lambda: eg.pairwise_mi(np.column_stack((x[:, :2], np.ones(n)))),
+        "nan_elsewhere": lambda: eg.estimate_mi(y, xn, lag=[5, 6]),
+    }
+    flags_seen = []
+    run = oracle_run_tasks(oracle)
+
+    def recording(tasks, flags=0, **kw):
+        flags_seen.append(flags)
+        return run(tasks, flags=flags, **kw)
+
+    monkeypatch.setattr(_native, "run_tasks", recording)
+    with warnings.catch_warnings(record=True) as w_dev:
+        warnings.simplefilter("always")
+        dev = calls[case]()
+    used = any(f & _native.RESCALE for f in flags_seen)
+    monkeypatch.setattr(_driver, "device_prep", False)
+    with warnings.catch_warnings(record=True) as w_host:
+        warnings.simplefilter("always")
+        host = calls[case]()
+    assert np.array_equal(dev, host, equal_nan=True)
+    assert len(w_dev) == len(w_host)
+    # the device path is taken exactly where its conditions hold
+    assert used == (case not in ("lags_cond2", "nan_elsewhere"))
+
+
+def test_numpy_sums_in_pairwise_order():
+    """The run-time check that enables device preprocessing holds for this NumPy,
+    and the restatement agrees with np.add.reduce on a longer array."""
+    assert _driver._numpy_sums_pairwise()
+    a = np.random.default_rng(3).standard_normal(50_001)
+    assert _driver._pairwise_sum(a.tolist()) == float(np.add.reduce(a))

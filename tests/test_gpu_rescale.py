@@ -1,0 +1,107 @@
+"""Device preprocessing (EGB_RESCALE + sample index) on the GPU.
+
+The working columns the estimators use must equal the reference's
+_rescale_data output (_driver.py:871-902) bit for bit: NumPy's mean and std
+of the indexed column, then (x - mean) / std + noise at the reference's noise
+positions.  The public API must give the same estimates with device and host
+preparation.
+"""
+
+import numpy as np
+import pytest
+
+import ennemi_gb300 as eg
+from ennemi_gb300 import _driver
+from ennemi_gb300 import _native as N
+
+pytestmark = pytest.mark.gpu
+
+
+def _noise(m):
+    return _driver._noise.take(0, (m,))
+
+
+def _reference_rescale(col, pos, n):
+    return (col - col.mean()) / col.std() + _driver._noise.take(pos, (n,))
+
+
+@pytest.mark.parametrize("n", [9, 100, 128, 129, 136, 1000, 8193, 20011, 180000])
+@pytest.mark.parametrize("indexed", [False, True])
+def test_rescaled_columns_equal_numpy(n, indexed):
+    rng = np.random.default_rng(n)
+    rows = n + 57
+    raw = rng.normal(size=(rows, 3)) * [2.0, 0.5, 7.0] + [1.0, -3.0, 0.25]   # strided views
+    y = rng.standard_t(3, size=rows)
+    idx = np.sort(rng.choice(rows - 5, size=n, replace=False)).astype(np.int32) if indexed else None
+    xv, yv, zv = raw[5:, 0], y[5:], raw[5:, 2]
+    tasks = [N.Task(N.MI, 3, [xv], [yv], n=n, index=idx),
+             N.Task(N.CMI, 3, [xv], [yv], [zv], n=n, index=idx)]
+    res = []
+    N.run_tasks(tasks, flags=N.RESCALE | N.KEEP_INTERNALS, results_out=res, noise=_noise)
+    assert all(r.status == 0 for r in res)
+    sel = np.arange(n) if idx is None else idx
+    want = [_reference_rescale(c[sel], i * n, n) for i, c in enumerate((xv, yv, zv))]
+    for t, ncol in ((0, 2), (1, 3)):
+        for c in range(ncol):
+            got = N.fetch(t, 16 + c, n)
+            assert np.array_equal(got.view(np.uint64), want[c].view(np.uint64)), (t, c)
+
+
+def test_semidiscrete_columns_with_index():
+    """Labels and an index together: the class order is applied on top of the
+    index; the continuous column is rescaled from noise position 0."""
+    rng = np.random.default_rng(5)
+    rows, n = 30000, 25000
+    x = rng.normal(size=rows) * 4 + 2
+    z = rng.normal(size=rows)
+    idx = np.sort(rng.choice(rows, size=n, replace=False)).astype(np.int32)
+    lab = rng.integers(0, 5, size=n).astype(np.int32)
+    tasks = [N.Task(N.SEMI, 3, [x], labels=lab, nclass=5, n=n, index=idx),
+             N.Task(N.CSEMI, 3, [x], z=[z], labels=lab, nclass=5, n=n, index=idx)]
+    N.run_tasks(tasks, flags=N.RESCALE | N.KEEP_INTERNALS, noise=_noise)
+    assert np.array_equal(N.fetch(0, 16, n), _reference_rescale(x[idx], 0, n))
+    assert np.array_equal(N.fetch(1, 16, n), _reference_rescale(x[idx], 0, n))
+    assert np.array_equal(N.fetch(1, 17, n), _reference_rescale(z[idx], n, n))
+    # the same tasks prepared on the host
+    host = [N.Task(N.SEMI, 3, [_reference_rescale(x[idx], 0, n)], labels=lab, nclass=5),
+            N.Task(N.CSEMI, 3, [_reference_rescale(x[idx], 0, n)],
+                   z=[_reference_rescale(z[idx], n, n)], labels=lab, nclass=5)]
+    assert np.array_equal(N.run_tasks(tasks, flags=N.RESCALE, noise=_noise), N.run_tasks(host))
+
+
+def test_constant_column_reported():
+    rng = np.random.default_rng(2)
+    n = 5000
+    x = rng.normal(size=n)
+    tasks = [N.Task(N.MI, 3, [x], [np.full(n, 3.5)], n=n), N.Task(N.MI, 3, [x], [x[::-1].copy()], n=n)]
+    res = []
+    v = N.run_tasks(tasks, flags=N.RESCALE, results_out=res, noise=_noise)
+    assert res[0].status == N.TASK_CONSTANT and np.isnan(v[0])
+    assert res[1].status == 0 and np.isfinite(v[1])
+
+
+def test_rescale_needs_one_column_per_variable():
+    x = np.random.default_rng(1).normal(size=(500, 2))
+    with pytest.raises(RuntimeError, match="one column per variable"):
+        N.run_tasks([N.Task(N.MI, 3, [x[:, 0], x[:, 1]], [x[:, 0]])], flags=N.RESCALE, noise=_noise)
+
+
+@pytest.mark.parametrize("case", ["lags_mask", "lags_cond", "pairwise_mask", "constant"])
+def test_public_api_same_with_device_and_host_preparation(case, monkeypatch):
+    rng = np.random.default_rng(17)
+    n = 20000
+    x = rng.normal(size=(n, 4))
+    x[:, 1] += 0.6 * x[:, 0]
+    y = x[:, 0] + rng.normal(size=n)
+    z = rng.normal(size=n)
+    mask = rng.random(n) > 0.1
+    calls = {
+        "lags_mask": lambda: eg.estimate_mi(y, x, lag=[0, 1, 7], mask=mask),
+        "lags_cond": lambda: eg.estimate_mi(y, x[:, :2], lag=[0, 3], cond=z, cond_lag=2, mask=mask),
+        "pairwise_mask": lambda: eg.pairwise_mi(x, mask=mask),
+        "constant": lambda: eg.pairwise_mi(np.column_stack((x[:, :2], np.full(n, 2.0)))),
+    }
+    dev = calls[case]()
+    monkeypatch.setattr(_driver, "device_prep", False)
+    host = calls[case]()
+    assert np.array_equal(dev, host, equal_nan=True)
