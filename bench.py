@@ -393,9 +393,16 @@ def main():
         bf_ops = sum(float(args.n) ** 2 * (2 * (2 if kind == "mi" else 3) + 1) for kind, _ in work)
     else:
         bf_ops = sum(2 * float(args.n) ** 2 * 5 for kind, _ in work if kind == "cmi")
+    # DRAM bytes read + written per launch, from one `ncu --set full` capture
+    # of `bench.py --profile --n 1000000 --steps 1 --warmup 1` (the walk: the
+    # 2-D and the 3-D launch averaged); measured for this workload only
+    ncu_traffic = {"wwalk_kernel": ((114.40 + 16.89) + (40.60 + 0.08)) / 2 * 1e6,
+                   "wcount_kernel": (49.06 + 0.78) * 1e6}
+    traffic = ncu_traffic.get(kname) if args.n == 1_000_000 else None
     roofline = {"bound": "alu", "kernel": kname, "achieved": achieved / 1e9,
                 "peak": peak_ops / 1e9, "unit": "Gop/s", "frac": achieved / peak_ops,
-                "traffic": None, "ms": kms, "pairs": kpairs,
+                "traffic": traffic, "traffic_unit": "bytes per launch (ncu)", "ms": kms,
+                "pairs": kpairs,
                 "peak_source": (f"nominal FP32 lane rate: {sms} SMs x 128 lanes x {max_mhz:.0f} MHz "
                                 "(MEASURED_PEAKS.json holds only HBM and bf16 figures)"),
                 "ops_per_pair": "2d+1 (d differences, d max-of-abs, 1 compare)",
