@@ -345,7 +345,7 @@ def _estimate_mi(y: FloatArray, x: FloatArray, lag: FloatArray, k: int,
         specs = []
         for li, vi in indices:
             xv = x if x.ndim == 1 else x[:, vi]
-            zv = None if cond is None else cond[hi - cond_lag[li][0]:, 0]
+            zv = None if cond is None else [cond[hi - cond_lag[li][c]:, c] for c in range(cond.shape[1])]
             specs.append((xv[hi - lag[li]:], y[hi:], zv))
         values = _run_device_prep(specs, n, k, prep.idx, jobs, max_threads)
     else:
@@ -476,7 +476,8 @@ def _pairwise_mi(data: FloatArray, k: int, cond: Optional[FloatArray], preproces
     if pairs and _device_prep_ok((data,) + (() if cond is None else (cond,)), cond, preprocess,
                                  drop_nan, bool(np.any(discrete))):
         n = len(data) if prep.idx is None else len(prep.idx)
-        specs = [(data[:, i], data[:, j], None if cond is None else cond[:, 0]) for i, j in pairs]
+        zv = None if cond is None else [cond[:, c] for c in range(cond.shape[1])]
+        specs = [(data[:, i], data[:, j], zv) for i, j in pairs]
         values = _run_device_prep(specs, n, k, prep.idx, jobs, max_threads)
     else:
         batch = _Batch()
@@ -493,9 +494,10 @@ def _pairwise_mi(data: FloatArray, k: int, cond: Optional[FloatArray], preproces
 
 # ------------------------------------------------- device preprocessing --
 
-# Tasks whose variables are all continuous float64 arrays free of NaNs, with
-# at most one condition column, are sliced, masked and rescaled on the device
-# (EGB_RESCALE): the library sums in NumPy's pairwise order, and
+# Tasks whose variables are all continuous float64 arrays free of NaNs are
+# sliced, masked and rescaled on the device (EGB_RESCALE): the library sums a
+# variable in NumPy's pairwise order and a condition of two or more columns
+# row by row, as NumPy reduces axis 0 of such an array, and
 # _numpy_sums_pairwise() confirms once per process that this NumPy sums that
 # way, so the preprocessed columns equal the reference's bit for bit.  Any
 # other task, and a task with a constant column (which the reference leaves
@@ -531,9 +533,18 @@ def _pairwise_sum(a) -> float:
     return _pairwise_sum(a[:n2]) + _pairwise_sum(a[n2:])
 
 
+def _sequential_sum(a) -> float:
+    s = a[0]
+    for v in a[1:]:
+        s += v
+    return s
+
+
 def _numpy_sums_pairwise() -> bool:
-    """True when this NumPy's sum, mean and std of 1-D float64 arrays follow
-    _pairwise_sum (sizes around every branch and beyond one 8192-value block)."""
+    """True when this NumPy's sum, mean and std of 1-D float64 arrays (and of
+    (n, 1) arrays along axis 0) follow _pairwise_sum, and those of (n, 2) and
+    (n, 3) arrays along axis 0 add the rows in order (sizes around every
+    branch and beyond one 8192-value block)."""
     global _pairwise_checked
     if _pairwise_checked is None:
         rng = np.random.default_rng(12345)
@@ -546,14 +557,23 @@ def _numpy_sums_pairwise() -> bool:
             d = [(v - m) * (v - m) for v in vals]
             sd = float(np.sqrt(_pairwise_sum(d) / n))
             ok = ok and float(np.add.reduce(a)) == s and float(a.mean()) == m and float(a.std()) == sd
+            col = a.reshape(n, 1)
+            ok = ok and float(col.mean(axis=0)[0]) == m and float(col.std(axis=0)[0]) == sd
+        for n in (3, 129, 8193, 20011):
+            for dz in (2, 3):
+                z = rng.standard_normal((n, dz)) * 2.0 - 0.5
+                means, sds = z.mean(axis=0), z.std(axis=0)
+                for c in range(dz):
+                    vals = z[:, c].tolist()
+                    m = _sequential_sum(vals) / n
+                    sd = float(np.sqrt(_sequential_sum([(v - m) * (v - m) for v in vals]) / n))
+                    ok = ok and float(means[c]) == m and float(sds[c]) == sd
         _pairwise_checked = ok
     return _pairwise_checked
 
 
 def _device_prep_ok(arrays, cond, preprocess: bool, drop_nan: bool, any_discrete: bool) -> bool:
     if not (device_prep and preprocess) or drop_nan or any_discrete:
-        return False
-    if cond is not None and cond.shape[1] != 1:
         return False
     for a in arrays:
         if a.dtype != np.float64 or np.isnan(a).any():
@@ -562,10 +582,10 @@ def _device_prep_ok(arrays, cond, preprocess: bool, drop_nan: bool, any_discrete
 
 
 def _run_device_prep(specs, n: int, k: int, idx, jobs, max_threads) -> np.ndarray:
-    """Estimates of the tasks (x, y, z or None): the columns are lagged views
-    of the caller's arrays, sample w at view[idx[w]] (idx None: the first n),
-    rescaled on the device.  Tasks with a constant column are prepared on the
-    host (`jobs`, same order) and run in a second batch."""
+    """Estimates of the tasks (x, y, condition columns or None): the columns
+    are lagged views of the caller's arrays, sample w at view[idx[w]] (idx
+    None: the first n), rescaled on the device.  Tasks with a constant column
+    are prepared on the host (`jobs`, same order) and run in a second batch."""
     if n <= k:
         raise ValueError(K_TOO_LARGE_MSG)
     index = None if idx is None else np.ascontiguousarray(idx, dtype=np.int32)
@@ -574,7 +594,7 @@ def _run_device_prep(specs, n: int, k: int, idx, jobs, max_threads) -> np.ndarra
         if zv is None:
             tasks.append(_native.Task(_native.MI, k, [xv], [yv], n=n, index=index))
         else:
-            tasks.append(_native.Task(_native.CMI, k, [xv], [yv], [zv], n=n, index=index))
+            tasks.append(_native.Task(_native.CMI, k, [xv], [yv], list(zv), n=n, index=index))
     res = []
     values = _native.run_tasks(tasks, flags=run_flags | _native.RESCALE, results_out=res,
                                noise=lambda m: _noise.take(0, (m,)))

@@ -509,8 +509,8 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
     }
     if (rescale && T.kind != EGB_ENTROPY) {
       if (internal) return fail(ctx, EGB_ERR_ARG, who + "EGB_RESCALE applies to estimator tasks only");
-      if (T.dx != 1 || T.dy > 1 || T.dz > 1)
-        return fail(ctx, EGB_ERR_ARG, who + "EGB_RESCALE needs one column per variable");
+      if (T.dx != 1 || T.dy > 1)
+        return fail(ctx, EGB_ERR_ARG, who + "EGB_RESCALE needs one x column and at most one y column");
       const int64_t draws = T.n * (int64_t)(T.dx + T.dy + T.dz);
       if (!ctx->noise_d || draws > ctx->noise_len)
         return fail(ctx, EGB_ERR_ARG, who + "EGB_RESCALE needs " + std::to_string(draws) +
@@ -995,11 +995,15 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   std::vector<int2> pw_nodes;
   std::vector<int32_t> pw_levels;
   std::vector<RescaleCol> rcols;
+  std::vector<RescaleStat> rstats;        // distinct columns (mean and std once each)
   std::vector<int32_t> rinv;              // inverse class orders, concatenated
   std::vector<size_t> rinv_task;          // per task: offset in rinv, or SIZE_MAX
-  size_t off_pw_scratch = 0;
+  size_t off_pw_scratch = 0, off_pw_ms = 0;
   if (rescale) {
     std::map<int64_t, int32_t> tree_of;
+    // a column read through the same pointer, stride and sample index (and
+    // summed the same way) has the same statistics in every task
+    std::map<std::tuple<uintptr_t, int64_t, uintptr_t, int64_t, int>, int32_t> stat_of;
     size_t scratch_elems = 0;
     for (int t = 0; t < ntasks; ++t) {
       const TaskPlan& p = P[(size_t)t];
@@ -1018,14 +1022,33 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
         RescaleCol rc{};
         rc.task = t;
         rc.col = c;
-        rc.tree = it->second;
-        rc.noise_pos = (int64_t)c * p.n;
-        rc.scratch = (int64_t)scratch_elems;
-        scratch_elems += (size_t)pw_trees[(size_t)it->second].nnode;
+        // x from noise position 0, then y, then z (n x dz, row-major)
+        const int zc = c - p.dx - p.dy;  // condition column, or negative
+        rc.group = zc >= 0 && p.dz > 1 ? p.dz : 1;
+        rc.noise_pos = zc >= 0 ? (int64_t)(p.dx + p.dy) * p.n + zc : (int64_t)c * p.n;
+        const auto key = std::make_tuple((uintptr_t)tasks[t].cols[c].data, tasks[t].cols[c].stride,
+                                         (uintptr_t)p.index, p.n, rc.group);
+        const bool ordered = !p.perm.empty();  // its own class order: not shared
+        auto f = ordered ? stat_of.end() : stat_of.find(key);
+        if (f == stat_of.end()) {
+          RescaleStat rs{};
+          rs.task = t;
+          rs.col = c;
+          rs.tree = it->second;
+          rs.group = rc.group;
+          rs.scratch = (int64_t)scratch_elems;
+          if (rs.group == 1) scratch_elems += (size_t)pw_trees[(size_t)it->second].nnode;
+          rc.stat = (int32_t)rstats.size();
+          rstats.push_back(rs);
+          if (!ordered) stat_of.emplace(key, rc.stat);
+        } else {
+          rc.stat = f->second;
+        }
         rcols.push_back(rc);
       }
     }
     off_pw_scratch = dl.take(sizeof(double) * std::max<size_t>(scratch_elems, 1));
+    off_pw_ms = dl.take(sizeof(double2) * std::max<size_t>(rstats.size(), 1));
   }
 
   // tables (pinned blob -> device)
@@ -1047,6 +1070,7 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   const size_t tab_pwnodes = tl.take(sizeof(int2) * std::max<size_t>(pw_nodes.size(), 1));
   const size_t tab_pwlevels = tl.take(sizeof(int32_t) * std::max<size_t>(pw_levels.size(), 1));
   const size_t tab_rcols = tl.take(sizeof(RescaleCol) * std::max<size_t>(rcols.size(), 1));
+  const size_t tab_rstats = tl.take(sizeof(RescaleStat) * std::max<size_t>(rstats.size(), 1));
   const size_t tab_rinv = tl.take(sizeof(int32_t) * std::max<size_t>(rinv.size(), 1));
   // shared sample indices: one copy per (array, n)
   std::map<std::pair<const int32_t*, int64_t>, size_t> index_tab;
@@ -1140,11 +1164,14 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
     std::memcpy(H + tab_pwtrees, pw_trees.data(), sizeof(PwTree) * pw_trees.size());
     std::memcpy(H + tab_pwnodes, pw_nodes.data(), sizeof(int2) * pw_nodes.size());
     std::memcpy(H + tab_pwlevels, pw_levels.data(), sizeof(int32_t) * pw_levels.size());
-    for (RescaleCol& rc : rcols) {
-      const size_t o = rinv_task[(size_t)rc.task];
-      rc.inv = o == SIZE_MAX ? nullptr : (const int32_t*)(A + off_tab + tab_rinv) + o;
-    }
+    auto inv_of = [&](int32_t task) -> const int32_t* {
+      const size_t o = rinv_task[(size_t)task];
+      return o == SIZE_MAX ? nullptr : (const int32_t*)(A + off_tab + tab_rinv) + o;
+    };
+    for (RescaleCol& rc : rcols) rc.inv = inv_of(rc.task);
+    for (RescaleStat& rs : rstats) rs.inv = inv_of(rs.task);
     std::memcpy(H + tab_rcols, rcols.data(), sizeof(RescaleCol) * rcols.size());
+    std::memcpy(H + tab_rstats, rstats.data(), sizeof(RescaleStat) * rstats.size());
     if (!rinv.empty()) std::memcpy(H + tab_rinv, rinv.data(), sizeof(int32_t) * rinv.size());
   }
   std::memcpy(H + tab_coltask, col_task.data(), sizeof(int32_t) * col_task.size());
@@ -1263,10 +1290,11 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
                         (WorkItem*)(A + G.off_items), st);
   launch_gather(tasks_d, (const GatherCol*)dtab(tab_gcols), ncols_total, max_ld, st);
   if (!rcols.empty())
-    launch_rescale(tasks_d, (const RescaleCol*)dtab(tab_rcols), (int)rcols.size(),
+    launch_rescale(tasks_d, (const RescaleStat*)dtab(tab_rstats), (int)rstats.size(),
+                   (const RescaleCol*)dtab(tab_rcols), (int)rcols.size(),
                    (const PwTree*)dtab(tab_pwtrees), (const int2*)dtab(tab_pwnodes),
-                   (const int32_t*)dtab(tab_pwlevels), (double*)(A + off_pw_scratch), ctx->noise_d,
-                   zero_d, st);
+                   (const int32_t*)dtab(tab_pwlevels), (double*)(A + off_pw_scratch),
+                   (double2*)(A + off_pw_ms), ctx->noise_d, zero_d, st);
   launch_prepare(tasks_d, (const int32_t*)dtab(tab_coltask), (const int32_t*)dtab(tab_colidx),
                  ncols_total, (unsigned long long*)(A + off_minmax), (double*)(A + off_centers), st);
   if (timing) EGB_CUDA(cudaEventRecord(ctx->ev[2], st));

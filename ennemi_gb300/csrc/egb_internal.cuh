@@ -370,18 +370,30 @@ struct GatherCol {        // working column <- caller column (strided, permuted)
 struct PwTree {
   int32_t node0, nleaf, nnode, lvl0, nlvl;
 };
-struct RescaleCol {       // one column to rescale in place
-  int32_t task, col, tree, pad_;
-  int64_t noise_pos;      // first noise value of the column
+struct RescaleStat {      // one distinct column of the batch: its mean and std
+  int32_t task, col;      // a task column holding it (working order)
+  int32_t tree;           // its summation tree (group == 1)
+  int32_t group;          // > 1: one of `group` condition columns, which NumPy
+                          // reduces along axis 0 -- row by row, in order
   int64_t scratch;        // first node-sum slot (tree.nnode doubles)
   const int32_t* inv;     // sample -> working position (class-ordered tasks), or null
+};
+struct RescaleCol {       // one task column to rescale in place
+  int32_t task, col;
+  int32_t stat;           // its RescaleStat
+  int32_t group;          // noise stride: condition columns of an n x group array
+  int64_t noise_pos;      // noise value of the column's first sample
+  const int32_t* inv;
 };
 // zero_flags bit of a task with a column whose standard deviation was below
 // 1e-20: left as given, the task is reported EGB_TASK_CONSTANT
 constexpr uint32_t RESCALE_CONSTANT = 1u << 31;
-void launch_rescale(const TaskDev* tasks_d, const RescaleCol* cols_d, int ncols,
-                    const PwTree* trees_d, const int2* nodes_d, const int32_t* levels_d,
-                    double* scratch, const double* noise, uint32_t* zero_flags, cudaStream_t st);
+// stats: one block per distinct column -> ms[u] = (mean, std); then one block
+// per task column: x = (x - mean) / std + noise
+void launch_rescale(const TaskDev* tasks_d, const RescaleStat* stats_d, int nstats,
+                    const RescaleCol* cols_d, int ncols, const PwTree* trees_d,
+                    const int2* nodes_d, const int32_t* levels_d, double* scratch, double2* ms,
+                    const double* noise, uint32_t* zero_flags, cudaStream_t st);
 
 struct CombineJob {       // per-task reduction of per-sample terms
   int32_t task;

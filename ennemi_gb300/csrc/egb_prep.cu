@@ -123,19 +123,42 @@ __device__ double pw_sum(const double* x, const int32_t* inv, const PwTree& tr,
 }
 
 __global__ void __launch_bounds__(PREP_THREADS)
-rescale_kernel(const TaskDev* __restrict__ tasks, const RescaleCol* __restrict__ cols,
-               const PwTree* __restrict__ trees, const int2* __restrict__ nodes,
-               const int32_t* __restrict__ levels, double* __restrict__ scratch,
-               const double* __restrict__ noise, uint32_t* __restrict__ zero_flags) {
+rescale_stats_kernel(const TaskDev* __restrict__ tasks, const RescaleStat* __restrict__ stats,
+                     const PwTree* __restrict__ trees, const int2* __restrict__ nodes,
+                     const int32_t* __restrict__ levels, double* __restrict__ scratch,
+                     double2* __restrict__ ms) {
+  const RescaleStat rs = stats[blockIdx.x];
+  const TaskDev t = tasks[rs.task];
+  const double* x = t.x64 + (int64_t)rs.col * t.ld;
+  const double n = (double)t.n;
+  if (rs.group > 1) {  // axis-0 reduction of an (n, group) array: in row order
+    if (threadIdx.x == 0) {
+      double s = pw_value(x, rs.inv, 0, false, 0.0);
+      for (int i = 1; i < t.n; ++i) s = __dadd_rn(s, pw_value(x, rs.inv, i, false, 0.0));
+      const double m = __ddiv_rn(s, n);
+      double q = pw_value(x, rs.inv, 0, true, m);
+      for (int i = 1; i < t.n; ++i) q = __dadd_rn(q, pw_value(x, rs.inv, i, true, m));
+      ms[blockIdx.x] = make_double2(m, __dsqrt_rn(__ddiv_rn(q, n)));
+    }
+    return;
+  }
+  const PwTree tr = trees[rs.tree];
+  double* ns = scratch + rs.scratch;
+  const double mean = __ddiv_rn(pw_sum(x, rs.inv, tr, nodes, levels, ns, false, 0.0), n);
+  __syncthreads();  // every thread has read the root before the slots are reused
+  const double sd = __dsqrt_rn(__ddiv_rn(pw_sum(x, rs.inv, tr, nodes, levels, ns, true, mean), n));
+  if (threadIdx.x == 0) ms[blockIdx.x] = make_double2(mean, sd);
+}
+
+__global__ void __launch_bounds__(PREP_THREADS)
+rescale_apply_kernel(const TaskDev* __restrict__ tasks, const RescaleCol* __restrict__ cols,
+                     const double2* __restrict__ ms, const double* __restrict__ noise,
+                     uint32_t* __restrict__ zero_flags) {
   const RescaleCol rc = cols[blockIdx.x];
   const TaskDev t = tasks[rc.task];
   double* x = const_cast<double*>(t.x64) + (int64_t)rc.col * t.ld;
-  const PwTree tr = trees[rc.tree];
-  double* ns = scratch + rc.scratch;
-  const double n = (double)t.n;
-  const double mean = __ddiv_rn(pw_sum(x, rc.inv, tr, nodes, levels, ns, false, 0.0), n);
-  __syncthreads();  // every thread has read the root before the slots are reused
-  const double sd = __dsqrt_rn(__ddiv_rn(pw_sum(x, rc.inv, tr, nodes, levels, ns, true, mean), n));
+  const double2 m = ms[rc.stat];
+  const double mean = m.x, sd = m.y;
   if (fabs(sd) < 1e-20) {  // np.abs(std) < 1e-20: the reference warns and keeps x
     if (threadIdx.x == 0) atomicOr(zero_flags + rc.task, RESCALE_CONSTANT);
     return;
@@ -143,7 +166,7 @@ rescale_kernel(const TaskDev* __restrict__ tasks, const RescaleCol* __restrict__
   const double* nz = noise + rc.noise_pos;
   for (int i = threadIdx.x; i < t.n; i += blockDim.x) {  // sample i
     const int w = rc.inv ? rc.inv[i] : i;
-    x[w] = __dadd_rn(__ddiv_rn(__dsub_rn(x[w], mean), sd), nz[i]);
+    x[w] = __dadd_rn(__ddiv_rn(__dsub_rn(x[w], mean), sd), nz[(int64_t)i * rc.group]);
   }
 }
 
@@ -394,12 +417,15 @@ void launch_gather(const TaskDev* tasks_d, const GatherCol* cols_d, int ncols, i
   count_launch();
 }
 
-void launch_rescale(const TaskDev* tasks_d, const RescaleCol* cols_d, int ncols,
-                    const PwTree* trees_d, const int2* nodes_d, const int32_t* levels_d,
-                    double* scratch, const double* noise, uint32_t* zero_flags, cudaStream_t st) {
-  if (ncols <= 0) return;
-  rescale_kernel<<<ncols, PREP_THREADS, 0, st>>>(tasks_d, cols_d, trees_d, nodes_d, levels_d, scratch,
-                                                 noise, zero_flags);
+void launch_rescale(const TaskDev* tasks_d, const RescaleStat* stats_d, int nstats,
+                    const RescaleCol* cols_d, int ncols, const PwTree* trees_d,
+                    const int2* nodes_d, const int32_t* levels_d, double* scratch, double2* ms,
+                    const double* noise, uint32_t* zero_flags, cudaStream_t st) {
+  if (ncols <= 0 || nstats <= 0) return;
+  rescale_stats_kernel<<<nstats, PREP_THREADS, 0, st>>>(tasks_d, stats_d, trees_d, nodes_d, levels_d,
+                                                        scratch, ms);
+  count_launch();
+  rescale_apply_kernel<<<ncols, PREP_THREADS, 0, st>>>(tasks_d, cols_d, ms, noise, zero_flags);
   count_launch();
 }
 

@@ -104,8 +104,12 @@ enum egb_flags {
                                   NumPy's pairwise summation (bit-identical), the
                                   noise from the stream set by egb_set_noise at
                                   the reference's positions (x from 0, then y,
-                                  then z).  Requires one column per variable;
-                                  ENTROPY tasks are left as given             */
+                                  then the condition as an n x dz row-major
+                                  array).  A condition of two or more columns
+                                  is reduced as NumPy reduces axis 0 of such an
+                                  array: row by row.  Requires one x column and
+                                  at most one y column; ENTROPY tasks are left
+                                  as given                                   */
 };
 
 /* One float64 column: sample i at data[i * stride] (stride in elements). */

@@ -74,7 +74,12 @@ def oracle_run_tasks(O, calls=None):
                     if results_out is not None:
                         results_out.append(Result(np.nan, _native.TASK_CONSTANT))
                     continue
-                cols = [(c - c.mean()) / c.std() + nz[i * n:(i + 1) * n] for i, c in enumerate(cols)]
+                nxy = len(t.x) + len(t.y)
+                z = np.column_stack(cols[nxy:]) if len(t.z) else None
+                cols = [(c - c.mean()) / c.std() + nz[i * n:(i + 1) * n] for i, c in enumerate(cols[:nxy])]
+                if z is not None:   # (n, dz) along axis 0, noise row-major
+                    z = (z - z.mean(axis=0)) / z.std(axis=0) + nz[nxy * n:].reshape(n, -1)[:, :z.shape[1]]
+                    cols += [z[:, j] for j in range(z.shape[1])]
             dx, dy = len(t.x), len(t.y)
             x = np.column_stack(cols[:dx])
             y = np.column_stack(cols[dx:dx + dy]) if dy else None

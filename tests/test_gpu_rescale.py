@@ -47,6 +47,28 @@ def test_rescaled_columns_equal_numpy(n, indexed):
             assert np.array_equal(got.view(np.uint64), want[c].view(np.uint64)), (t, c)
 
 
+@pytest.mark.parametrize("n", [9, 129, 8193, 50000])
+@pytest.mark.parametrize("dz", [2, 3])
+def test_condition_columns_reduce_row_by_row(n, dz):
+    """A condition of dz >= 2 columns: NumPy's axis-0 mean / std of the (n, dz)
+    array (rows added in order), noise drawn row-major after x and y."""
+    rng = np.random.default_rng(100 * n + dz)
+    rows = n + 40
+    raw = rng.normal(size=(rows, dz + 2)) * 3.0 - 1.0
+    idx = np.sort(rng.choice(rows - 3, size=n, replace=False)).astype(np.int32)
+    views = [raw[3:, c] for c in range(dz + 2)]
+    task = N.Task(N.CMI, 3, [views[0]], [views[1]], views[2:], n=n, index=idx)
+    res = []
+    N.run_tasks([task], flags=N.RESCALE | N.KEEP_INTERNALS, results_out=res, noise=_noise)
+    assert res[0].status == 0
+    Z = np.column_stack([v[idx] for v in views[2:]])
+    Zr = (Z - Z.mean(axis=0)) / Z.std(axis=0) + _driver._noise.take(2 * n, (n, dz))
+    assert np.array_equal(N.fetch(0, 16, n), _reference_rescale(views[0][idx], 0, n))
+    assert np.array_equal(N.fetch(0, 17, n), _reference_rescale(views[1][idx], n, n))
+    for c in range(dz):
+        assert np.array_equal(N.fetch(0, 18 + c, n).view(np.uint64), Zr[:, c].view(np.uint64)), c
+
+
 def test_semidiscrete_columns_with_index():
     """Labels and an index together: the class order is applied on top of the
     index; the continuous column is rescaled from noise position 0."""
@@ -80,13 +102,14 @@ def test_constant_column_reported():
     assert res[1].status == 0 and np.isfinite(v[1])
 
 
-def test_rescale_needs_one_column_per_variable():
+def test_rescale_needs_one_x_and_y_column():
     x = np.random.default_rng(1).normal(size=(500, 2))
-    with pytest.raises(RuntimeError, match="one column per variable"):
+    with pytest.raises(RuntimeError, match="one x column"):
         N.run_tasks([N.Task(N.MI, 3, [x[:, 0], x[:, 1]], [x[:, 0]])], flags=N.RESCALE, noise=_noise)
 
 
-@pytest.mark.parametrize("case", ["lags_mask", "lags_cond", "pairwise_mask", "constant"])
+@pytest.mark.parametrize("case", ["lags_mask", "lags_cond", "lags_cond2", "pairwise_mask",
+                                  "pairwise_cond2", "constant"])
 def test_public_api_same_with_device_and_host_preparation(case, monkeypatch):
     rng = np.random.default_rng(17)
     n = 20000
@@ -98,7 +121,10 @@ def test_public_api_same_with_device_and_host_preparation(case, monkeypatch):
     calls = {
         "lags_mask": lambda: eg.estimate_mi(y, x, lag=[0, 1, 7], mask=mask),
         "lags_cond": lambda: eg.estimate_mi(y, x[:, :2], lag=[0, 3], cond=z, cond_lag=2, mask=mask),
+        "lags_cond2": lambda: eg.estimate_mi(y, x[:, :2], lag=[0, 3], cond=x[:, 2:],
+                                             cond_lag=[[1, 0], [2, 4]], mask=mask),
         "pairwise_mask": lambda: eg.pairwise_mi(x, mask=mask),
+        "pairwise_cond2": lambda: eg.pairwise_mi(x[:, :3], cond=np.column_stack((z, y)), mask=mask),
         "constant": lambda: eg.pairwise_mi(np.column_stack((x[:, :2], np.full(n, 2.0)))),
     }
     dev = calls[case]()
