@@ -343,10 +343,18 @@ def _estimate_mi(y: FloatArray, x: FloatArray, lag: FloatArray, k: int,
         lo, hi = min(min_lag, 0), max(max_lag, 0)
         n = len(y) - hi + lo if prep.idx is None else len(prep.idx)
         specs = []
+        ycol = _native.Col(y[hi:])
+        zcols = {}   # condition columns by lag: shared by the tasks of a lag row
         for li, vi in indices:
             xv = x if x.ndim == 1 else x[:, vi]
-            zv = None if cond is None else [cond[hi - cond_lag[li][c]:, c] for c in range(cond.shape[1])]
-            specs.append((xv[hi - lag[li]:], y[hi:], zv))
+            zv = None
+            if cond is not None:
+                zkey = tuple(int(c) for c in cond_lag[li])
+                zv = zcols.get(zkey)
+                if zv is None:
+                    zv = zcols[zkey] = [_native.Col(cond[hi - cond_lag[li][c]:, c])
+                                        for c in range(cond.shape[1])]
+            specs.append((_native.Col(xv[hi - lag[li]:]), ycol, zv))
         values = _run_device_prep(specs, n, k, prep.idx, jobs, max_threads)
     else:
         batch = _Batch()
@@ -476,8 +484,9 @@ def _pairwise_mi(data: FloatArray, k: int, cond: Optional[FloatArray], preproces
     if pairs and _device_prep_ok((data,) + (() if cond is None else (cond,)), cond, preprocess,
                                  drop_nan, bool(np.any(discrete))):
         n = len(data) if prep.idx is None else len(prep.idx)
-        zv = None if cond is None else [cond[:, c] for c in range(cond.shape[1])]
-        specs = [(data[:, i], data[:, j], zv) for i, j in pairs]
+        cols = [_native.Col(data[:, i]) for i in range(nvar)]
+        zv = None if cond is None else [_native.Col(cond[:, c]) for c in range(cond.shape[1])]
+        specs = [(cols[i], cols[j], zv) for i, j in pairs]
         values = _run_device_prep(specs, n, k, prep.idx, jobs, max_threads)
     else:
         batch = _Batch()

@@ -254,6 +254,22 @@ def _col_struct(col, device: bool):
     return EgbColumn(c.ctypes.data, s // 8), c
 
 
+class Col:
+    """A column resolved once and shared by many tasks: its address, stride
+    (elements) and length, and the array that keeps the memory alive."""
+
+    __slots__ = ("ptr", "stride", "length", "ref")
+
+    def __init__(self, col, device: bool = False):
+        s, ref = _col_struct(col, device)
+        self.ptr, self.stride, self.ref = s.data, s.stride, ref
+        self.length = int(ref.shape[0])
+
+
+def _length(col) -> int:
+    return col.length if type(col) is Col else len(col)
+
+
 def run_tasks(tasks: List[Task], flags: int = 0, device: int = 0,
               results_out: Optional[list] = None, noise=None) -> np.ndarray:
     """Evaluate the tasks in one batched call; returns the estimates.
@@ -265,7 +281,7 @@ def run_tasks(tasks: List[Task], flags: int = 0, device: int = 0,
         return np.empty(0)
     ctx = context(device)
     if flags & RESCALE:
-        need = max((t.n or len(t.x[0])) * (len(t.x) + len(t.y) + len(t.z)) for t in tasks)
+        need = max((t.n or _length(t.x[0])) * (len(t.x) + len(t.y) + len(t.z)) for t in tasks)
         if ctx.noise_len < need:
             if noise is None:
                 raise ValueError("RESCALE needs the noise stream")
@@ -274,18 +290,31 @@ def run_tasks(tasks: List[Task], flags: int = 0, device: int = 0,
     ctasks = (EgbTask * len(tasks))()
     keep = []
     index_ptr = {}   # one int32 copy per index array shared by tasks
+    # every task's columns in one array
+    allcols = (EgbColumn * sum(len(t.x) + len(t.y) + len(t.z) for t in tasks))()
+    base, csize = ctypes.addressof(allcols), ctypes.sizeof(EgbColumn)
+    colp = ctypes.POINTER(EgbColumn)
+    off = 0
     for i, t in enumerate(tasks):
-        cols = list(t.x) + list(t.y) + list(t.z)
-        arr = (EgbColumn * len(cols))()
-        for c, col in enumerate(cols):
-            arr[c], ref = _col_struct(col, is_dev)
-            keep.append(ref)
-        keep.append(arr)
-        n = t.n or (cols[0].shape[0])
+        first = off
+        n0 = None
+        for col in (*t.x, *t.y, *t.z):
+            e = allcols[off]
+            if type(col) is Col:
+                e.data, e.stride = col.ptr, col.stride
+                length = col.length
+            else:
+                st, ref = _col_struct(col, is_dev)
+                e.data, e.stride = st.data, st.stride
+                keep.append(ref)
+                length = ref.shape[0]
+            if n0 is None:
+                n0 = length
+            off += 1
         ct = ctasks[i]
-        ct.kind, ct.k, ct.n = t.kind, int(t.k), int(n)
+        ct.kind, ct.k, ct.n = t.kind, int(t.k), int(t.n or n0)
         ct.dx, ct.dy, ct.dz = len(t.x), len(t.y), len(t.z)
-        ct.cols = arr
+        ct.cols = ctypes.cast(base + first * csize, colp)
         if t.labels is not None:
             lab = np.ascontiguousarray(t.labels, dtype=np.int32)
             keep.append(lab)
@@ -298,6 +327,7 @@ def run_tasks(tasks: List[Task], flags: int = 0, device: int = 0,
                 keep.append(ix)
                 ptr = index_ptr[id(t.index)] = ix.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
             ct.index = ptr
+    keep.append(allcols)
     res = (EgbResult * len(tasks))()
     with ctx.lock:
         rc = ctx.lib.egb_run_batch(ctx.h, ctasks, len(tasks), flags, res)

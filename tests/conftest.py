@@ -62,9 +62,10 @@ def oracle_run_tasks(O, calls=None):
             calls.append(len(tasks))
         out = []
         for t in tasks:
-            n = t.n or len(t.x[0])
+            n = t.n or (t.x[0].length if isinstance(t.x[0], _native.Col) else len(t.x[0]))
             ix = np.arange(n) if t.index is None else np.asarray(t.index)
-            cols = [np.asarray(c)[ix] for c in list(t.x) + list(t.y) + list(t.z)]
+            cols = [(c.ref if isinstance(c, _native.Col) else np.asarray(c))[ix]
+                    for c in list(t.x) + list(t.y) + list(t.z)]
             if flags & _native.RESCALE and t.kind != _native.ENTROPY:
                 # the library's EGB_RESCALE, as the reference's _rescale_data
                 # computes it (x from noise position 0, then y, then z)
