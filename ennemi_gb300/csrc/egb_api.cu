@@ -811,9 +811,10 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
       const int64_t cap = m.mode == 3 ? (m.is_knn ? GRID_STRIPS_KNN : GRID_STRIPS_COUNT) : 256;
       J.nstrips = (int32_t)std::max<int64_t>(1, std::min<int64_t>(cap, len / GRID_MIN_STRIP));
       if (m.sort_seg_c >= 0) {
-        // nested: about NEST_CELL points per cell, as many strips as cells
+        // nested: about NEST_CELL_* points per cell, as many strips as cells
         // per strip, every cell at least GRID_MIN_STRIP / 2 points
-        int64_t side = (int64_t)std::lround(std::sqrt((double)len / (m.is_knn ? NEST_CELL : NEST_CELL_COUNT)));
+        const int target = m.is_knn ? (d == 3 ? NEST_CELL_3D : NEST_CELL_4D) : NEST_CELL_COUNT;
+        int64_t side = (int64_t)std::lround(std::sqrt((double)len / target));
         side = std::max<int64_t>(1, std::min<int64_t>(256, side));
         while (side > 1 && len / (side * side) < GRID_MIN_STRIP / 2) --side;
         J.nstrips = (int32_t)side;

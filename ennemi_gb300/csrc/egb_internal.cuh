@@ -292,7 +292,8 @@ __host__ __device__ __forceinline__ int32_t cell_start(int32_t s0, int32_t L, in
                                                        int32_t nsub) {
   return s0 + strip_start(c2, L, nsub);
 }
-constexpr int NEST_CELL = 768;        // target points per nested-grid cell (kNN jobs)
+constexpr int NEST_CELL_3D = 384;     // target points per nested-grid cell, kNN jobs of d = 3
+constexpr int NEST_CELL_4D = 256;     // the same for d >= 4 (measured best for each)
 constexpr int NEST_CELL_COUNT = 768;  // the same for key-range count jobs
 constexpr int GRID_QB = 128;     // queries per grid work item
 constexpr int GRID_TILE = 128;   // candidates per grid tile
