@@ -806,10 +806,21 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
       J.c32g = (float*)(uintptr_t)dl.take(sizeof(float) * (size_t)(d * J.lds));
       J.idxg = (int32_t*)(uintptr_t)dl.take(sizeof(int32_t) * (size_t)J.lds);
       J.posg = (int32_t*)(uintptr_t)dl.take(sizeof(int32_t) * (size_t)J.lds);
-      // strips of at least GRID_MIN_STRIP points, at most GRID_STRIPS_KNN /
-      // GRID_STRIPS_COUNT of them (warp-grid jobs; 256 for the CTA grid)
-      const int64_t cap = m.mode == 3 ? (m.is_knn ? GRID_STRIPS_KNN : GRID_STRIPS_COUNT) : 256;
-      J.nstrips = (int32_t)std::max<int64_t>(1, std::min<int64_t>(cap, len / GRID_MIN_STRIP));
+      // strips of at least GRID_MIN_STRIP points: about c * len^(1/dj) of them
+      // for warp-grid jobs (GRID_STRIPS_*_C), 256 for the CTA grid
+      int64_t want = 256;
+      if (m.mode == 3) {
+        const TaskPlan& tp = P[(size_t)m.s.task];
+        // the radii of a count job come from the task's joint kNN (per class,
+        // hence wider balls, for the semidiscrete kinds: one more dimension)
+        const int dj = m.is_knn ? d
+                       : tp.kind == KIND_COUNT_ONLY ? d + 1
+                       : (tp.kind == EGB_SEMI || tp.kind == EGB_CSEMI) ? tp.ncol + 1
+                       : std::max(tp.ncol, d + 1);
+        const double c = m.is_knn ? GRID_STRIPS_KNN_C : GRID_STRIPS_COUNT_C;
+        want = std::min<int64_t>(GRID_STRIPS_MAX, std::llround(c * std::pow((double)len, 1.0 / dj)));
+      }
+      J.nstrips = (int32_t)std::max<int64_t>(1, std::min<int64_t>(want, len / GRID_MIN_STRIP));
       if (m.sort_seg_c >= 0) {
         // nested: about NEST_CELL_* points per cell, as many strips as cells
         // per strip, every cell at least GRID_MIN_STRIP / 2 points

@@ -298,8 +298,14 @@ constexpr int NEST_CELL_COUNT = 768;  // the same for key-range count jobs
 constexpr int GRID_QB = 128;     // queries per grid work item
 constexpr int GRID_TILE = 128;   // candidates per grid tile
 constexpr int GRID_MIN_STRIP = 64;
-constexpr int GRID_STRIPS_KNN = 256;    // most strips of a 2-D warp-grid kNN job
-constexpr int GRID_STRIPS_COUNT = 256;  // most strips of a 2-D warp-grid count job
+// Strips of a 2-D warp-grid job: about c * len^(1/dj), dj the dimension of
+// the kNN search that sets the job's radii (the job's own for a kNN job, the
+// task's joint space for a count job), so that a strip stays a few ball widths
+// wide (balls shrink as len^(-1/dj)).  c measured on GB300: 500 kNN strips
+// and 128 count strips (3-D joint kNN) at 1e6 points.
+constexpr double GRID_STRIPS_KNN_C = 0.5;
+constexpr double GRID_STRIPS_COUNT_C = 1.28;
+constexpr int GRID_STRIPS_MAX = 1024;
 
 struct WorkItem {         // one tile of queries of one job
   int32_t job;
