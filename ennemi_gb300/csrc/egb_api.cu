@@ -826,6 +826,15 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
         // per strip, every cell at least GRID_MIN_STRIP / 2 points
         const int target = m.is_knn ? (d == 3 ? NEST_CELL_3D : NEST_CELL_4D) : NEST_CELL_COUNT;
         int64_t side = (int64_t)std::lround(std::sqrt((double)len / target));
+        const TaskPlan& tq = P[(size_t)m.s.task];
+        if (!m.is_knn && tq.kind != EGB_SEMI && tq.kind != EGB_CSEMI) {
+          // count jobs of small spaces with wide balls take finer cells: at
+          // least NEST_SIDE_C * len^(1/dj) per side, dj as for the strips
+          // (the semidiscrete kinds, whose radii come from per-class kNN,
+          // measured best with NEST_CELL_COUNT alone)
+          const int dj = tq.kind == KIND_COUNT_ONLY ? d + 1 : std::max(tq.ncol, d + 1);
+          side = std::max<int64_t>(side, std::llround(NEST_SIDE_C * std::pow((double)len, 1.0 / dj)));
+        }
         side = std::max<int64_t>(1, std::min<int64_t>(256, side));
         while (side > 1 && len / (side * side) < GRID_MIN_STRIP / 2) --side;
         J.nstrips = (int32_t)side;

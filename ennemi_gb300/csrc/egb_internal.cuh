@@ -294,7 +294,8 @@ __host__ __device__ __forceinline__ int32_t cell_start(int32_t s0, int32_t L, in
 }
 constexpr int NEST_CELL_3D = 384;     // target points per nested-grid cell, kNN jobs of d = 3
 constexpr int NEST_CELL_4D = 256;     // the same for d >= 4 (measured best for each)
-constexpr int NEST_CELL_COUNT = 768;  // the same for key-range count jobs
+constexpr int NEST_CELL_COUNT = 768;  // the same for count jobs, which also take at least
+constexpr double NEST_SIDE_C = 1.07;  // NEST_SIDE_C * len^(1/dj) cells per side (dj: see strips)
 constexpr int GRID_QB = 128;     // queries per grid work item
 constexpr int GRID_TILE = 128;   // candidates per grid tile
 constexpr int GRID_MIN_STRIP = 64;
