@@ -406,8 +406,8 @@ def main():
     # DRAM bytes read + written per launch, from one `ncu --set full` capture
     # of `bench.py --profile --n 1000000 --steps 1 --warmup 1` (the walk: the
     # 2-D and the 3-D launch averaged); measured for this workload only
-    ncu_traffic = {"wwalk_kernel": ((114.40 + 16.89) + (40.60 + 0.08)) / 2 * 1e6,
-                   "wcount_kernel": (49.06 + 0.78) * 1e6}
+    ncu_traffic = {"wwalk_kernel": ((114.37 + 16.81) + (40.62 + 0.10)) / 2 * 1e6,
+                   "wcount_kernel": (49.06 + 1.09) * 1e6}
     traffic = ncu_traffic.get(kname) if args.n == 1_000_000 else None
     roofline = {"bound": "alu", "kernel": kname, "achieved": achieved / 1e9,
                 "peak": peak_ops / 1e9, "unit": "Gop/s", "frac": achieved / peak_ops,
