@@ -32,6 +32,7 @@ import json
 import os
 import statistics
 import subprocess
+import tempfile
 import sys
 import time
 
@@ -73,7 +74,10 @@ class ClockSampler:
     def __init__(self, device_index: int):
         self.dev = device_index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_bench_{os.getpid()}.csv")
+        # raw samples (the JSON line carries their summary); BENCH_CLOCKS_DIR
+        # keeps them somewhere else
+        out = os.environ.get("BENCH_CLOCKS_DIR") or tempfile.gettempdir()
+        self.path = os.path.join(out, f"clocks_bench_{os.getpid()}.csv")
 
     def __enter__(self):
         try:
