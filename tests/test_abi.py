@@ -83,6 +83,8 @@ def test_null_arguments_rejected_without_device(lib):
     assert lib.egb_run_batch(None, None, 0, 0, None) == -1
     lib.egb_create.argtypes = [ctypes.c_int, ctypes.c_void_p]
     assert lib.egb_create(0, None) == -1
+    lib.egb_set_noise.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64]
+    assert lib.egb_set_noise(None, None, 0) == -1
 
 
 def test_library_is_built_for_sm103a():

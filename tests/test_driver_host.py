@@ -262,3 +262,63 @@ def test_numpy_sums_in_pairwise_order():
     assert _driver._numpy_sums_pairwise()
     a = np.random.default_rng(3).standard_normal(50_001)
     assert _driver._pairwise_sum(a.tolist()) == float(np.add.reduce(a))
+
+
+@pytest.mark.parametrize("case", ["lags_mask", "lags_nomask", "lags_negative", "lags_cond2",
+                                  "pairwise_cond_mask"])
+def test_device_preprocessing_columns_are_the_reference_slices(monkeypatch, case):
+    """Every task of the EGB_RESCALE path reads, through its column views and
+    shared sample index, exactly the lagged and masked samples the reference's
+    _lagged_mi slices (_driver.py:795-806, :834-842), in task order, with n
+    and the noise layout (x, y, then the condition) implied by the columns."""
+    rng = np.random.default_rng(29)
+    n = 500
+    x = rng.normal(size=(n, 3))
+    y = rng.normal(size=n)
+    cond = rng.normal(size=(n, 2))
+    mask = rng.random(n) > 0.25
+    lags = {"lags_mask": [0, 1, 5], "lags_nomask": [0, 2, 7], "lags_negative": [-2, 0, 3],
+            "lags_cond2": [0, 4]}
+    seen = []
+
+    def run(tasks, flags=0, device=0, results_out=None, noise=None):
+        assert flags & _native.RESCALE
+        for t in tasks:
+            ix = np.arange(t.n) if t.index is None else np.asarray(t.index)
+            cols = [(c.ref if isinstance(c, _native.Col) else np.asarray(c))[ix]
+                    for c in list(t.x) + list(t.y) + list(t.z)]
+            seen.append((t.kind, len(t.x), len(t.y), len(t.z), t.n, cols))
+        return np.zeros(len(tasks))
+
+    monkeypatch.setattr(_native, "run_tasks", run)
+    want = []
+    if case.startswith("lags"):
+        lag = lags[case]
+        c2 = case == "lags_cond2"
+        cond_lag = [[1, 0], [3, 2]] if c2 else None
+        eg.estimate_mi(y, x, lag=lag, mask=None if case == "lags_nomask" else mask,
+                       cond=cond if c2 else None, cond_lag=cond_lag if c2 else 0)
+        m = None if case == "lags_nomask" else mask
+        lo = min(min(lag), 0 if not c2 else min(min(r) for r in cond_lag))
+        hi = max(max(lag), 0 if not c2 else max(max(r) for r in cond_lag))
+        lo, hi = min(lo, 0), max(hi, 0)
+        for li, lg in enumerate(lag):
+            for vi in range(3):
+                xs = x[hi - lg: n - lg + lo, vi]
+                ys = y[hi: n + lo]
+                zs = (np.column_stack([cond[hi - cond_lag[li][i]: n - cond_lag[li][i] + lo, i]
+                                       for i in range(2)]) if c2 else None)
+                xs, ys, zs = _driver._apply_masks(xs, ys, zs, m, lo, hi, False)
+                want.append([xs, ys] + ([zs[:, 0], zs[:, 1]] if c2 else []))
+    else:
+        eg.pairwise_mi(x, cond=cond, mask=mask)
+        for i in range(3):
+            for j in range(i + 1, 3):
+                xs, ys, zs = _driver._apply_masks(x[:, i], x[:, j], cond, mask, 0, 0, False)
+                want.append([xs, ys, zs[:, 0], zs[:, 1]])
+    assert len(seen) == len(want)
+    for (kind, dx, dy, dz, tn, cols), ref in zip(seen, want):
+        assert (dx, dy, dz) == (1, 1, len(ref) - 2) and tn == len(ref[0])
+        assert kind == (_native.CMI if dz else _native.MI)
+        for got, r in zip(cols, ref):
+            assert np.array_equal(got.view(np.uint64), np.ascontiguousarray(r).view(np.uint64))
