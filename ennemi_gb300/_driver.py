@@ -558,7 +558,7 @@ def _numpy_sums_pairwise() -> bool:
     if _pairwise_checked is None:
         rng = np.random.default_rng(12345)
         ok = True
-        for n in (1, 5, 8, 9, 100, 128, 129, 136, 1000, 8191, 8193, 20011):
+        for n in (1, 5, 8, 9, 100, 128, 129, 136, 1000, 8191, 8193, 16411):
             a = rng.standard_normal(n) * 3.0 + 1.0
             vals = a.tolist()
             s = _pairwise_sum(vals)
@@ -568,7 +568,7 @@ def _numpy_sums_pairwise() -> bool:
             ok = ok and float(np.add.reduce(a)) == s and float(a.mean()) == m and float(a.std()) == sd
             col = a.reshape(n, 1)
             ok = ok and float(col.mean(axis=0)[0]) == m and float(col.std(axis=0)[0]) == sd
-        for n in (3, 129, 8193, 20011):
+        for n in (3, 129, 8193):
             for dz in (2, 3):
                 z = rng.standard_normal((n, dz)) * 2.0 - 0.5
                 means, sds = z.mean(axis=0), z.std(axis=0)
