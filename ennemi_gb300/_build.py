@@ -38,6 +38,7 @@ def _sources():
 
 def _inputs():
     return _sources() + sorted(glob.glob(os.path.join(CSRC, "*.cuh"))) + \
+        sorted(glob.glob(os.path.join(CSRC, "*.h"))) + \
         sorted(glob.glob(os.path.join(INCLUDE, "*.h")))
 
 
