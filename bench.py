@@ -148,43 +148,127 @@ def timed_steps(run, steps, torch, flush_buf):
     return total, per
 
 
-def cpu_baseline(work, k, fraction, threads):
+def _versions():
+    import scipy
+    return f"numpy {np.__version__}, scipy {scipy.__version__}"
+
+
+def cpu_baseline(work, k, slices, nslices, threads):
+    """The reference's calls over SciPy cKDTree on a bounded sample of the
+    batch: every tree built over all N points, `slices` of `nslices` query
+    slices of every task searched and counted, tasks on a pool of `threads`
+    workers as the reference's driver runs them; scaled to the batch."""
     from oracle import ref_port
     tasks = [(kind, tuple(cols)) for kind, cols in work]
     t0 = time.perf_counter()
-    r = ref_port.sample_rate(tasks, k, fraction, threads=threads)
+    r = ref_port.sample_rate(tasks, k, slices, nslices, threads=threads)
     wall = time.perf_counter() - t0
-    return {"value": len(tasks) / r["extrapolated_s"], "unit": UNIT, "cores": r["threads"],
-            "kind": "port",
-            "sample": (f"SciPy cKDTree (the reference's calls), trees built over all N, "
-                       f"{r['fraction']:.3f} of the query points searched/counted, time scaled to "
-                       f"the full batch; measured {wall:.1f} s"),
+    return {"value": len(tasks) / r["extrapolated_s"], "unit": UNIT,
+            "cores": min(r["threads"], len(tasks)), "kind": "port",
+            "max_threads": r["threads"],
+            "sample": (f"SciPy cKDTree (the reference's calls, {_versions()}): every tree built "
+                       f"over all N points, {slices} of {nslices} query slices of every task "
+                       f"searched and counted, one task per worker of a {r['threads']}-thread pool "
+                       f"(each task single-threaded, as the reference's driver runs them); "
+                       f"time scaled to the whole batch; measured {wall:.1f} s"),
             "seconds_per_batch_extrapolated": r["extrapolated_s"]}
 
 
+def config_of(args, ntask):
+    """The workload, identical in both arms' lines."""
+    return {"workload": "4x bivariate Gaussian KSG MI (rho 0/.3/.6/.9) + 1x 3-D Gaussian CMI "
+                        "(corr .5/.4/.4), float64, seeded",
+            "n": args.n, "k": args.k, "seed": args.seed, "tasks_per_step": ntask,
+            "l2": "GPU arm: flushed between timed steps (512 MB write)"}
+
+
+GOLDEN_HEADLINE = os.path.join(ROOT, "tests", "golden", "golden_headline.json")
+
+
+def parity_check(N, dev_tasks, work, args, dev):
+    """The batch once more (outside the timed region) with its internals
+    kept: eps and every count array hashed and compared with the digests the
+    reference produced on the same inputs (tests/golden/golden_headline.json,
+    made by tests/golden/make_golden.py --headline)."""
+    import hashlib
+    try:
+        gold = json.load(open(GOLDEN_HEADLINE))["large_sample"]
+    except (OSError, ValueError, KeyError):
+        return {"checked": False, "why": "no reference digests"}
+    if gold["n"] != args.n or gold["k"] != args.k or gold["seed"] != args.seed:
+        return {"checked": False, "why": "reference digests exist for n=1e6, k=3, seed 0 only"}
+
+    def h(a, dt):
+        return hashlib.sha256(np.ascontiguousarray(a, dtype=dt).tobytes()).hexdigest()
+
+    inputs_same = all([h(c, "<f8") for c in cols] == g["inputs"] for (_, cols), g in zip(work, gold["tasks"]))
+    vals = N.run_tasks(dev_tasks, flags=N.INPUT_DEVICE | N.KEEP_INTERNALS, device=dev)
+    eps_ok, cnt_ok, dmi = True, True, 0.0
+    for t, ((kind, _), g) in enumerate(zip(work, gold["tasks"])):
+        eps_ok &= h(N.fetch(t, 0, args.n, device=dev), "<f8") == g["eps"]
+        for s, name in enumerate(["nx", "ny"] if kind == "mi" else ["nxz", "nyz", "nz"]):
+            cnt_ok &= h(N.fetch(t, 1 + s, args.n, device=dev), "<i8") == g[name]
+        dmi = max(dmi, abs(float(vals[t]) - g["value"]))
+    return {"checked": True, "inputs_same": bool(inputs_same), "eps_bitexact": bool(eps_ok),
+            "counts_exact": bool(cnt_ok), "max_abs_dmi": dmi,
+            "against": "SHA-256 of eps and counts from the reference's cKDTree calls on the same "
+                       "inputs (tests/golden/golden_headline.json)"}
+
+
 def run_reference(args):
+    """The reference CPU arm: the whole batch, measured.
+
+    The tasks run on a thread pool of os.cpu_count() workers, one task per
+    worker and each task single-threaded, as the reference's driver runs them
+    with max_threads=None (_driver.py:736-785).  Each task builds its trees
+    once (timed); each of the K timed steps then searches and counts one
+    contiguous 1/K slice of every task's query points, so the K steps together
+    evaluate every query point of the batch exactly once.  value = tasks /
+    (tree builds + sum of the steps).  The W warm-up steps run the same code
+    on a 20,000-point copy of the workload."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    work = make_workload(args.n, args.seed)
+    from oracle import ref_port
     threads = os.cpu_count() or 1
-    for _ in range(args.warmup if args.warmup < 1 else 1):
-        cpu_baseline(make_workload(20000, args.seed), args.k, 0.05, threads)
-    vals, secs = [], []
-    for _ in range(args.steps):
-        cb = cpu_baseline(work, args.k, args.ref_fraction, threads)
-        vals.append(cb["value"])
-        secs.append(cb["seconds_per_batch_extrapolated"])
-    value = len(work) / (sum(secs) / len(secs))
-    cb["value"] = value
+    small = make_workload(20_000, args.seed)
+    wb = ref_port.SlicedBatch([(kd, tuple(c)) for kd, c in small], args.k, max(args.warmup, 1), threads)
+    try:
+        wb.build()
+        for s in range(args.warmup):
+            wb.step(s)
+    finally:
+        wb.close()
+    work = make_workload(args.n, args.seed)
+    b = ref_port.SlicedBatch([(kd, tuple(c)) for kd, c in work], args.k, args.steps, threads)
+    try:
+        build_s = b.build()
+        steps = [b.step(s) for s in range(args.steps)]
+    finally:
+        b.close()
+    batch_s = build_s + sum(steps)
+    value = len(work) / batch_s
+    serial_s = sum(b.task_seconds)
+    cb = {"value": value, "unit": UNIT, "cores": min(threads, len(work)), "kind": "port",
+          "max_threads": threads,
+          "sample": (f"the whole batch, every query point, in {args.steps} slices of every task "
+                     f"(SciPy cKDTree, the reference's calls, {_versions()}); one task per worker "
+                     f"of a {threads}-thread pool, each task single-threaded, as the reference's "
+                     f"driver with max_threads=None"),
+          "batch_s": batch_s, "tree_build_s": build_s,
+          "max_threads_1_s": serial_s,
+          "max_threads_1_note": "sum of the tasks' own times in this run: the reference's "
+                                "max_threads=1 path runs the same tasks one after another"}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": 1000.0 * sum(secs) / len(secs), "higher_is_better": True,
+            "ms_per_step": 1000.0 * batch_s / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "impl": "reference",
-            "config": {"workload": "4x bivariate Gaussian KSG MI (rho 0/.3/.6/.9) + 1x 3-D Gaussian CMI",
-                       "n": args.n, "k": args.k, "tasks_per_step": len(work),
-                       "host_threads": threads},
+            "config": config_of(args, len(work)),
+            "step": f"1/{args.steps} of every task's query points (the steps together are one "
+                    f"whole batch; tree builds timed once and included in value)",
+            "estimates": b.estimates(),
+            "per_step_s": steps,
             "cpu_baseline": cb,
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
@@ -292,8 +376,11 @@ def main():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--cpu-fraction", type=float, default=0.01)
-    ap.add_argument("--ref-fraction", type=float, default=0.01)
+    ap.add_argument("--cpu-slices", type=int, default=2,
+                    help="query slices (of --cpu-nslices) timed for cpu_baseline")
+    ap.add_argument("--cpu-nslices", type=int, default=50)
+    ap.add_argument("--plain-steps", type=int, default=5,
+                    help="timed steps of the all-FP64 comparator (median reported)")
     ap.add_argument("--profile", action="store_true", help="device-resident steps only (ncu)")
     ap.add_argument("--config", default="large", choices=["large", "lags", "pairwise", "semidiscrete"],
                     help="large: the headline workload; the others time one public-API call "
@@ -401,8 +488,8 @@ def main():
              work_stats.get("knn_tile_pairs", 0))]
     kname, kms, kops, kpairs = max(cand, key=lambda c: c[1])
     achieved = kops / (kms / 1000.0) if kms > 0 else 0.0
-    # the brute-force work the same kernel replaces (N_q * N_c * (2d+1) per
-    # job: every query against every point of its space)
+    # the brute-force work of the same jobs (N_q * N_c * (2d+1): every query
+    # against every point of its space), over the pairs actually screened
     if kname == "wwalk_kernel":
         bf_ops = sum(float(args.n) ** 2 * (2 * (2 if kind == "mi" else 3) + 1) for kind, _ in work)
     else:
@@ -421,11 +508,29 @@ def main():
                                 "(MEASURED_PEAKS.json holds only HBM and bf16 figures)"),
                 "ops_per_pair": "2d+1 (d differences, d max-of-abs, 1 compare)",
                 "hbm_peak_gbs": peaks.get("hbm_gbs"),
-                "bruteforce_equivalent": {
-                    "ops": bf_ops, "achieved": bf_ops / (kms / 1000.0) / 1e9 if kms > 0 else 0.0,
-                    "unit": "Gop/s",
-                    "note": "all-pairs work of the same jobs over the same time: the grid "
-                            "screens a small fraction of the pairs"}}
+                "algorithmic_savings": {
+                    "bruteforce_ops": bf_ops, "counted_ops": kops,
+                    "ratio": bf_ops / kops if kops else None,
+                    "note": "all-pairs work of the same jobs divided by the work the grid "
+                            "layout screens: an algorithmic ratio, not a roofline fraction"}}
+
+    # sort and 1-D search passes (HBM-bound): 32 N algorithmic bytes per 1-D
+    # marginal (8 N keys read, 8 N sorted keys written, 8 N eps read, 8 N
+    # counts written), over the radix sort's and the 1-D counts' event times
+    n1d = sum(2 if kind == "mi" else 1 for kind, _ in work)
+    sort_ms, c1_ms = phases.get("sort_radix", 0.0), phases.get("count_1d", 0.0)
+    ss_bytes = 32.0 * args.n * n1d
+    hbm = peaks.get("hbm_gbs")
+    ss_gbs = ss_bytes / ((sort_ms + c1_ms) / 1000.0) / 1e9 if sort_ms + c1_ms > 0 else 0.0
+    roofline_sort = {"bound": "hbm", "kernels": "radix sort (histogram, scan, scatter) + "
+                                                "sorted_jobs_kernel 1-D counts",
+                     "marginals_1d": n1d, "algorithmic_bytes": ss_bytes,
+                     "sort_ms": sort_ms, "count_1d_ms": c1_ms,
+                     "achieved": ss_gbs, "peak": hbm, "unit": "GB/s",
+                     "frac": ss_gbs / hbm if hbm else None,
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs" if hbm else "absent",
+                     "sorted_segments": work_stats.get("sort_segments"),
+                     "sorted_keys": work_stats.get("sort_keys")}
 
     ms_dev = dev_ms / args.steps
     ms_e2e = e2e_ms / args.steps
@@ -438,44 +543,61 @@ def main():
 
     plain = None
     if not args.no_plain:
-        # the plain comparator: all-FP64 distances, one task per call
+        # the plain comparator: all-FP64 distances, one task per call; and the
+        # same arithmetic batched, which splits the speed-up into its batching
+        # and its FP32-screen parts
         def step_plain():
             for t in dev_tasks:
                 N.run_tasks([t], flags=N.INPUT_DEVICE | N.PLAIN_FP64, device=dev)
+
+        def step_plain_batched():
+            N.run_tasks(dev_tasks, flags=N.INPUT_DEVICE | N.PLAIN_FP64, device=dev)
+        psteps = max(args.plain_steps, 1)
         step_plain()
-        p_ms, _ = timed_steps(step_plain, 1, torch, flush_buf)
+        _, p_per = timed_steps(step_plain, psteps, torch, flush_buf)
+        step_plain_batched()
+        _, pb_per = timed_steps(step_plain_batched, psteps, torch, flush_buf)
+        p_ms, pb_ms = statistics.median(p_per), statistics.median(pb_per)
         plain = {"value": ntask / (p_ms / 1000.0), "unit": UNIT, "ms_per_step": p_ms,
-                 "form": "all-FP64 distances, one task per egb_run_batch call, device inputs"}
+                 "steps": psteps, "per_step_ms": p_per, "statistic": "median",
+                 "form": "all-FP64 distances, one task per egb_run_batch call, device inputs",
+                 "batched": {"value": ntask / (pb_ms / 1000.0), "ms_per_step": pb_ms,
+                             "per_step_ms": pb_per,
+                             "form": "all-FP64 distances, the five tasks in one batch"}}
 
     if rank != 0:
         if world > 1:
             torch.distributed.destroy_process_group()
         return
 
+    parity = parity_check(N, dev_tasks, work, args, dev) if rank == 0 else None
+
     cpu = None
     if not args.no_cpu:
-        cpu = cpu_baseline(work, args.k, args.cpu_fraction, os.cpu_count())
+        cpu = cpu_baseline(work, args.k, args.cpu_slices, args.cpu_nslices, os.cpu_count())
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_dev, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
-        "config": {"workload": "4x bivariate Gaussian KSG MI (rho 0/.3/.6/.9) + 1x 3-D Gaussian CMI "
-                               "(corr .5/.4/.4), float64, seeded",
-                   "n": args.n, "k": args.k, "tasks_per_step": ntask,
-                   "l2": "flushed between timed steps (512 MB write)",
-                   "value_path": "device-resident columns, CUDA graph replay of the batch",
-                   "e2e_path": "pinned host columns through egb_run_batch, planned every step"},
+        "config": config_of(args, ntask),
+        "paths": {"value": "device-resident columns, CUDA graph replay of the batch",
+                  "e2e": "pinned host columns through egb_run_batch, planned every step"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": ms_e2e},
         "gpu_launches": work_stats.get("kernel_launches"),
         "roofline": roofline,
+        "roofline_sort": roofline_sort,
+        "parity": parity,
         "phases_ms": phases,
         "work": work_stats,
         "estimates": [r.value for r in res],
         "clocks": clocks,
         "plain": plain,
         "speedup_vs_plain": (value / plain["value"]) if plain else None,
+        "speedup_split": ({"batching": plain["ms_per_step"] / plain["batched"]["ms_per_step"],
+                           "fp32_screen": plain["batched"]["ms_per_step"] / ms_dev}
+                          if plain else None),
         "cpu_baseline": cpu,
         "per_step_ms": per,
     }

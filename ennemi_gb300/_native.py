@@ -52,7 +52,7 @@ def policy_index(search: int, d: int, K: int, length: int) -> int:
 
 
 PHASES = ("upload", "prepare", "sort", "knn", "counts", "combine", "total",
-          "knn_tile", "knn_defer", "count_tile", "count_defer")
+          "knn_tile", "knn_defer", "count_tile", "count_defer", "sort_radix", "count_1d")
 
 
 class EgbColumn(ctypes.Structure):
@@ -122,6 +122,8 @@ def load():
         lib.egb_get_policy.restype = ctypes.c_int
         lib.egb_device_info.argtypes = [vp, ctypes.c_char_p, i32, ctypes.POINTER(i32)]
         lib.egb_device_info.restype = ctypes.c_int
+        lib.egb_debug_inject_device_error.argtypes = [vp, ctypes.c_uint32]
+        lib.egb_debug_inject_device_error.restype = ctypes.c_int
         lib.egb_version.argtypes = []
         lib.egb_version.restype = ctypes.c_char_p
         _lib = lib
@@ -165,7 +167,8 @@ class Context:
     def stats(self) -> dict:
         names = ("knn_tile_pairs", "knn_defer_pairs", "knn_deferred",
                  "count_tile_pairs", "count_defer_pairs", "count_deferred",
-                 "knn_tile_ops", "count_tile_ops", "kernel_launches")
+                 "knn_tile_ops", "count_tile_ops", "kernel_launches", "sort_keys", "sort_segments",
+                 "planned", "graph")
         buf = (ctypes.c_int64 * len(names))()
         n = self.lib.egb_last_stats(self.h, buf, len(names))
         return {names[i]: int(buf[i]) for i in range(n)}
@@ -195,6 +198,13 @@ class Context:
             self.check(self.lib.egb_set_noise(
                 self.h, v.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), len(v)), "egb_set_noise")
             self.noise_len = len(v)
+
+    def inject_device_error(self, word: int) -> None:
+        """Test hook: the next batch starts with `word` in its device error
+        word and reports it (egb_debug_inject_device_error)."""
+        with self.lock:
+            self.check(self.lib.egb_debug_inject_device_error(self.h, int(word)),
+                       "egb_debug_inject_device_error")
 
     def get_policy(self) -> np.ndarray:
         m = np.empty(POLICY_ENTRIES, dtype=np.int8)

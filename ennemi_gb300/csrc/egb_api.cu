@@ -55,8 +55,9 @@ constexpr int KIND_KNN_ONLY = 100;    // egb_knn_eps
 constexpr int KIND_COUNT_ONLY = 101;  // egb_ball_count
 constexpr int SLAB_MIN = 4096;        // shorter multi-D segments use brute force
 constexpr int NPHASE = 7;
-constexpr int NKTIME = 4;   // kNN tile, kNN deferred, count tile, count deferred
-constexpr int NSTATS = 9;
+constexpr int NKTIME = 6;   // kNN tile, kNN deferred, count tile, count deferred,
+                            // radix sort, 1-D counts
+constexpr int NSTATS = 13;
 
 // Digamma of a positive integer with the reference's formula
 // (ennemi/_entropy_estimators.py:341-348): the SciPy constant for psi(1),
@@ -127,6 +128,7 @@ struct ReplayState {
   size_t pin_rb = 0, pin_zr = 0, zr_stats = 0, zr_err = 0, zr_zero = 0;
   size_t tab_bytes = 0, zr_bytes = 0;
   int nchunks = 0;
+  int64_t sort_keys = 0, sort_segs = 0;  // keys and segments of the batch's radix sort
 };
 
 }  // namespace
@@ -167,6 +169,8 @@ struct egb_ctx {
   // kNN: tile pairs, deferred pairs, deferred queries; counts: the same;
   // [6] kNN tile ops, [7] count tile ops ((2d+1) per pair); [8] kernels launched
   int64_t stats[NSTATS] = {};
+  // egb_debug_inject_device_error: error word the next batch starts with
+  uint32_t inject_err = 0;
   // internals of the last batch (egb_fetch)
   bool kept = false;
   std::vector<TaskPlan> keep;
@@ -254,6 +258,8 @@ int finish_batch(egb_ctx* ctx, const ReplayState& R, const char* H, int64_t laun
       ctx->stats[R.groups[g].is_knn ? 6 : 7] += (int64_t)st4[4 * g] * (2 * R.groups[g].d + 1);
     }
     ctx->stats[8] = launches;
+    ctx->stats[9] = R.sort_keys;
+    ctx->stats[10] = R.sort_segs;
   }
   const uint32_t dev_err = *(const uint32_t*)(H + R.pin_zr + R.zr_err);
   if (dev_err) {
@@ -369,16 +375,23 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   const bool timing = (flags & EGB_TIMING) != 0;
   cudaStream_t st = ctx->stream;
   const long long launches0 = g_launches.load();
+  // an injected error word (test hook) is consumed by this batch, which is
+  // then planned and issued directly, never replayed from a graph
+  const uint32_t inject = ctx->inject_err;
+  ctx->inject_err = 0;
   // an unchanged device-resident batch replays its graph without planning
   const uint64_t rkey = replay_key(ctx, tasks, ntasks, flags, count_radius);
-  if (rkey && ctx->replay.valid && ctx->replay.key == rkey && ctx->graph_exec) {
+  if (rkey && !inject && ctx->replay.valid && ctx->replay.key == rkey && ctx->graph_exec) {
     ctx->kept = false;
     ctx->keep.clear();
     EGB_CUDA(cudaGraphLaunch(ctx->graph_exec, st));
     EGB_CUDA(cudaStreamSynchronize(st));
     ctx->h2d_bytes = (int64_t)ctx->replay.tab_bytes;
     ctx->d2h_bytes = (int64_t)(ctx->replay.zr_bytes + sizeof(double) * (size_t)ctx->replay.nchunks);
-    return finish_batch(ctx, ctx->replay, (const char*)ctx->pinned, ctx->graph_launches, results);
+    const int rc_rep = finish_batch(ctx, ctx->replay, (const char*)ctx->pinned, ctx->graph_launches, results);
+    ctx->stats[11] = 0;  // not planned
+    ctx->stats[12] = 1;  // graph launched
+    return rc_rep;
   }
   ctx->replay.valid = false;  // this batch rewrites the pinned tables
   ctx->kept = false;
@@ -1217,6 +1230,9 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   auto enqueue = [&]() -> int {
   EGB_CUDA(cudaMemcpyAsync(A + off_tab, H, tab_bytes, cudaMemcpyHostToDevice, st));
   EGB_CUDA(cudaMemsetAsync(A + off_zr, 0, zr_bytes, st));
+  if (inject)  // the device error word as if a kernel had set these bits
+    for (int i = 0; i < 4; ++i)
+      EGB_CUDA(cudaMemsetAsync((char*)err_d + i, (int)((inject >> (8 * i)) & 0xffu), 1, st));
   if (dev_in)
     for (int t = 0; t < ntasks; ++t)
       if (P[(size_t)t].kind == KIND_COUNT_ONLY)
@@ -1247,9 +1263,11 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
 
   uint64_t* keys = (uint64_t*)(A + off_keys_a);
   int32_t* vals = (int32_t*)(A + off_vals_a);
+  if (timing) EGB_CUDA(cudaEventRecord(ctx->kev[8], st));
   launch_sort(tasks_d, (const SortSeg*)dtab(tab_segs), (const int32_t*)dtab(tab_blkseg), nblk_sort,
               keys, (uint64_t*)(A + off_keys_b), vals, (int32_t*)(A + off_vals_b),
               (uint32_t*)(A + off_hist), (uint32_t*)(A + off_scan), st);
+  if (timing) EGB_CUDA(cudaEventRecord(ctx->kev[9], st));
   launch_materialize(tasks_d, (const JobDev*)dtab(tab_jobs), (int)jobs.size(), vals,
                      (const SortSeg*)dtab(tab_segs), max_lds, st);
   if (!grid_jobs.empty()) {
@@ -1321,7 +1339,9 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   if (timing) EGB_CUDA(cudaEventRecord(ctx->ev[4], st));
 
   launch_radius(tasks_d, ntasks, max_ld, st);
+  if (timing) EGB_CUDA(cudaEventRecord(ctx->kev[10], st));
   launch_sorted_jobs(tasks_d, (const SortedJob*)dtab(tab_sjc), (int)sj_cnt.size(), blk_cnt, keys, vals, st);
+  if (timing) EGB_CUDA(cudaEventRecord(ctx->kev[11], st));
   if (timing) EGB_CUDA(cudaEventRecord(ctx->kev[4], st));
   for (size_t g = 0; g < groups.size(); ++g) {
     Group& G = groups[g];
@@ -1368,7 +1388,7 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   return EGB_OK;
   };
 
-  const bool use_graph = (flags & EGB_GRAPH) != 0 && !timing;
+  const bool use_graph = (flags & EGB_GRAPH) != 0 && !timing && !inject;
   if (use_graph) {
     // signature of the batch: the descriptor blob (all device pointers,
     // sizes, job tables) plus the arena, pinned buffer and flags
@@ -1439,9 +1459,13 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   R.nchunks = nchunks;
   R.tab_bytes = tab_bytes;
   R.zr_bytes = zr_bytes;
+  R.sort_keys = sort_total;
+  R.sort_segs = (int64_t)segs.size();
   const int64_t launches =
       use_graph ? (int64_t)ctx->graph_launches : (int64_t)(g_launches.load() - launches0);
   const int rc_fin = finish_batch(ctx, R, H, launches, results);
+  ctx->stats[11] = 1;
+  ctx->stats[12] = use_graph ? 1 : 0;
   if (rc_fin != EGB_OK) return rc_fin;
   if (flags & EGB_KEEP_INTERNALS) {
     ctx->keep = std::move(R.P);
@@ -1636,6 +1660,12 @@ int egb_get_policy(const egb_ctx* ctx, int8_t* modes, int32_t n) {
   const int m = std::min<int>(n, EGB_POLICY_ENTRIES);
   std::memcpy(modes, ctx->policy, (size_t)m);
   return m;
+}
+
+int egb_debug_inject_device_error(egb_ctx* ctx, uint32_t word) {
+  if (!ctx) return EGB_ERR_ARG;
+  ctx->inject_err = word;
+  return EGB_OK;
 }
 
 int egb_timings(const egb_ctx* ctx, double* ms, int32_t max) {

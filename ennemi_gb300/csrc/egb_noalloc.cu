@@ -140,6 +140,15 @@ extern "C" int egb_knn_eps_noalloc(const double* points, int64_t n, int32_t d, i
   const Layout L = layout_for(n, d, nitems);
   if (L.end > sizeof(g_noalloc_scratch)) return EGB_ERR_ARG;
 
+  // An error the caller left pending stays pending: only a different error
+  // raised by this call's own launches is consumed and reported.
+  const cudaError_t prior = cudaPeekAtLastError();
+  auto own_error = [prior]() {
+    const cudaError_t now = cudaPeekAtLastError();
+    if (now == cudaSuccess || now == prior) return false;
+    cudaGetLastError();
+    return true;
+  };
   int blocks = (int)((n + 255) / 256);
   if (blocks > 256) blocks = 256;
   noalloc_setup_kernel<<<blocks, 256, 0, st>>>(scratch, L, points, n, d, K, qb, nitems, eps);
@@ -148,11 +157,11 @@ extern "C" int egb_knn_eps_noalloc(const double* points, int64_t n, int32_t d, i
                        reinterpret_cast<const egb::WorkItem*>(scratch + L.items), nitems, kclass,
                        dclass, /*plain=*/1, /*slab=*/0, d, reinterpret_cast<int*>(cnt),
                        reinterpret_cast<uint32_t*>(cnt + 4), nullptr, nullptr, g_num_sms[dev], st);
-  if (cudaGetLastError() != cudaSuccess) return EGB_ERR_CUDA;
+  if (own_error()) return EGB_ERR_CUDA;
   uint32_t err = 0;
   if (cudaMemcpyAsync(&err, cnt + 4, sizeof(err), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
       cudaStreamSynchronize(st) != cudaSuccess) {
-    cudaGetLastError();
+    own_error();
     return EGB_ERR_CUDA;
   }
   return err ? EGB_ERR_DEVICE : EGB_OK;

@@ -1,6 +1,7 @@
 """Seeded synthetic workloads with the shapes of the large-sample benchmark
 configurations (no dataset involved).  Used by bench.py and the tests.
 
+plain_ksg(n)         one bivariate Gaussian, rho = .6 (the single estimate_mi case)
 large_sample(n)      bivariate Gaussians rho in {0, .3, .6, .9} and a trivariate
                      Gaussian (corr(x,y) = .5, corr(x,z) = corr(y,z) = .4)
 lagged_ar(length)    16 coupled AR(1) series (phi = .8, coupling .3 from the
@@ -17,6 +18,8 @@ semidiscrete_mix(n)  x of dimension 1-4 from 3-component Gaussian mixtures,
 
 from __future__ import annotations
 
+import math
+
 import numpy as np
 from scipy.signal import lfilter
 
@@ -24,15 +27,58 @@ RHOS = (0.0, 0.3, 0.6, 0.9)
 CMI_COV = [[1, 0.5, 0.4], [0.5, 1, 0.4], [0.4, 0.4, 1]]
 
 
+def _cholesky(cov):
+    """Lower Cholesky factor of a small covariance matrix, in Python floats
+    (every operation a correctly rounded IEEE-754 one)."""
+    d = len(cov)
+    L = [[0.0] * d for _ in range(d)]
+    for i in range(d):
+        for j in range(i + 1):
+            s = float(cov[i][j])
+            for m in range(j):
+                s -= L[i][m] * L[j][m]
+            L[i][j] = math.sqrt(s) if i == j else s / L[j][j]
+    return L
+
+
+def gaussian(rng, cov, n: int):
+    """n draws of N(0, cov) as a list of contiguous float64 columns.
+
+    Column i is sum_j L[i][j] * z_j over j <= i, left to right, with z the
+    generator's standard normals (n x d, row-major) and L the Cholesky factor
+    of ``_cholesky``.  Only elementwise products and sums of NumPy arrays
+    are used, each rounded once, so the columns are the same bits on every
+    IEEE-754 platform (``multivariate_normal`` goes through a LAPACK
+    factorisation and a BLAS product, whose last bits differ between x86-64
+    and AArch64 builds).
+    """
+    L = _cholesky(cov)
+    z = rng.standard_normal((n, len(cov)))
+    cols = []
+    for i in range(len(cov)):
+        acc = None
+        for j in range(i + 1):
+            if L[i][j] == 0.0:
+                continue
+            term = L[i][j] * z[:, j]
+            acc = term if acc is None else acc + term
+        cols.append(np.ascontiguousarray(acc if acc is not None else np.zeros(n)))
+    return cols
+
+
+def plain_ksg(n: int = 10_000, seed: int = 0, rho: float = 0.6):
+    """(x, y): the bivariate Gaussian of the single ``estimate_mi(y, x)`` case."""
+    x, y = gaussian(np.random.default_rng(seed), [[1.0, rho], [rho, 1.0]], n)
+    return x, y
+
+
 def large_sample(n: int = 1_000_000, seed: int = 0):
     """[(kind, [columns])]: four 'mi' (x, y) tasks and one 'cmi' (x, y, z)."""
     rng = np.random.default_rng(seed)
     work = []
     for rho in RHOS:
-        d = rng.multivariate_normal([0, 0], [[1, rho], [rho, 1]], size=n)
-        work.append(("mi", [np.ascontiguousarray(d[:, 0]), np.ascontiguousarray(d[:, 1])]))
-    d = rng.multivariate_normal([0, 0, 0], CMI_COV, size=n)
-    work.append(("cmi", [np.ascontiguousarray(d[:, c]) for c in range(3)]))
+        work.append(("mi", gaussian(rng, [[1.0, rho], [rho, 1.0]], n)))
+    work.append(("cmi", gaussian(rng, CMI_COV, n)))
     return work
 
 

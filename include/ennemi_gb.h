@@ -205,7 +205,9 @@ int egb_ball_count(egb_ctx* ctx, const double* points, int64_t n, int32_t d,
  * [0] upload, [1] gather+prepare, [2] sort+materialise, [3] kNN, [4] counts,
  * [5] combine+download, [6] whole batch; then the multi-D kernels alone:
  * [7] kNN tile kernels, [8] kNN deferred-query kernels, [9] count tile
- * kernels, [10] count deferred-query kernels.  Returns the number written.
+ * kernels, [10] count deferred-query kernels; then [11] the radix sort of
+ * the batch's columns (part of [2]) and [12] the 1-D counts on the sorted
+ * columns (part of [4]).  Returns the number written.
  */
 int egb_timings(const egb_ctx* ctx, double* ms, int32_t max);
 
@@ -217,8 +219,10 @@ int egb_last_transfer(const egb_ctx* ctx, int64_t* h2d_bytes, int64_t* d2h_bytes
  * tile work items, [1] kNN pairs screened for deferred queries, [2] kNN
  * queries deferred, [3..5] the same for the multi-D counts, [6] / [7]
  * algorithmic operations of the kNN / count tile kernels ((2d+1) per pair:
- * d differences, d max-of-abs, one compare), [8] kernels launched.  Returns
- * the number written. */
+ * d differences, d max-of-abs, one compare), [8] kernels launched, [9] keys
+ * and [10] segments of the batch's radix sort, [11] 1 if the batch was
+ * planned on the host (0: an EGB_GRAPH replay without planning), [12] 1 if
+ * its device work ran as a CUDA graph.  Returns the number written. */
 int egb_last_stats(const egb_ctx* ctx, int64_t* out, int32_t max);
 
 /*
@@ -295,7 +299,11 @@ int egb_set_noise(egb_ctx* ctx, const double* noise, int64_t len);
  *
  * The first call on a device looks up the device address of the scratch
  * array (cudaGetSymbolAddress) with that device current; make that first
- * call before any stream capture.  Every call on a device shares the one
+ * call before any stream capture.  The address is kept for the life of the
+ * process: after cudaDeviceReset() on a device, do not call this entry point
+ * on that device again.  A CUDA error that the caller left pending before
+ * the call stays pending; EGB_ERR_CUDA reports only an error of this call's
+ * own launches or copies.  Every call on a device shares the one
  * scratch array: calls that overlap on the GPU (different streams, different
  * host threads) race and must be serialised by the caller.
  */
@@ -304,6 +312,17 @@ int egb_set_noise(egb_ctx* ctx, const double* noise, int64_t len);
 #define EGB_NOALLOC_SCRATCH_BYTES (1152u * 1024u)
 int egb_knn_eps_noalloc(const double* points, int64_t n, int32_t d, int32_t k, double* eps,
                         void* stream);
+
+/*
+ * Test hook for the device-error path: the next egb_run_batch on this context
+ * starts with `word` already in its device error word, as though one of its
+ * kernels had reported it (bit 0: a bounded wait gave up; bit 1: an index
+ * guard tripped).  That batch runs its kernels as usual, without a CUDA
+ * graph, and returns EGB_ERR_DEVICE with the message a real report gives;
+ * later batches start clean.  No kernel is made to fail.  It has no
+ * counterpart in the reference, whose code never runs on a device.
+ */
+int egb_debug_inject_device_error(egb_ctx* ctx, uint32_t word);
 
 /* Name of the context's CUDA device (cudaDeviceProp::name) into name[0 ..
  * len), NUL-terminated; *sms = its multiprocessor count.  Returns 0. */

@@ -14,10 +14,15 @@ builds, the same ``query(.., k=[k+1], p=inf)`` for eps, the same
 the same digamma combination.  Those steps must be alike to measure the same
 algorithm; the code around them is written for this project.
 
-``sample_rate`` times a bounded sample: the trees are built over all N points
-and only a subset of query points is searched and counted, spread over a
-thread pool (cKDTree releases the GIL).  The per-point cost is scaled to the
-full task to give estimates per second.
+``SlicedBatch`` times a batch the way the reference's driver runs it: the
+tasks go to a thread pool of ``max_threads`` workers (_driver.py:736-785;
+cKDTree releases the GIL), one task per worker, each task single-threaded.
+Each task builds its trees over all N points once; its query points are
+then processed in ``nslices`` contiguous slices, one slice of every task per
+step, so that the steps together search and count every query point exactly
+once.  The time of the whole batch is the tree builds plus the sum of the
+steps: a measurement, not an extrapolation.  ``sample_rate`` times a few
+slices only and scales them to the batch (the bounded CPU baseline).
 """
 
 from __future__ import annotations
@@ -75,18 +80,19 @@ def entropy(x, k: int = 3) -> float:
 
 
 # --------------------------------------------------------------------------
-# Bounded-sample timing (bench.py reference arm and cpu_baseline)
+# Timing (bench.py reference arm and cpu_baseline)
 # --------------------------------------------------------------------------
 
 def _ksg_point_kernel(xs, ys, k):
     """Trees over all N points; returns a function that processes query rows."""
     joint = _cols(xs, ys)
     tj, tx, ty = cKDTree(joint), cKDTree(_cols(xs)), cKDTree(_cols(ys))
+    xc, yc = _cols(xs), _cols(ys)
 
-    def run(idx: np.ndarray) -> float:
-        r = tj.query(joint[idx], k=[k + 1], p=np.inf)[0].ravel() - RADIUS_SHRINK
-        nx = tx.query_ball_point(_cols(xs[idx]), r, p=np.inf, return_length=True)
-        ny = ty.query_ball_point(_cols(ys[idx]), r, p=np.inf, return_length=True)
+    def run(lo: int, hi: int) -> float:
+        r = tj.query(joint[lo:hi], k=[k + 1], p=np.inf)[0].ravel() - RADIUS_SHRINK
+        nx = tx.query_ball_point(xc[lo:hi], r, p=np.inf, return_length=True)
+        ny = ty.query_ball_point(yc[lo:hi], r, p=np.inf, return_length=True)
         return float(np.sum(psi(nx) + psi(ny)))
     return run
 
@@ -96,53 +102,95 @@ def _cmi_point_kernel(xs, ys, zs, k):
     xz, yz, z = _cols(xs, zs), _cols(ys, zs), _cols(zs)
     tj, txz, tyz, tz = cKDTree(joint), cKDTree(xz), cKDTree(yz), cKDTree(z)
 
-    def run(idx: np.ndarray) -> float:
-        r = tj.query(joint[idx], k=[k + 1], p=np.inf)[0].ravel() - RADIUS_SHRINK
-        a = txz.query_ball_point(xz[idx], r, p=np.inf, return_length=True)
-        b = tyz.query_ball_point(yz[idx], r, p=np.inf, return_length=True)
-        c = tz.query_ball_point(z[idx], r, p=np.inf, return_length=True)
+    def run(lo: int, hi: int) -> float:
+        r = tj.query(joint[lo:hi], k=[k + 1], p=np.inf)[0].ravel() - RADIUS_SHRINK
+        a = txz.query_ball_point(xz[lo:hi], r, p=np.inf, return_length=True)
+        b = tyz.query_ball_point(yz[lo:hi], r, p=np.inf, return_length=True)
+        c = tz.query_ball_point(z[lo:hi], r, p=np.inf, return_length=True)
         return float(np.sum(psi(a) + psi(b) - psi(c)))
     return run
 
 
-def sample_rate(tasks: List[Tuple[str, tuple]], k: int, fraction: float,
-                threads: int | None = None, seed: int = 0) -> Dict[str, float]:
-    """Time the reference algorithm on a bounded sample of a batch of tasks.
+def _builder(kind: str, cols, k: int):
+    if kind == "mi":
+        return lambda: _ksg_point_kernel(cols[0], cols[1], k)
+    if kind == "cmi":
+        return lambda: _cmi_point_kernel(cols[0], cols[1], cols[2], k)
+    raise ValueError(kind)
 
-    tasks: list of ("mi", (x, y)) or ("cmi", (x, y, z)) with float64 columns.
-    For each task the trees are built over all N points (timed in full) and a
-    random ``fraction`` of the query points is searched and counted on a
-    thread pool of ``threads`` workers.  Returns the measured seconds and the
-    extrapolated seconds for the whole batch (tree builds + queries / fraction).
+
+class SlicedBatch:
+    """A batch of ("mi", (x, y)) / ("cmi", (x, y, z)) tasks, timed in steps.
+
+    ``build()`` builds every task's trees on the pool (one task per worker)
+    and returns its wall time; ``step(s)`` processes query slice s of every
+    task on the pool and returns its wall time.  ``task_seconds`` holds each
+    task's own time (its thread's work), whose sum is what the reference's
+    max_threads=1 path would take.
     """
-    threads = threads or os.cpu_count() or 1
-    rng = np.random.default_rng(seed)
-    build_s = 0.0
-    query_s = 0.0
-    sampled = 0
-    total = 0
-    with concurrent.futures.ThreadPoolExecutor(threads) as pool:
-        for kind, cols in tasks:
+
+    def __init__(self, tasks: List[Tuple[str, tuple]], k: int, nslices: int,
+                 threads: int | None = None):
+        self.tasks = tasks
+        self.k = k
+        self.nslices = nslices
+        self.threads = threads or os.cpu_count() or 1
+        self.pool = concurrent.futures.ThreadPoolExecutor(self.threads)
+        self.runs: List[Callable[[int, int], float]] = []
+        self.task_seconds = [0.0] * len(tasks)
+        self.term_sums = [0.0] * len(tasks)
+
+    def close(self):
+        self.pool.shutdown()
+
+    def _timed(self, t: int, fn):
+        t0 = time.perf_counter()
+        out = fn()
+        self.task_seconds[t] += time.perf_counter() - t0
+        return out
+
+    def build(self) -> float:
+        t0 = time.perf_counter()
+        futs = [self.pool.submit(self._timed, t, _builder(kind, cols, self.k))
+                for t, (kind, cols) in enumerate(self.tasks)]
+        self.runs = [f.result() for f in futs]
+        return time.perf_counter() - t0
+
+    def step(self, s: int) -> float:
+        t0 = time.perf_counter()
+        futs = []
+        for t, (kind, cols) in enumerate(self.tasks):
             n = len(cols[0])
-            t0 = time.perf_counter()
-            run: Callable[[np.ndarray], float]
+            lo, hi = n * s // self.nslices, n * (s + 1) // self.nslices
+            futs.append(self.pool.submit(self._timed, t, lambda r=self.runs[t], a=lo, b=hi: r(a, b)))
+        for t, f in enumerate(futs):
+            self.term_sums[t] += f.result()
+        return time.perf_counter() - t0
+
+    def estimates(self) -> List[float]:
+        """The estimates once every slice has run (the reference's formulas)."""
+        out = []
+        for (kind, cols), ts in zip(self.tasks, self.term_sums):
+            n = len(cols[0])
             if kind == "mi":
-                run = _ksg_point_kernel(cols[0], cols[1], k)
-            elif kind == "cmi":
-                run = _cmi_point_kernel(cols[0], cols[1], cols[2], k)
+                out.append(float(psi(n) + psi(self.k) - ts / n))
             else:
-                raise ValueError(kind)
-            t1 = time.perf_counter()
-            m = max(threads, int(round(n * fraction)))
-            idx = np.sort(rng.choice(n, size=min(m, n), replace=False))
-            chunks = np.array_split(idx, threads)
-            list(pool.map(run, chunks))
-            t2 = time.perf_counter()
-            build_s += t1 - t0
-            query_s += t2 - t1
-            sampled += len(idx)
-            total += n
-    frac = sampled / total
-    return {"build_s": build_s, "query_s": query_s, "measured_s": build_s + query_s,
-            "extrapolated_s": build_s + query_s / frac, "fraction": frac,
-            "threads": threads, "points_sampled": sampled}
+                out.append(float(psi(self.k) - ts / n))
+        return out
+
+
+def sample_rate(tasks: List[Tuple[str, tuple]], k: int, slices: int, nslices: int,
+                threads: int | None = None) -> Dict[str, float]:
+    """Time the reference algorithm on a bounded sample of a batch: the tree
+    builds in full and ``slices`` of ``nslices`` query slices of every task,
+    tasks on a pool as the reference's driver runs them.  Returns the measured
+    seconds and the batch time scaled from them (builds + mean step x nslices)."""
+    b = SlicedBatch(tasks, k, nslices, threads)
+    try:
+        build_s = b.build()
+        steps = [b.step(s) for s in range(slices)]
+    finally:
+        b.close()
+    return {"build_s": build_s, "step_s": steps, "measured_s": build_s + sum(steps),
+            "extrapolated_s": build_s + sum(steps) / len(steps) * nslices,
+            "fraction": slices / nslices, "threads": b.threads}

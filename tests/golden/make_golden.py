@@ -1,10 +1,14 @@
 """Generate golden vectors from the live reference (ennemi + scipy cKDTree).
 
-Run in a checkout where the reference package is importable, e.g.
+Run in a checkout where the reference package is importable, giving the
+directory that holds its ``ennemi`` package:
 
-    python tests/golden/make_golden.py --reference /root/reference
+    python tests/golden/make_golden.py --reference <path to the ennemi checkout>
+    python tests/golden/make_golden.py --reference <...> --headline
 
-It writes ``tests/golden/golden_estimators.npz`` and
+(or set ENNEMI_REFERENCE instead of passing --reference).
+
+The first form writes ``tests/golden/golden_estimators.npz`` and
 ``tests/golden/golden_driver.npz``.  Inputs are seeded synthetic arrays; the
 outputs are
 
@@ -17,6 +21,22 @@ outputs are
 The fixtures are small (N <= 3000) so that the CPU oracle and the GPU
 parity tests can use them directly.  Nothing at test time reads the
 reference: only these committed files.
+
+``--headline`` writes ``tests/golden/golden_headline.json`` for the two
+headline configurations, too large to store as arrays:
+
+* the single ``estimate_mi(y, x)`` of a bivariate Gaussian (rho = 0.6,
+  N = 10,000, k = 3, seed 0) through the reference's public path with its
+  preprocessing;
+* the large-sample batch (four bivariate Gaussian KSG MI, rho = 0, .3, .6,
+  .9, and one trivariate Gaussian conditional MI; N = 1,000,000, k = 3,
+  seed 0) through the reference's estimator functions.
+
+For each task it records the reference's estimate, and SHA-256 digests of
+the inputs, of eps (float64 little-endian) and of every neighbour-count
+array (int64 little-endian), with a few plain sums for diagnosis.  The
+inputs come from ``ennemi_gb300.synthetic``, whose generator gives the same
+bits on x86-64 and AArch64, so the digests can be checked on either.
 """
 
 from __future__ import annotations
@@ -207,12 +227,100 @@ def _driver_cases():
     yield "drv_entropy_mask", "estimate_entropy", (ar[:, 0],), dict(mask=mask)
 
 
+def digest(arr, dtype) -> str:
+    """SHA-256 of the array's values as little-endian `dtype` bytes."""
+    import hashlib
+    return hashlib.sha256(np.ascontiguousarray(arr, dtype=dtype).tobytes()).hexdigest()
+
+
+def _summary(name, arr):
+    a = np.asarray(arr)
+    if name == "eps":
+        return {"eps": digest(a, "<f8"), "eps_sum": float(np.sum(a))}
+    return {name: digest(a, "<i8"), name + "_sum": int(np.sum(a.astype(np.int64)))}
+
+
+def headline(args) -> None:
+    """golden_headline.json: the two headline configurations (see the module
+    docstring)."""
+    import concurrent.futures
+    import json
+    import warnings
+    root = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    sys.path.insert(0, root)
+    import ennemi
+    from ennemi import _driver as rd
+    from ennemi import _entropy_estimators as ee
+    from scipy.spatial import cKDTree
+    from ennemi_gb300 import synthetic
+
+    out = {"generator": "ennemi_gb300.synthetic (plain_ksg, large_sample)",
+           "reference": f"ennemi {getattr(ennemi, '__version__', '?')} with scipy cKDTree "
+                        f"{__import__('scipy').__version__}, numpy {np.__version__}"}
+
+    # the single estimate_mi(y, x) through the public path
+    n1, k = 10_000, 3
+    x, y = synthetic.plain_ksg(n1, 0, 0.6)
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        value = float(np.asarray(ennemi.estimate_mi(y, x, k=k)).item())
+        xs, ys, _ = rd._rescale_data(x, y, None, False, False)
+    inter = _internals("mi", k, dict(x=xs, y=ys), cKDTree)
+    c1 = {"n": n1, "k": k, "rho": 0.6, "seed": 0, "call": "estimate_mi(y, x, k=3)",
+          "value": value, "analytic": -0.5 * float(np.log(1 - 0.36)),
+          "inputs": {"x": digest(x, "<f8"), "y": digest(y, "<f8")},
+          "prepared": {"x": digest(xs, "<f8"), "y": digest(ys, "<f8")}}
+    for key, arr in inter.items():
+        c1.update(_summary(key, arr))
+    out["plain_ksg"] = c1
+    print("plain_ksg", value)
+
+    # the large-sample batch through the estimator functions
+    n2 = 1_000_000
+    work = synthetic.large_sample(n2, 0)
+
+    def one(item):
+        kind, cols = item
+        if kind == "mi":
+            val = float(ee._estimate_single_mi(cols[0], cols[1], k))
+            inter = _internals("mi", k, dict(x=cols[0], y=cols[1]), cKDTree)
+        else:
+            val = float(ee._estimate_conditional_mi(cols[0], cols[1], cols[2], k))
+            inter = _internals("cmi", k, dict(x=cols[0], y=cols[1], z=cols[2]), cKDTree)
+        rec = {"kind": kind, "value": val, "inputs": [digest(c, "<f8") for c in cols]}
+        for key, arr in inter.items():
+            rec.update(_summary(key, arr))
+        return rec
+
+    with concurrent.futures.ThreadPoolExecutor(len(work)) as pool:
+        tasks = list(pool.map(one, work))
+    for rho, t in zip(synthetic.RHOS, tasks):
+        t["rho"] = rho
+    tasks[-1]["cov"] = synthetic.CMI_COV
+    out["large_sample"] = {"n": n2, "k": k, "seed": 0, "tasks": tasks}
+    print("large_sample", [t["value"] for t in tasks])
+    path = os.path.join(args.out, "golden_headline.json")
+    with open(path, "w") as fh:
+        json.dump(out, fh, indent=1)
+        fh.write("\n")
+    print("wrote", path)
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=os.environ.get("ENNEMI_REFERENCE"),
+                    help="directory holding the reference's ennemi package "
+                         "(default: $ENNEMI_REFERENCE)")
     ap.add_argument("--out", default=os.path.dirname(os.path.abspath(__file__)))
+    ap.add_argument("--headline", action="store_true",
+                    help="write golden_headline.json (the two headline configurations)")
     args = ap.parse_args()
+    if not args.reference:
+        ap.error("--reference (or ENNEMI_REFERENCE) is required")
     sys.path.insert(0, args.reference)
+    if args.headline:
+        headline(args)
+        return
     import ennemi
     from ennemi import _entropy_estimators as ee
     from scipy.spatial import cKDTree

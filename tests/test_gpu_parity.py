@@ -216,18 +216,37 @@ def test_public_estimators_on_gpu():
 
 
 def test_graph_replay_matches_direct_launch():
+    """The streaming pattern: capture once, then refill the same device
+    buffers and replay without planning.  The expected values of both data
+    sets are computed first, by direct launches on other buffers, so that no
+    other batch runs on the context between the graph calls."""
     torch = pytest.importorskip("torch")
     rng = np.random.default_rng(21)
     n = 50000
-    cols = [torch.from_numpy(rng.normal(size=n)).cuda() for _ in range(3)]
-    tasks = [N.Task(N.MI, 3, [cols[0]], [cols[1]], n=n),
-             N.Task(N.CMI, 3, [cols[0]], [cols[1]], [cols[2]], n=n)]
-    direct = N.run_tasks(tasks, flags=N.INPUT_DEVICE)
-    first = N.run_tasks(tasks, flags=N.INPUT_DEVICE | N.GRAPH)   # captures
-    again = N.run_tasks(tasks, flags=N.INPUT_DEVICE | N.GRAPH)   # replays
-    assert np.array_equal(direct, first) and np.array_equal(direct, again)
-    # new data in the same buffers: the replayed graph reads them
-    cols[1].copy_(torch.from_numpy(0.7 * cols[0].cpu().numpy() + rng.normal(size=n)))
-    direct2 = N.run_tasks(tasks, flags=N.INPUT_DEVICE)
-    replay2 = N.run_tasks(tasks, flags=N.INPUT_DEVICE | N.GRAPH)
-    assert np.array_equal(direct2, replay2) and not np.array_equal(direct, direct2)
+    host_a = [rng.normal(size=n) for _ in range(3)]
+    host_b = [host_a[0], 0.7 * host_a[0] + rng.normal(size=n), host_a[2]]
+
+    def tasks_of(cols):
+        return [N.Task(N.MI, 3, [cols[0]], [cols[1]], n=n),
+                N.Task(N.CMI, 3, [cols[0]], [cols[1]], [cols[2]], n=n)]
+    ctx = N.context(0)
+    direct_a = N.run_tasks(tasks_of([torch.from_numpy(c).cuda() for c in host_a]), flags=N.INPUT_DEVICE)
+    direct_b = N.run_tasks(tasks_of([torch.from_numpy(c).cuda() for c in host_b]), flags=N.INPUT_DEVICE)
+    assert not np.array_equal(direct_a, direct_b)
+
+    cols = [torch.from_numpy(c).cuda() for c in host_a]
+    tasks = tasks_of(cols)
+    first = N.run_tasks(tasks, flags=N.INPUT_DEVICE | N.GRAPH)   # plans and captures
+    st = ctx.stats()
+    assert st["planned"] == 1 and st["graph"] == 1
+    again = N.run_tasks(tasks, flags=N.INPUT_DEVICE | N.GRAPH)   # replays, no planning
+    st = ctx.stats()
+    assert st["planned"] == 0 and st["graph"] == 1
+    assert np.array_equal(direct_a, first) and np.array_equal(direct_a, again)
+    # new data in the same buffers: the replay (still without planning) reads them
+    cols[1].copy_(torch.from_numpy(host_b[1]))
+    torch.cuda.synchronize()
+    replay_b = N.run_tasks(tasks, flags=N.INPUT_DEVICE | N.GRAPH)
+    st = ctx.stats()
+    assert st["planned"] == 0 and st["graph"] == 1
+    assert np.array_equal(direct_b, replay_b)
