@@ -35,10 +35,11 @@ FORCE_CTA_GRID = 1 << 7
 GRAPH = 1 << 8
 STAGE_HOST = 1 << 9
 RESCALE = 1 << 10
+FORCE_RANK = 1 << 11
 TASK_CONSTANT = 1        # egb_result.status: constant column under RESCALE
 
 # layout policy (include/ennemi_gb.h)
-MODE_AUTO, MODE_BRUTE, MODE_SLAB, MODE_GRID, MODE_WARP_GRID = -1, 0, 1, 2, 3
+MODE_AUTO, MODE_BRUTE, MODE_SLAB, MODE_GRID, MODE_WARP_GRID, MODE_RANK = -1, 0, 1, 2, 3, 4
 POLICY_SIZE_CLASSES = 32
 POLICY_ENTRIES = 2 * 4 * 4 * POLICY_SIZE_CLASSES
 

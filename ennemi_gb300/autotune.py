@@ -31,9 +31,9 @@ import numpy as np
 
 from . import _native as N
 
-MODES = (N.MODE_BRUTE, N.MODE_SLAB, N.MODE_GRID, N.MODE_WARP_GRID)
+MODES = (N.MODE_BRUTE, N.MODE_SLAB, N.MODE_GRID, N.MODE_WARP_GRID, N.MODE_RANK)
 MODE_NAMES = {N.MODE_AUTO: "auto", N.MODE_BRUTE: "brute", N.MODE_SLAB: "slab",
-              N.MODE_GRID: "grid", N.MODE_WARP_GRID: "warp_grid"}
+              N.MODE_GRID: "grid", N.MODE_WARP_GRID: "warp_grid", N.MODE_RANK: "rank"}
 K_OF_CLASS = (4, 8, 16, 32)   # K = k + 1 measured for each kNN K class
 CACHE_ENV = "ENNEMI_GB300_POLICY"
 
@@ -82,6 +82,8 @@ def _tune_key(ctx, key: Key, size_classes: Sequence[int], repeats: int,
     alive = list(MODES)
     if search == 0 and K > 8:
         alive.remove(N.MODE_WARP_GRID)     # the warp grid runs kNN only for K <= 8
+    if search == 0 or d != 2:
+        alive.remove(N.MODE_RANK)          # rank-space counts: d = 2 ball counts only
     out = {}
     for sc in sorted(size_classes):
         n = int(round(2 ** (sc + 0.5)))
@@ -222,7 +224,7 @@ def load(path: str) -> Optional[np.ndarray]:
     if doc.get("entries") != N.POLICY_ENTRIES or len(doc.get("modes", ())) != N.POLICY_ENTRIES:
         return None
     table = np.array(doc["modes"], dtype=np.int8)
-    if table.min() < N.MODE_AUTO or table.max() > N.MODE_WARP_GRID:
+    if table.min() < N.MODE_AUTO or table.max() > N.MODE_RANK:
         return None
     return table
 

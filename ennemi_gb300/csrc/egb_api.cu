@@ -372,6 +372,7 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   const bool force_slab = (flags & EGB_FORCE_SLAB) != 0 && !force_brute;
   const bool force_grid = (flags & EGB_FORCE_GRID) != 0 && !force_brute && !force_slab;
   const bool cta_grid = (flags & EGB_FORCE_CTA_GRID) != 0;  // grid without the warp form
+  const bool force_rank = (flags & EGB_FORCE_RANK) != 0 && !plain;
   const bool timing = (flags & EGB_TIMING) != 0;
   cudaStream_t st = ctx->stream;
   const long long launches0 = g_launches.load();
@@ -572,19 +573,25 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   };
   // layout of a multi-D job: EGB_FORCE_* flags, else the context's policy
   // table, else the built-in rule; warp grid kNN needs K <= 8
+  // mode 4: rank-space counts (d = 2 ball counts, FP32 path only)
   auto pick_mode = [&](bool is_knn, const Space& s) {
     const int64_t len = s.e - s.b;
+    const bool rank_ok = !is_knn && s.sp.d == 2 && !plain;
     int mode;
-    if (force_brute) mode = 0;
+    if (force_rank && rank_ok) mode = 4;
+    else if (force_brute) mode = 0;
     else if (force_slab) mode = 1;
-    else if (force_grid) mode = 3;
+    else if (force_grid || cta_grid) mode = 3;
     else {
       mode = ctx->policy[egb_policy_index(is_knn ? 0 : 1, s.sp.d, s.K, len)];
-      if (mode == EGB_MODE_AUTO) mode = len >= SLAB_MIN ? 3 : 0;
+      if (mode == EGB_MODE_AUTO) mode = len >= SLAB_MIN ? (rank_ok ? 4 : 3) : 0;
     }
+    if (mode == 4 && !rank_ok) mode = 3;
     if (mode == 3 && (cta_grid || (is_knn && s.K > 8))) mode = 2;
     return mode;
   };
+  struct WmPlan { Space s; int seg_a, seg_b; };
+  std::vector<WmPlan> wplans;
   std::vector<std::pair<int, Space>> sorted_knn, sorted_cnt;  // (seg, space)
   std::vector<MJob> mjobs;
   for (const Space& s : knn) {
@@ -609,6 +616,11 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
     } else {
       MJob m{s, false, 0, -1, 0, -1, 0, -1};
       m.mode = pick_mode(false, s);
+      if (m.mode == 4) {
+        wplans.push_back({s, seg_for(s.task, s.sp.cols[0], s.b, s.e),
+                          seg_for(s.task, s.sp.cols[1], s.b, s.e)});
+        continue;
+      }
       m.slab = m.mode >= 1 ? 1 : 0;
       if (m.slab) {
         m.sort_seg = seg_for(s.task, s.sp.cols[0], s.b, s.e);
@@ -834,6 +846,43 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
     sj_cnt.push_back(j);
   }
 
+  // rank-space count jobs (wavelet matrices); their tile sums are zeroed
+  // by one memset at the start of the batch
+  std::vector<WmJob> wjobs;
+  int wm_tiles = 0, wm_qblocks = 0, wm_levels = 0;
+  size_t wmz_bytes = 0;
+  std::vector<size_t> wm_tc_off;  // per job: offset of its sums in the zeroed block
+  for (const WmPlan& w : wplans) {
+    WmJob J{};
+    const int64_t len = w.s.e - w.s.b;
+    J.task = w.s.task;
+    J.slot = w.s.slot;
+    J.len = (int32_t)len;
+    int L = 1;
+    while (((int64_t)1 << L) <= len) ++L;
+    J.L = L;
+    J.nwords = (int32_t)((len >> 5) + 1);
+    J.ntiles = (int32_t)((len + WM_TILE - 1) / WM_TILE);
+    J.nsuper = (J.ntiles + WM_SUPER - 1) / WM_SUPER;
+    J.tile0 = wm_tiles;
+    J.qblk0 = wm_qblocks;
+    J.seg_begin = (int32_t)w.s.b;
+    J.base_a = segs[(size_t)w.seg_a].out_base;
+    J.base_b = segs[(size_t)w.seg_b].out_base;
+    J.levels = (uint2*)(uintptr_t)dl.take(sizeof(uint2) * (size_t)L * (size_t)J.nwords);
+    J.zeros = (int32_t*)(uintptr_t)dl.take(sizeof(int32_t) * (size_t)L);
+    J.seq0 = (int32_t*)(uintptr_t)dl.take(sizeof(int32_t) * (size_t)len);
+    J.seq1 = (int32_t*)(uintptr_t)dl.take(sizeof(int32_t) * (size_t)len);
+    J.inv_b = (int32_t*)(uintptr_t)dl.take(sizeof(int32_t) * (size_t)len);
+    wm_tc_off.push_back(wmz_bytes);
+    wmz_bytes += sizeof(uint32_t) * (size_t)L * (size_t)(J.ntiles + J.nsuper);
+    wm_tiles += J.ntiles;
+    wm_qblocks += (int)((len + WM_QBLOCK - 1) / WM_QBLOCK);
+    wm_levels = std::max(wm_levels, L);
+    wjobs.push_back(J);
+  }
+  const size_t off_wmz = dl.take(std::max<size_t>(wmz_bytes, 16));
+
   // tile launch groups
   struct Group {
     int is_knn, sel, kclass, dclass, slab, dmax, mode;
@@ -1052,6 +1101,7 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
     G.tab_runs = tl.take(sizeof(ItemRun) * G.runs.size());
     G.tab_cum = tl.take(sizeof(int32_t) * G.cum.size());
   }
+  const size_t tab_wjobs = tl.take(sizeof(WmJob) * std::max<size_t>(wjobs.size(), 1));
   const size_t tab_cjobs = tl.take(sizeof(CombineJob) * std::max<size_t>(cjobs.size(), 1));
   const size_t tab_chunkjob = tl.take(sizeof(int32_t) * (size_t)std::max(nchunks, 1));
   const size_t tab_bytes = align_up(tl.off, 256);
@@ -1202,6 +1252,17 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
     if (!G.runs.empty()) std::memcpy(H + G.tab_runs, G.runs.data(), sizeof(ItemRun) * G.runs.size());
     if (!G.cum.empty()) std::memcpy(H + G.tab_cum, G.cum.data(), sizeof(int32_t) * G.cum.size());
   }
+  for (size_t w = 0; w < wjobs.size(); ++w) {
+    WmJob J = wjobs[w];
+    J.levels = (uint2*)(A + (uintptr_t)J.levels);
+    J.zeros = (int32_t*)(A + (uintptr_t)J.zeros);
+    J.seq0 = (int32_t*)(A + (uintptr_t)J.seq0);
+    J.seq1 = (int32_t*)(A + (uintptr_t)J.seq1);
+    J.inv_b = (int32_t*)(A + (uintptr_t)J.inv_b);
+    J.tcount = (uint32_t*)(A + off_wmz + wm_tc_off[w]);
+    J.scount = J.tcount + (size_t)J.L * (size_t)J.ntiles;
+    std::memcpy(H + tab_wjobs + sizeof(WmJob) * w, &J, sizeof(WmJob));
+  }
   if (!cjobs.empty()) std::memcpy(H + tab_cjobs, cjobs.data(), sizeof(CombineJob) * cjobs.size());
   if (nchunks) std::memcpy(H + tab_chunkjob, chunk_job.data(), sizeof(int32_t) * (size_t)nchunks);
 
@@ -1230,6 +1291,7 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   auto enqueue = [&]() -> int {
   EGB_CUDA(cudaMemcpyAsync(A + off_tab, H, tab_bytes, cudaMemcpyHostToDevice, st));
   EGB_CUDA(cudaMemsetAsync(A + off_zr, 0, zr_bytes, st));
+  if (wmz_bytes) EGB_CUDA(cudaMemsetAsync(A + off_wmz, 0, wmz_bytes, st));
   if (inject)  // the device error word as if a kernel had set these bits
     for (int i = 0; i < 4; ++i)
       EGB_CUDA(cudaMemsetAsync((char*)err_d + i, (int)((inject >> (8 * i)) & 0xffu), 1, st));
@@ -1302,6 +1364,7 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
                             max_gkey > 256 ? gva : gvb, (const SortSeg*)dtab(tab_gsegs),
                             max_lds, st);
   }
+  launch_wm_build((const WmJob*)dtab(tab_wjobs), (int)wjobs.size(), wm_tiles, wm_levels, vals, st);
   if (timing) EGB_CUDA(cudaEventRecord(ctx->ev[3], st));
 
   launch_sorted_jobs(tasks_d, (const SortedJob*)dtab(tab_sjk), (int)sj_knn.size(), blk_knn, keys, vals, st);
@@ -1343,6 +1406,7 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   launch_sorted_jobs(tasks_d, (const SortedJob*)dtab(tab_sjc), (int)sj_cnt.size(), blk_cnt, keys, vals, st);
   if (timing) EGB_CUDA(cudaEventRecord(ctx->kev[11], st));
   if (timing) EGB_CUDA(cudaEventRecord(ctx->kev[4], st));
+  launch_wm_count(tasks_d, (const WmJob*)dtab(tab_wjobs), (int)wjobs.size(), wm_qblocks, keys, vals, st);
   for (size_t g = 0; g < groups.size(); ++g) {
     Group& G = groups[g];
     if (G.is_knn || G.nitems == 0) continue;
@@ -1625,7 +1689,7 @@ int egb_set_policy(egb_ctx* ctx, const int8_t* modes, int32_t n) {
   }
   if (n != EGB_POLICY_ENTRIES) return fail(ctx, EGB_ERR_ARG, "egb_set_policy: table size mismatch");
   for (int i = 0; i < n; ++i)
-    if (modes[i] < EGB_MODE_AUTO || modes[i] > EGB_MODE_WARP_GRID)
+    if (modes[i] < EGB_MODE_AUTO || modes[i] > EGB_MODE_RANK)
       return fail(ctx, EGB_ERR_ARG, "egb_set_policy: invalid mode at entry " + std::to_string(i));
   std::memcpy(ctx->policy, modes, sizeof(ctx->policy));
   ctx->replay.valid = false;  // the plan of a replayed batch may change

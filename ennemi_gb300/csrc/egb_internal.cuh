@@ -527,6 +527,48 @@ void launch_count_keys(const JobDev* jobs_d, const WorkItem* items_d, int nitems
 void launch_count_wgrid(const JobDev* jobs_d, const WorkItem* items_d, int nitems, int dclass,
                         int plain, int dmax, int* counter, int num_sms, cudaStream_t st);
 
+// egb_wavelet.cu: exact 2-D ball counts in rank space.  A count space of
+// columns (a, b) over len points is the permutation S[i] = position in the
+// b order of the point at position i of the a order; the ball of a query is
+// the rectangle of key ranges [a_lo, a_hi) x [b_lo, b_hi) in those orders, and
+// its count is #{i in [a_lo, a_hi) : S[i] in [b_lo, b_hi)}, answered by a
+// wavelet matrix over S: L = bit_length(len) levels, level l holding bit
+// L-1-l of every value in the order of the level (zeros of the level above
+// first, then ones, each stable).  Every level is a bit vector with the ones
+// before each 32-bit word; a count descends the levels with two rank
+// operations per range end.
+constexpr int WM_TILE = 2048;      // values per block of the level passes
+constexpr int WM_SUPER = 64;       // tiles per super tile (prefix sums of ones)
+constexpr int WM_QBLOCK = 256;     // queries per block of the count kernel
+struct WmJob {
+  uint2* levels;          // [L][nwords]: .x = 32 bits of the level, .y = ones
+                          // of the level before that word
+  int32_t* zeros;         // [L] zeros of each level
+  int32_t* seq0;          // [len] the sequence of even levels
+  int32_t* seq1;          // [len] the sequence of odd levels
+  int32_t* inv_b;         // [len] working offset -> position in the b order
+  uint32_t* tcount;       // [L][ntiles] ones of each level per tile (zeroed)
+  uint32_t* scount;       // [L][nsuper] ones per super tile (zeroed)
+  int64_t base_a;         // sorted segment of column a in the key / value buffers
+  int64_t base_b;         // sorted segment of column b
+  int32_t task, slot;
+  int32_t len;            // points of the space (= queries)
+  int32_t L;              // levels: bit_length(len), so len < 2^L
+  int32_t nwords;         // (len >> 5) + 1 words per level
+  int32_t ntiles;         // ceil(len / WM_TILE)
+  int32_t nsuper;         // ceil(ntiles / WM_SUPER)
+  int32_t tile0;          // first block of the job in the level launches
+  int32_t qblk0;          // first block of the job in the count launch
+  int32_t seg_begin;      // first working index of the space
+};
+// Build (after the batch sort): inverse b order, the level-0 sequence, then
+// one launch per level for every job at once (max_levels launches).
+void launch_wm_build(const WmJob* jobs_d, int njobs, int total_tiles, int max_levels,
+                     const int32_t* sorted_vals, cudaStream_t st);
+// Counts: one thread per query, in the a order; writes cnt[slot] of the task.
+void launch_wm_count(const TaskDev* tasks_d, const WmJob* jobs_d, int njobs, int total_blocks,
+                     const uint64_t* sorted_keys, const int32_t* sorted_vals, cudaStream_t st);
+
 // egb_select.cu: any K (one warp per query, radix select on FP64 bits)
 constexpr int SELECT_WARPS = 8;
 void launch_knn_select(const JobDev* jobs_d, const WorkItem* items_d, int nitems, uint32_t* err,

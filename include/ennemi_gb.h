@@ -97,7 +97,7 @@ enum egb_flags {
                                   gather even where the device reads pageable
                                   host memory directly (by default contiguous
                                   host columns are then read in place)           */
-  EGB_RESCALE = 1 << 10        /* preprocess on the device as the reference's
+  EGB_RESCALE = 1 << 10,       /* preprocess on the device as the reference's
                                   _rescale_data (_driver.py:871-902) does: every
                                   column of MI, CMI, SEMI and CSEMI tasks becomes
                                   (x - mean) / std + noise, mean and std by
@@ -110,6 +110,9 @@ enum egb_flags {
                                   array: row by row.  Requires one x column and
                                   at most one y column; ENTROPY tasks are left
                                   as given                                   */
+  EGB_FORCE_RANK = 1 << 11     /* every d = 2 ball count uses the rank-space
+                                  wavelet-matrix counts, whatever its size
+                                  (tests; ignored with EGB_PLAIN_FP64)        */
 };
 
 /* One float64 column: sample i at data[i * stride] (stride in elements). */
@@ -229,17 +232,21 @@ int egb_last_stats(const egb_ctx* ctx, int64_t* out, int32_t max);
  * Layout policy (the table an autotuner fills; no counterpart in the
  * reference, whose cKDTree has a single layout).  Every multi-dimensional
  * search job of a batch -- a kNN search or a ball count over d >= 2 columns --
- * runs in one of four layouts:
+ * runs in one of five layouts:
  *   EGB_MODE_BRUTE      tiles of all points against all points
  *   EGB_MODE_SLAB       points sorted by column 0, tiles from a window
  *   EGB_MODE_GRID       equal-count strips, 128-query CTA work items
  *   EGB_MODE_WARP_GRID  equal-count strips, 32-query warp work items
  *                       (kNN only for K = k + 1 <= 8; otherwise GRID)
+ *   EGB_MODE_RANK       ball counts of d = 2 only: rank-space rectangle
+ *                       counts on a wavelet matrix (otherwise WARP_GRID;
+ *                       the all-FP64 comparator keeps WARP_GRID too)
  * Each layout gives the same results bit for bit; only speed differs.  The
  * planner reads the context's table at egb_policy_index(search, d, K, len);
  * EGB_MODE_AUTO (every entry of a new context) selects the built-in rule:
- * brute force below 4096 points, otherwise the warp grid (CTA grid for kNN
- * with 9 <= K <= 32).  K > 32 kNN always uses the select kernel, and the
+ * brute force below 4096 points, otherwise the rank-space counts for d = 2
+ * ball counts and the warp grid for the rest (CTA grid for kNN with
+ * 9 <= K <= 32).  K > 32 kNN always uses the select kernel, and the
  * EGB_FORCE_* flags override the table.
  */
 #define EGB_MODE_AUTO (-1)
@@ -247,6 +254,7 @@ int egb_last_stats(const egb_ctx* ctx, int64_t* out, int32_t max);
 #define EGB_MODE_SLAB 1
 #define EGB_MODE_GRID 2
 #define EGB_MODE_WARP_GRID 3
+#define EGB_MODE_RANK 4
 #define EGB_POLICY_SIZE_CLASSES 32 /* floor(log2(len)) */
 #define EGB_POLICY_ENTRIES (2 * 4 * 4 * EGB_POLICY_SIZE_CLASSES)
 
@@ -262,7 +270,7 @@ static inline int egb_policy_index(int search, int d, int K, int64_t len) {
 }
 
 /* Replace the context's table with modes[0 .. n) (n == EGB_POLICY_ENTRIES;
- * each entry EGB_MODE_AUTO .. EGB_MODE_WARP_GRID).  modes == NULL resets every
+ * each entry EGB_MODE_AUTO .. EGB_MODE_RANK).  modes == NULL resets every
  * entry to EGB_MODE_AUTO. */
 int egb_set_policy(egb_ctx* ctx, const int8_t* modes, int32_t n);
 

@@ -30,10 +30,10 @@ def test_every_policy_gives_identical_results(n):
     ctx.set_policy(None)
     base = N.run_tasks(tasks)
     try:
-        for mode in (N.MODE_BRUTE, N.MODE_SLAB, N.MODE_GRID, N.MODE_WARP_GRID):
+        for mode in (N.MODE_BRUTE, N.MODE_SLAB, N.MODE_GRID, N.MODE_WARP_GRID, N.MODE_RANK):
             ctx.set_policy(np.full(N.POLICY_ENTRIES, mode, dtype=np.int8))
             assert np.array_equal(N.run_tasks(tasks), base), mode
-        mixed = np.random.default_rng(1).integers(-1, 4, N.POLICY_ENTRIES).astype(np.int8)
+        mixed = np.random.default_rng(1).integers(-1, 5, N.POLICY_ENTRIES).astype(np.int8)
         ctx.set_policy(mixed)
         assert np.array_equal(ctx.get_policy(), mixed)
         assert np.array_equal(N.run_tasks(tasks), base)
@@ -44,7 +44,7 @@ def test_every_policy_gives_identical_results(n):
 def test_invalid_policy_rejected():
     ctx = N.context()
     bad = np.zeros(N.POLICY_ENTRIES, dtype=np.int8)
-    bad[3] = 4
+    bad[3] = 5
     with pytest.raises(RuntimeError, match="invalid mode"):
         ctx.set_policy(bad)
     assert np.all(ctx.get_policy() == N.MODE_AUTO)

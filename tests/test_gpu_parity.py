@@ -22,6 +22,7 @@ VARIANTS = {
     "fp32-slab": N.FORCE_SLAB,
     "fp32-grid": N.FORCE_GRID,
     "fp32-ctagrid": N.FORCE_GRID | N.FORCE_CTA_GRID,
+    "fp32-rank": N.FORCE_RANK,
     "fp64-brute": N.PLAIN_FP64 | N.FORCE_BRUTE,
     "fp64-slab": N.PLAIN_FP64 | N.FORCE_SLAB,
     "fp64-grid": N.PLAIN_FP64 | N.FORCE_GRID,
@@ -73,7 +74,7 @@ def test_golden_estimators(case, variant):
     assert same_value(vals[0], float(case["value"])), (vals[0], float(case["value"]))
 
 
-@pytest.mark.parametrize("variant", ["fp32", "fp64-slab", "fp32-grid"])
+@pytest.mark.parametrize("variant", ["fp32", "fp64-slab", "fp32-grid", "fp32-rank"])
 def test_golden_all_in_one_batch(variant):
     tasks = [make_task(str(c["kind"]), int(c["k"]), inputs_of(c)) for c in CASES]
     vals = N.run_tasks(tasks, flags=VARIANTS[variant] | N.KEEP_INTERNALS)
