@@ -38,6 +38,7 @@
 #include <vector>
 
 #include "egb_internal.cuh"
+#include "egb_search.cuh"
 #include "egb_pwtree.h"
 #include "ennemi_gb.h"
 
@@ -630,10 +631,14 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
       mjobs.push_back(m);
     }
   }
-  int64_t sort_total = 0;
+  int64_t sort_total = 0, s1_total = 0, s2_total = 0;
   int nblk_sort = 0;
   for (SortSeg& s : segs) {
     s.out_base = sort_total;
+    s.s1_base = s1_total;
+    s.s2_base = s2_total;
+    s1_total += samples1_of(s.len);
+    s2_total += samples2_of(s.len);
     s.blk0 = nblk_sort;
     s.nblk = (s.len + SORT_TILE - 1) / SORT_TILE;
     sort_total += s.len;
@@ -707,6 +712,8 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   const size_t off_keys_b = dl.take(sizeof(uint64_t) * (size_t)std::max<int64_t>(sort_total, 1));
   const size_t off_vals_a = dl.take(sizeof(int32_t) * (size_t)std::max<int64_t>(sort_total, 1));
   const size_t off_vals_b = dl.take(sizeof(int32_t) * (size_t)std::max<int64_t>(sort_total, 1));
+  const size_t off_s1 = dl.take(sizeof(uint64_t) * (size_t)std::max<int64_t>(s1_total, 1));
+  const size_t off_s2 = dl.take(sizeof(uint64_t) * (size_t)std::max<int64_t>(s2_total, 1));
   const size_t off_hist = dl.take(sizeof(uint32_t) * 256 * (size_t)std::max(nblk_sort, 1));
   const size_t off_scan = dl.take(sizeof(uint32_t) * sort_scan_tmp_elems(std::max(nblk_sort, 1)));
 
@@ -833,7 +840,8 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
     const SortSeg& sg = segs[(size_t)pr.first];
     SortedJob j{};
     j.task = pr.second.task; j.kind = 0; j.slot = 0; j.K = pr.second.K;
-    j.base = sg.out_base; j.len = sg.len; j.blk0 = blk_knn;
+    j.base = sg.out_base; j.s1_base = sg.s1_base; j.s2_base = sg.s2_base;
+    j.len = sg.len; j.blk0 = blk_knn;
     blk_knn += (sg.len + SORTED_BLOCK - 1) / SORTED_BLOCK;
     sj_knn.push_back(j);
   }
@@ -841,7 +849,8 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
     const SortSeg& sg = segs[(size_t)pr.first];
     SortedJob j{};
     j.task = pr.second.task; j.kind = 1; j.slot = pr.second.slot; j.K = 0;
-    j.base = sg.out_base; j.len = sg.len; j.blk0 = blk_cnt;
+    j.base = sg.out_base; j.s1_base = sg.s1_base; j.s2_base = sg.s2_base;
+    j.len = sg.len; j.blk0 = blk_cnt;
     blk_cnt += (sg.len + SORTED_BLOCK - 1) / SORTED_BLOCK;
     sj_cnt.push_back(j);
   }
@@ -858,27 +867,33 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
     J.task = w.s.task;
     J.slot = w.s.slot;
     J.len = (int32_t)len;
-    int L = 1;
-    while (((int64_t)1 << L) <= len) ++L;
-    J.L = L;
-    J.nwords = (int32_t)((len >> 5) + 1);
+    int D = 1;
+    while (((int64_t)1 << (2 * D)) <= len) ++D;   // 4^D > len
+    J.D = D;
+    J.nblocks = (int32_t)((len >> 6) + 1);
     J.ntiles = (int32_t)((len + WM_TILE - 1) / WM_TILE);
     J.nsuper = (J.ntiles + WM_SUPER - 1) / WM_SUPER;
     J.tile0 = wm_tiles;
     J.qblk0 = wm_qblocks;
     J.seg_begin = (int32_t)w.s.b;
-    J.base_a = segs[(size_t)w.seg_a].out_base;
-    J.base_b = segs[(size_t)w.seg_b].out_base;
-    J.levels = (uint2*)(uintptr_t)dl.take(sizeof(uint2) * (size_t)L * (size_t)J.nwords);
-    J.zeros = (int32_t*)(uintptr_t)dl.take(sizeof(int32_t) * (size_t)L);
+    const SortSeg& sa = segs[(size_t)w.seg_a];
+    const SortSeg& sb = segs[(size_t)w.seg_b];
+    J.base_a = sa.out_base;
+    J.base_b = sb.out_base;
+    J.s1_a = sa.s1_base;
+    J.s2_a = sa.s2_base;
+    J.s1_b = sb.s1_base;
+    J.s2_b = sb.s2_base;
+    J.levels = (WmBlock*)(uintptr_t)dl.take(sizeof(WmBlock) * (size_t)D * (size_t)J.nblocks);
+    J.bucket = (int32_t*)(uintptr_t)dl.take(sizeof(int32_t) * 4 * (size_t)D);
     J.seq0 = (int32_t*)(uintptr_t)dl.take(sizeof(int32_t) * (size_t)len);
     J.seq1 = (int32_t*)(uintptr_t)dl.take(sizeof(int32_t) * (size_t)len);
     J.inv_b = (int32_t*)(uintptr_t)dl.take(sizeof(int32_t) * (size_t)len);
     wm_tc_off.push_back(wmz_bytes);
-    wmz_bytes += sizeof(uint32_t) * (size_t)L * (size_t)(J.ntiles + J.nsuper);
+    wmz_bytes += 4 * sizeof(uint32_t) * (size_t)D * (size_t)(J.ntiles + J.nsuper);
     wm_tiles += J.ntiles;
     wm_qblocks += (int)((len + WM_QBLOCK - 1) / WM_QBLOCK);
-    wm_levels = std::max(wm_levels, L);
+    wm_levels = std::max(wm_levels, D);
     wjobs.push_back(J);
   }
   const size_t off_wmz = dl.take(std::max<size_t>(wmz_bytes, 16));
@@ -1254,13 +1269,13 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   }
   for (size_t w = 0; w < wjobs.size(); ++w) {
     WmJob J = wjobs[w];
-    J.levels = (uint2*)(A + (uintptr_t)J.levels);
-    J.zeros = (int32_t*)(A + (uintptr_t)J.zeros);
+    J.levels = (WmBlock*)(A + (uintptr_t)J.levels);
+    J.bucket = (int32_t*)(A + (uintptr_t)J.bucket);
     J.seq0 = (int32_t*)(A + (uintptr_t)J.seq0);
     J.seq1 = (int32_t*)(A + (uintptr_t)J.seq1);
     J.inv_b = (int32_t*)(A + (uintptr_t)J.inv_b);
     J.tcount = (uint32_t*)(A + off_wmz + wm_tc_off[w]);
-    J.scount = J.tcount + (size_t)J.L * (size_t)J.ntiles;
+    J.scount = J.tcount + 4 * (size_t)J.D * (size_t)J.ntiles;
     std::memcpy(H + tab_wjobs + sizeof(WmJob) * w, &J, sizeof(WmJob));
   }
   if (!cjobs.empty()) std::memcpy(H + tab_cjobs, cjobs.data(), sizeof(CombineJob) * cjobs.size());
@@ -1329,6 +1344,8 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   launch_sort(tasks_d, (const SortSeg*)dtab(tab_segs), (const int32_t*)dtab(tab_blkseg), nblk_sort,
               keys, (uint64_t*)(A + off_keys_b), vals, (int32_t*)(A + off_vals_b),
               (uint32_t*)(A + off_hist), (uint32_t*)(A + off_scan), st);
+  launch_samples((const SortSeg*)dtab(tab_segs), (const int32_t*)dtab(tab_blkseg), nblk_sort, keys,
+                 (uint64_t*)(A + off_s1), (uint64_t*)(A + off_s2), st);
   if (timing) EGB_CUDA(cudaEventRecord(ctx->kev[9], st));
   launch_materialize(tasks_d, (const JobDev*)dtab(tab_jobs), (int)jobs.size(), vals,
                      (const SortSeg*)dtab(tab_segs), max_lds, st);
@@ -1367,7 +1384,8 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   launch_wm_build((const WmJob*)dtab(tab_wjobs), (int)wjobs.size(), wm_tiles, wm_levels, vals, st);
   if (timing) EGB_CUDA(cudaEventRecord(ctx->ev[3], st));
 
-  launch_sorted_jobs(tasks_d, (const SortedJob*)dtab(tab_sjk), (int)sj_knn.size(), blk_knn, keys, vals, st);
+  launch_sorted_jobs(tasks_d, (const SortedJob*)dtab(tab_sjk), (int)sj_knn.size(), blk_knn, keys,
+                     (const uint64_t*)(A + off_s1), (const uint64_t*)(A + off_s2), vals, st);
   if (timing) EGB_CUDA(cudaEventRecord(ctx->kev[0], st));
   for (size_t g = 0; g < groups.size(); ++g) {
     Group& G = groups[g];
@@ -1403,10 +1421,12 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
 
   launch_radius(tasks_d, ntasks, max_ld, st);
   if (timing) EGB_CUDA(cudaEventRecord(ctx->kev[10], st));
-  launch_sorted_jobs(tasks_d, (const SortedJob*)dtab(tab_sjc), (int)sj_cnt.size(), blk_cnt, keys, vals, st);
+  launch_sorted_jobs(tasks_d, (const SortedJob*)dtab(tab_sjc), (int)sj_cnt.size(), blk_cnt, keys,
+                     (const uint64_t*)(A + off_s1), (const uint64_t*)(A + off_s2), vals, st);
   if (timing) EGB_CUDA(cudaEventRecord(ctx->kev[11], st));
   if (timing) EGB_CUDA(cudaEventRecord(ctx->kev[4], st));
-  launch_wm_count(tasks_d, (const WmJob*)dtab(tab_wjobs), (int)wjobs.size(), wm_qblocks, keys, vals, st);
+  launch_wm_count(tasks_d, (const WmJob*)dtab(tab_wjobs), (int)wjobs.size(), wm_qblocks, keys,
+                  (const uint64_t*)(A + off_s1), (const uint64_t*)(A + off_s2), vals, st);
   for (size_t g = 0; g < groups.size(); ++g) {
     Group& G = groups[g];
     if (G.is_knn || G.nitems == 0) continue;

@@ -347,12 +347,16 @@ struct SortedJob {
   int32_t slot;
   int32_t K;              // k + 1 for kNN
   int64_t base;           // offset of the sorted segment in the key buffer
+  int64_t s1_base;        // its samples (egb_search.cuh)
+  int64_t s2_base;
   int32_t len;            // its length
   int32_t blk0;           // first block of this job in the launch
 };
 
 struct SortSeg {          // one segment of the batched radix sort
   int64_t out_base;       // offset into the concatenated key buffer
+  int64_t s1_base;        // offset of its samples keys[32 j] (egb_search.cuh)
+  int64_t s2_base;        // offset of its samples keys[1024 j]
   int32_t len;
   int32_t blk0;           // first tile (block) of the segment
   int32_t nblk;
@@ -475,8 +479,8 @@ void launch_sort(const TaskDev* tasks_d, const SortSeg* segs_d, const int32_t* b
                  int32_t* vals_b, uint32_t* hist, uint32_t* scan_tmp, cudaStream_t st);
 constexpr int SORTED_BLOCK = 256;
 void launch_sorted_jobs(const TaskDev* tasks_d, const SortedJob* jobs_d, int njobs,
-                        int total_blocks, const uint64_t* keys, const int32_t* perm,
-                        cudaStream_t st);
+                        int total_blocks, const uint64_t* keys, const uint64_t* samples1,
+                        const uint64_t* samples2, const int32_t* perm, cudaStream_t st);
 
 // egb_knn.cu / egb_count.cu: tile kernels over materialised jobs.
 // dclass in {2, 3, 4} or 0 (generic d <= EGB_DMAX); kclass in {4, 8, 16, 32}.
@@ -532,29 +536,37 @@ void launch_count_wgrid(const JobDev* jobs_d, const WorkItem* items_d, int nitem
 // b order of the point at position i of the a order; the ball of a query is
 // the rectangle of key ranges [a_lo, a_hi) x [b_lo, b_hi) in those orders, and
 // its count is #{i in [a_lo, a_hi) : S[i] in [b_lo, b_hi)}, answered by a
-// wavelet matrix over S: L = bit_length(len) levels, level l holding bit
-// L-1-l of every value in the order of the level (zeros of the level above
-// first, then ones, each stable).  Every level is a bit vector with the ones
-// before each 32-bit word; a count descends the levels with two rank
-// operations per range end.
+// 4-ary wavelet matrix over S: D levels of 2-bit digits (4^D > len), level
+// l holding digit D-1-l of every value in the order of the level (the level
+// above stably partitioned by its digit).  Each level is a sequence of
+// 32-byte blocks of 64 digits: two bit planes and the counts of digits
+// <= 0, <= 1, <= 2 before the block, so a rank is one block read.
 constexpr int WM_TILE = 2048;      // values per block of the level passes
-constexpr int WM_SUPER = 64;       // tiles per super tile (prefix sums of ones)
+constexpr int WM_SUPER = 64;       // tiles per super tile (prefix sums of digits)
 constexpr int WM_QBLOCK = 256;     // queries per block of the count kernel
+struct WmBlock {                   // 64 digits of one level
+  uint32_t hi[2];                  // bit 1 of digit j at bit j % 32 of hi[j / 32]
+  uint32_t lo[2];                  // bit 0
+  uint32_t le[3];                  // digits <= 0, <= 1, <= 2 before the block
+  uint32_t pad;
+};
 struct WmJob {
-  uint2* levels;          // [L][nwords]: .x = 32 bits of the level, .y = ones
-                          // of the level before that word
-  int32_t* zeros;         // [L] zeros of each level
+  WmBlock* levels;        // [D][nblocks]
+  int32_t* bucket;        // [D][4] first position of each digit's run in the
+                          // next level (digits below it in the whole level)
   int32_t* seq0;          // [len] the sequence of even levels
   int32_t* seq1;          // [len] the sequence of odd levels
   int32_t* inv_b;         // [len] working offset -> position in the b order
-  uint32_t* tcount;       // [L][ntiles] ones of each level per tile (zeroed)
-  uint32_t* scount;       // [L][nsuper] ones per super tile (zeroed)
+  uint32_t* tcount;       // [D][ntiles][4] digits of each level per tile (zeroed)
+  uint32_t* scount;       // [D][nsuper][4] per super tile (zeroed)
   int64_t base_a;         // sorted segment of column a in the key / value buffers
   int64_t base_b;         // sorted segment of column b
+  int64_t s1_a, s2_a;     // its samples (egb_search.cuh)
+  int64_t s1_b, s2_b;
   int32_t task, slot;
   int32_t len;            // points of the space (= queries)
-  int32_t L;              // levels: bit_length(len), so len < 2^L
-  int32_t nwords;         // (len >> 5) + 1 words per level
+  int32_t D;              // levels: 4^D > len
+  int32_t nblocks;        // (len >> 6) + 1 blocks per level
   int32_t ntiles;         // ceil(len / WM_TILE)
   int32_t nsuper;         // ceil(ntiles / WM_SUPER)
   int32_t tile0;          // first block of the job in the level launches
@@ -567,7 +579,11 @@ void launch_wm_build(const WmJob* jobs_d, int njobs, int total_tiles, int max_le
                      const int32_t* sorted_vals, cudaStream_t st);
 // Counts: one thread per query, in the a order; writes cnt[slot] of the task.
 void launch_wm_count(const TaskDev* tasks_d, const WmJob* jobs_d, int njobs, int total_blocks,
-                     const uint64_t* sorted_keys, const int32_t* sorted_vals, cudaStream_t st);
+                     const uint64_t* sorted_keys, const uint64_t* samples1,
+                     const uint64_t* samples2, const int32_t* sorted_vals, cudaStream_t st);
+// Samples of every sorted segment (egb_search.cuh), after the sort.
+void launch_samples(const SortSeg* segs_d, const int32_t* blk_seg_d, int nblk,
+                    const uint64_t* keys, uint64_t* samples1, uint64_t* samples2, cudaStream_t st);
 
 // egb_select.cu: any K (one warp per query, radix select on FP64 bits)
 constexpr int SELECT_WARPS = 8;

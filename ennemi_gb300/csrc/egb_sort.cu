@@ -16,9 +16,10 @@
 // 1-D counts (marginal spaces of KSG / CMI): #{j : fl64(|x_j - q|) <= r},
 // r = fl64(eps - 1e-12).  fl64(s_j - q) is monotone in s_j (rounding is
 // monotone), so on each side of q the predicate holds on one contiguous run
-// of sorted positions.  Its ends are found by galloping out from p and
-// bisecting, evaluating the exact FP64 predicate only -- O(log count) probes.
+// of sorted positions -- one key range (ball_keys), whose ends are found
+// through the segment's samples (egb_search.cuh).
 #include "egb_internal.cuh"
+#include "egb_search.cuh"
 
 namespace egb {
 
@@ -231,6 +232,8 @@ __global__ void scan_down_kernel(uint32_t* __restrict__ data, int64_t n,
 __global__ void sorted_jobs_kernel(const TaskDev* __restrict__ tasks,
                                    const SortedJob* __restrict__ jobs, int njobs,
                                    const uint64_t* __restrict__ keys_all,
+                                   const uint64_t* __restrict__ s1_all,
+                                   const uint64_t* __restrict__ s2_all,
                                    const int32_t* __restrict__ perm_all) {
   // the job of this block: last j with jobs[j].blk0 <= blockIdx.x
   int lo = 0, hi = njobs;
@@ -269,37 +272,18 @@ __global__ void sorted_jobs_kernel(const TaskDev* __restrict__ tasks,
   } else if (r == INF) {
     count = (int32_t)len;
   } else {
-    // The ball is one key range (ball_keys); the searches compare integer
-    // keys (the FP64 pipe is a small fraction of the integer rate on GB300).
-    // The sorted keys fold -0 into +0, as the predicate does.
+    // The ball is one key range (ball_keys); its ends are found through the
+    // segment's two levels of samples (integer compares only; the FP64
+    // pipe is a small fraction of the integer rate on GB300).  The sorted
+    // keys fold -0 into +0, as the predicate does.
     uint64_t kL, kR;
     ball_keys(q, r, kL, kR);
     kL = kL == 0x7fffffffffffffffull ? 0x8000000000000000ull : kL;  // raw -0 -> +0
-    // right end: last j >= p with keys[j] <= kR   (true at j = p)
-    int64_t a = p, step = 1;
-    while (a + step < len && keys[a + step] <= kR) {
-      a += step;
-      step <<= 1;
-    }
-    int64_t b = a + step < len ? a + step : len;
-    while (b - a > 1) {
-      const int64_t m = a + ((b - a) >> 1);
-      if (keys[m] <= kR) a = m; else b = m;
-    }
-    const int64_t R = a;
-    // left end: first j <= p with keys[j] >= kL   (true at j = p)
-    a = p;
-    step = 1;
-    while (a - step >= 0 && keys[a - step] >= kL) {
-      a -= step;
-      step <<= 1;
-    }
-    b = a - step >= 0 ? a - step : -1;
-    while (a - b > 1) {
-      const int64_t m = b + ((a - b) >> 1);
-      if (keys[m] >= kL) a = m; else b = m;
-    }
-    count = (int32_t)(R - a + 1);
+    const uint64_t* s1 = s1_all + jb.s1_base;
+    const uint64_t* s2 = s2_all + jb.s2_base;
+    const int lo = sampled_bound<false>(keys, s1, s2, (int)len, kL);
+    const int hi = sampled_bound<true>(keys, s1, s2, (int)len, kR);
+    count = (int32_t)(hi - lo);
   }
   t.cnt[jb.slot][i] = count;
 }
@@ -511,11 +495,12 @@ void launch_radix_pass(const SortSeg* segs_d, const int32_t* blk_seg_d, int nblk
 }
 
 void launch_sorted_jobs(const TaskDev* tasks_d, const SortedJob* jobs_d, int njobs,
-                        int total_blocks, const uint64_t* keys, const int32_t* perm,
-                        cudaStream_t st) {
+                        int total_blocks, const uint64_t* keys, const uint64_t* samples1,
+                        const uint64_t* samples2, const int32_t* perm, cudaStream_t st) {
   if (njobs <= 0 || total_blocks <= 0) return;
   sorted_jobs_kernel<<<(unsigned)total_blocks, SORTED_THREADS, 0, st>>>(tasks_d, jobs_d, njobs,
-                                                                        keys, perm);
+                                                                        keys, samples1, samples2,
+                                                                        perm);
   count_launch();
 }
 

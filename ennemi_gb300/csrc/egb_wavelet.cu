@@ -1,4 +1,4 @@
-// egb_wavelet.cu -- exact 2-D ball counts in rank space (wavelet matrix).
+// egb_wavelet.cu -- exact 2-D ball counts in rank space (4-ary wavelet matrix).
 //
 // query_ball_point(..., r, p=inf, return_length=True) in two dimensions
 // (ennemi/_entropy_estimators.py:152-154 for the (x, z) and (y, z) spaces of
@@ -10,30 +10,39 @@
 // i of the a order, the count is #{i in [a_lo, a_hi) : S[i] in [b_lo, b_hi)}
 // -- integer arithmetic on ranks, exact for any data, ties included.
 //
-// The wavelet matrix answers that in O(log len): level l (l = 0 .. L-1)
-// stores bit L-1-l of every value of the sequence S_l, where S_0 = S and
-// S_{l+1} is S_l stably partitioned by that bit (zeros first).  A value range
-// [c, d) is descended bit by bit; at each level a position range [a, b)
-// maps to [rank0(a), rank0(b)) on the zero side or [Z + rank1(a), Z +
-// rank1(b)) on the one side.  While c and d agree on their leading bits both
-// descend together; below the first differing bit the count splits into "at
-// least c" on the zero side and "below d" on the one side.
+// The wavelet matrix answers that in O(log len).  Values are written as D
+// base-4 digits; level l (l = 0 .. D-1) stores digit D-1-l of every value
+// of the sequence S_l, where S_0 = S and S_{l+1} is S_l stably partitioned
+// by that digit (digit 0 first, then 1, 2, 3).  A position range [a, b) of
+// level l maps, for digit t, to [B_t + rank_t(a), B_t + rank_t(b)) in level
+// l + 1 (B_t: digits below t in the whole level).  A value range [c, d) is
+// descended digit by digit: while c and d share their leading digits both
+// descend together; at the first digit where they differ the values with a
+// digit strictly between count whole, and two descents continue -- "at
+// least c" in c's digit and "below d" in d's.
+//
+// Storage: each level is a sequence of 32-byte blocks of 64 digits (two bit
+// planes and the counts of digits <= 0, <= 1, <= 2 before the block), so a
+// rank costs one block read.  Range ends come from the sorted keys through
+// their two levels of samples (egb_search.cuh).
 //
 // Build: one block per tile of WM_TILE values and one launch per level.  A
-// block needs the ones of its level before its tile: the previous level's
-// pass adds the ones it sends to each destination tile (and super tile) of
-// the next level, so the sums are ready when the next launch starts.
+// block needs the digit counts of its level before its tile: the previous
+// level's pass adds the digits it sends to each destination tile (and super
+// tile) of the next level, so the sums are complete when the next launch
+// starts.
 #include "egb_internal.cuh"
+#include "egb_search.cuh"
 
 namespace egb {
 namespace {
 
 constexpr int WM_THREADS = 256;
-constexpr int WM_PER = WM_TILE / WM_THREADS;  // values per thread (k-major)
-static_assert(WM_TILE % (32 * WM_THREADS / 32) == 0, "tiles hold whole warps");
-static_assert(WM_PER == 8, "eight values per thread");
+constexpr int WM_WARPS = WM_THREADS / 32;
+constexpr int WM_ROUNDS = WM_TILE / WM_THREADS;  // rounds of 32 values per warp
+static_assert(WM_ROUNDS == 8 && WM_ROUNDS % 2 == 0, "pairs of rounds fill 64-digit blocks");
 
-// job of a block: last j with jobs[j].first <= b
+// job of a block: last j with first(jobs[j]) <= b
 template <typename F>
 __device__ __forceinline__ int job_of(const WmJob* __restrict__ jobs, int njobs, int b, F first) {
   int lo = 0, hi = njobs;
@@ -44,259 +53,317 @@ __device__ __forceinline__ int job_of(const WmJob* __restrict__ jobs, int njobs,
   return lo;
 }
 
-__device__ __forceinline__ uint32_t block_sum(uint32_t v, uint32_t* red) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  v = __reduce_add_sync(0xffffffffu, v);
-  if (lane == 0) red[warp] = v;
-  __syncthreads();
-  uint32_t t = 0;
-#pragma unroll
-  for (int w = 0; w < WM_THREADS / 32; ++w) t += red[w];
-  __syncthreads();
-  return t;
-}
-
 // inv_b[w] = position of working offset w in the b order
 __global__ void __launch_bounds__(WM_THREADS)
 wm_inv_kernel(const WmJob* __restrict__ jobs, int njobs, const int32_t* __restrict__ vals) {
-  const WmJob J = jobs[job_of(jobs, njobs, blockIdx.x, [](const WmJob& j) { return j.tile0; })];
+  const WmJob& J = jobs[job_of(jobs, njobs, blockIdx.x, [](const WmJob& j) { return j.tile0; })];
+  const int len = J.len;
   const int t0 = ((int)blockIdx.x - J.tile0) * WM_TILE;
-  const int t1 = min(t0 + WM_TILE, J.len);
+  const int t1 = min(t0 + WM_TILE, len);
+  const int32_t* __restrict__ vb = vals + J.base_b;
+  int32_t* __restrict__ inv = J.inv_b;
+  const int sb = J.seg_begin;
   for (int p = t0 + threadIdx.x; p < t1; p += WM_THREADS) {
-    const int w = vals[J.base_b + p] - J.seg_begin;
-    if ((unsigned)w < (unsigned)J.len) J.inv_b[w] = p;
+    const int w = vb[p] - sb;
+    if ((unsigned)w < (unsigned)len) inv[w] = p;
   }
 }
 
-// S_0[i] = inv_b[point at position i of the a order]; ones of the top bit
-// per tile and super tile
+// S_0[i] = inv_b[point at position i of the a order], and the digits of
+// level 0 per tile and super tile
 __global__ void __launch_bounds__(WM_THREADS)
 wm_seq_kernel(const WmJob* __restrict__ jobs, int njobs, const int32_t* __restrict__ vals) {
-  __shared__ uint32_t red[WM_THREADS / 32];
-  const WmJob J = jobs[job_of(jobs, njobs, blockIdx.x, [](const WmJob& j) { return j.tile0; })];
+  __shared__ uint32_t cnt[4];
+  const WmJob& J = jobs[job_of(jobs, njobs, blockIdx.x, [](const WmJob& j) { return j.tile0; })];
+  const int len = J.len;
   const int tile = (int)blockIdx.x - J.tile0;
   const int t0 = tile * WM_TILE;
-  const int t1 = min(t0 + WM_TILE, J.len);
-  const int top = J.L - 1;
-  uint32_t ones = 0;
+  const int t1 = min(t0 + WM_TILE, len);
+  const int sh = 2 * (J.D - 1);
+  const int32_t* __restrict__ va = vals + J.base_a;
+  const int32_t* __restrict__ inv = J.inv_b;
+  int32_t* __restrict__ seq = J.seq0;
+  const int sb = J.seg_begin;
+  if (threadIdx.x < 4) cnt[threadIdx.x] = 0;
+  __syncthreads();
+  uint32_t c[4] = {0, 0, 0, 0};
   for (int i = t0 + threadIdx.x; i < t1; i += WM_THREADS) {
-    const int w = vals[J.base_a + i] - J.seg_begin;
-    const int s = (unsigned)w < (unsigned)J.len ? J.inv_b[w] : 0;
-    J.seq0[i] = s;
-    ones += (uint32_t)(s >> top) & 1u;
+    const int w = va[i] - sb;
+    const int s = (unsigned)w < (unsigned)len ? inv[w] : 0;
+    seq[i] = s;
+    const int dg = (s >> sh) & 3;
+#pragma unroll
+    for (int t = 0; t < 4; ++t) c[t] += dg == t;
   }
-  const uint32_t tot = block_sum(ones, red);
-  if (threadIdx.x == 0 && tot) {
-    J.tcount[tile] = tot;
-    atomicAdd(J.scount + tile / WM_SUPER, tot);
+#pragma unroll
+  for (int t = 0; t < 4; ++t) {
+    const uint32_t v = __reduce_add_sync(0xffffffffu, c[t]);
+    if ((threadIdx.x & 31) == 0 && v) atomicAdd(&cnt[t], v);
+  }
+  __syncthreads();
+  if (threadIdx.x < 4 && cnt[threadIdx.x]) {
+    J.tcount[(size_t)tile * 4 + threadIdx.x] = cnt[threadIdx.x];
+    atomicAdd(J.scount + (size_t)(tile / WM_SUPER) * 4 + threadIdx.x, cnt[threadIdx.x]);
   }
 }
 
-// One level of every job: bits and word prefixes of level l, the stable
-// partition into the sequence of level l + 1, and that level's ones per
-// destination tile.
+// One level of every job: the 64-digit blocks of level l, the stable
+// partition into the sequence of level l + 1, and that level's digits per
+// destination tile.  Warp w holds the values [w * 256, (w + 1) * 256) of the
+// tile in eight rounds of 32; rounds 2m and 2m + 1 form one block.
 __global__ void __launch_bounds__(WM_THREADS)
 wm_level_kernel(const WmJob* __restrict__ jobs, int njobs, int l) {
-  __shared__ uint32_t red[WM_THREADS / 32];
-  __shared__ uint32_t wpre[WM_PER][WM_THREADS / 32];  // ones of (k, warp), then their prefix
-  __shared__ uint32_t next[4];                        // next level's ones per destination tile
-  const WmJob J = jobs[job_of(jobs, njobs, blockIdx.x, [](const WmJob& j) { return j.tile0; })];
-  if (l >= J.L) return;
+  __shared__ uint32_t red[WM_WARPS][8];
+  __shared__ uint32_t wtot[WM_WARPS][4];     // digits of each warp's 256 values
+  __shared__ uint32_t nxt[32];               // next level: [digit t][tile offset][next digit]
+  __shared__ int32_t base[4];                // first destination of each digit from this tile
+  __shared__ uint32_t before_s[4];           // digits of this level before the tile
+  __shared__ uint32_t total_s[4];            // digits of the whole level
+  const WmJob& J = jobs[job_of(jobs, njobs, blockIdx.x, [](const WmJob& j) { return j.tile0; })];
+  const int D = J.D;
+  if (l >= D) return;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int len = J.len;
+  const int ntiles = J.ntiles, nsuper = J.nsuper;
   const int tile = (int)blockIdx.x - J.tile0;
   const int t0 = tile * WM_TILE;
-  const int len = J.len;
-  const int bit = J.L - 1 - l;
+  const int sh = 2 * (D - 1 - l);
   const int32_t* __restrict__ src = (l & 1) ? J.seq1 : J.seq0;
   int32_t* __restrict__ dst = (l & 1) ? J.seq0 : J.seq1;
-  const uint32_t* __restrict__ tc = J.tcount + (size_t)l * J.ntiles;
-  const uint32_t* __restrict__ sc = J.scount + (size_t)l * J.nsuper;
-  uint2* __restrict__ lv = J.levels + (size_t)l * J.nwords;
+  const uint4* __restrict__ tc = reinterpret_cast<const uint4*>(J.tcount) + (size_t)l * ntiles;
+  const uint4* __restrict__ sc = reinterpret_cast<const uint4*>(J.scount) + (size_t)l * nsuper;
+  WmBlock* __restrict__ lv = J.levels + (size_t)l * J.nblocks;
 
-  // ones of this level before the tile, and in all
-  uint32_t before = 0, total = 0;
+  // digits of this level before the tile, and in all
+  uint32_t bf[4] = {0, 0, 0, 0}, tt[4] = {0, 0, 0, 0};
   const int sup = tile / WM_SUPER;
-  for (int s = tid; s < J.nsuper; s += WM_THREADS) {
-    const uint32_t v = sc[s];
-    total += v;
-    before += s < sup ? v : 0u;
+  for (int s = tid; s < nsuper; s += WM_THREADS) {
+    const uint4 v = sc[s];
+    tt[0] += v.x; tt[1] += v.y; tt[2] += v.z; tt[3] += v.w;
+    if (s < sup) { bf[0] += v.x; bf[1] += v.y; bf[2] += v.z; bf[3] += v.w; }
   }
-  for (int t = sup * WM_SUPER + tid; t < tile; t += WM_THREADS) before += tc[t];
-  if (tid < 4) next[tid] = 0;
-  const uint32_t ones_before = block_sum(before, red);
-  const uint32_t ones_total = block_sum(total, red);
-  const int Z = len - (int)ones_total;
-  if (tile == 0 && tid == 0) J.zeros[l] = Z;
-  const int zeros_before = t0 - (int)ones_before;
-
-  int32_t v[WM_PER];
-  uint32_t bal[WM_PER];
-#pragma unroll
-  for (int k = 0; k < WM_PER; ++k) {
-    const int e = t0 + k * WM_THREADS + tid;
-    const bool ok = e < len;
-    v[k] = ok ? src[e] : 0;
-    bal[k] = __ballot_sync(0xffffffffu, ok && ((v[k] >> bit) & 1));
-    if (lane == 0) wpre[k][warp] = __popc(bal[k]);
+  for (int t = sup * WM_SUPER + tid; t < tile; t += WM_THREADS) {
+    const uint4 v = tc[t];
+    bf[0] += v.x; bf[1] += v.y; bf[2] += v.z; bf[3] += v.w;
   }
-  __syncthreads();
-  if (tid == 0) {  // exclusive prefix in value order: (k, warp) k-major
-    uint32_t run = 0;
 #pragma unroll
-    for (int k = 0; k < WM_PER; ++k)
-      for (int w = 0; w < WM_THREADS / 32; ++w) {
-        const uint32_t c = wpre[k][w];
-        wpre[k][w] = run;
-        run += c;
-      }
+  for (int t = 0; t < 4; ++t) {
+    bf[t] = __reduce_add_sync(0xffffffffu, bf[t]);
+    tt[t] = __reduce_add_sync(0xffffffffu, tt[t]);
   }
-  __syncthreads();
-  const bool more = l + 1 < J.L;
-  const int nbit = bit - 1;
-  const int zt0 = zeros_before / WM_TILE;                 // first destination tile, zeros
-  const int ot0 = (Z + (int)ones_before) / WM_TILE;       // ... ones
-  const uint32_t lt = (1u << lane) - 1u;
+  if (lane == 0) {
 #pragma unroll
-  for (int k = 0; k < WM_PER; ++k) {
-    const int w0 = t0 + k * WM_THREADS + warp * 32;       // first value of this word
-    if (lane == 0 && w0 < len) lv[w0 >> 5] = make_uint2(bal[k], ones_before + wpre[k][warp]);
-    const int e = w0 + lane;
-    const bool ok = e < len;
-    const int r1 = (int)(wpre[k][warp] + __popc(bal[k] & lt));   // ones before e in the tile
-    const int r0 = (e - t0) - r1;
-    const bool one = (bal[k] >> lane) & 1u;
-    const int dest = one ? Z + (int)ones_before + r1 : zeros_before + r0;
-    if (more) {
-      if (ok && (unsigned)dest < (unsigned)len) dst[dest] = v[k];
-      const bool nb = ok && ((v[k] >> nbit) & 1);
-      const int slot = one ? 2 + (dest / WM_TILE - ot0) : (dest / WM_TILE - zt0);
-#pragma unroll
-      for (int s = 0; s < 4; ++s) {
-        const uint32_t c = __popc(__ballot_sync(0xffffffffu, nb && slot == s));
-        if (lane == 0 && c) atomicAdd(&next[s], c);
-      }
+    for (int t = 0; t < 4; ++t) {
+      red[warp][t] = bf[t];
+      red[warp][4 + t] = tt[t];
     }
   }
-  // a length that is a multiple of 32 leaves one more word: no bits, every one
-  if (tid == 0 && (len & 31) == 0 && t0 + WM_TILE >= len) lv[len >> 5] = make_uint2(0u, ones_total);
+  if (tid < 32) nxt[tid] = 0;
+
+  // this warp's values and their digits
+  const int wbase = t0 + warp * (WM_TILE / WM_WARPS);
+  int32_t v[WM_ROUNDS];
+  uint32_t bh[WM_ROUNDS], bl[WM_ROUNDS], bv[WM_ROUNDS];
+  uint32_t wc[4] = {0, 0, 0, 0};
+#pragma unroll
+  for (int k = 0; k < WM_ROUNDS; ++k) {
+    const int e = wbase + k * 32 + lane;
+    const bool ok = e < len;
+    v[k] = ok ? src[e] : 0;
+    const int dg = (v[k] >> sh) & 3;
+    bh[k] = __ballot_sync(0xffffffffu, ok && (dg & 2));
+    bl[k] = __ballot_sync(0xffffffffu, ok && (dg & 1));
+    bv[k] = __ballot_sync(0xffffffffu, ok);
+    wc[0] += __popc(bv[k] & ~bh[k] & ~bl[k]);
+    wc[1] += __popc(bv[k] & ~bh[k] & bl[k]);
+    wc[2] += __popc(bh[k] & ~bl[k]);
+    wc[3] += __popc(bh[k] & bl[k]);
+  }
+  if (lane == 0) {
+#pragma unroll
+    for (int t = 0; t < 4; ++t) wtot[warp][t] = wc[t];
+  }
+  __syncthreads();
+  if (tid == 0) {
+    int32_t run = 0;
+    for (int t = 0; t < 4; ++t) {
+      uint32_t b = 0, tot = 0;
+      for (int w = 0; w < WM_WARPS; ++w) {
+        b += red[w][t];
+        tot += red[w][4 + t];
+      }
+      before_s[t] = b;
+      total_s[t] = tot;
+      if (tile == 0) J.bucket[l * 4 + t] = run;   // first position of digit t next level
+      base[t] = run + (int32_t)b;
+      run += (int32_t)tot;
+    }
+  }
+  __syncthreads();
+  // digits before this warp's values in the tile
+  uint32_t wp[4] = {0, 0, 0, 0};
+  for (int w = 0; w < warp; ++w) {
+#pragma unroll
+    for (int t = 0; t < 4; ++t) wp[t] += wtot[w][t];
+  }
+  const uint32_t lt = (1u << lane) - 1u;
+  const bool more = l + 1 < D;
+  const int nsh = sh - 2;
+  int32_t dbase[4], dtile0[4];
+  uint32_t gb[4];
+#pragma unroll
+  for (int t = 0; t < 4; ++t) {
+    dbase[t] = base[t] + (int32_t)wp[t];     // this warp's first destination per digit
+    dtile0[t] = base[t] / WM_TILE;
+    gb[t] = before_s[t] + wp[t];             // digits of the level before this warp
+  }
+#pragma unroll
+  for (int k = 0; k < WM_ROUNDS; ++k) {
+    const uint32_t m0 = bv[k] & ~bh[k] & ~bl[k], m1 = bv[k] & ~bh[k] & bl[k];
+    const uint32_t m2 = bh[k] & ~bl[k], m3 = bh[k] & bl[k];
+    const int e0 = wbase + k * 32;
+    if ((k & 1) == 0 && lane == 0 && e0 < len) {
+      WmBlock B;
+      B.hi[0] = bh[k];
+      B.hi[1] = bh[k + 1];
+      B.lo[0] = bl[k];
+      B.lo[1] = bl[k + 1];
+      B.le[0] = gb[0];
+      B.le[1] = gb[0] + gb[1];
+      B.le[2] = gb[0] + gb[1] + gb[2];
+      B.pad = 0;
+      lv[e0 >> 6] = B;
+    }
+    const int e = e0 + lane;
+    const bool ok = e < len;
+    const int dg = (int)((bh[k] >> lane) & 1u) * 2 + (int)((bl[k] >> lane) & 1u);
+    const uint32_t mine = dg == 0 ? m0 : dg == 1 ? m1 : dg == 2 ? m2 : m3;
+    const int db = dg == 0 ? dbase[0] : dg == 1 ? dbase[1] : dg == 2 ? dbase[2] : dbase[3];
+    const int dt0 = dg == 0 ? dtile0[0] : dg == 1 ? dtile0[1] : dg == 2 ? dtile0[2] : dtile0[3];
+    const int dest = db + __popc(mine & lt);
+    if (more) {
+      if (ok && (unsigned)dest < (unsigned)len) dst[dest] = v[k];
+      const int off = dest / WM_TILE - dt0;
+      const int key = ok && off >= 0 && off < 2 ? dg * 8 + off * 4 + ((v[k] >> nsh) & 3) : -1;
+      const uint32_t peers = __match_any_sync(0xffffffffu, key);
+      if (key >= 0 && (peers & lt) == 0) atomicAdd(&nxt[key], (uint32_t)__popc(peers));
+    }
+    dbase[0] += __popc(m0); dbase[1] += __popc(m1); dbase[2] += __popc(m2); dbase[3] += __popc(m3);
+    gb[0] += __popc(m0); gb[1] += __popc(m1); gb[2] += __popc(m2); gb[3] += __popc(m3);
+  }
+  // a length that is a multiple of 64 leaves one more block: no digits, every count
+  if (tid == 0 && (len & 63) == 0 && t0 + WM_TILE >= len) {
+    WmBlock B;
+    B.hi[0] = B.hi[1] = B.lo[0] = B.lo[1] = 0u;
+    B.le[0] = total_s[0];
+    B.le[1] = total_s[0] + total_s[1];
+    B.le[2] = total_s[0] + total_s[1] + total_s[2];
+    B.pad = 0;
+    lv[len >> 6] = B;
+  }
   if (more) {
     __syncthreads();
-    if (tid < 4 && next[tid]) {
-      const int dtile = tid < 2 ? zt0 + tid : ot0 + (tid - 2);
-      if (dtile >= 0 && dtile < J.ntiles) {
-        atomicAdd(J.tcount + (size_t)(l + 1) * J.ntiles + dtile, next[tid]);
-        atomicAdd(J.scount + (size_t)(l + 1) * J.nsuper + dtile / WM_SUPER, next[tid]);
+    if (tid < 32 && nxt[tid]) {
+      const int t = tid >> 3, off = (tid >> 2) & 1, nd = tid & 3;
+      const int dt = base[t] / WM_TILE + off;
+      if (dt >= 0 && dt < ntiles) {
+        atomicAdd(J.tcount + ((size_t)(l + 1) * ntiles + dt) * 4 + nd, nxt[tid]);
+        atomicAdd(J.scount + ((size_t)(l + 1) * nsuper + dt / WM_SUPER) * 4 + nd, nxt[tid]);
       }
     }
   }
 }
 
 // ------------------------------------------------------------- queries --
-// i is clamped into [0, len]: positions of a consistent matrix never leave
-// it, and the clamp keeps every read inside the level
-__device__ __forceinline__ int rank1(const uint2* __restrict__ lv, int i, int len) {
+// Digits <= t (t = 0, 1, 2) before position i of a level, i clamped to
+// [0, len] (positions of a consistent matrix never leave it; the clamp keeps
+// every read inside the level).
+struct Rank4 {
+  uint32_t le[3];
+};
+__device__ __forceinline__ Rank4 rank4(const WmBlock* __restrict__ lv, int i, int len) {
   i = min(max(i, 0), len);
-  const uint2 w = __ldg(lv + (i >> 5));
-  return (int)w.y + __popc(w.x & ((1u << (i & 31)) - 1u));
+  const uint4* p = reinterpret_cast<const uint4*>(lv + (i >> 6));
+  const uint4 planes = __ldg(p);
+  const uint4 cnts = __ldg(p + 1);
+  const int r = i & 63;
+  const uint64_t mask = r ? (~0ull >> (64 - r)) : 0ull;
+  const uint64_t hi = ((uint64_t)planes.y << 32) | planes.x;
+  const uint64_t lo = ((uint64_t)planes.w << 32) | planes.z;
+  Rank4 R;
+  R.le[0] = cnts.x + (uint32_t)__popcll(~hi & ~lo & mask);
+  R.le[1] = cnts.y + (uint32_t)__popcll(~hi & mask);
+  R.le[2] = cnts.z + (uint32_t)__popcll(~(hi & lo) & mask);
+  return R;
+}
+// digits <= t before i (t = -1 .. 3); selects, not an indexed array, so
+// the ranks stay in registers
+__device__ __forceinline__ int le_of(const Rank4& R, int t, int i) {
+  return t < 0 ? 0 : t == 0 ? (int)R.le[0] : t == 1 ? (int)R.le[1] : t == 2 ? (int)R.le[2] : i;
 }
 
 // #{i in [a, b) : S[i] in [c, d)} for 0 <= a <= b <= len, 0 <= c <= d <= len.
 __device__ int wm_rect(const WmJob& J, int a, int b, int c, int d) {
   if (a >= b || c >= d) return 0;
-  const uint2* __restrict__ base = J.levels;
-  const int L = J.L;
-  int l = 0;
-  for (; l < L; ++l) {  // c and d agree on this bit: one descent
-    const int sh = L - 1 - l;
-    const int cb = (c >> sh) & 1;
-    if (cb != ((d >> sh) & 1)) break;
-    const uint2* lv = base + (size_t)l * J.nwords;
-    const int ra = a - rank1(lv, a, J.len), rb = b - rank1(lv, b, J.len);
-    if (cb) {
-      const int Z = __ldg(J.zeros + l);
-      a = Z + (a - ra);
-      b = Z + (b - rb);
-    } else {
-      a = ra;
-      b = rb;
-    }
+  const WmBlock* __restrict__ levels = J.levels;
+  const int32_t* __restrict__ bucket = J.bucket;
+  const int D = J.D, nb = J.nblocks, len = J.len;
+  int l = 0, tc = 0, td = 0;
+  for (; l < D; ++l) {  // c and d share this digit: one descent
+    const int sh = 2 * (D - 1 - l);
+    tc = (c >> sh) & 3;
+    td = (d >> sh) & 3;
+    if (tc != td) break;
+    const WmBlock* lv = levels + (size_t)l * nb;
+    const Rank4 A = rank4(lv, a, len), B = rank4(lv, b, len);
+    const int bt = __ldg(bucket + 4 * l + tc);
+    a = bt + le_of(A, tc, a) - le_of(A, tc - 1, a);
+    b = bt + le_of(B, tc, b) - le_of(B, tc - 1, b);
     if (a >= b) return 0;
   }
-  if (l >= L) return 0;  // c == d (excluded above)
-  // c has bit 0 here and d bit 1: the zero side counts values >= c, the
-  // one side values < d; the two descents run side by side
-  const uint2* lv = base + (size_t)l * J.nwords;
-  const int ra = a - rank1(lv, a, J.len), rb = b - rank1(lv, b, J.len);
-  const int Zl = __ldg(J.zeros + l);
-  int a0 = ra, b0 = rb;                          // zero side: count < c, subtract
-  int a1 = Zl + (a - ra), b1 = Zl + (b - rb);    // one side: count < d
-  int res = b0 - a0;
-  for (++l; l < L; ++l) {
-    const int sh = L - 1 - l;
-    const uint2* lv2 = base + (size_t)l * J.nwords;
-    const int Z = __ldg(J.zeros + l);
-    if (a0 < b0) {
-      const int r0a = a0 - rank1(lv2, a0, J.len), r0b = b0 - rank1(lv2, b0, J.len);
-      if ((c >> sh) & 1) {
-        res -= r0b - r0a;
-        a0 = Z + (a0 - r0a);
-        b0 = Z + (b0 - r0b);
-      } else {
-        a0 = r0a;
-        b0 = r0b;
-      }
+  if (l >= D) return 0;  // c == d (excluded above)
+  // first differing digit tc < td: digits strictly between count whole
+  const WmBlock* lv = levels + (size_t)l * nb;
+  const Rank4 A = rank4(lv, a, len), B = rank4(lv, b, len);
+  int res = (le_of(B, td - 1, b) - le_of(A, td - 1, a)) - (le_of(B, tc, b) - le_of(A, tc, a));
+  const int bc = __ldg(bucket + 4 * l + tc), bd = __ldg(bucket + 4 * l + td);
+  int a0 = bc + le_of(A, tc, a) - le_of(A, tc - 1, a);   // digit tc: count values >= c
+  int b0 = bc + le_of(B, tc, b) - le_of(B, tc - 1, b);
+  int a1 = bd + le_of(A, td, a) - le_of(A, td - 1, a);   // digit td: count values < d
+  int b1 = bd + le_of(B, td, b) - le_of(B, td - 1, b);
+  res += b0 - a0;
+  for (++l; l < D; ++l) {
+    const int sh = 2 * (D - 1 - l);
+    const WmBlock* lv2 = levels + (size_t)l * nb;
+    if (a0 < b0) {  // values >= c: subtract those below c's digit
+      const int t = (c >> sh) & 3;
+      const Rank4 P = rank4(lv2, a0, len), Q = rank4(lv2, b0, len);
+      res -= le_of(Q, t - 1, b0) - le_of(P, t - 1, a0);
+      const int bt = __ldg(bucket + 4 * l + t);
+      a0 = bt + le_of(P, t, a0) - le_of(P, t - 1, a0);
+      b0 = bt + le_of(Q, t, b0) - le_of(Q, t - 1, b0);
     }
-    if (a1 < b1) {
-      const int r1a = a1 - rank1(lv2, a1, J.len), r1b = b1 - rank1(lv2, b1, J.len);
-      if ((d >> sh) & 1) {
-        res += r1b - r1a;
-        a1 = Z + (a1 - r1a);
-        b1 = Z + (b1 - r1b);
-      } else {
-        a1 = r1a;
-        b1 = r1b;
-      }
+    if (a1 < b1) {  // values < d: add those below d's digit
+      const int t = (d >> sh) & 3;
+      const Rank4 P = rank4(lv2, a1, len), Q = rank4(lv2, b1, len);
+      res += le_of(Q, t - 1, b1) - le_of(P, t - 1, a1);
+      const int bt = __ldg(bucket + 4 * l + t);
+      a1 = bt + le_of(P, t, a1) - le_of(P, t - 1, a1);
+      b1 = bt + le_of(Q, t, b1) - le_of(Q, t - 1, b1);
     }
     if (a0 >= b0 && a1 >= b1) break;
   }
   return res;
 }
 
-// [lo, hi): the positions of the sorted keys within [kl, kr], around p (whose
-// key lies inside): gallop outward, then bisect.
-__device__ __forceinline__ void key_range(const uint64_t* __restrict__ keys, int len, int p,
-                                          uint64_t kl, uint64_t kr, int& lo, int& hi) {
-  int a = p, step = 1;
-  while (a + step < len && __ldg(keys + a + step) <= kr) {
-    a += step;
-    step <<= 1;
-  }
-  int b = a + step < len ? a + step : len;
-  while (b - a > 1) {
-    const int m = a + ((b - a) >> 1);
-    if (__ldg(keys + m) <= kr) a = m; else b = m;
-  }
-  hi = a + 1;
-  a = p;
-  step = 1;
-  while (a - step >= 0 && __ldg(keys + a - step) >= kl) {
-    a -= step;
-    step <<= 1;
-  }
-  b = a - step >= 0 ? a - step : -1;
-  while (a - b > 1) {
-    const int m = b + ((a - b) >> 1);
-    if (__ldg(keys + m) >= kl) a = m; else b = m;
-  }
-  lo = a;
-}
-
 __global__ void __launch_bounds__(WM_QBLOCK)
 wm_count_kernel(const TaskDev* __restrict__ tasks, const WmJob* __restrict__ jobs, int njobs,
-                const uint64_t* __restrict__ keys_all, const int32_t* __restrict__ vals_all) {
+                const uint64_t* __restrict__ keys_all, const uint64_t* __restrict__ s1_all,
+                const uint64_t* __restrict__ s2_all, const int32_t* __restrict__ vals_all) {
   const WmJob& J = jobs[job_of(jobs, njobs, blockIdx.x, [](const WmJob& j) { return j.qblk0; })];
+  const int len = J.len;
   const int i = ((int)blockIdx.x - J.qblk0) * WM_QBLOCK + threadIdx.x;
-  if (i >= J.len) return;
+  if (i >= len) return;
   const TaskDev& t = tasks[J.task];
   const int32_t w = vals_all[J.base_a + i];          // working index of the query
   const double r = t.rad[w];
@@ -304,24 +371,44 @@ wm_count_kernel(const TaskDev* __restrict__ tasks, const WmJob* __restrict__ job
   if (!(r >= 0.0)) {
     count = 0;
   } else if (isinf(r)) {
-    count = J.len;
+    count = len;
   } else {
     const uint64_t* __restrict__ ka = keys_all + J.base_a;
     const uint64_t* __restrict__ kb = keys_all + J.base_b;
-    const int jb = min(max(J.inv_b[w - J.seg_begin], 0), J.len - 1);
+    const int jb = min(max(J.inv_b[w - J.seg_begin], 0), len - 1);
     uint64_t al, ar, bl, br;
     ball_keys(value_of(ka[i]), r, al, ar);
-    ball_keys(value_of(kb[jb]), r, bl, br);
+    ball_keys(value_of(__ldg(kb + jb)), r, bl, br);
     // the sorted keys fold -0 into +0, as the predicate does
     al = al == 0x7fffffffffffffffull ? 0x8000000000000000ull : al;
     bl = bl == 0x7fffffffffffffffull ? 0x8000000000000000ull : bl;
-    int alo, ahi, blo, bhi;
-    key_range(ka, J.len, i, al, ar, alo, ahi);
-    key_range(kb, J.len, jb, bl, br, blo, bhi);
+    const uint64_t* s1a = s1_all + J.s1_a;
+    const uint64_t* s2a = s2_all + J.s2_a;
+    const uint64_t* s1b = s1_all + J.s1_b;
+    const uint64_t* s2b = s2_all + J.s2_b;
+    const int alo = sampled_bound<false>(ka, s1a, s2a, len, al);
+    const int ahi = sampled_bound<true>(ka, s1a, s2a, len, ar);
+    const int blo = sampled_bound<false>(kb, s1b, s2b, len, bl);
+    const int bhi = sampled_bound<true>(kb, s1b, s2b, len, br);
     count = wm_rect(J, alo, ahi, blo, bhi);
   }
   t.cnt[J.slot][w] = count;
 }
+
+// s1[j] = keys[32 j], s2[j] = keys[1024 j] of every sorted segment
+__global__ void samples_kernel(const SortSeg* __restrict__ segs, const int32_t* __restrict__ blk_seg,
+                               const uint64_t* __restrict__ keys, uint64_t* __restrict__ s1,
+                               uint64_t* __restrict__ s2) {
+  const SortSeg sg = segs[blk_seg[blockIdx.x]];
+  const int i0 = ((int)blockIdx.x - sg.blk0) * SORT_TILE;
+  const int j = i0 / SAMPLE1 + (int)threadIdx.x;   // SORT_TILE / SAMPLE1 threads
+  const int p = j * SAMPLE1;
+  if (p >= sg.len || p >= i0 + SORT_TILE) return;
+  const uint64_t k = keys[sg.out_base + p];
+  s1[sg.s1_base + j] = k;
+  if (p % SAMPLE2 == 0) s2[sg.s2_base + p / SAMPLE2] = k;
+}
+static_assert(SORT_TILE % SAMPLE1 == 0, "sample grid");
 
 }  // namespace
 
@@ -339,10 +426,18 @@ void launch_wm_build(const WmJob* jobs_d, int njobs, int total_tiles, int max_le
 }
 
 void launch_wm_count(const TaskDev* tasks_d, const WmJob* jobs_d, int njobs, int total_blocks,
-                     const uint64_t* sorted_keys, const int32_t* sorted_vals, cudaStream_t st) {
+                     const uint64_t* sorted_keys, const uint64_t* samples1,
+                     const uint64_t* samples2, const int32_t* sorted_vals, cudaStream_t st) {
   if (njobs <= 0 || total_blocks <= 0) return;
-  wm_count_kernel<<<total_blocks, WM_QBLOCK, 0, st>>>(tasks_d, jobs_d, njobs, sorted_keys,
-                                                      sorted_vals);
+  wm_count_kernel<<<total_blocks, WM_QBLOCK, 0, st>>>(tasks_d, jobs_d, njobs, sorted_keys, samples1,
+                                                      samples2, sorted_vals);
+  count_launch();
+}
+
+void launch_samples(const SortSeg* segs_d, const int32_t* blk_seg_d, int nblk,
+                    const uint64_t* keys, uint64_t* samples1, uint64_t* samples2, cudaStream_t st) {
+  if (nblk <= 0) return;
+  samples_kernel<<<nblk, SORT_TILE / SAMPLE1, 0, st>>>(segs_d, blk_seg_d, keys, samples1, samples2);
   count_launch();
 }
 
