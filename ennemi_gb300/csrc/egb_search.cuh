@@ -59,6 +59,104 @@ __device__ __forceinline__ int sampled_bound(const uint64_t* __restrict__ keys,
   const int b0 = (c1 - 1) * SAMPLE1;
   return first_above<UPPER>(keys, b0 + 1, min(b0 + SAMPLE1, len), x);
 }
+
+// ---------------------------------------------------- ball as positions --
+// Largest float <= the non-negative double with bit pattern u (integer
+// operations only; 0 below the normal range, FLT_MAX above it).
+__device__ __forceinline__ float f32_down_of_bits(uint64_t u) {
+  const int e = (int)(u >> 52);
+  if (e >= 1023 + 128) return __int_as_float(0x7f7fffff);
+  if (e < 1023 - 126) return 0.0f;
+  return __int_as_float((int)(((uint32_t)(e - 1023 + 127) << 23) |
+                              (uint32_t)((u & 0xfffffffffffffull) >> 29)));
+}
+// Floats bounding a double from below and above (integer operations only).
+__device__ __forceinline__ float f32_below(double v) {
+  const uint64_t u = (uint64_t)__double_as_longlong(v);
+  const uint64_t a = u & 0x7fffffffffffffffull;
+  return (u >> 63) ? -f32_up_of_bits(a) : f32_down_of_bits(a);
+}
+__device__ __forceinline__ float f32_above(double v) {
+  const uint64_t u = (uint64_t)__double_as_longlong(v);
+  const uint64_t a = u & 0x7fffffffffffffffull;
+  return (u >> 63) ? -f32_down_of_bits(a) : f32_up_of_bits(a);
+}
+// Sort key (key_of) of the double equal to a finite float, by integer
+// widening: exact, -0 folded into +0.
+__device__ __forceinline__ uint64_t key_of_f32(float f) {
+  const uint32_t b = (uint32_t)__float_as_int(f);
+  const uint64_t s = (uint64_t)(b >> 31) << 63;
+  const uint32_t e = (b >> 23) & 0xffu, m = b & 0x7fffffu;
+  uint64_t d;
+  if (e != 0) {
+    d = s | ((uint64_t)(e - 127 + 1023) << 52) | ((uint64_t)m << 29);
+  } else if (m != 0) {  // subnormal float: a normal double
+    const int p = 31 - __clz((int)m);                 // highest set bit, 0 .. 22
+    d = s | ((uint64_t)(p - 149 + 1023) << 52) | (((uint64_t)m << (52 - p)) & 0xfffffffffffffull);
+  } else {
+    d = 0;  // +0 and -0
+  }
+  return (d >> 63) ? ~d : (d | 0x8000000000000000ull);
+}
+
+// Positions [lo, hi) of the sorted keys of a segment whose values x have
+// fl64(|x - q|) <= r (q finite, r finite and >= 0): the inclusive ball of
+// query_ball_point in one coordinate.
+//
+// The ends come from FP32 brackets, not from FP64 arithmetic (GB300 issues
+// FP64 at a small fraction of its FP32 and integer rates).  With P(x) =
+// [fl64(x - q) <= r] (true for small x) and Q(x) = [fl64(q - x) <= r] (true
+// for large x), both monotone because rounding is:
+//   x <= q + r            => P(x)   (x - q <= r, r representable)
+//   x >= q + next_up(r)   => !P(x)  (x - q >= next_up(r) rounds to >= it)
+// and symmetrically for Q.  The floats a1 <= q + r, b1 >= q + next_up(r)
+// (and b0 >= q - r, a0 <= q - next_up(r)) come from FP32 additions rounded
+// down / up on floats bounding q and r.  Every key below key(a1) satisfies
+// P, every key above key(b1) fails it; the few keys between -- usually
+// none -- are decided by the exact FP64 predicate.  A bracket that is not
+// finite or holds more than BALL_SCAN keys (values far outside the FP32
+// range, or all crowded into a few FP32 ulps) takes the exact FP64 search
+// of ball_keys instead.
+constexpr int BALL_SCAN = 16;
+__device__ __forceinline__ void ball_positions(const uint64_t* __restrict__ keys,
+                                               const uint64_t* __restrict__ s1,
+                                               const uint64_t* __restrict__ s2, int len, double q,
+                                               double r, int& lo, int& hi) {
+  const float qd = f32_below(q), qu = f32_above(q), rd = f32_below(r), ru = f32_above(r);
+  const float rn = __int_as_float(__float_as_int(ru) + 1);   // next float above ru (ru >= 0)
+  const float a1 = __fadd_rd(qd, rd), b1 = __fadd_ru(qu, rn);
+  const float a0 = __fsub_rd(qd, rn), b0 = __fsub_ru(qu, rd);
+  bool exact = isfinite(a1) && isfinite(b1) && isfinite(a0) && isfinite(b0) && isfinite(q);
+  if (exact) {
+    const uint64_t ka1 = key_of_f32(a1), kb1 = key_of_f32(b1);
+    int p = sampled_bound<false>(keys, s1, s2, len, ka1);
+    int n = 0;
+    for (; p < len; ++p, ++n) {
+      const uint64_t k = __ldg(keys + p);
+      if (k > kb1 || n == BALL_SCAN || !(value_of(k) - q <= r)) break;
+    }
+    hi = p;
+    exact = n < BALL_SCAN;
+  }
+  if (exact) {
+    const uint64_t ka0 = key_of_f32(a0), kb0 = key_of_f32(b0);
+    int p = sampled_bound<true>(keys, s1, s2, len, kb0);
+    int n = 0;
+    for (; p > 0; --p, ++n) {
+      const uint64_t k = __ldg(keys + p - 1);
+      if (k < ka0 || n == BALL_SCAN || !(q - value_of(k) <= r)) break;
+    }
+    lo = p;
+    exact = n < BALL_SCAN;
+  }
+  if (!exact) {  // the exact key range, then its positions
+    uint64_t kl, kr;
+    ball_keys(q, r, kl, kr);
+    kl = kl == 0x7fffffffffffffffull ? 0x8000000000000000ull : kl;  // raw -0 -> +0
+    lo = sampled_bound<false>(keys, s1, s2, len, kl);
+    hi = sampled_bound<true>(keys, s1, s2, len, kr);
+  }
+}
 #endif
 
 }  // namespace egb

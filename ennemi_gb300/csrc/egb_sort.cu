@@ -272,17 +272,10 @@ __global__ void sorted_jobs_kernel(const TaskDev* __restrict__ tasks,
   } else if (r == INF) {
     count = (int32_t)len;
   } else {
-    // The ball is one key range (ball_keys); its ends are found through the
-    // segment's two levels of samples (integer compares only; the FP64
-    // pipe is a small fraction of the integer rate on GB300).  The sorted
-    // keys fold -0 into +0, as the predicate does.
-    uint64_t kL, kR;
-    ball_keys(q, r, kL, kR);
-    kL = kL == 0x7fffffffffffffffull ? 0x8000000000000000ull : kL;  // raw -0 -> +0
-    const uint64_t* s1 = s1_all + jb.s1_base;
-    const uint64_t* s2 = s2_all + jb.s2_base;
-    const int lo = sampled_bound<false>(keys, s1, s2, (int)len, kL);
-    const int hi = sampled_bound<true>(keys, s1, s2, (int)len, kR);
+    // The ball is one run of sorted positions; its ends come from FP32
+    // brackets and the segment's samples (ball_positions, egb_search.cuh).
+    int lo, hi;
+    ball_positions(keys, s1_all + jb.s1_base, s2_all + jb.s2_base, (int)len, q, r, lo, hi);
     count = (int32_t)(hi - lo);
   }
   t.cnt[jb.slot][i] = count;

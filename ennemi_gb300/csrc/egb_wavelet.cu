@@ -24,7 +24,7 @@
 // Storage: each level is a sequence of 32-byte blocks of 64 digits (two bit
 // planes and the counts of digits <= 0, <= 1, <= 2 before the block), so a
 // rank costs one block read.  Range ends come from the sorted keys through
-// their two levels of samples (egb_search.cuh).
+// FP32 brackets and two levels of samples (ball_positions, egb_search.cuh).
 //
 // Build: one block per tile of WM_TILE values and one launch per level.  A
 // block needs the digit counts of its level before its tile: the previous
@@ -376,20 +376,9 @@ wm_count_kernel(const TaskDev* __restrict__ tasks, const WmJob* __restrict__ job
     const uint64_t* __restrict__ ka = keys_all + J.base_a;
     const uint64_t* __restrict__ kb = keys_all + J.base_b;
     const int jb = min(max(J.inv_b[w - J.seg_begin], 0), len - 1);
-    uint64_t al, ar, bl, br;
-    ball_keys(value_of(ka[i]), r, al, ar);
-    ball_keys(value_of(__ldg(kb + jb)), r, bl, br);
-    // the sorted keys fold -0 into +0, as the predicate does
-    al = al == 0x7fffffffffffffffull ? 0x8000000000000000ull : al;
-    bl = bl == 0x7fffffffffffffffull ? 0x8000000000000000ull : bl;
-    const uint64_t* s1a = s1_all + J.s1_a;
-    const uint64_t* s2a = s2_all + J.s2_a;
-    const uint64_t* s1b = s1_all + J.s1_b;
-    const uint64_t* s2b = s2_all + J.s2_b;
-    const int alo = sampled_bound<false>(ka, s1a, s2a, len, al);
-    const int ahi = sampled_bound<true>(ka, s1a, s2a, len, ar);
-    const int blo = sampled_bound<false>(kb, s1b, s2b, len, bl);
-    const int bhi = sampled_bound<true>(kb, s1b, s2b, len, br);
+    int alo, ahi, blo, bhi;
+    ball_positions(ka, s1_all + J.s1_a, s2_all + J.s2_a, len, value_of(ka[i]), r, alo, ahi);
+    ball_positions(kb, s1_all + J.s1_b, s2_all + J.s2_b, len, value_of(__ldg(kb + jb)), r, blo, bhi);
     count = wm_rect(J, alo, ahi, blo, bhi);
   }
   t.cnt[J.slot][w] = count;

@@ -135,6 +135,15 @@ def _medium_cases():
     yield "mi_4100", "mi", 3, dict(x=g[:4100, 0], y=g[:4100, 1])
     yield "cmi_dup_z_15k", "cmi", 3, dict(x=c3[:15000, 0], y=c3[:15000, 1],
                                            z=np.round(c3[:15000, 2:], 0))
+    # ball ends from FP32 brackets: values far below the FP32 normal range
+    # (bracket holds everything -> exact path), scales spread over 40 decades,
+    # and balls whose left end crosses zero
+    yield "mi_tiny_scales_12k", "mi", 3, dict(x=1e-30 * g[:12000, 0], y=1e-42 * g[:12000, 1])
+    spread = 10.0 ** rng.uniform(-20, 20, size=n)
+    yield "mi_spread_scales_20k", "mi", 3, dict(x=g[:, 0] * spread, y=g[:, 1])
+    near0 = np.concatenate([rng.uniform(-1e-3, 1e-3, size=10000), rng.normal(size=10000)])
+    yield "cmi_near_zero_20k", "cmi", 3, dict(x=near0, y=near0[::-1] + 0.1 * g[:, 1],
+                                               z=np.abs(near0)[:, None])
 
 
 MEDIUM = list(_medium_cases())
@@ -149,6 +158,19 @@ def test_medium_against_oracle(oracle, case, variant):
     vals = N.run_tasks([task], flags=VARIANTS[variant] | N.KEEP_INTERNALS)
     check_internals(0, kind, task.n, ref["eps"], ref)
     assert same_value(vals[0], ref_value), (vals[0], ref_value)
+
+
+def test_ball_count_radius_on_exact_distances(oracle):
+    """Radii equal to exact coordinate distances of dyadic data: every
+    boundary is a tie that the inclusive test keeps."""
+    rng = np.random.default_rng(11)
+    for d in [1, 2]:
+        pts = rng.integers(-4000, 4000, size=(9000, d)) / 64.0
+        r = rng.integers(0, 200, size=9000) / 64.0
+        r[::50] = 0.0
+        r[7::50] = -0.0
+        cnt = N.ball_count(pts, r)
+        assert np.array_equal(cnt, oracle.ball_count(pts, r)), d
 
 
 def test_primitives_against_oracle(oracle):
