@@ -714,8 +714,8 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   const size_t off_vals_b = dl.take(sizeof(int32_t) * (size_t)std::max<int64_t>(sort_total, 1));
   const size_t off_s1 = dl.take(sizeof(uint64_t) * (size_t)std::max<int64_t>(s1_total, 1));
   const size_t off_s2 = dl.take(sizeof(uint64_t) * (size_t)std::max<int64_t>(s2_total, 1));
-  const size_t off_hist = dl.take(sizeof(uint32_t) * 256 * (size_t)std::max(nblk_sort, 1));
-  const size_t off_scan = dl.take(sizeof(uint32_t) * sort_scan_tmp_elems(std::max(nblk_sort, 1)));
+  const size_t sweep_bytes = sort_sweep_bytes(nblk_sort, (int)segs.size());
+  const size_t off_sweep = dl.take(sweep_bytes);
 
   // multi-D job blocks
   std::vector<JobDev> jobs(mjobs.size());
@@ -1307,6 +1307,7 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   EGB_CUDA(cudaMemcpyAsync(A + off_tab, H, tab_bytes, cudaMemcpyHostToDevice, st));
   EGB_CUDA(cudaMemsetAsync(A + off_zr, 0, zr_bytes, st));
   if (wmz_bytes) EGB_CUDA(cudaMemsetAsync(A + off_wmz, 0, wmz_bytes, st));
+  if (nblk_sort) EGB_CUDA(cudaMemsetAsync(A + off_sweep, 0, sweep_bytes, st));
   if (inject)  // the device error word as if a kernel had set these bits
     for (int i = 0; i < 4; ++i)
       EGB_CUDA(cudaMemsetAsync((char*)err_d + i, (int)((inject >> (8 * i)) & 0xffu), 1, st));
@@ -1342,8 +1343,8 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   int32_t* vals = (int32_t*)(A + off_vals_a);
   if (timing) EGB_CUDA(cudaEventRecord(ctx->kev[8], st));
   launch_sort(tasks_d, (const SortSeg*)dtab(tab_segs), (const int32_t*)dtab(tab_blkseg), nblk_sort,
-              keys, (uint64_t*)(A + off_keys_b), vals, (int32_t*)(A + off_vals_b),
-              (uint32_t*)(A + off_hist), (uint32_t*)(A + off_scan), st);
+              (int)segs.size(), keys, (uint64_t*)(A + off_keys_b), vals, (int32_t*)(A + off_vals_b),
+              A + off_sweep, err_d, st);
   launch_samples((const SortSeg*)dtab(tab_segs), (const int32_t*)dtab(tab_blkseg), nblk_sort, keys,
                  (uint64_t*)(A + off_s1), (uint64_t*)(A + off_s2), st);
   if (timing) EGB_CUDA(cudaEventRecord(ctx->kev[9], st));

@@ -474,9 +474,12 @@ void launch_radix_pass(const SortSeg* segs_d, const int32_t* blk_seg_d, int nblk
                        const uint64_t* kin, const int32_t* vin, uint64_t* kout, int32_t* vout,
                        int shift, uint32_t* hist, uint32_t* scan_tmp, cudaStream_t st);
 size_t sort_scan_tmp_elems(int nblk);
+// The batch sort: single-sweep LSD passes; `sweep` (sort_sweep_bytes, zeroed
+// before the launch) holds its look-back flags, digit totals and tile counters.
+size_t sort_sweep_bytes(int nblk, int nseg);
 void launch_sort(const TaskDev* tasks_d, const SortSeg* segs_d, const int32_t* blk_seg_d,
-                 int nblk, uint64_t* keys_a, uint64_t* keys_b, int32_t* vals_a,
-                 int32_t* vals_b, uint32_t* hist, uint32_t* scan_tmp, cudaStream_t st);
+                 int nblk, int nseg, uint64_t* keys_a, uint64_t* keys_b, int32_t* vals_a,
+                 int32_t* vals_b, void* sweep, uint32_t* err, cudaStream_t st);
 constexpr int SORTED_BLOCK = 256;
 void launch_sorted_jobs(const TaskDev* tasks_d, const SortedJob* jobs_d, int njobs,
                         int total_blocks, const uint64_t* keys, const uint64_t* samples1,

@@ -2,7 +2,9 @@
 // 1-D estimator kernels that run on the sorted arrays.
 //
 // Sort.  Every requested (task, column, segment) is one segment of a single
-// concatenated key array.  Keys are the order-preserving uint64 image of the
+// concatenated key array (the single-sweep passes below; the three-kernel
+// pass -- histogram, scan, scatter -- serves the strip-key passes of the
+// grid layouts).  Keys are the order-preserving uint64 image of the
 // FP64 value (key_of), the payload is the working index of the point.  Eight
 // stable 8-bit LSD passes; each pass is histogram -> exclusive scan ->
 // stable scatter.  Per-block histograms are laid out segment-major,
@@ -18,6 +20,8 @@
 // monotone), so on each side of q the predicate holds on one contiguous run
 // of sorted positions -- one key range (ball_keys), whose ends are found
 // through the segment's samples (egb_search.cuh).
+#include <algorithm>
+
 #include "egb_internal.cuh"
 #include "egb_search.cuh"
 
@@ -57,23 +61,6 @@ __device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* total)
   const uint32_t r = wprefix + x - v;
   __syncthreads();
   return r;
-}
-
-__global__ void sort_load_kernel(const TaskDev* __restrict__ tasks,
-                                 const SortSeg* __restrict__ segs,
-                                 const int32_t* __restrict__ blk_seg,
-                                 uint64_t* __restrict__ keys,
-                                 int32_t* __restrict__ vals) {
-  const int b = blockIdx.x;
-  const SortSeg s = segs[blk_seg[b]];
-  const TaskDev t = tasks[s.task];
-  const double* x = t.x64 + (int64_t)s.col * t.ld + s.src_begin;
-  const int i0 = (b - s.blk0) * SORT_TILE;
-  const int i1 = min(i0 + SORT_TILE, s.len);
-  for (int i = i0 + threadIdx.x; i < i1; i += SORT_THREADS) {
-    keys[s.out_base + i] = key_of(x[i]);
-    vals[s.out_base + i] = s.src_begin + i;
-  }
 }
 
 __global__ void sort_hist_kernel(const SortSeg* __restrict__ segs,
@@ -178,6 +165,175 @@ sort_scatter_kernel(const SortSeg* __restrict__ segs, const int32_t* __restrict_
     const uint32_t pos = gbase[d] + ((uint32_t)t - dstart[d]);
     kout[pos] = k;
     vout[pos] = sv[t];
+  }
+}
+
+// ------------------------------------------------------- single sweep --
+// The batch sort proper: eight stable 8-bit LSD passes, one launch each,
+// after Adinets and Merrill's single-sweep radix sort (Onesweep, 2022).  The
+// load kernel computes the digit totals of all eight passes per segment at
+// once; each pass then needs, per tile and digit, only the count of that
+// digit in the segment's earlier tiles.  A tile takes its id from an atomic
+// counter (so every earlier tile of its segment has started), publishes its
+// own digit counts at once, and looks back over its predecessors' published
+// words -- aggregates or inclusive prefixes -- until it meets an inclusive
+// one; it then publishes its own inclusive prefix and scatters.  A flag word
+// holds the pass + 1 (bits 56-63; other passes' words read as "not yet"),
+// an inclusive bit (55) and the count (bits 0-31), and is written and read
+// whole, so no other data needs ordering.  Every wait is bounded: past
+// OS_SPIN_LIMIT polls the tile records DERR_WAIT_TIMEOUT (the batch then
+// reports EGB_ERR_DEVICE) and goes on.
+constexpr int OS_PASSES = 8;
+constexpr int OS_SPIN_LIMIT = 1 << 22;
+
+__device__ __forceinline__ uint64_t key_of_bits(uint64_t u) {
+  u = u == 0x8000000000000000ull ? 0ull : u;  // -0 -> +0
+  return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
+}
+
+__global__ void __launch_bounds__(SORT_THREADS)
+onesweep_load_kernel(const TaskDev* __restrict__ tasks, const SortSeg* __restrict__ segs,
+                     const int32_t* __restrict__ blk_seg, uint64_t* __restrict__ keys,
+                     int32_t* __restrict__ vals, uint32_t* __restrict__ seg_hist) {
+  __shared__ uint32_t h[OS_PASSES * 256];
+  const int b = blockIdx.x;
+  const int si = blk_seg[b];
+  const SortSeg s = segs[si];
+  for (int i = threadIdx.x; i < OS_PASSES * 256; i += SORT_THREADS) h[i] = 0;
+  __syncthreads();
+  const TaskDev& t = tasks[s.task];
+  const uint64_t* __restrict__ x =
+      reinterpret_cast<const uint64_t*>(t.x64 + (int64_t)s.col * t.ld + s.src_begin);
+  const int i0 = (b - s.blk0) * SORT_TILE;
+  const int i1 = min(i0 + SORT_TILE, s.len);
+  for (int i = i0 + threadIdx.x; i < i1; i += SORT_THREADS) {
+    const uint64_t k = key_of_bits(x[i]);
+    keys[s.out_base + i] = k;
+    vals[s.out_base + i] = s.src_begin + i;
+#pragma unroll
+    for (int p = 0; p < OS_PASSES; ++p) atomicAdd(&h[p * 256 + (uint32_t)((k >> (8 * p)) & 255u)], 1u);
+  }
+  __syncthreads();
+  uint32_t* g = seg_hist + (size_t)si * OS_PASSES * 256;
+  for (int i = threadIdx.x; i < OS_PASSES * 256; i += SORT_THREADS)
+    if (h[i]) atomicAdd(g + i, h[i]);
+}
+
+__global__ void __launch_bounds__(SORT_THREADS)
+onesweep_pass_kernel(const SortSeg* __restrict__ segs, const int32_t* __restrict__ blk_seg,
+                     const uint64_t* __restrict__ kin, const int32_t* __restrict__ vin,
+                     uint64_t* __restrict__ kout, int32_t* __restrict__ vout, int pass,
+                     const uint32_t* __restrict__ seg_hist, unsigned long long* flags,
+                     int* tile_counter, uint32_t* err) {
+  constexpr int NW = SORT_THREADS / 32;
+  constexpr int CH = SORT_TILE / NW;  // keys per warp
+  constexpr int R = CH / 32;          // rounds per warp
+  __shared__ uint32_t wcnt[NW][256];  // per-warp digit counts, then offsets
+  __shared__ uint32_t dstart[256];    // first tile slot of each digit
+  __shared__ uint32_t gbase[256];     // first output position of each digit
+  __shared__ uint64_t sk[SORT_TILE];
+  __shared__ int32_t sv[SORT_TILE];
+  __shared__ int tile_s;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (tid == 0) tile_s = atomicAdd(tile_counter, 1);
+#pragma unroll
+  for (int w = 0; w < NW; ++w) wcnt[w][tid] = 0;
+  __syncthreads();
+  const int b = tile_s;
+  const int si = blk_seg[b];
+  const SortSeg s = segs[si];
+  const int lb = b - s.blk0;
+  const int shift = 8 * pass;
+  const int i0 = lb * SORT_TILE;
+  const int n = min(SORT_TILE, s.len - i0);
+  const uint32_t lt = (1u << lane) - 1u;
+  uint64_t key[R];
+  int32_t val[R];
+  uint32_t dg[R], rk[R];
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const int t = warp * CH + r * 32 + lane;
+    const bool valid = t < n;
+    key[r] = valid ? kin[s.out_base + i0 + t] : 0ull;
+    val[r] = valid ? vin[s.out_base + i0 + t] : 0;
+    const uint32_t d = valid ? (uint32_t)(key[r] >> shift) & 255u : 256u + lane;
+    dg[r] = d;
+    uint32_t peers = 0xffffffffu;  // lanes with the same 9-bit digit
+#pragma unroll
+    for (int bit = 0; bit < 9; ++bit) {
+      const uint32_t bb = __ballot_sync(0xffffffffu, (d >> bit) & 1u);
+      peers &= ((d >> bit) & 1u) ? bb : ~bb;
+    }
+    const uint32_t before = valid ? wcnt[warp][d] : 0u;
+    __syncwarp();
+    if (valid && (peers & lt) == 0) wcnt[warp][d] = before + __popc(peers);
+    __syncwarp();
+    rk[r] = before + __popc(peers & lt);
+  }
+  __syncthreads();
+  uint32_t cnt = 0;  // digit tid: offsets of the warps, then its count in the tile
+#pragma unroll
+  for (int w = 0; w < NW; ++w) {
+    const uint32_t c = wcnt[w][tid];
+    wcnt[w][tid] = cnt;
+    cnt += c;
+  }
+  // publish this tile's count of digit tid, then look back for the count of
+  // digit tid in the segment's earlier tiles
+  const unsigned long long tag = (unsigned long long)(pass + 1) << 56;
+  const unsigned long long INCL = 1ull << 55;
+  unsigned long long* mine = flags + (size_t)b * 256 + tid;
+  uint32_t excl = 0;
+  if (lb == 0) {
+    atomicExch(mine, tag | INCL | cnt);
+  } else {
+    atomicExch(mine, tag | cnt);
+    int pb = b - 1;
+    for (;;) {
+      const volatile unsigned long long* f = flags + (size_t)pb * 256 + tid;
+      unsigned long long w = *f;
+      int spins = 0;
+      while ((w >> 56) != (unsigned long long)(pass + 1)) {
+        if (++spins > OS_SPIN_LIMIT) {
+          atomicOr(err, DERR_WAIT_TIMEOUT);
+          w = tag | INCL;
+          break;
+        }
+        w = *f;
+      }
+      excl += (uint32_t)w;
+      if ((w & INCL) || pb <= s.blk0) break;
+      --pb;
+    }
+    atomicExch(mine, tag | INCL | (excl + cnt));
+  }
+  // digit tid of the whole segment starts after the smaller digits
+  const uint32_t seg_tot = seg_hist[((size_t)si * OS_PASSES + pass) * 256 + tid];
+  const uint32_t seg_off = block_excl_scan(seg_tot, nullptr);
+  gbase[tid] = seg_off + excl;
+  dstart[tid] = block_excl_scan(cnt, nullptr);
+  __syncthreads();
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const int t = warp * CH + r * 32 + lane;
+    if (t < n) {
+      const uint32_t d = dg[r];
+      const uint32_t slot = dstart[d] + wcnt[warp][d] + rk[r];
+      sk[slot] = key[r];
+      sv[slot] = val[r];
+    }
+  }
+  __syncthreads();
+  for (int t = tid; t < n; t += SORT_THREADS) {
+    const uint64_t k = sk[t];
+    const uint32_t d = (uint32_t)(k >> shift) & 255u;
+    const uint32_t pos = gbase[d] + ((uint32_t)t - dstart[d]);
+    if (pos < (uint32_t)s.len) {
+      kout[s.out_base + pos] = k;
+      vout[s.out_base + pos] = sv[t];
+    } else {
+      atomicOr(err, DERR_BAD_INDEX);
+    }
   }
 }
 
@@ -451,23 +607,29 @@ static void excl_scan(uint32_t* data, int64_t n, uint32_t* tmp, cudaStream_t st)
   count_launch();
 }
 
+size_t sort_sweep_bytes(int nblk, int nseg) {
+  return sizeof(unsigned long long) * 256 * (size_t)std::max(nblk, 1) +
+         sizeof(uint32_t) * OS_PASSES * 256 * (size_t)std::max(nseg, 1) + 64;
+}
+
 void launch_sort(const TaskDev* tasks_d, const SortSeg* segs_d, const int32_t* blk_seg_d,
-                 int nblk, uint64_t* keys_a, uint64_t* keys_b, int32_t* vals_a,
-                 int32_t* vals_b, uint32_t* hist, uint32_t* scan_tmp, cudaStream_t st) {
+                 int nblk, int nseg, uint64_t* keys_a, uint64_t* keys_b, int32_t* vals_a,
+                 int32_t* vals_b, void* sweep, uint32_t* err, cudaStream_t st) {
   if (nblk <= 0) return;
-  sort_load_kernel<<<nblk, SORT_THREADS, 0, st>>>(tasks_d, segs_d, blk_seg_d, keys_a, vals_a);
+  // sweep (zeroed by the caller): flag words, segment digit totals, tile counters
+  unsigned long long* flags = (unsigned long long*)sweep;
+  uint32_t* seg_hist = (uint32_t*)(flags + 256 * (size_t)nblk);
+  int* counters = (int*)(seg_hist + OS_PASSES * 256 * (size_t)std::max(nseg, 1));
+  onesweep_load_kernel<<<nblk, SORT_THREADS, 0, st>>>(tasks_d, segs_d, blk_seg_d, keys_a, vals_a,
+                                                     seg_hist);
   count_launch();
   uint64_t* kin = keys_a;
   uint64_t* kout = keys_b;
   int32_t* vin = vals_a;
   int32_t* vout = vals_b;
-  for (int pass = 0; pass < 8; ++pass) {
-    const int shift = 8 * pass;
-    sort_hist_kernel<<<nblk, SORT_THREADS, 0, st>>>(segs_d, blk_seg_d, kin, shift, hist);
-    count_launch();
-    excl_scan(hist, (int64_t)256 * nblk, scan_tmp, st);
-    sort_scatter_kernel<<<nblk, SORT_THREADS, 0, st>>>(segs_d, blk_seg_d, kin, vin, shift,
-                                                       hist, kout, vout);
+  for (int pass = 0; pass < OS_PASSES; ++pass) {
+    onesweep_pass_kernel<<<nblk, SORT_THREADS, 0, st>>>(segs_d, blk_seg_d, kin, vin, kout, vout,
+                                                       pass, seg_hist, flags, counters + pass, err);
     count_launch();
     uint64_t* tk = kin; kin = kout; kout = tk;
     int32_t* tv = vin; vin = vout; vout = tv;
