@@ -99,11 +99,13 @@ struct TaskPlan {
   int center0 = 0;                // first column of the task in the centre array
 };
 
+// A sort segment: a range of one working column, named by the column's
+// identity (equal ids: equal working columns bit for bit, in every task).
 struct SegKey {
-  int task, col;
+  int colid;
   int64_t b, e;
   bool operator<(const SegKey& o) const {
-    return std::tie(task, col, b, e) < std::tie(o.task, o.col, o.b, o.e);
+    return std::tie(colid, b, e) < std::tie(o.colid, o.b, o.e);
   }
 };
 
@@ -546,10 +548,40 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   }
 
   // ------------------------------------------------------ sort segments --
+  // Working columns of different tasks are the same bits when they come from
+  // the same caller column (pointer, stride), the same sample index and
+  // length, in sample order (no class order), with the same preprocessing
+  // (EGB_RESCALE: the same noise positions; statistics depend on the rest):
+  // such columns share one sort segment -- the y column of every task of a
+  // lagged estimate_mi, every column of a pairwise_mi, a shared condition.
+  std::vector<std::vector<int>> colid((size_t)ntasks);
+  {
+    std::map<std::tuple<uintptr_t, int64_t, uintptr_t, int64_t, int64_t, int>, int> ids;
+    int next_id = 0;
+    for (int t = 0; t < ntasks; ++t) {
+      const TaskPlan& p = P[(size_t)t];
+      colid[(size_t)t].resize((size_t)p.ncol);
+      const bool resc = rescale && p.kind != EGB_ENTROPY;
+      for (int c = 0; c < p.ncol; ++c) {
+        if (!p.perm.empty()) {  // class-ordered working columns are the task's own
+          colid[(size_t)t][(size_t)c] = next_id++;
+          continue;
+        }
+        const int zc = c - p.dx - p.dy;
+        const int64_t noise_pos = !resc ? -1 : zc >= 0 ? (int64_t)(p.dx + p.dy) * p.n + zc : (int64_t)c * p.n;
+        const int group = !resc ? 0 : (zc >= 0 && p.dz > 1 ? p.dz : 1);
+        const auto key = std::make_tuple((uintptr_t)tasks[t].cols[c].data, tasks[t].cols[c].stride,
+                                         (uintptr_t)p.index, p.n, noise_pos, group);
+        auto it = ids.find(key);
+        if (it == ids.end()) it = ids.emplace(key, next_id++).first;
+        colid[(size_t)t][(size_t)c] = it->second;
+      }
+    }
+  }
   std::map<SegKey, int> seg_index;
   std::vector<SortSeg> segs;
   auto seg_for = [&](int task, int col, int64_t b, int64_t e) {
-    const SegKey key{task, col, b, e};
+    const SegKey key{colid[(size_t)task][(size_t)col], b, e};
     auto it = seg_index.find(key);
     if (it != seg_index.end()) return it->second;
     SortSeg s{};
@@ -856,12 +888,26 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   }
 
   // rank-space count jobs (wavelet matrices); their tile sums are zeroed
-  // by one memset at the start of the batch
-  std::vector<WmJob> wjobs;
+  // by one memset at the start of the batch.  A matrix depends only on its
+  // two sort segments: count jobs over the same pair (a condition shared by
+  // the tasks of a pairwise_mi) query one matrix, built once (wbuild).
+  std::vector<WmJob> wjobs, wbuild;
+  std::map<std::pair<int, int>, size_t> build_of;
   int wm_tiles = 0, wm_qblocks = 0, wm_levels = 0;
   size_t wmz_bytes = 0;
-  std::vector<size_t> wm_tc_off;  // per job: offset of its sums in the zeroed block
+  std::vector<size_t> wm_tc_off;  // per build: offset of its sums in the zeroed block
   for (const WmPlan& w : wplans) {
+    const auto bkey = std::make_pair(w.seg_a, w.seg_b);
+    auto bit = build_of.find(bkey);
+    if (bit != build_of.end()) {
+      WmJob Q = wbuild[bit->second];
+      Q.task = w.s.task;
+      Q.slot = w.s.slot;
+      Q.qblk0 = wm_qblocks;
+      wm_qblocks += (int)((Q.len + WM_QBLOCK - 1) / WM_QBLOCK);
+      wjobs.push_back(Q);
+      continue;
+    }
     WmJob J{};
     const int64_t len = w.s.e - w.s.b;
     J.task = w.s.task;
@@ -894,6 +940,8 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
     wm_tiles += J.ntiles;
     wm_qblocks += (int)((len + WM_QBLOCK - 1) / WM_QBLOCK);
     wm_levels = std::max(wm_levels, D);
+    build_of.emplace(bkey, wbuild.size());
+    wbuild.push_back(J);
     wjobs.push_back(J);
   }
   const size_t off_wmz = dl.take(std::max<size_t>(wmz_bytes, 16));
@@ -1117,6 +1165,7 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
     G.tab_cum = tl.take(sizeof(int32_t) * G.cum.size());
   }
   const size_t tab_wjobs = tl.take(sizeof(WmJob) * std::max<size_t>(wjobs.size(), 1));
+  const size_t tab_wbuild = tl.take(sizeof(WmJob) * std::max<size_t>(wbuild.size(), 1));
   const size_t tab_cjobs = tl.take(sizeof(CombineJob) * std::max<size_t>(cjobs.size(), 1));
   const size_t tab_chunkjob = tl.take(sizeof(int32_t) * (size_t)std::max(nchunks, 1));
   const size_t tab_bytes = align_up(tl.off, 256);
@@ -1267,16 +1316,29 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
     if (!G.runs.empty()) std::memcpy(H + G.tab_runs, G.runs.data(), sizeof(ItemRun) * G.runs.size());
     if (!G.cum.empty()) std::memcpy(H + G.tab_cum, G.cum.data(), sizeof(int32_t) * G.cum.size());
   }
-  for (size_t w = 0; w < wjobs.size(); ++w) {
-    WmJob J = wjobs[w];
-    J.levels = (WmBlock*)(A + (uintptr_t)J.levels);
-    J.bucket = (int32_t*)(A + (uintptr_t)J.bucket);
-    J.seq0 = (int32_t*)(A + (uintptr_t)J.seq0);
-    J.seq1 = (int32_t*)(A + (uintptr_t)J.seq1);
-    J.inv_b = (int32_t*)(A + (uintptr_t)J.inv_b);
-    J.tcount = (uint32_t*)(A + off_wmz + wm_tc_off[w]);
-    J.scount = J.tcount + 4 * (size_t)J.D * (size_t)J.ntiles;
-    std::memcpy(H + tab_wjobs + sizeof(WmJob) * w, &J, sizeof(WmJob));
+  {
+    // arena offsets -> device pointers; a build's zeroed sums by its index
+    std::map<uintptr_t, size_t> build_index;  // levels offset -> build
+    for (size_t w = 0; w < wbuild.size(); ++w) build_index[(uintptr_t)wbuild[w].levels] = w;
+    auto fix = [&](WmJob J) {
+      const size_t bi = build_index.at((uintptr_t)J.levels);
+      J.levels = (WmBlock*)(A + (uintptr_t)J.levels);
+      J.bucket = (int32_t*)(A + (uintptr_t)J.bucket);
+      J.seq0 = (int32_t*)(A + (uintptr_t)J.seq0);
+      J.seq1 = (int32_t*)(A + (uintptr_t)J.seq1);
+      J.inv_b = (int32_t*)(A + (uintptr_t)J.inv_b);
+      J.tcount = (uint32_t*)(A + off_wmz + wm_tc_off[bi]);
+      J.scount = J.tcount + 4 * (size_t)J.D * (size_t)J.ntiles;
+      return J;
+    };
+    for (size_t w = 0; w < wjobs.size(); ++w) {
+      const WmJob J = fix(wjobs[w]);
+      std::memcpy(H + tab_wjobs + sizeof(WmJob) * w, &J, sizeof(WmJob));
+    }
+    for (size_t w = 0; w < wbuild.size(); ++w) {
+      const WmJob J = fix(wbuild[w]);
+      std::memcpy(H + tab_wbuild + sizeof(WmJob) * w, &J, sizeof(WmJob));
+    }
   }
   if (!cjobs.empty()) std::memcpy(H + tab_cjobs, cjobs.data(), sizeof(CombineJob) * cjobs.size());
   if (nchunks) std::memcpy(H + tab_chunkjob, chunk_job.data(), sizeof(int32_t) * (size_t)nchunks);
@@ -1382,7 +1444,7 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
                             max_gkey > 256 ? gva : gvb, (const SortSeg*)dtab(tab_gsegs),
                             max_lds, st);
   }
-  launch_wm_build((const WmJob*)dtab(tab_wjobs), (int)wjobs.size(), wm_tiles, wm_levels, vals, st);
+  launch_wm_build((const WmJob*)dtab(tab_wbuild), (int)wbuild.size(), wm_tiles, wm_levels, vals, st);
   if (timing) EGB_CUDA(cudaEventRecord(ctx->ev[3], st));
 
   launch_sorted_jobs(tasks_d, (const SortedJob*)dtab(tab_sjk), (int)sj_knn.size(), blk_knn, keys,

@@ -273,3 +273,28 @@ def test_graph_replay_matches_direct_launch():
     st = ctx.stats()
     assert st["planned"] == 0 and st["graph"] == 1
     assert np.array_equal(direct_b, replay_b)
+
+
+def test_tasks_sharing_columns_match_tasks_alone():
+    """Tasks that read the same caller columns share their sort segments and
+    rank-space matrices in one batch; every result equals the task run alone
+    (eps bit for bit, counts exactly)."""
+    rng = np.random.default_rng(31)
+    n = 20000
+    a, b, c = rng.normal(size=(3, n))
+    b += 0.5 * a
+    z = rng.normal(size=(n, 2))
+    z1, z2 = np.ascontiguousarray(z[:, 0]), np.ascontiguousarray(z[:, 1])
+    tasks = [N.Task(N.MI, 3, [a], [b], n=n), N.Task(N.MI, 3, [a], [c], n=n),
+             N.Task(N.MI, 3, [b], [c], n=n), N.Task(N.MI, 3, [c], [a], n=n),
+             N.Task(N.CMI, 3, [a], [b], [z1], n=n), N.Task(N.CMI, 3, [a], [c], [z1], n=n),
+             N.Task(N.CMI, 3, [a], [b], [z1, z2], n=n), N.Task(N.CMI, 3, [b], [c], [z1, z2], n=n),
+             N.Task(N.ENTROPY, 3, [a, z1], n=n)]
+    slots = {N.MI: 2, N.CMI: 3, N.ENTROPY: 0}
+    together = N.run_tasks(tasks, flags=N.KEEP_INTERNALS)
+    kept = [[N.fetch(i, w, n) for w in range(1 + slots[t.kind])] for i, t in enumerate(tasks)]
+    for i, t in enumerate(tasks):
+        alone = N.run_tasks([t], flags=N.KEEP_INTERNALS)
+        assert alone[0] == together[i], i
+        for w in range(1 + slots[t.kind]):
+            assert np.array_equal(N.fetch(0, w, n), kept[i][w]), (i, w)
