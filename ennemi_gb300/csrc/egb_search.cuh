@@ -60,6 +60,44 @@ __device__ __forceinline__ int sampled_bound(const uint64_t* __restrict__ keys,
   return first_above<UPPER>(keys, b0 + 1, min(b0 + SAMPLE1, len), x);
 }
 
+// The same from a position g of the segment near the bound (the query's
+// own position): a gallop over s1 from g's sample, then the 32 keys under
+// the sample found.  Lanes holding consecutive positions read the same
+// sample lines, and no search starts from the top of the segment.
+template <bool UPPER>
+__device__ __forceinline__ int sampled_bound_from(const uint64_t* __restrict__ keys,
+                                                  const uint64_t* __restrict__ s1, int len,
+                                                  uint64_t x, int g) {
+  const int n1 = (int)samples1_of(len);
+  auto before = [&](uint64_t v) { return UPPER ? (v <= x) : (v < x); };  // v precedes the bound
+  int j = min(max(g, 0), len - 1) / SAMPLE1;
+  int c1;  // first sample index that does not precede the bound (n1 if none)
+  if (before(__ldg(s1 + j))) {
+    int lo = j, step = 1, hi;  // s1[lo] precedes
+    for (;;) {
+      const int t = lo + step;
+      if (t >= n1) { hi = n1; break; }
+      if (!before(__ldg(s1 + t))) { hi = t; break; }
+      lo = t;
+      step <<= 1;
+    }
+    c1 = first_above<UPPER>(s1, lo + 1, hi, x);
+  } else {
+    int hi = j, step = 1, lo;  // s1[hi] does not precede
+    for (;;) {
+      const int t = hi - step;
+      if (t < 0) { lo = -1; break; }
+      if (before(__ldg(s1 + t))) { lo = t; break; }
+      hi = t;
+      step <<= 1;
+    }
+    c1 = first_above<UPPER>(s1, lo + 1, hi, x);
+  }
+  if (c1 == 0) return 0;
+  const int b0 = (c1 - 1) * SAMPLE1;
+  return first_above<UPPER>(keys, b0 + 1, min(b0 + SAMPLE1, len), x);
+}
+
 // ---------------------------------------------------- ball as positions --
 // Largest float <= the non-negative double with bit pattern u (integer
 // operations only; 0 below the normal range, FLT_MAX above it).
@@ -118,10 +156,13 @@ __device__ __forceinline__ uint64_t key_of_f32(float f) {
 // range, or all crowded into a few FP32 ulps) takes the exact FP64 search
 // of ball_keys instead.
 constexpr int BALL_SCAN = 16;
+// g: the query's own position in the segment (where q sits), the start of
+// galloping bound searches (measured faster for the 1-D counts, whose warps
+// hold consecutive positions), or -1: searches from the top of the samples.
 __device__ __forceinline__ void ball_positions(const uint64_t* __restrict__ keys,
                                                const uint64_t* __restrict__ s1,
                                                const uint64_t* __restrict__ s2, int len, double q,
-                                               double r, int& lo, int& hi) {
+                                               double r, int g, int& lo, int& hi) {
   const float qd = f32_below(q), qu = f32_above(q), rd = f32_below(r), ru = f32_above(r);
   const float rn = __int_as_float(__float_as_int(ru) + 1);   // next float above ru (ru >= 0)
   const float a1 = __fadd_rd(qd, rd), b1 = __fadd_ru(qu, rn);
@@ -129,7 +170,8 @@ __device__ __forceinline__ void ball_positions(const uint64_t* __restrict__ keys
   bool exact = isfinite(a1) && isfinite(b1) && isfinite(a0) && isfinite(b0) && isfinite(q);
   if (exact) {
     const uint64_t ka1 = key_of_f32(a1), kb1 = key_of_f32(b1);
-    int p = sampled_bound<false>(keys, s1, s2, len, ka1);
+    int p = g >= 0 ? sampled_bound_from<false>(keys, s1, len, ka1, g)
+                   : sampled_bound<false>(keys, s1, s2, len, ka1);
     int n = 0;
     for (; p < len; ++p, ++n) {
       const uint64_t k = __ldg(keys + p);
@@ -140,7 +182,8 @@ __device__ __forceinline__ void ball_positions(const uint64_t* __restrict__ keys
   }
   if (exact) {
     const uint64_t ka0 = key_of_f32(a0), kb0 = key_of_f32(b0);
-    int p = sampled_bound<true>(keys, s1, s2, len, kb0);
+    int p = g >= 0 ? sampled_bound_from<true>(keys, s1, len, kb0, g)
+                   : sampled_bound<true>(keys, s1, s2, len, kb0);
     int n = 0;
     for (; p > 0; --p, ++n) {
       const uint64_t k = __ldg(keys + p - 1);

@@ -431,7 +431,7 @@ __global__ void sorted_jobs_kernel(const TaskDev* __restrict__ tasks,
     // The ball is one run of sorted positions; its ends come from FP32
     // brackets and the segment's samples (ball_positions, egb_search.cuh).
     int lo, hi;
-    ball_positions(keys, s1_all + jb.s1_base, s2_all + jb.s2_base, (int)len, q, r, lo, hi);
+    ball_positions(keys, s1_all + jb.s1_base, s2_all + jb.s2_base, (int)len, q, r, (int)p, lo, hi);
     count = (int32_t)(hi - lo);
   }
   t.cnt[jb.slot][i] = count;

@@ -377,8 +377,8 @@ wm_count_kernel(const TaskDev* __restrict__ tasks, const WmJob* __restrict__ job
     const uint64_t* __restrict__ kb = keys_all + J.base_b;
     const int jb = min(max(J.inv_b[w - J.seg_begin], 0), len - 1);
     int alo, ahi, blo, bhi;
-    ball_positions(ka, s1_all + J.s1_a, s2_all + J.s2_a, len, value_of(ka[i]), r, alo, ahi);
-    ball_positions(kb, s1_all + J.s1_b, s2_all + J.s2_b, len, value_of(__ldg(kb + jb)), r, blo, bhi);
+    ball_positions(ka, s1_all + J.s1_a, s2_all + J.s2_a, len, value_of(ka[i]), r, -1, alo, ahi);
+    ball_positions(kb, s1_all + J.s1_b, s2_all + J.s2_b, len, value_of(__ldg(kb + jb)), r, -1, blo, bhi);
     count = wm_rect(J, alo, ahi, blo, bhi);
   }
   t.cnt[J.slot][w] = count;
