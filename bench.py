@@ -469,64 +469,75 @@ def main():
     phases = ctx.timings()
     work_stats = ctx.stats()
 
-    # roofline of the dominant multi-D kernel (FP32/INT-pipe bound): counted
-    # algorithmic operations ((2d+1) per candidate-query pair) over its own
-    # event-timed duration, against the nominal FP32 lane rate of the part
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
     except (OSError, ValueError):
         pass
-    sms = torch.cuda.get_device_properties(dev).multi_processor_count
-    max_mhz = clocks.get("sm_max_mhz") or peaks.get("sm_max_mhz") or 2070.0
-    peak_ops = sms * 128 * max_mhz * 1e6
-    # multi-D kernels of the workload: the kNN walk (2-D MI and 3-D CMI joint
-    # spaces) and the exact key-range counts (2-D CMI marginals)
-    cand = [("wcount_kernel", phases.get("count_tile", 0.0), work_stats.get("count_tile_ops", 0),
-             work_stats.get("count_tile_pairs", 0)),
-            ("wwalk_kernel", phases.get("knn_tile", 0.0), work_stats.get("knn_tile_ops", 0),
-             work_stats.get("knn_tile_pairs", 0))]
-    kname, kms, kops, kpairs = max(cand, key=lambda c: c[1])
-    achieved = kops / (kms / 1000.0) if kms > 0 else 0.0
-    # the brute-force work of the same jobs (N_q * N_c * (2d+1): every query
-    # against every point of its space), over the pairs actually screened
-    if kname == "wwalk_kernel":
-        bf_ops = sum(float(args.n) ** 2 * (2 * (2 if kind == "mi" else 3) + 1) for kind, _ in work)
-    else:
-        bf_ops = sum(2 * float(args.n) ** 2 * 5 for kind, _ in work if kind == "cmi")
-    # DRAM bytes read + written per launch, from one `ncu --set full` capture
-    # of `bench.py --profile --n 1000000 --steps 1 --warmup 1` (the walk: the
-    # 2-D and the 3-D launch averaged); measured for this workload only
-    ncu_traffic = {"wwalk_kernel": ((114.37 + 16.81) + (40.62 + 0.10)) / 2 * 1e6,
-                   "wcount_kernel": (49.06 + 1.09) * 1e6}
-    traffic = ncu_traffic.get(kname) if args.n == 1_000_000 else None
-    roofline = {"bound": "alu", "kernel": kname, "achieved": achieved / 1e9,
-                "peak": peak_ops / 1e9, "unit": "Gop/s", "frac": achieved / peak_ops,
-                "traffic": traffic, "traffic_unit": "bytes per launch (ncu)", "ms": kms,
-                "pairs": kpairs,
-                "peak_source": (f"nominal FP32 lane rate: {sms} SMs x 128 lanes x {max_mhz:.0f} MHz "
-                                "(MEASURED_PEAKS.json holds only HBM and bf16 figures)"),
-                "ops_per_pair": "2d+1 (d differences, d max-of-abs, 1 compare)",
-                "hbm_peak_gbs": peaks.get("hbm_gbs"),
-                "algorithmic_savings": {
-                    "bruteforce_ops": bf_ops, "counted_ops": kops,
-                    "ratio": bf_ops / kops if kops else None,
-                    "note": "all-pairs work of the same jobs divided by the work the grid "
-                            "layout screens: an algorithmic ratio, not a roofline fraction"}}
-
-    # sort and 1-D search passes (HBM-bound): 32 N algorithmic bytes per 1-D
-    # marginal (8 N keys read, 8 N sorted keys written, 8 N eps read, 8 N
-    # counts written), over the radix sort's and the 1-D counts' event times
-    n1d = sum(2 if kind == "mi" else 1 for kind, _ in work)
-    sort_ms, c1_ms = phases.get("sort_radix", 0.0), phases.get("count_1d", 0.0)
-    ss_bytes = 32.0 * args.n * n1d
     # HBM copy bandwidth measured on the GB300s; without the file,
     # one earlier STREAM-style measurement on a GB300 (6.8 TB/s)
     hbm = peaks.get("hbm_gbs") or 6800.0
     hbm_src = "of measured (MEASURED_PEAKS.json hbm_gbs)" if peaks.get("hbm_gbs") else \
         "of fallback (6.8 TB/s, an earlier copy measurement on a GB300)"
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    max_mhz = clocks.get("sm_max_mhz") or peaks.get("sm_max_mhz") or 2070.0
+    peak_ops = sms * 128 * max_mhz * 1e6
+
+    # The dominant kernel (largest share of the step in the ncu launch list)
+    # is the radix sort's pass, HBM-bound: per launch it reads and writes
+    # every key (8 B) and index (4 B) of the batch's sort once.  Its time per
+    # launch is the event-timed sort (load kernel + 8 passes) over 8, which
+    # slightly overstates it.  DRAM traffic per launch from one ncu capture
+    # of this workload (cold cache): 143.3 MB read + 89.2 MB written.
+    keys = work_stats.get("sort_keys", 0)
+    sort_ms = phases.get("sort_radix", 0.0)
+    pass_ms = sort_ms / 8.0
+    pass_bytes = 24.0 * keys
+    pass_gbs = pass_bytes / (pass_ms / 1000.0) / 1e9 if pass_ms > 0 else 0.0
+    roofline = {"bound": "hbm", "kernel": "onesweep_pass_kernel (radix sort pass)",
+                "achieved": pass_gbs, "peak": hbm, "unit": "GB/s", "frac": pass_gbs / hbm,
+                "traffic": (143.31 + 89.22) * 1e6 if args.n == 1_000_000 else None,
+                "traffic_unit": "bytes per launch (ncu, cold cache)",
+                "algorithmic_bytes_per_launch": pass_bytes, "ms_per_launch": pass_ms,
+                "launches_per_step": 8, "peak_source": hbm_src}
+
+    # the multi-D kernels: latency- and L1-bound, far from any pipe or HBM
+    # roofline; counted algorithmic operations ((2d+1) per screened
+    # candidate-query pair) against the nominal FP32 lane rate, and the
+    # all-pairs work of the same jobs over the screened work (an algorithmic
+    # ratio, not a roofline fraction)
+    knn_ms, cnt_ms = phases.get("knn_tile", 0.0), phases.get("count_tile", 0.0)
+    knn_ops = work_stats.get("knn_tile_ops", 0)
+    bf_ops = sum(float(args.n) ** 2 * (2 * (2 if kind == "mi" else 3) + 1) for kind, _ in work)
+    kernels = {
+        "wwalk_kernel (kNN, 4 x 2-D + 1 x 3-D)": {
+            "ms": knn_ms, "screened_pairs": work_stats.get("knn_tile_pairs", 0),
+            "achieved_gops": knn_ops / (knn_ms / 1000.0) / 1e9 if knn_ms > 0 else 0.0,
+            "nominal_fp32_lane_gops": peak_ops / 1e9,
+            "frac_of_nominal": (knn_ops / (knn_ms / 1000.0)) / peak_ops if knn_ms > 0 else 0.0,
+            "dram_traffic_per_launch": ((114.16 + 16.46) + (40.63 + 0.09)) / 2 * 1e6
+            if args.n == 1_000_000 else None,
+            "algorithmic_savings": {"bruteforce_ops": bf_ops, "counted_ops": knn_ops,
+                                    "ratio": bf_ops / knn_ops if knn_ops else None}},
+        "wm_count_kernel (rank-space counts, 2 x 2-D)": {
+            "ms": cnt_ms, "queries": 2 * args.n,
+            "ns_per_query": cnt_ms * 1e6 / (2 * args.n) if cnt_ms > 0 else None,
+            "dram_traffic_per_launch": (58.82 + 2.06) * 1e6 if args.n == 1_000_000 else None},
+        "sorted_jobs_kernel (1-D counts)": {
+            "ms": phases.get("count_1d", 0.0), "queries": sum(2 if kind == "mi" else 1
+                                                              for kind, _ in work) * args.n},
+    }
+
+    # sort and 1-D search passes together, on the minimal byte count of a 1-D
+    # marginal: 32 N (8 N keys read, 8 N sorted keys written, 8 N eps read,
+    # 8 N counts written) over the radix sort's and the 1-D counts' event
+    # times -- a bound no multi-pass sort reaches (the sort moves 24 B per
+    # key and pass, and sorts the grid-only columns too)
+    n1d = sum(2 if kind == "mi" else 1 for kind, _ in work)
+    sort_ms, c1_ms = phases.get("sort_radix", 0.0), phases.get("count_1d", 0.0)
+    ss_bytes = 32.0 * args.n * n1d
     ss_gbs = ss_bytes / ((sort_ms + c1_ms) / 1000.0) / 1e9 if sort_ms + c1_ms > 0 else 0.0
-    roofline_sort = {"bound": "hbm", "kernels": "radix sort (histogram, scan, scatter) + "
+    roofline_sort = {"bound": "hbm", "kernels": "radix sort (load + 8 single-sweep passes) + "
                                                 "sorted_jobs_kernel 1-D counts",
                      "marginals_1d": n1d, "algorithmic_bytes": ss_bytes,
                      "sort_ms": sort_ms, "count_1d_ms": c1_ms,
@@ -592,6 +603,7 @@ def main():
         "gpu_launches": work_stats.get("kernel_launches"),
         "roofline": roofline,
         "roofline_sort": roofline_sort,
+        "kernels": kernels,
         "parity": parity,
         "phases_ms": phases,
         "work": work_stats,

@@ -138,7 +138,10 @@ def normalize_mi(mi: Union[float, GenArrayLike]) -> GenArrayLike:
         import pandas
         if isinstance(mi, (pandas.DataFrame, pandas.Series)):
             return mi.map(_normalize)
-    return np.vectorize(_normalize, otypes=[float])(mi)
+    arr = np.asarray(mi)
+    if arr.dtype.kind not in "biuf":   # the reference's error for anything else
+        return np.vectorize(_normalize, otypes=[float])(mi)
+    return _native.normalize(arr)      # sqrt(1 - exp(-2 mi)) on the device
 
 
 def _normalize(mi: float) -> float:
@@ -492,11 +495,10 @@ def _pairwise_mi(data: FloatArray, k: int, cond: Optional[FloatArray], preproces
         batch = _Batch()
         slots = [_add_prepared(batch, p) for p in _prepare_all(jobs, max_threads)]
         values = batch.run()[slots] if slots else np.empty(0)
-    result = np.full((nvar, nvar), np.nan)
-    for (i, j), v in zip(pairs, values):
-        result[i, j] = v
-        result[j, i] = v
-        if callback is not None:
+    # the symmetric matrix with a NaN diagonal, assembled on the device
+    result = _native.pairwise_matrix(values, pairs, nvar) if pairs else np.full((nvar, nvar), np.nan)
+    if callback is not None:
+        for i, j in pairs:
             callback(i, j)
     return result
 

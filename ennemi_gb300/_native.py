@@ -123,6 +123,10 @@ def load():
         lib.egb_get_policy.restype = ctypes.c_int
         lib.egb_device_info.argtypes = [vp, ctypes.c_char_p, i32, ctypes.POINTER(i32)]
         lib.egb_device_info.restype = ctypes.c_int
+        lib.egb_pairwise_matrix.argtypes = [vp, vp, vp, i32, i32, i32, i32, vp]
+        lib.egb_pairwise_matrix.restype = ctypes.c_int
+        lib.egb_normalize.argtypes = [vp, vp, i64, i32, vp]
+        lib.egb_normalize.restype = ctypes.c_int
         lib.egb_debug_inject_device_error.argtypes = [vp, ctypes.c_uint32]
         lib.egb_debug_inject_device_error.restype = ctypes.c_int
         lib.egb_version.argtypes = []
@@ -382,4 +386,33 @@ def ball_count(points, radius, flags: int = 0, device: int = 0) -> np.ndarray:
     with ctx.lock:
         ctx.check(ctx.lib.egb_ball_count(ctx.h, p.ctypes.data, p.shape[0], p.shape[1], r.ctypes.data,
                                          flags & ~INPUT_DEVICE, out.ctypes.data), "egb_ball_count")
+    return out
+
+
+def pairwise_matrix(values, pairs, nvar: int, normalize: bool = False, device: int = 0) -> np.ndarray:
+    """The symmetric nvar x nvar matrix of per-pair estimates with a NaN
+    diagonal, assembled on the device (egb_pairwise_matrix); `normalize`
+    applies normalize_mi to the values."""
+    ctx = context(device)
+    v = np.ascontiguousarray(values, dtype=np.float64)
+    p = np.ascontiguousarray(pairs, dtype=np.int32).reshape(-1, 2)
+    if len(v) != len(p):
+        raise ValueError("one pair per value")
+    out = np.empty((nvar, nvar), dtype=np.float64)
+    with ctx.lock:
+        ctx.check(ctx.lib.egb_pairwise_matrix(ctx.h, v.ctypes.data, p.ctypes.data, len(v), int(nvar),
+                                              1 if normalize else 0, 0, out.ctypes.data),
+                  "egb_pairwise_matrix")
+    return out
+
+
+def normalize(values, device: int = 0) -> np.ndarray:
+    """normalize_mi of a float64 array on the device (egb_normalize); the
+    result has the shape of `values`."""
+    ctx = context(device)
+    v = np.ascontiguousarray(values, dtype=np.float64)
+    out = np.empty_like(v)
+    with ctx.lock:
+        ctx.check(ctx.lib.egb_normalize(ctx.h, v.ctypes.data, v.size, 0, out.ctypes.data),
+                  "egb_normalize")
     return out

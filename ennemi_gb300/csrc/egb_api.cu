@@ -174,6 +174,10 @@ struct egb_ctx {
   int64_t stats[NSTATS] = {};
   // egb_debug_inject_device_error: error word the next batch starts with
   uint32_t inject_err = 0;
+  // device buffer of the matrix / normalize calls (apart from the batch
+  // arena, so that they keep a batch's internals and captured graph intact)
+  void* aux = nullptr;
+  size_t aux_cap = 0;
   // internals of the last batch (egb_fetch)
   bool kept = false;
   std::vector<TaskPlan> keep;
@@ -1662,6 +1666,7 @@ void egb_destroy(egb_ctx* ctx) {
   if (ctx->pinned) cudaFreeHost(ctx->pinned);
   if (ctx->psi_d) cudaFree(ctx->psi_d);
   if (ctx->noise_d) cudaFree(ctx->noise_d);
+  if (ctx->aux) cudaFree(ctx->aux);
   for (auto& e : ctx->ev)
     if (e) cudaEventDestroy(e);
   for (auto& e : ctx->kev)
@@ -1807,6 +1812,86 @@ int egb_get_policy(const egb_ctx* ctx, int8_t* modes, int32_t n) {
   const int m = std::min<int>(n, EGB_POLICY_ENTRIES);
   std::memcpy(modes, ctx->policy, (size_t)m);
   return m;
+}
+
+namespace {
+int ensure_aux(egb_ctx* ctx, size_t bytes) {
+  if (bytes <= ctx->aux_cap) return EGB_OK;
+  if (ctx->aux) cudaFree(ctx->aux);
+  ctx->aux = nullptr;
+  ctx->aux_cap = 0;
+  const size_t want = align_up(bytes, 1 << 16);
+  if (cudaMalloc(&ctx->aux, want) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(ctx, EGB_ERR_NOMEM, "device allocation of " + std::to_string(want) + " bytes failed");
+  }
+  ctx->aux_cap = want;
+  return EGB_OK;
+}
+}  // namespace
+
+int egb_pairwise_matrix(egb_ctx* ctx, const double* values, const int32_t* pairs, int32_t ntasks,
+                        int32_t nvar, int32_t normalize, int32_t flags, double* out) {
+  if (!ctx) return EGB_ERR_ARG;
+  if (ntasks < 0 || nvar < 0 || (ntasks > 0 && (!values || !pairs)) || (nvar > 0 && !out))
+    return fail(ctx, EGB_ERR_ARG, "egb_pairwise_matrix: invalid arguments");
+  if ((int64_t)nvar * nvar > ((int64_t)1 << 31))
+    return fail(ctx, EGB_ERR_ARG, "egb_pairwise_matrix: nvar too large");
+  const bool dev = (flags & EGB_INPUT_DEVICE) != 0;
+  if (!dev)
+    for (int t = 0; t < ntasks; ++t)
+      if (pairs[2 * t] < 0 || pairs[2 * t] >= nvar || pairs[2 * t + 1] < 0 || pairs[2 * t + 1] >= nvar)
+        return fail(ctx, EGB_ERR_ARG, "egb_pairwise_matrix: pair " + std::to_string(t) + " out of range");
+  cudaSetDevice(ctx->device);
+  cudaStream_t st = ctx->stream;
+  const size_t nn = (size_t)nvar * (size_t)nvar;
+  const double* vals_d = values;
+  const int32_t* pairs_d = pairs;
+  double* out_d = out;
+  if (!dev) {
+    const size_t op = align_up(sizeof(double) * (size_t)ntasks, 256);
+    const size_t oo = op + align_up(sizeof(int32_t) * 2 * (size_t)ntasks, 256);
+    const int rc = ensure_aux(ctx, oo + sizeof(double) * std::max<size_t>(nn, 1));
+    if (rc) return rc;
+    char* B = (char*)ctx->aux;
+    vals_d = (const double*)B;
+    pairs_d = (const int32_t*)(B + op);
+    out_d = (double*)(B + oo);
+    if (ntasks > 0) {
+      EGB_CUDA(cudaMemcpyAsync(B, values, sizeof(double) * (size_t)ntasks, cudaMemcpyHostToDevice, st));
+      EGB_CUDA(cudaMemcpyAsync(B + op, pairs, sizeof(int32_t) * 2 * (size_t)ntasks,
+                               cudaMemcpyHostToDevice, st));
+    }
+  }
+  launch_pairwise_matrix(vals_d, pairs_d, ntasks, nvar, normalize ? 1 : 0, out_d, st);
+  EGB_CUDA(cudaGetLastError());
+  if (!dev && nn) EGB_CUDA(cudaMemcpyAsync(out, out_d, sizeof(double) * nn, cudaMemcpyDeviceToHost, st));
+  EGB_CUDA(cudaStreamSynchronize(st));
+  return EGB_OK;
+}
+
+int egb_normalize(egb_ctx* ctx, const double* mi, int64_t n, int32_t flags, double* out) {
+  if (!ctx) return EGB_ERR_ARG;
+  if (n < 0 || (n > 0 && (!mi || !out))) return fail(ctx, EGB_ERR_ARG, "egb_normalize: invalid arguments");
+  if (n == 0) return EGB_OK;
+  cudaSetDevice(ctx->device);
+  cudaStream_t st = ctx->stream;
+  const bool dev = (flags & EGB_INPUT_DEVICE) != 0;
+  const double* in_d = mi;
+  double* out_d = out;
+  if (!dev) {
+    const size_t half = align_up(sizeof(double) * (size_t)n, 256);
+    const int rc = ensure_aux(ctx, 2 * half);
+    if (rc) return rc;
+    in_d = (const double*)ctx->aux;
+    out_d = (double*)((char*)ctx->aux + half);
+    EGB_CUDA(cudaMemcpyAsync((void*)in_d, mi, sizeof(double) * (size_t)n, cudaMemcpyHostToDevice, st));
+  }
+  launch_normalize(in_d, n, out_d, st);
+  EGB_CUDA(cudaGetLastError());
+  if (!dev) EGB_CUDA(cudaMemcpyAsync(out, out_d, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost, st));
+  EGB_CUDA(cudaStreamSynchronize(st));
+  return EGB_OK;
 }
 
 int egb_debug_inject_device_error(egb_ctx* ctx, uint32_t word) {

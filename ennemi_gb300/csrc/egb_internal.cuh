@@ -588,6 +588,12 @@ void launch_wm_count(const TaskDev* tasks_d, const WmJob* jobs_d, int njobs, int
 void launch_samples(const SortSeg* segs_d, const int32_t* blk_seg_d, int nblk,
                     const uint64_t* keys, uint64_t* samples1, uint64_t* samples2, cudaStream_t st);
 
+// egb_matrix.cu: the symmetric pairwise matrix (NaN diagonal) of per-pair
+// estimates, optionally normalized, and normalize_mi of a value array.
+void launch_pairwise_matrix(const double* vals_d, const int32_t* pairs_d, int ntasks, int nvar,
+                            int normalize, double* out_d, cudaStream_t st);
+void launch_normalize(const double* in_d, int64_t n, double* out_d, cudaStream_t st);
+
 // egb_select.cu: any K (one warp per query, radix select on FP64 bits)
 constexpr int SELECT_WARPS = 8;
 void launch_knn_select(const JobDev* jobs_d, const WorkItem* items_d, int nitems, uint32_t* err,

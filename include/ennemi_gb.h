@@ -322,6 +322,27 @@ int egb_knn_eps_noalloc(const double* points, int64_t n, int32_t d, int32_t k, d
                         void* stream);
 
 /*
+ * The matrix of pairwise_mi (ennemi/_driver.py:716-721): out[i * nvar + j] =
+ * out[j * nvar + i] = values[t] for the pair (i, j) = (pairs[2 t],
+ * pairs[2 t + 1]) of each of the ntasks estimates; every other entry (the
+ * diagonal included) NaN.  normalize != 0 applies normalize_mi to each value
+ * on the way (egb_normalize).  values, pairs and out are host memory, or
+ * device memory with EGB_INPUT_DEVICE; out holds nvar * nvar doubles.
+ */
+int egb_pairwise_matrix(egb_ctx* ctx, const double* values, const int32_t* pairs, int32_t ntasks,
+                        int32_t nvar, int32_t normalize, int32_t flags, double* out);
+
+/*
+ * normalize_mi (ennemi/_driver.py:60-81): out[i] = sqrt(1 - exp(-2 mi[i]))
+ * where mi[i] > 0, otherwise mi[i] unchanged (zero, negative, -inf, NaN).
+ * Host memory, or device memory with EGB_INPUT_DEVICE; out may equal mi.
+ * The device exp may differ from the host's in the last bit, which the
+ * cancellation in 1 - exp(-2 mi) turns into up to 2^-53 / out[i] (1e-14
+ * at out = 0.005; negligible for MI values of practical size).
+ */
+int egb_normalize(egb_ctx* ctx, const double* mi, int64_t n, int32_t flags, double* out);
+
+/*
  * Test hook for the device-error path: the next egb_run_batch on this context
  * starts with `word` already in its device error word, as though one of its
  * kernels had reported it (bit 0: a bounded wait gave up; bit 1: an index

@@ -104,6 +104,23 @@ def oracle_run_tasks(O, calls=None):
     return run
 
 
+def oracle_pairwise_matrix(values, pairs, nvar, normalize=False, device=0):
+    """Stand-in for _native.pairwise_matrix on the host (tests only): the
+    reference's matrix fill (_driver.py:716-721)."""
+    out = np.full((nvar, nvar), np.nan)
+    for (i, j), v in zip(pairs, values):
+        out[i, j] = out[j, i] = oracle_normalize(np.asarray(v))[()] if normalize else v
+    return out
+
+
+def oracle_normalize(values, device=0):
+    """Stand-in for _native.normalize on the host (tests only): the
+    reference's _normalize (_driver.py:77-81) elementwise."""
+    v = np.asarray(values, dtype=np.float64)
+    with np.errstate(invalid="ignore"):
+        return np.where(v <= 0.0, v, np.sqrt(1 - np.exp(-2 * v)))
+
+
 @pytest.fixture(scope="session")
 def oracle():
     from oracle import oracle as O

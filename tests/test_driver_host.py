@@ -14,7 +14,7 @@ import pytest
 
 import ennemi_gb300 as eg
 from ennemi_gb300 import _driver, _native
-from conftest import driver_cases, oracle_run_tasks
+from conftest import driver_cases, oracle_normalize, oracle_pairwise_matrix, oracle_run_tasks
 
 DCASES = driver_cases()
 
@@ -28,6 +28,8 @@ def _py(v):
 def on_oracle(oracle, monkeypatch):
     calls = []
     monkeypatch.setattr(_native, "run_tasks", oracle_run_tasks(oracle, calls))
+    monkeypatch.setattr(_native, "pairwise_matrix", oracle_pairwise_matrix)
+    monkeypatch.setattr(_native, "normalize", oracle_normalize)
     return calls
 
 
@@ -135,9 +137,21 @@ def test_aliases_exactly_equal(on_oracle):
     assert np.array_equal(eg.pairwise_corr(data), eg.pairwise_mi(data, normalize=True), equal_nan=True)
 
 
-def test_normalize_mi():
+def test_normalize_mi(monkeypatch):
+    """Numeric input goes to the device kernel (here its host stand-in) and
+    keeps its shape; anything else raises as the reference does."""
+    seen = []
+
+    def fake(values, device=0):
+        seen.append(np.shape(values))
+        return oracle_normalize(values)
+    monkeypatch.setattr(_native, "normalize", fake)
     assert eg.normalize_mi(-0.5) == -0.5
     assert np.isclose(eg.normalize_mi(-0.5 * np.log(1 - 0.36)), 0.6)
+    assert eg.normalize_mi([[0.1, 0.0], [np.nan, -np.inf]]).shape == (2, 2)
+    assert seen == [(), (), (2, 2)]
+    with pytest.raises(TypeError):
+        eg.normalize_mi(["a"])
 
 
 def test_trivial_pairwise():
@@ -165,6 +179,7 @@ def _captured_inputs(monkeypatch, call, unshared):
 
     with monkeypatch.context() as m:
         m.setattr(_native, "run_tasks", run)
+        m.setattr(_native, "pairwise_matrix", oracle_pairwise_matrix)
         m.setattr(_driver, "device_prep", False)   # the host preparation itself
         if unshared:
             m.setattr(_driver, "_task_job",
@@ -242,6 +257,8 @@ def test_device_preprocessing_matches_host_preparation(oracle, monkeypatch, case
         return run(tasks, flags=flags, **kw)
 
     monkeypatch.setattr(_native, "run_tasks", recording)
+    monkeypatch.setattr(_native, "pairwise_matrix", oracle_pairwise_matrix)
+    monkeypatch.setattr(_native, "normalize", oracle_normalize)
     with warnings.catch_warnings(record=True) as w_dev:
         warnings.simplefilter("always")
         dev = calls[case]()
@@ -291,6 +308,8 @@ def test_device_preprocessing_columns_are_the_reference_slices(monkeypatch, case
         return np.zeros(len(tasks))
 
     monkeypatch.setattr(_native, "run_tasks", run)
+    monkeypatch.setattr(_native, "pairwise_matrix", oracle_pairwise_matrix)
+    monkeypatch.setattr(_native, "normalize", oracle_normalize)
     want = []
     if case.startswith("lags"):
         lag = lags[case]
