@@ -29,8 +29,10 @@ import numpy.typing as npt
 
 from . import _native
 from ._entropy_estimators import (
-    _estimate_conditional_discrete_mi, _estimate_discrete_entropy, _estimate_discrete_mi,
-    cmi_task, conditional_semidiscrete_task, entropy_task, mi_task, semidiscrete_task)
+    _assert_not_object, _discrete_on_device, _estimate_conditional_discrete_mi,
+    _estimate_discrete_entropy, _estimate_discrete_mi, cmi_task, conditional_semidiscrete_task,
+    discrete_cmi_task, discrete_entropy_task, discrete_mi_task, discrete_warnings, entropy_task,
+    mi_task, semidiscrete_task)
 
 FloatArray = npt.NDArray[np.float64]
 ArrayLike = npt.ArrayLike
@@ -87,7 +89,11 @@ class _Batch:
         return len(self.slots) - 1
 
     def run(self) -> np.ndarray:
-        gpu = _native.run_tasks(self.tasks, flags=run_flags) if self.tasks else np.empty(0)
+        groups = {}
+        gpu = _native.run_tasks(self.tasks, flags=run_flags, groups_out=groups) if self.tasks \
+            else np.empty(0)
+        for i in sorted(groups):   # the discrete estimators' warnings
+            discrete_warnings(self.tasks[i], groups[i])
         out = np.empty(len(self.slots))
         for i, (kind, v) in enumerate(self.slots):
             out[i] = gpu[v] if kind == "gpu" else v
@@ -226,6 +232,8 @@ def _mask_and_validate_entropy(x: FloatArray, mask, drop_nan: bool, discrete: bo
 
 def _entropy_slot(batch: _Batch, xs: FloatArray, k: int, discrete: bool) -> int:
     if discrete:
+        if _discrete_on_device(xs):
+            return batch.add_task(discrete_entropy_task(xs))
         return batch.add_value(_estimate_discrete_entropy(xs))
     return batch.add_task(entropy_task(xs, k))
 
@@ -739,6 +747,9 @@ def _task_of(xs, ys, zs, k: int, discrete_x: bool, discrete_y: bool):
     """The estimator a prepared task calls (_driver.py:814-832)."""
     if zs is None:
         if discrete_x and discrete_y:
+            if _discrete_on_device(xs, ys):
+                _assert_not_object(np.column_stack((xs, ys)))
+                return ("task", discrete_mi_task(xs, ys))
             return ("value", _estimate_discrete_mi(xs, ys))
         if discrete_x:
             return ("task", semidiscrete_task(ys, xs, k))
@@ -746,6 +757,8 @@ def _task_of(xs, ys, zs, k: int, discrete_x: bool, discrete_y: bool):
             return ("task", semidiscrete_task(xs, ys, k))
         return ("task", mi_task(xs, ys, k))
     if discrete_x and discrete_y:
+        if _discrete_on_device(xs, ys, zs):
+            return ("task", discrete_cmi_task(xs, ys, zs))
         return ("value", _estimate_conditional_discrete_mi(xs, ys, zs))
     if discrete_x:
         return ("task", conditional_semidiscrete_task(ys, xs, zs, k))

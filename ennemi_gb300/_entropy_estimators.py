@@ -135,17 +135,75 @@ def _verify_not_continuous(values, n: int) -> None:
         warn(NOT_CONTINUOUS_WARNING, UserWarning)
 
 
-# ------------------------------------------------- discrete (host, NumPy) --
+# ------------------------------------------------------------- discrete --
 
 def _assert_not_object(x) -> None:
     if np.asarray(x).dtype.kind == "O":
         raise TypeError(OBJECT_DTYPE_MESSAGE)
 
 
+def _discrete_on_device(*arrays) -> bool:
+    """Numeric data whose values float64 holds exactly goes to the device;
+    strings, objects and integers beyond 2^53 keep NumPy's np.unique."""
+    for a in arrays:
+        a = np.asarray(a)
+        if a.dtype.kind not in "biuf" or a.size == 0:
+            return False
+        if a.dtype.kind in "iu" and np.abs(a.astype(np.float64)).max() >= 2.0 ** 53:
+            return False
+    return True
+
+
+def _float_columns(a) -> list:
+    a = np.asarray(a)
+    a = a.reshape(-1, 1) if a.ndim == 1 else a
+    return [np.ascontiguousarray(a[:, c], dtype=np.float64) for c in range(a.shape[1])]
+
+
+def discrete_entropy_task(x) -> Task:
+    """_estimate_discrete_entropy as a device task (rows of x, any width)."""
+    cols = _float_columns(x)
+    return Task(_native.DISCRETE_ENTROPY, 1, cols, n=len(cols[0]))
+
+
+def discrete_mi_task(x, y) -> Task:
+    """_estimate_discrete_mi as a device task."""
+    xs, ys = _float_columns(x), _float_columns(y)
+    return Task(_native.DISCRETE_MI, 1, xs, ys, n=len(xs[0]))
+
+
+def discrete_cmi_task(x, y, cond) -> Task:
+    """_estimate_conditional_discrete_mi as a device task."""
+    xs, ys, zs = _float_columns(x), _float_columns(y), _float_columns(cond)
+    return Task(_native.DISCRETE_CMI, 1, xs, ys, zs, n=len(xs[0]))
+
+
+def discrete_warnings(task: Task, groups) -> None:
+    """The reference's warnings for a discrete task, from the device's
+    distinct-value figures (_entropy_estimators.py:249-254, :280-281)."""
+    n = task.n
+    if task.kind == _native.DISCRETE_MI:
+        for g in (groups[1], groups[2]):
+            if g > n / 4:
+                warn(NOT_CONTINUOUS_WARNING, UserWarning)
+    elif task.kind == _native.DISCRETE_CMI:
+        for _ in range(groups[4] + groups[5]):
+            warn(NOT_CONTINUOUS_WARNING, UserWarning)
+
+
+def _run_discrete(task: Task) -> float:
+    groups = {}
+    value = _native.run_tasks([task], groups_out=groups)[0]
+    discrete_warnings(task, groups[0])
+    return float(value)
+
+
 def _estimate_discrete_entropy(x) -> float:
     """Plug-in entropy -sum p log p of the distinct rows of x (_entropy_estimators.py:44-56)."""
     x = np.asarray(x)
     _assert_not_object(x)
+    if _discrete_on_device(x):
+        return _run_discrete(discrete_entropy_task(x))
     _, counts = np.unique(x, axis=0, return_counts=True)
     p = counts / x.shape[0]
     return float(-np.sum(p * np.log(p)))
@@ -155,6 +213,8 @@ def _estimate_discrete_mi(x, y) -> float:
     """Plug-in MI of two discrete variables (_entropy_estimators.py:257-289)."""
     data = np.column_stack((x, y))
     _assert_not_object(data)
+    if _discrete_on_device(x, y):
+        return _run_discrete(discrete_mi_task(x, y))
     n = data.shape[0]
     _, xi, xc = np.unique(data[:, 0], return_inverse=True, return_counts=True)
     _, yi, yc = np.unique(data[:, 1], return_inverse=True, return_counts=True)
@@ -173,6 +233,8 @@ def _estimate_conditional_discrete_mi(x, y, cond) -> float:
     n = len(x)
     cond = np.asarray(cond)
     _assert_not_object(cond)
+    if _discrete_on_device(x, y, cond):
+        return _run_discrete(discrete_cmi_task(x, y, cond))
     _, inv, counts = np.unique(cond, axis=0, return_inverse=True, return_counts=True)
     inv = np.ravel(inv)
     x, y = np.asarray(x), np.asarray(y)

@@ -23,6 +23,8 @@ import numpy as np
 from . import _build
 
 MI, CMI, SEMI, CSEMI, ENTROPY = 0, 1, 2, 3, 4
+DISCRETE_ENTROPY, DISCRETE_MI, DISCRETE_CMI = 5, 6, 7
+DISCRETE_KINDS = (DISCRETE_ENTROPY, DISCRETE_MI, DISCRETE_CMI)
 
 INPUT_DEVICE = 1 << 0
 PLAIN_FP64 = 1 << 1
@@ -123,6 +125,8 @@ def load():
         lib.egb_get_policy.restype = ctypes.c_int
         lib.egb_device_info.argtypes = [vp, ctypes.c_char_p, i32, ctypes.POINTER(i32)]
         lib.egb_device_info.restype = ctypes.c_int
+        lib.egb_last_groups.argtypes = [vp, i32, ctypes.POINTER(i64), i32]
+        lib.egb_last_groups.restype = ctypes.c_int
         lib.egb_pairwise_matrix.argtypes = [vp, vp, vp, i32, i32, i32, i32, vp]
         lib.egb_pairwise_matrix.restype = ctypes.c_int
         lib.egb_normalize.argtypes = [vp, vp, i64, i32, vp]
@@ -286,8 +290,12 @@ def _length(col) -> int:
 
 
 def run_tasks(tasks: List[Task], flags: int = 0, device: int = 0,
-              results_out: Optional[list] = None, noise=None) -> np.ndarray:
+              results_out: Optional[list] = None, noise=None,
+              groups_out: Optional[dict] = None) -> np.ndarray:
     """Evaluate the tasks in one batched call; returns the estimates.
+
+    groups_out (a dict) receives, for each task of a discrete kind, the six
+    distinct-value figures of egb_last_groups under the task's index.
 
     With RESCALE, `noise(m)` returns the first m values (at least) of the
     preprocessing noise stream; the device copy is extended when a batch needs
@@ -347,6 +355,12 @@ def run_tasks(tasks: List[Task], flags: int = 0, device: int = 0,
     with ctx.lock:
         rc = ctx.lib.egb_run_batch(ctx.h, ctasks, len(tasks), flags, res)
         ctx.check(rc, "egb_run_batch")
+        if groups_out is not None:
+            buf = (ctypes.c_int64 * 6)()
+            for i, t in enumerate(tasks):
+                if t.kind in DISCRETE_KINDS:
+                    ctx.lib.egb_last_groups(ctx.h, i, buf, 6)
+                    groups_out[i] = [int(v) for v in buf]
     if results_out is not None:
         results_out.extend(res)
     return np.array([r.value for r in res], dtype=np.float64)

@@ -28,6 +28,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <atomic>
 #include <cmath>
 #include <cstdio>
@@ -93,7 +94,7 @@ struct TaskPlan {
   int64_t src_len = 0;            // samples the caller's columns must hold
   size_t tab_index = 0;           // offset of the shared index in the table blob
   std::vector<int64_t> cls_off;   // class segment starts (nclass + 1)
-  size_t off_x64 = 0, off_eps = 0, off_rad = 0, off_cnt[3] = {0, 0, 0};
+  size_t off_x64 = 0, off_eps = 0, off_rad = 0, off_cnt[4] = {0, 0, 0, 0};
   size_t tab_perm = 0;            // offset of perm inside the table blob
   size_t tab_rad = 0;             // KIND_COUNT_ONLY: caller radii (host input)
   int center0 = 0;                // first column of the task in the centre array
@@ -128,7 +129,9 @@ struct ReplayState {
   std::vector<TaskPlan> P;
   std::vector<CombineJob> cjobs;
   std::vector<GroupStat> groups;
-  size_t pin_rb = 0, pin_zr = 0, zr_stats = 0, zr_err = 0, zr_zero = 0;
+  size_t pin_rb = 0, pin_zr = 0, zr_stats = 0, zr_err = 0, zr_zero = 0, zr_groups = 0, zr_warn = 0;
+  std::vector<std::pair<int, int>> group_of;  // per group job: (task, slot)
+  std::vector<int> warn_of;                   // per level check: its task
   size_t tab_bytes = 0, zr_bytes = 0;
   int nchunks = 0;
   int64_t sort_keys = 0, sort_segs = 0;  // keys and segments of the batch's radix sort
@@ -174,6 +177,8 @@ struct egb_ctx {
   int64_t stats[NSTATS] = {};
   // egb_debug_inject_device_error: error word the next batch starts with
   uint32_t inject_err = 0;
+  // distinct rows per count slot of each task of the last batch (discrete kinds)
+  std::vector<std::array<int64_t, 6>> groups;
   // device buffer of the matrix / normalize calls (apart from the batch
   // arena, so that they keep a batch's internals and captured graph intact)
   void* aux = nullptr;
@@ -276,6 +281,17 @@ int finish_batch(egb_ctx* ctx, const ReplayState& R, const char* H, int64_t laun
     return fail(ctx, EGB_ERR_DEVICE, buf);
   }
 
+  ctx->groups.assign(R.P.size(), std::array<int64_t, 6>{0, 0, 0, 0, 0, 0});
+  {
+    const unsigned long long* gz = (const unsigned long long*)(H + R.pin_zr + R.zr_groups);
+    for (size_t g = 0; g < R.group_of.size(); ++g)
+      ctx->groups[(size_t)R.group_of[g].first][(size_t)R.group_of[g].second] = (int64_t)gz[g];
+    const unsigned long long* wz = (const unsigned long long*)(H + R.pin_zr + R.zr_warn);
+    for (size_t c = 0; c < R.warn_of.size(); ++c) {
+      ctx->groups[(size_t)R.warn_of[c]][4] = (int64_t)wz[2 * c];
+      ctx->groups[(size_t)R.warn_of[c]][5] = (int64_t)wz[2 * c + 1];
+    }
+  }
   const double* partial = (const double*)(H + R.pin_rb);
   const uint32_t* zf = (const uint32_t*)(H + R.pin_zr + R.zr_zero);
   const double INF = HUGE_VAL;
@@ -326,6 +342,13 @@ int finish_batch(egb_ctx* ctx, const ReplayState& R, const char* H, int64_t laun
       }
       case EGB_ENTROPY:
         v = psi_int(N) - psi_int(p.k) + (double)p.ncol * (mean + std::log(2.0));
+        break;
+      case EGB_DISCRETE_ENTROPY:  // -(1/N) sum_rows log(c / N)
+        v = -mean;
+        break;
+      case EGB_DISCRETE_MI:       // (1/N) sum_rows log(N c_xy / (c_x c_y))
+      case EGB_DISCRETE_CMI:      // (1/N) sum_rows log(c_z c_xyz / (c_xz c_yz))
+        v = mean;
         break;
     }
     r.value = v;
@@ -424,14 +447,15 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
     p.dz = T.dz;
     p.ncol = T.dx + T.dy + T.dz;
     const bool internal = T.kind == KIND_KNN_ONLY || T.kind == KIND_COUNT_ONLY;
-    if (!(T.kind >= EGB_MI && T.kind <= EGB_ENTROPY) && !internal)
+    if (!(T.kind >= EGB_MI && T.kind <= EGB_DISCRETE_CMI) && !internal)
       return fail(ctx, EGB_ERR_ARG, who + "unknown estimator kind");
     if (T.n < 1 || T.n > (int64_t)0x3fffffff) return fail(ctx, EGB_ERR_ARG, who + "n out of range");
     if (T.k < 1 && T.kind != KIND_COUNT_ONLY) return fail(ctx, EGB_ERR_ARG, who + "k must be greater than zero");
     if (T.dx < 1 || T.dy < 0 || T.dz < 0 || p.ncol > EGB_DMAX)
       return fail(ctx, EGB_ERR_ARG, who + "column counts out of range (at most 32 columns)");
-    const bool needs_y = T.kind == EGB_MI || T.kind == EGB_CMI;
-    const bool needs_z = T.kind == EGB_CMI || T.kind == EGB_CSEMI;
+    const bool needs_y = T.kind == EGB_MI || T.kind == EGB_CMI || T.kind == EGB_DISCRETE_MI ||
+                         T.kind == EGB_DISCRETE_CMI;
+    const bool needs_z = T.kind == EGB_CMI || T.kind == EGB_CSEMI || T.kind == EGB_DISCRETE_CMI;
     if ((needs_y != (T.dy > 0)) || (needs_z != (T.dz > 0)))
       return fail(ctx, EGB_ERR_ARG, who + "column counts do not match the estimator kind");
     if (!T.cols) return fail(ctx, EGB_ERR_ARG, who + "null column list");
@@ -453,7 +477,7 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
       p.src_len = it->second + 1;
       p.index = T.index;
     }
-    if (rescale && T.kind != EGB_ENTROPY) {
+    if (rescale && T.kind >= EGB_MI && T.kind <= EGB_CSEMI) {
       if (internal) return fail(ctx, EGB_ERR_ARG, who + "EGB_RESCALE applies to estimator tasks only");
       if (T.dx != 1 || T.dy > 1)
         return fail(ctx, EGB_ERR_ARG, who + "EGB_RESCALE needs one x column and at most one y column");
@@ -468,7 +492,9 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
     ncols_total += p.ncol;
     max_n = std::max(max_n, T.n);
     max_ld = std::max(max_ld, p.ld);
-    p.nslot = T.kind == EGB_MI ? 2 : (T.kind == EGB_CMI || T.kind == EGB_CSEMI) ? 3
+    p.nslot = T.kind == EGB_DISCRETE_ENTROPY ? 1 : T.kind == EGB_DISCRETE_MI ? 3
+              : T.kind == EGB_DISCRETE_CMI ? 4
+              : T.kind == EGB_MI ? 2 : (T.kind == EGB_CMI || T.kind == EGB_CSEMI) ? 3
               : (T.kind == EGB_SEMI || T.kind == KIND_COUNT_ONLY) ? 1 : 0;
     if (T.kind == EGB_SEMI || T.kind == EGB_CSEMI) {
       if (!T.labels || T.nclass < 1) return fail(ctx, EGB_ERR_ARG, who + "labels required");
@@ -565,7 +591,7 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
     for (int t = 0; t < ntasks; ++t) {
       const TaskPlan& p = P[(size_t)t];
       colid[(size_t)t].resize((size_t)p.ncol);
-      const bool resc = rescale && p.kind != EGB_ENTROPY;
+      const bool resc = rescale && p.kind >= EGB_MI && p.kind <= EGB_CSEMI;
       for (int c = 0; c < p.ncol; ++c) {
         if (!p.perm.empty()) {  // class-ordered working columns are the task's own
           colid[(size_t)t][(size_t)c] = next_id++;
@@ -950,6 +976,67 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   }
   const size_t off_wmz = dl.take(std::max<size_t>(wmz_bytes, 16));
 
+  // discrete tasks: one exact group-by per column subset (egb_discrete.cu);
+  // hash tables of twice the rows, zeroed by one memset with the rest
+  std::vector<GroupJob> gbjobs;
+  std::vector<std::pair<int, int>> gb_owner;  // (task, slot) per group job
+  size_t gbz_bytes = 0;
+  int gb_blocks = 0;
+  for (int t = 0; t < ntasks; ++t) {
+    const TaskPlan& p = P[(size_t)t];
+    if (p.kind < EGB_DISCRETE_ENTROPY || p.kind > EGB_DISCRETE_CMI) continue;
+    const int X = 0, Y = p.dx, Z = p.dx + p.dy;
+    std::vector<SpaceCols> subs;
+    SpaceCols sc{};
+    if (p.kind == EGB_DISCRETE_ENTROPY) {
+      set_cols(sc, {{X, p.dx}}); subs.push_back(sc);
+    } else if (p.kind == EGB_DISCRETE_MI) {
+      set_cols(sc, {{X, p.dx}, {Y, p.dy}}); subs.push_back(sc);
+      set_cols(sc, {{X, p.dx}}); subs.push_back(sc);
+      set_cols(sc, {{Y, p.dy}}); subs.push_back(sc);
+    } else {
+      set_cols(sc, {{X, p.dx}, {Y, p.dy}, {Z, p.dz}}); subs.push_back(sc);
+      set_cols(sc, {{X, p.dx}, {Z, p.dz}}); subs.push_back(sc);
+      set_cols(sc, {{Y, p.dy}, {Z, p.dz}}); subs.push_back(sc);
+      set_cols(sc, {{Z, p.dz}}); subs.push_back(sc);
+    }
+    for (size_t k = 0; k < subs.size(); ++k) {
+      GroupJob G{};
+      G.sp = subs[k];
+      G.task = t;
+      G.slot = (int32_t)k;
+      G.n = (int32_t)p.n;
+      int lg = 6;
+      while (((int64_t)1 << lg) < 2 * p.n) ++lg;
+      G.cap_log2 = lg;
+      G.blk0 = gb_blocks;
+      gb_blocks += (int)((p.n + 255) / 256);
+      G.table = (int32_t*)(uintptr_t)gbz_bytes;    // offsets in the zeroed block for now
+      gbz_bytes += align_up(sizeof(int32_t) * ((size_t)1 << lg), 256);
+      G.count = (int32_t*)(uintptr_t)gbz_bytes;
+      gbz_bytes += align_up(sizeof(int32_t) * ((size_t)1 << lg), 256);
+      G.rowslot = (int32_t*)(uintptr_t)dl.take(sizeof(int32_t) * (size_t)p.n);
+      gbjobs.push_back(G);
+      gb_owner.push_back({t, (int)k});
+    }
+  }
+  // conditional discrete MI: per-level distinct counts for the warnings
+  std::vector<LevelCheck> lchecks;
+  std::vector<std::array<int, 4>> lcheck_jobs;   // group jobs xz, yz, z and the task
+  for (size_t g = 0; g < gbjobs.size(); ++g) {
+    const GroupJob& G = gbjobs[g];
+    if (P[(size_t)G.task].kind != EGB_DISCRETE_CMI || G.slot != 3) continue;
+    LevelCheck L{};
+    L.n = G.n;
+    L.xd = (int32_t*)(uintptr_t)gbz_bytes;
+    gbz_bytes += align_up(sizeof(int32_t) * ((size_t)1 << G.cap_log2), 256);
+    L.yd = (int32_t*)(uintptr_t)gbz_bytes;
+    gbz_bytes += align_up(sizeof(int32_t) * ((size_t)1 << G.cap_log2), 256);
+    lchecks.push_back(L);
+    lcheck_jobs.push_back({(int)g - 2, (int)g - 1, (int)g, G.task});
+  }
+  const size_t off_gbz = dl.take(std::max<size_t>(gbz_bytes, 16));
+
   // tile launch groups
   struct Group {
     int is_knn, sel, kclass, dclass, slab, dmax, mode;
@@ -1170,6 +1257,8 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   }
   const size_t tab_wjobs = tl.take(sizeof(WmJob) * std::max<size_t>(wjobs.size(), 1));
   const size_t tab_wbuild = tl.take(sizeof(WmJob) * std::max<size_t>(wbuild.size(), 1));
+  const size_t tab_gbjobs = tl.take(sizeof(GroupJob) * std::max<size_t>(gbjobs.size(), 1));
+  const size_t tab_lchecks = tl.take(sizeof(LevelCheck) * std::max<size_t>(lchecks.size(), 1));
   const size_t tab_cjobs = tl.take(sizeof(CombineJob) * std::max<size_t>(cjobs.size(), 1));
   const size_t tab_chunkjob = tl.take(sizeof(int32_t) * (size_t)std::max(nchunks, 1));
   const size_t tab_bytes = align_up(tl.off, 256);
@@ -1181,7 +1270,9 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   const size_t zr_jflags = align_up(zr_counters + sizeof(int) * (size_t)std::max(ncounters, 1), 16);
   const size_t zr_zero = align_up(zr_jflags + sizeof(uint32_t) * std::max<size_t>(jobs.size(), 1), 16);
   const size_t zr_err = align_up(zr_zero + sizeof(uint32_t) * (size_t)ntasks, 16);
-  const size_t zr_bytes = align_up(zr_err + 16, 256);
+  const size_t zr_groups = align_up(zr_err + 16, 16);  // distinct rows per group job
+  const size_t zr_warn = zr_groups + sizeof(unsigned long long) * gbjobs.size();  // 2 per check
+  const size_t zr_bytes = align_up(zr_warn + 2 * sizeof(unsigned long long) * lchecks.size(), 256);
   const size_t off_zr = dl.take(zr_bytes);
   // readback region: partial sums, then a copy of zero flags + error word
   const size_t off_partial = dl.take(sizeof(double) * (size_t)std::max(nchunks, 1));
@@ -1344,6 +1435,36 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
       std::memcpy(H + tab_wbuild + sizeof(WmJob) * w, &J, sizeof(WmJob));
     }
   }
+  for (size_t g = 0; g < gbjobs.size(); ++g) {
+    GroupJob G = gbjobs[g];
+    G.table = (int32_t*)(A + off_gbz + (uintptr_t)G.table);
+    G.count = (int32_t*)(A + off_gbz + (uintptr_t)G.count);
+    G.rowslot = (int32_t*)(A + (uintptr_t)G.rowslot);
+    G.groups = (unsigned long long*)(A + off_zr + zr_groups) + g;
+    std::memcpy(H + tab_gbjobs + sizeof(GroupJob) * g, &G, sizeof(GroupJob));
+  }
+  int lcheck_max_n = 1;
+  for (size_t c = 0; c < lchecks.size(); ++c) {
+    LevelCheck L = lchecks[c];
+    auto dev_of = [&](const GroupJob& G, bool table) {
+      return (const int32_t*)(A + off_gbz + (uintptr_t)(table ? G.table : G.count));
+    };
+    const GroupJob& Gxz = gbjobs[(size_t)lcheck_jobs[c][0]];
+    const GroupJob& Gyz = gbjobs[(size_t)lcheck_jobs[c][1]];
+    const GroupJob& Gz = gbjobs[(size_t)lcheck_jobs[c][2]];
+    L.xz_table = dev_of(Gxz, true);
+    L.yz_table = dev_of(Gyz, true);
+    L.z_table = dev_of(Gz, true);
+    L.z_count = dev_of(Gz, false);
+    L.xz_rowslot = (const int32_t*)(A + (uintptr_t)Gxz.rowslot);
+    L.yz_rowslot = (const int32_t*)(A + (uintptr_t)Gyz.rowslot);
+    L.z_rowslot = (const int32_t*)(A + (uintptr_t)Gz.rowslot);
+    L.xd = (int32_t*)(A + off_gbz + (uintptr_t)L.xd);
+    L.yd = (int32_t*)(A + off_gbz + (uintptr_t)L.yd);
+    L.warn = (unsigned long long*)(A + off_zr + zr_warn) + 2 * c;
+    lcheck_max_n = std::max(lcheck_max_n, L.n);
+    std::memcpy(H + tab_lchecks + sizeof(LevelCheck) * c, &L, sizeof(LevelCheck));
+  }
   if (!cjobs.empty()) std::memcpy(H + tab_cjobs, cjobs.data(), sizeof(CombineJob) * cjobs.size());
   if (nchunks) std::memcpy(H + tab_chunkjob, chunk_job.data(), sizeof(int32_t) * (size_t)nchunks);
 
@@ -1373,6 +1494,7 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   EGB_CUDA(cudaMemcpyAsync(A + off_tab, H, tab_bytes, cudaMemcpyHostToDevice, st));
   EGB_CUDA(cudaMemsetAsync(A + off_zr, 0, zr_bytes, st));
   if (wmz_bytes) EGB_CUDA(cudaMemsetAsync(A + off_wmz, 0, wmz_bytes, st));
+  if (gbz_bytes) EGB_CUDA(cudaMemsetAsync(A + off_gbz, 0, gbz_bytes, st));
   if (nblk_sort) EGB_CUDA(cudaMemsetAsync(A + off_sweep, 0, sweep_bytes, st));
   if (inject)  // the device error word as if a kernel had set these bits
     for (int i = 0; i < 4; ++i)
@@ -1492,6 +1614,8 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
                      (const uint64_t*)(A + off_s1), (const uint64_t*)(A + off_s2), vals, st);
   if (timing) EGB_CUDA(cudaEventRecord(ctx->kev[11], st));
   if (timing) EGB_CUDA(cudaEventRecord(ctx->kev[4], st));
+  launch_groups(tasks_d, (const GroupJob*)dtab(tab_gbjobs), (int)gbjobs.size(), gb_blocks, err_d, st);
+  launch_level_checks((const LevelCheck*)dtab(tab_lchecks), (int)lchecks.size(), lcheck_max_n, st);
   launch_wm_count(tasks_d, (const WmJob*)dtab(tab_wjobs), (int)wjobs.size(), wm_qblocks, keys,
                   (const uint64_t*)(A + off_s1), (const uint64_t*)(A + off_s2), vals, st);
   for (size_t g = 0; g < groups.size(); ++g) {
@@ -1606,6 +1730,10 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   R.pin_zr = pin_zr;
   R.zr_stats = zr_stats;
   R.zr_err = zr_err;
+  R.zr_groups = zr_groups;
+  R.group_of = gb_owner;
+  R.zr_warn = zr_warn;
+  for (const auto& j : lcheck_jobs) R.warn_of.push_back(j[3]);
   R.zr_zero = zr_zero;
   R.nchunks = nchunks;
   R.tab_bytes = tab_bytes;
@@ -1688,7 +1816,7 @@ int egb_run_batch(egb_ctx* ctx, const egb_task* tasks, int32_t ntasks, int32_t f
   if (!ctx) return EGB_ERR_ARG;
   cudaSetDevice(ctx->device);
   for (int t = 0; t < ntasks && tasks; ++t)
-    if (tasks[t].kind > EGB_ENTROPY || tasks[t].kind < EGB_MI)
+    if (tasks[t].kind > EGB_DISCRETE_CMI || tasks[t].kind < EGB_MI)
       return fail(ctx, EGB_ERR_ARG, "task " + std::to_string(t) + ": unknown estimator kind");
   return run_batch(ctx, tasks, ntasks, flags, results, nullptr);
 }
@@ -1892,6 +2020,13 @@ int egb_normalize(egb_ctx* ctx, const double* mi, int64_t n, int32_t flags, doub
   if (!dev) EGB_CUDA(cudaMemcpyAsync(out, out_d, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost, st));
   EGB_CUDA(cudaStreamSynchronize(st));
   return EGB_OK;
+}
+
+int egb_last_groups(const egb_ctx* ctx, int32_t task, int64_t* out, int32_t max) {
+  if (!ctx || !out || task < 0 || task >= (int)ctx->groups.size()) return 0;
+  const int n = std::min(max, 6);
+  for (int i = 0; i < n; ++i) out[i] = ctx->groups[(size_t)task][(size_t)i];
+  return n;
 }
 
 int egb_debug_inject_device_error(egb_ctx* ctx, uint32_t word) {

@@ -204,7 +204,7 @@ struct TaskDev {          // per-task device view
   const double* center;   // [ncol] column midranges (FP32 copies are x - center)
   double* eps;            // [ld]
   double* rad;            // [ld] count radius per sample
-  int32_t* cnt[3];        // count slots (working order)
+  int32_t* cnt[4];        // count slots (working order)
   int64_t ld;
   int32_t n;
   int32_t ncol;
@@ -587,6 +587,36 @@ void launch_wm_count(const TaskDev* tasks_d, const WmJob* jobs_d, int njobs, int
 // Samples of every sorted segment (egb_search.cuh), after the sort.
 void launch_samples(const SortSeg* segs_d, const int32_t* blk_seg_d, int nblk,
                     const uint64_t* keys, uint64_t* samples1, uint64_t* samples2, cudaStream_t st);
+
+// egb_discrete.cu: exact group-by of the rows of one column subset of a
+// discrete task: the rows equal to each row, into count slot `slot`.
+struct GroupJob {
+  int32_t* table;               // [2^cap_log2] row + 1 of each slot's owner, 0 = free (zeroed)
+  int32_t* count;               // [2^cap_log2] rows per slot (zeroed)
+  int32_t* rowslot;             // [n] slot of each row
+  unsigned long long* groups;   // distinct rows (zeroed)
+  SpaceCols sp;                 // the subset's columns
+  int32_t task, slot, n, cap_log2;
+  int32_t blk0;                 // first block of the job in the launches
+};
+void launch_groups(const TaskDev* tasks_d, const GroupJob* jobs_d, int njobs, int total_blocks,
+                   uint32_t* err, cudaStream_t st);
+// Conditional discrete MI: condition levels with more than a quarter of
+// their rows distinct in x (warn[0]) or in y (warn[1]).
+struct LevelCheck {
+  const int32_t* xz_table;
+  const int32_t* xz_rowslot;
+  const int32_t* yz_table;
+  const int32_t* yz_rowslot;
+  const int32_t* z_table;
+  const int32_t* z_rowslot;
+  const int32_t* z_count;
+  int32_t* xd;                 // [z table] distinct x per level (zeroed)
+  int32_t* yd;                 // [z table] distinct y per level (zeroed)
+  unsigned long long* warn;    // [2] (zeroed)
+  int32_t n, pad;
+};
+void launch_level_checks(const LevelCheck* checks_d, int nchecks, int max_n, cudaStream_t st);
 
 // egb_matrix.cu: the symmetric pairwise matrix (NaN diagonal) of per-pair
 // estimates, optionally normalized, and normalize_mi of a value array.

@@ -378,6 +378,22 @@ __global__ void combine_kernel(const TaskDev* __restrict__ tasks,
         term = psi_of(psi_tab, psi_len, a, bad);
         break;
       }
+      case EGB_DISCRETE_ENTROPY: {   // log(c / N)
+        term = log((double)t.cnt[0][i] / (double)t.n);
+        break;
+      }
+      case EGB_DISCRETE_MI: {        // log(N c_xy / (c_x c_y)), integer products exact
+        const int64_t num = (int64_t)t.n * t.cnt[0][i];
+        const int64_t den = (int64_t)t.cnt[1][i] * t.cnt[2][i];
+        term = log((double)num / (double)den);
+        break;
+      }
+      case EGB_DISCRETE_CMI: {       // log(c_z c_xyz / (c_xz c_yz))
+        const int64_t num = (int64_t)t.cnt[3][i] * t.cnt[0][i];
+        const int64_t den = (int64_t)t.cnt[1][i] * t.cnt[2][i];
+        term = log((double)num / (double)den);
+        break;
+      }
       default: {  // EGB_ENTROPY: log(0) = -inf propagates exactly as in NumPy
         const double e = t.eps[i];
         zf |= (e == 0.0 ? 1u : 0u);

@@ -47,7 +47,13 @@ enum egb_kind {
   EGB_CMI = 1,    /* _estimate_conditional_mi               _entropy_estimators.py:116-156 */
   EGB_SEMI = 2,   /* _estimate_semidiscrete_mi              _entropy_estimators.py:159-200 */
   EGB_CSEMI = 3,  /* _estimate_conditional_semidiscrete_mi  _entropy_estimators.py:203-247 */
-  EGB_ENTROPY = 4 /* _estimate_single_entropy               _entropy_estimators.py:21-42   */
+  EGB_ENTROPY = 4, /* _estimate_single_entropy              _entropy_estimators.py:21-42   */
+  /* Plug-in estimators of discrete variables, from exact counts of equal
+   * rows (values compared as doubles, -0 equal to +0; integer data must be
+   * exactly representable, |v| < 2^53).  k is not used.                     */
+  EGB_DISCRETE_ENTROPY = 5, /* _estimate_discrete_entropy       _entropy_estimators.py:44-56   */
+  EGB_DISCRETE_MI = 6,      /* _estimate_discrete_mi            _entropy_estimators.py:257-289 */
+  EGB_DISCRETE_CMI = 7      /* _estimate_conditional_discrete_mi _entropy_estimators.py:291-320 */
 };
 
 /* Status codes. */
@@ -128,6 +134,9 @@ typedef struct egb_column {
  *   EGB_SEMI     dx >= 1, dy = 0,  dz = 0      (discrete y given as labels)
  *   EGB_CSEMI    dx >= 1, dy = 0,  dz >= 1     (discrete y given as labels)
  *   EGB_ENTROPY  dx >= 1, dy = 0,  dz = 0
+ *   EGB_DISCRETE_ENTROPY  dx >= 1, dy = 0,  dz = 0
+ *   EGB_DISCRETE_MI       dx >= 1, dy >= 1, dz = 0
+ *   EGB_DISCRETE_CMI      dx >= 1, dy >= 1, dz >= 1
  * labels (host memory, SEMI/CSEMI only): class index of each sample in
  * [0, nclass); the caller maps the reference's np.unique(y) values to 0..C-1
  * in sorted order.
@@ -184,7 +193,9 @@ int egb_run_batch(egb_ctx* ctx, const egb_task* tasks, int32_t ntasks, int32_t f
  * sample order: which = 0 -> eps (double[n]); which = 1 + s -> count slot s
  * (int64[n]); which = 16 + c -> the task's column c as the estimator used it
  * (double[n]: after the index and EGB_RESCALE).  Slots: MI nx, ny; CMI nxz,
- * nyz, nz; SEMI n; CSEMI nxz, nyz, nz.
+ * nyz, nz; SEMI n; CSEMI nxz, nyz, nz; DISCRETE_ENTROPY c_x; DISCRETE_MI
+ * c_xy, c_x, c_y; DISCRETE_CMI c_xyz, c_xz, c_yz, c_z (rows equal to each
+ * row on those columns).
  */
 int egb_fetch(egb_ctx* ctx, int32_t task, int32_t which, void* host_out);
 
@@ -341,6 +352,18 @@ int egb_pairwise_matrix(egb_ctx* ctx, const double* values, const int32_t* pairs
  * at out = 0.005; negligible for MI values of practical size).
  */
 int egb_normalize(egb_ctx* ctx, const double* mi, int64_t n, int32_t flags, double* out);
+
+/*
+ * Distinct-value figures of task `task` of the last batch into
+ * out[0 .. min(max, 6)); returns the number written.  [0..3]: distinct rows
+ * of each count slot (discrete kinds: the distinct values of each column
+ * subset, in slot order; 0 for the other kinds); [4], [5]: for
+ * EGB_DISCRETE_CMI, the condition levels whose x (y) has more distinct
+ * values than a quarter of the level's rows.  The reference warns once for
+ * each variable, or each variable of each level, with more than n / 4
+ * distinct values (_entropy_estimators.py:249-254, :280-281).
+ */
+int egb_last_groups(const egb_ctx* ctx, int32_t task, int64_t* out, int32_t max);
 
 /*
  * Test hook for the device-error path: the next egb_run_batch on this context

@@ -198,3 +198,58 @@ def entropy(x, k: int = 3) -> Tuple[float, Dict[str, np.ndarray]]:
     with np.errstate(divide="ignore"):
         value = psi(n) - psi(k) + d * (np.mean(np.log(eps)) + np.log(2))
     return float(value), {"eps": eps}
+
+
+# --------------------------------------------------------------- discrete --
+# Plug-in estimators of discrete variables (_entropy_estimators.py:44-56,
+# :257-320), restated with per-row counts of equal rows -- the quantities the
+# device's group-by produces -- and the distinct-value figures behind the
+# reference's warnings (:249-254).
+
+def _row_counts(cols) -> Tuple[np.ndarray, int]:
+    """Per row, the number of rows equal to it on `cols`; and the number of
+    distinct rows."""
+    a = np.column_stack([np.asarray(c, dtype=np.float64) + 0.0 for c in cols])  # -0 -> +0
+    _, inv, cnt = np.unique(a, axis=0, return_inverse=True, return_counts=True)
+    return cnt[np.ravel(inv)].astype(np.int64), len(cnt)
+
+
+def discrete_entropy(x) -> Tuple[float, Dict[str, np.ndarray]]:
+    """-sum p log p over the distinct rows of x (_entropy_estimators.py:44-56)."""
+    cols = [x] if np.ndim(x) == 1 else list(np.asarray(x).T)
+    c, g = _row_counts(cols)
+    n = len(c)
+    return float(-np.sum(np.log(c / n)) / n), {"c": c, "groups": np.array([g, 0, 0, 0, 0, 0])}
+
+
+def discrete_mi(x, y) -> Tuple[float, Dict[str, np.ndarray]]:
+    """sum over joint values of c log(N c / (cx cy)) / N (_entropy_estimators.py:257-289)."""
+    cxy, gxy = _row_counts([x, y])
+    cx, gx = _row_counts([x])
+    cy, gy = _row_counts([y])
+    n = len(cxy)
+    v = float(np.sum(np.log((n * cxy).astype(np.float64) / (cx * cy).astype(np.float64))) / n)
+    return v, {"cxy": cxy, "cx": cx, "cy": cy, "groups": np.array([gxy, gx, gy, 0, 0, 0])}
+
+
+def conditional_discrete_mi(x, y, z) -> Tuple[float, Dict[str, np.ndarray]]:
+    """Count-weighted discrete MI within each condition level
+    (_entropy_estimators.py:291-320)."""
+    zc = [z] if np.ndim(z) == 1 else list(np.asarray(z).T)
+    cxyz, g0 = _row_counts([x, y] + zc)
+    cxz, g1 = _row_counts([x] + zc)
+    cyz, g2 = _row_counts([y] + zc)
+    cz, g3 = _row_counts(zc)
+    n = len(cz)
+    v = float(np.sum(np.log((cz * cxyz).astype(np.float64) / (cxz * cyz).astype(np.float64))) / n)
+    # levels with more than a quarter of their rows distinct in x (y)
+    zrows = np.column_stack([np.asarray(c, dtype=np.float64) + 0.0 for c in zc])
+    _, zinv, zcnt = np.unique(zrows, axis=0, return_inverse=True, return_counts=True)
+    zinv = np.ravel(zinv)
+    wx = wy = 0
+    for level in range(len(zcnt)):
+        sel = zinv == level
+        wx += len(np.unique(np.asarray(x, dtype=np.float64)[sel] + 0.0)) > zcnt[level] / 4
+        wy += len(np.unique(np.asarray(y, dtype=np.float64)[sel] + 0.0)) > zcnt[level] / 4
+    return v, {"cxyz": cxyz, "cxz": cxz, "cyz": cyz, "cz": cz,
+               "groups": np.array([g0, g1, g2, g3, wx, wy])}

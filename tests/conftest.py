@@ -57,11 +57,27 @@ def oracle_run_tasks(O, calls=None):
         def __init__(self, value, status):
             self.value, self.status = value, status
 
-    def run(tasks, flags=0, device=0, results_out=None, noise=None):
+    def run(tasks, flags=0, device=0, results_out=None, noise=None, groups_out=None):
         if calls is not None:
             calls.append(len(tasks))
         out = []
-        for t in tasks:
+        for ti, t in enumerate(tasks):
+            if t.kind in _native.DISCRETE_KINDS:
+                cols = [np.asarray(c) for c in list(t.x) + list(t.y) + list(t.z)]
+                dx, dy = len(t.x), len(t.y)
+                x = np.column_stack(cols[:dx])
+                if t.kind == _native.DISCRETE_ENTROPY:
+                    v, a = O.discrete_entropy(x)
+                elif t.kind == _native.DISCRETE_MI:
+                    v, a = O.discrete_mi(cols[0], cols[1])
+                else:
+                    v, a = O.conditional_discrete_mi(cols[0], cols[1], np.column_stack(cols[dx + dy:]))
+                out.append(v)
+                if groups_out is not None:
+                    groups_out[ti] = [int(g) for g in a["groups"]]
+                if results_out is not None:
+                    results_out.append(Result(v, 0))
+                continue
             n = t.n or (t.x[0].length if isinstance(t.x[0], _native.Col) else len(t.x[0]))
             ix = np.arange(n) if t.index is None else np.asarray(t.index)
             cols = [(c.ref if isinstance(c, _native.Col) else np.asarray(c))[ix]

@@ -138,6 +138,31 @@ def _cases(rng_seed_base: int = 0):
     rng = np.random.default_rng(44)
     yield "ent_5d_n700_k4", "ent", 4, dict(x=rng.normal(size=(700, 5)))
 
+    # discrete plug-in estimators (k unused)
+    rng = np.random.default_rng(50)
+    yield "dent_1d_n3000", "dent", 1, dict(x=rng.integers(0, 12, size=3000).astype(np.float64))
+    rng = np.random.default_rng(51)
+    yield "dent_2d_n2000", "dent", 1, dict(x=np.column_stack((rng.integers(0, 5, size=2000),
+                                                              rng.choice([-0.5, 0.0, 2.5], size=2000))))
+    rng = np.random.default_rng(52)
+    dx = rng.integers(0, 6, size=2500)
+    dy = (dx + rng.integers(0, 3, size=2500)) % 7
+    yield "dmi_n2500", "dmi", 1, dict(x=dx.astype(np.float64), y=dy.astype(np.float64))
+    rng = np.random.default_rng(53)
+    yield "dmi_manylevels_n400", "dmi", 1, dict(x=rng.integers(0, 300, size=400).astype(np.float64),
+                                                 y=rng.integers(0, 2, size=400).astype(np.float64))
+    rng = np.random.default_rng(54)
+    dz = rng.integers(0, 4, size=3000)
+    ddx = (dz + rng.integers(0, 3, size=3000)) % 5
+    ddy = (ddx + dz + rng.integers(0, 2, size=3000)) % 4
+    yield "dcmi_n3000", "dcmi", 1, dict(x=ddx.astype(np.float64), y=ddy.astype(np.float64),
+                                        z=dz.astype(np.float64).reshape(-1, 1))
+    rng = np.random.default_rng(55)
+    dz2 = rng.integers(0, 3, size=(1500, 2))
+    yield "dcmi_dz2_n1500", "dcmi", 1, dict(x=rng.integers(0, 4, size=1500).astype(np.float64),
+                                            y=(dz2[:, 0] + rng.integers(0, 2, size=1500)).astype(np.float64),
+                                            z=dz2.astype(np.float64))
+
 
 def _internals(kind, k, inp, cKDTree):
     """Recompute the estimator's internal arrays with its own cKDTree calls."""
@@ -196,6 +221,19 @@ def _internals(kind, k, inp, cKDTree):
             x = x.reshape(-1, 1)
         eps = cKDTree(x).query(x, k=[k + 1], p=np.inf)[0].flatten()
         return dict(eps=eps)
+    if kind in ("dent", "dmi", "dcmi"):
+        # rows equal to each row on each column subset, with np.unique as the
+        # reference counts them
+        def counts(*arrs):
+            rows = np.column_stack(arrs)
+            _, inv, cnt = np.unique(rows, axis=0, return_inverse=True, return_counts=True)
+            return cnt[np.ravel(inv)].astype(np.int64)
+        if kind == "dent":
+            return dict(c=counts(inp["x"]))
+        if kind == "dmi":
+            return dict(cxy=counts(inp["x"], inp["y"]), cx=counts(inp["x"]), cy=counts(inp["y"]))
+        return dict(cxyz=counts(inp["x"], inp["y"], inp["z"]), cxz=counts(inp["x"], inp["z"]),
+                    cyz=counts(inp["y"], inp["z"]), cz=counts(inp["z"]))
     raise ValueError(kind)
 
 
@@ -225,6 +263,15 @@ def _driver_cases():
     yield "drv_entropy_multidim", "estimate_entropy", (ar[:, :2],), dict(multidim=True, k=4)
     yield "drv_entropy_cond", "estimate_entropy", (ar[:, :2],), dict(cond=ar[:, 2], k=3)
     yield "drv_entropy_mask", "estimate_entropy", (ar[:, 0],), dict(mask=mask)
+    lv = np.round(ar * 0.8).astype(int)
+    yield "drv_discrete_both", "estimate_mi", (lv[:, 1], lv[:, [0, 2]], [0, 1, 2]), \
+        dict(discrete_x=True, discrete_y=True)
+    yield "drv_discrete_both_cond", "estimate_mi", (lv[:, 1], lv[:, 0]), \
+        dict(discrete_x=True, discrete_y=True, cond=lv[:, 2])
+    yield "drv_discrete_entropy", "estimate_entropy", (lv,), dict(discrete=True)
+    yield "drv_discrete_entropy_multidim", "estimate_entropy", (lv[:, :2],), \
+        dict(discrete=True, multidim=True)
+    yield "drv_discrete_pairwise", "pairwise_mi", (lv,), dict(discrete=True)
 
 
 def digest(arr, dtype) -> str:
@@ -329,7 +376,10 @@ def main() -> None:
              "cmi": lambda i, k: ee._estimate_conditional_mi(i["x"], i["y"], i["z"], k),
              "semi": lambda i, k: ee._estimate_semidiscrete_mi(i["x"], i["y"], k),
              "csemi": lambda i, k: ee._estimate_conditional_semidiscrete_mi(i["x"], i["y"], i["z"], k),
-             "ent": lambda i, k: ee._estimate_single_entropy(i["x"], k)}
+             "ent": lambda i, k: ee._estimate_single_entropy(i["x"], k),
+             "dent": lambda i, k: ee._estimate_discrete_entropy(i["x"]),
+             "dmi": lambda i, k: ee._estimate_discrete_mi(i["x"], i["y"]),
+             "dcmi": lambda i, k: ee._estimate_conditional_discrete_mi(i["x"], i["y"], i["z"])}
     out = {}
     names = []
     import warnings

@@ -171,7 +171,7 @@ def _captured_inputs(monkeypatch, call, unshared):
     """Columns of every task a public call hands to the GPU."""
     seen = []
 
-    def run(tasks, flags=0, device=0, results_out=None):
+    def run(tasks, flags=0, device=0, results_out=None, groups_out=None):
         for t in tasks:
             seen.append([np.array(c, copy=True) for c in list(t.x) + list(t.y) + list(t.z)] +
                         ([np.asarray(t.labels).copy()] if t.labels is not None else []))
@@ -298,7 +298,7 @@ def test_device_preprocessing_columns_are_the_reference_slices(monkeypatch, case
             "lags_cond2": [0, 4]}
     seen = []
 
-    def run(tasks, flags=0, device=0, results_out=None, noise=None):
+    def run(tasks, flags=0, device=0, results_out=None, noise=None, groups_out=None):
         assert flags & _native.RESCALE
         for t in tasks:
             ix = np.arange(t.n) if t.index is None else np.asarray(t.index)
