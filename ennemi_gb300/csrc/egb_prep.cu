@@ -37,20 +37,34 @@ int grid_x_for(int64_t n) {
 }
 int grid_y_for(int n) { return n > 65535 ? 65535 : (n < 1 ? 1 : n); }
 
+// Four loads in flight per thread before its stores: columns read in place
+// from host memory cross the CPU-GPU link, where throughput follows the
+// requests outstanding.
+constexpr int GATHER_UNROLL = 4;
 __global__ void gather_kernel(const TaskDev* __restrict__ tasks,
                               const GatherCol* __restrict__ cols, int ncols) {
   for (int g = blockIdx.y; g < ncols; g += gridDim.y) {
     const GatherCol gc = cols[g];
     const TaskDev t = tasks[gc.task];
     double* dst = const_cast<double*>(t.x64) + (int64_t)gc.col * t.ld;
-    for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < t.ld;
-         w += (int64_t)gridDim.x * blockDim.x) {
-      double v = 0.0;
-      if (w < t.n) {
-        const int64_t s = gc.perm ? (int64_t)gc.perm[w] : w;
-        v = gc.src[s * gc.stride];
+    const int64_t step = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t w0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w0 < t.ld;
+         w0 += GATHER_UNROLL * step) {
+      double v[GATHER_UNROLL];
+#pragma unroll
+      for (int u = 0; u < GATHER_UNROLL; ++u) {
+        const int64_t w = w0 + u * step;
+        v[u] = 0.0;
+        if (w < t.n) {
+          const int64_t s = gc.perm ? (int64_t)gc.perm[w] : w;
+          v[u] = gc.src[s * gc.stride];
+        }
       }
-      dst[w] = v;
+#pragma unroll
+      for (int u = 0; u < GATHER_UNROLL; ++u) {
+        const int64_t w = w0 + u * step;
+        if (w < t.ld) dst[w] = v[u];
+      }
     }
   }
 }
@@ -428,7 +442,7 @@ __global__ void combine_kernel(const TaskDev* __restrict__ tasks,
 void launch_gather(const TaskDev* tasks_d, const GatherCol* cols_d, int ncols, int64_t max_ld,
                    cudaStream_t st) {
   if (ncols <= 0) return;
-  dim3 grid(grid_x_for(max_ld), grid_y_for(ncols));
+  dim3 grid(grid_x_for((max_ld + GATHER_UNROLL - 1) / GATHER_UNROLL), grid_y_for(ncols));
   gather_kernel<<<grid, PREP_THREADS, 0, st>>>(tasks_d, cols_d, ncols);
   count_launch();
 }

@@ -126,6 +126,16 @@ __device__ __forceinline__ float up_band32(float t, float mq) {
   if (!(t < __int_as_float(0x7f800000))) return __int_as_float(0x7f800000);
   return __fmaf_ru(t, 1.0f + 0x1p-21f, __fmaf_ru(mq, 0x1p-21f, 0x1p-100f));
 }
+// FP32 value bounding from below the FP64 distance of a candidate whose FP32
+// distance is t (t >= 0 finite).  From |t - D| <= 2^-23 (M + D)(1 + 2^-20)
+// + 2^-148 (egb_internal.cuh), D >= (t - 2^-23 M (1 + 2^-20) - 2^-148) /
+// (1 + 2^-23 (1 + 2^-20)); with mq >= M and the factors taken four times
+// over, (t - 2^-21 mq - 2^-100)(1 - 2^-21) rounded down is below that.
+__device__ __forceinline__ float dn_band32(float t, float mq) {
+  if (!(t < __int_as_float(0x7f800000))) return 0.0f;
+  const float a = __fsub_rd(t, __fmaf_ru(mq, 0x1p-21f, 0x1p-100f));
+  return a > 0.0f ? __fmul_rd(a, 1.0f - 0x1p-21f) : 0.0f;
+}
 
 template <int KMAX>
 __device__ __forceinline__ void insert_sorted_f(float (&l)[KMAX], float v) {

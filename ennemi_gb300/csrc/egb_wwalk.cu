@@ -41,6 +41,7 @@ using wgrid_detail::insert_sorted;
 using wgrid_detail::insert_sorted_fi;
 using wgrid_detail::plan_margin;
 using wgrid_detail::up_band32;
+using wgrid_detail::dn_band32;
 
 constexpr int WW_WARPS = 4;
 // A lane whose walks screen more candidates than this in pass 0 leaves its
@@ -483,11 +484,16 @@ wwalk_kernel(const JobDev* __restrict__ jobs, const WorkItem* __restrict__ items
         const float u32 = up_band32(l32[KMAX - 1], mq);
         const float s32 = up_band32(u32, mq);
         if (rej > s32) {
-          // every left-out candidate is farther than U >= the exact K-th
+          // every left-out candidate is farther than U >= the exact K-th,
+          // which is the largest exact distance of the K listed ones; a
+          // listed candidate whose FP32 upper bound does not exceed the last
+          // one's FP32 lower bound cannot be larger, so usually only the
+          // last is evaluated in FP64
+          const float lo_last = dn_band32(l32[KMAX - 1], mq);
           uint64_t mx = 0;
 #pragma unroll
           for (int s = 0; s < KMAX; ++s) {
-            if (s >= KMAX - K) {
+            if (s >= KMAX - K && (s == KMAX - 1 || up_band32(l32[s], mq) > lo_last)) {
               const uint64_t e = exact_dist(i32[s]);
               mx = e > mx ? e : mx;
             }
