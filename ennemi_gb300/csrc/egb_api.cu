@@ -776,6 +776,9 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   const size_t off_vals_b = dl.take(sizeof(int32_t) * (size_t)std::max<int64_t>(sort_total, 1));
   const size_t off_s1 = dl.take(sizeof(uint64_t) * (size_t)std::max<int64_t>(s1_total, 1));
   const size_t off_s2 = dl.take(sizeof(uint64_t) * (size_t)std::max<int64_t>(s2_total, 1));
+  const size_t off_fk = dl.take(sizeof(float) * (size_t)std::max<int64_t>(sort_total, 1));
+  const size_t off_fs1 = dl.take(sizeof(float) * (size_t)std::max<int64_t>(s1_total, 1));
+  const size_t off_fs2 = dl.take(sizeof(float) * (size_t)std::max<int64_t>(s2_total, 1));
   const size_t sweep_bytes = sort_sweep_bytes(nblk_sort, (int)segs.size());
   const size_t off_sweep = dl.take(sweep_bytes);
 
@@ -1533,8 +1536,10 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   launch_sort(tasks_d, (const SortSeg*)dtab(tab_segs), (const int32_t*)dtab(tab_blkseg), nblk_sort,
               (int)segs.size(), keys, (uint64_t*)(A + off_keys_b), vals, (int32_t*)(A + off_vals_b),
               A + off_sweep, err_d, st);
-  launch_samples((const SortSeg*)dtab(tab_segs), (const int32_t*)dtab(tab_blkseg), nblk_sort, keys,
-                 (uint64_t*)(A + off_s1), (uint64_t*)(A + off_s2), st);
+  const KeyIndex kx{keys, (const float*)(A + off_fk), (const uint64_t*)(A + off_s1),
+                    (const uint64_t*)(A + off_s2), (const float*)(A + off_fs1),
+                    (const float*)(A + off_fs2)};
+  launch_samples((const SortSeg*)dtab(tab_segs), (const int32_t*)dtab(tab_blkseg), nblk_sort, kx, st);
   if (timing) EGB_CUDA(cudaEventRecord(ctx->kev[9], st));
   launch_materialize(tasks_d, (const JobDev*)dtab(tab_jobs), (int)jobs.size(), vals,
                      (const SortSeg*)dtab(tab_segs), max_lds, st);
@@ -1573,8 +1578,8 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   launch_wm_build((const WmJob*)dtab(tab_wbuild), (int)wbuild.size(), wm_tiles, wm_levels, vals, st);
   if (timing) EGB_CUDA(cudaEventRecord(ctx->ev[3], st));
 
-  launch_sorted_jobs(tasks_d, (const SortedJob*)dtab(tab_sjk), (int)sj_knn.size(), blk_knn, keys,
-                     (const uint64_t*)(A + off_s1), (const uint64_t*)(A + off_s2), vals, st);
+  launch_sorted_jobs(tasks_d, (const SortedJob*)dtab(tab_sjk), (int)sj_knn.size(), blk_knn, kx, vals,
+                     st);
   if (timing) EGB_CUDA(cudaEventRecord(ctx->kev[0], st));
   for (size_t g = 0; g < groups.size(); ++g) {
     Group& G = groups[g];
@@ -1610,14 +1615,13 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
 
   launch_radius(tasks_d, ntasks, max_ld, st);
   if (timing) EGB_CUDA(cudaEventRecord(ctx->kev[10], st));
-  launch_sorted_jobs(tasks_d, (const SortedJob*)dtab(tab_sjc), (int)sj_cnt.size(), blk_cnt, keys,
-                     (const uint64_t*)(A + off_s1), (const uint64_t*)(A + off_s2), vals, st);
+  launch_sorted_jobs(tasks_d, (const SortedJob*)dtab(tab_sjc), (int)sj_cnt.size(), blk_cnt, kx, vals,
+                     st);
   if (timing) EGB_CUDA(cudaEventRecord(ctx->kev[11], st));
   if (timing) EGB_CUDA(cudaEventRecord(ctx->kev[4], st));
   launch_groups(tasks_d, (const GroupJob*)dtab(tab_gbjobs), (int)gbjobs.size(), gb_blocks, err_d, st);
   launch_level_checks((const LevelCheck*)dtab(tab_lchecks), (int)lchecks.size(), lcheck_max_n, st);
-  launch_wm_count(tasks_d, (const WmJob*)dtab(tab_wjobs), (int)wjobs.size(), wm_qblocks, keys,
-                  (const uint64_t*)(A + off_s1), (const uint64_t*)(A + off_s2), vals, st);
+  launch_wm_count(tasks_d, (const WmJob*)dtab(tab_wjobs), (int)wjobs.size(), wm_qblocks, kx, vals, st);
   for (size_t g = 0; g < groups.size(); ++g) {
     Group& G = groups[g];
     if (G.is_knn || G.nitems == 0) continue;

@@ -445,6 +445,18 @@ void launch_combine(const TaskDev* tasks_d, const CombineJob* jobs_d, const int3
 
 // egb_sort.cu
 constexpr int SORT_TILE = 2048;
+// The batch's sorted keys and the arrays searched in their place: each
+// key's value rounded down to FP32 (exact comparisons against FP32 bounds in
+// half the bytes), and samples of both (egb_search.cuh), at each segment's
+// out_base / s1_base / s2_base.
+struct KeyIndex {
+  const uint64_t* keys;   // sorted keys of every segment (key_of)
+  const float* fkeys;     // the largest float <= each key's value
+  const uint64_t* s1;     // keys[32 j]
+  const uint64_t* s2;     // keys[1024 j]
+  const float* fs1;       // fkeys[32 j]
+  const float* fs2;       // fkeys[1024 j]
+};
 // Strip keys of the grid jobs.  launch_grid_inv: inv[p_B] = column-1 rank
 // of each point (by working offset).  launch_grid_key: keys[p] = cell key of
 // the point at column-0 position p -- its strip (column-1 rank * nstrips /
@@ -482,8 +494,7 @@ void launch_sort(const TaskDev* tasks_d, const SortSeg* segs_d, const int32_t* b
                  int32_t* vals_b, void* sweep, uint32_t* err, cudaStream_t st);
 constexpr int SORTED_BLOCK = 256;
 void launch_sorted_jobs(const TaskDev* tasks_d, const SortedJob* jobs_d, int njobs,
-                        int total_blocks, const uint64_t* keys, const uint64_t* samples1,
-                        const uint64_t* samples2, const int32_t* perm, cudaStream_t st);
+                        int total_blocks, const KeyIndex& kx, const int32_t* perm, cudaStream_t st);
 
 // egb_knn.cu / egb_count.cu: tile kernels over materialised jobs.
 // dclass in {2, 3, 4} or 0 (generic d <= EGB_DMAX); kclass in {4, 8, 16, 32}.
@@ -582,11 +593,11 @@ void launch_wm_build(const WmJob* jobs_d, int njobs, int total_tiles, int max_le
                      const int32_t* sorted_vals, cudaStream_t st);
 // Counts: one thread per query, in the a order; writes cnt[slot] of the task.
 void launch_wm_count(const TaskDev* tasks_d, const WmJob* jobs_d, int njobs, int total_blocks,
-                     const uint64_t* sorted_keys, const uint64_t* samples1,
-                     const uint64_t* samples2, const int32_t* sorted_vals, cudaStream_t st);
-// Samples of every sorted segment (egb_search.cuh), after the sort.
-void launch_samples(const SortSeg* segs_d, const int32_t* blk_seg_d, int nblk,
-                    const uint64_t* keys, uint64_t* samples1, uint64_t* samples2, cudaStream_t st);
+                     const KeyIndex& kx, const int32_t* sorted_vals, cudaStream_t st);
+// The FP32 copy and the samples of every sorted segment (KeyIndex), after
+// the sort.
+void launch_samples(const SortSeg* segs_d, const int32_t* blk_seg_d, int nblk, const KeyIndex& kx,
+                    cudaStream_t st);
 
 // egb_discrete.cu: exact group-by of the rows of one column subset of a
 // discrete task: the rows equal to each row, into count slot `slot`.

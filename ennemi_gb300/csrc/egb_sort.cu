@@ -387,10 +387,7 @@ __global__ void scan_down_kernel(uint32_t* __restrict__ data, int64_t n,
 // --------------------------------------------------------- sorted jobs ----
 __global__ void sorted_jobs_kernel(const TaskDev* __restrict__ tasks,
                                    const SortedJob* __restrict__ jobs, int njobs,
-                                   const uint64_t* __restrict__ keys_all,
-                                   const uint64_t* __restrict__ s1_all,
-                                   const uint64_t* __restrict__ s2_all,
-                                   const int32_t* __restrict__ perm_all) {
+                                   const KeyIndex kx, const int32_t* __restrict__ perm_all) {
   // the job of this block: last j with jobs[j].blk0 <= blockIdx.x
   int lo = 0, hi = njobs;
   while (hi - lo > 1) {
@@ -401,7 +398,7 @@ __global__ void sorted_jobs_kernel(const TaskDev* __restrict__ tasks,
   const int64_t p = (int64_t)((int)blockIdx.x - jb.blk0) * SORTED_THREADS + threadIdx.x;
   const int64_t len = jb.len;
   if (p >= len) return;
-  const uint64_t* __restrict__ keys = keys_all + jb.base;
+  const uint64_t* __restrict__ keys = kx.keys + jb.base;
   const int32_t i = perm_all[jb.base + p];
   const TaskDev t = tasks[jb.task];
   const double q = value_of(keys[p]);
@@ -431,7 +428,7 @@ __global__ void sorted_jobs_kernel(const TaskDev* __restrict__ tasks,
     // The ball is one run of sorted positions; its ends come from FP32
     // brackets and the segment's samples (ball_positions, egb_search.cuh).
     int lo, hi;
-    ball_positions(keys, s1_all + jb.s1_base, s2_all + jb.s2_base, (int)len, q, r, (int)p, lo, hi);
+    ball_positions(seg_view(kx, jb.base, jb.s1_base, jb.s2_base, (int)len), q, r, (int)p, lo, hi);
     count = (int32_t)(hi - lo);
   }
   t.cnt[jb.slot][i] = count;
@@ -650,11 +647,9 @@ void launch_radix_pass(const SortSeg* segs_d, const int32_t* blk_seg_d, int nblk
 }
 
 void launch_sorted_jobs(const TaskDev* tasks_d, const SortedJob* jobs_d, int njobs,
-                        int total_blocks, const uint64_t* keys, const uint64_t* samples1,
-                        const uint64_t* samples2, const int32_t* perm, cudaStream_t st) {
+                        int total_blocks, const KeyIndex& kx, const int32_t* perm, cudaStream_t st) {
   if (njobs <= 0 || total_blocks <= 0) return;
-  sorted_jobs_kernel<<<(unsigned)total_blocks, SORTED_THREADS, 0, st>>>(tasks_d, jobs_d, njobs,
-                                                                        keys, samples1, samples2,
+  sorted_jobs_kernel<<<(unsigned)total_blocks, SORTED_THREADS, 0, st>>>(tasks_d, jobs_d, njobs, kx,
                                                                         perm);
   count_launch();
 }

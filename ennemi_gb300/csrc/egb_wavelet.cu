@@ -358,8 +358,7 @@ __device__ int wm_rect(const WmJob& J, int a, int b, int c, int d) {
 
 __global__ void __launch_bounds__(WM_QBLOCK)
 wm_count_kernel(const TaskDev* __restrict__ tasks, const WmJob* __restrict__ jobs, int njobs,
-                const uint64_t* __restrict__ keys_all, const uint64_t* __restrict__ s1_all,
-                const uint64_t* __restrict__ s2_all, const int32_t* __restrict__ vals_all) {
+                const KeyIndex kx, const int32_t* __restrict__ vals_all) {
   const WmJob& J = jobs[job_of(jobs, njobs, blockIdx.x, [](const WmJob& j) { return j.qblk0; })];
   const int len = J.len;
   const int i = ((int)blockIdx.x - J.qblk0) * WM_QBLOCK + threadIdx.x;
@@ -373,29 +372,40 @@ wm_count_kernel(const TaskDev* __restrict__ tasks, const WmJob* __restrict__ job
   } else if (isinf(r)) {
     count = len;
   } else {
-    const uint64_t* __restrict__ ka = keys_all + J.base_a;
-    const uint64_t* __restrict__ kb = keys_all + J.base_b;
+    const SegView va = seg_view(kx, J.base_a, J.s1_a, J.s2_a, len);
+    const SegView vb = seg_view(kx, J.base_b, J.s1_b, J.s2_b, len);
     const int jb = min(max(J.inv_b[w - J.seg_begin], 0), len - 1);
     int alo, ahi, blo, bhi;
-    ball_positions(ka, s1_all + J.s1_a, s2_all + J.s2_a, len, value_of(ka[i]), r, -1, alo, ahi);
-    ball_positions(kb, s1_all + J.s1_b, s2_all + J.s2_b, len, value_of(__ldg(kb + jb)), r, -1, blo, bhi);
+    ball_positions(va, value_of(va.keys[i]), r, -1, alo, ahi);
+    ball_positions(vb, value_of(__ldg(vb.keys + jb)), r, -1, blo, bhi);
     count = wm_rect(J, alo, ahi, blo, bhi);
   }
   t.cnt[J.slot][w] = count;
 }
 
-// s1[j] = keys[32 j], s2[j] = keys[1024 j] of every sorted segment
-__global__ void samples_kernel(const SortSeg* __restrict__ segs, const int32_t* __restrict__ blk_seg,
-                               const uint64_t* __restrict__ keys, uint64_t* __restrict__ s1,
-                               uint64_t* __restrict__ s2) {
+// fkeys[p] = the largest float <= the value of keys[p]; s1[j] = keys[32 j],
+// s2[j] = keys[1024 j] and the same of fkeys, for every sorted segment.
+// One block of SAMPLE_THREADS per 2048-key tile of the sort.
+constexpr int SAMPLE_THREADS = 256;
+__global__ void __launch_bounds__(SAMPLE_THREADS)
+samples_kernel(const SortSeg* __restrict__ segs, const int32_t* __restrict__ blk_seg, KeyIndex kx) {
   const SortSeg sg = segs[blk_seg[blockIdx.x]];
   const int i0 = ((int)blockIdx.x - sg.blk0) * SORT_TILE;
-  const int j = i0 / SAMPLE1 + (int)threadIdx.x;   // SORT_TILE / SAMPLE1 threads
-  const int p = j * SAMPLE1;
-  if (p >= sg.len || p >= i0 + SORT_TILE) return;
-  const uint64_t k = keys[sg.out_base + p];
-  s1[sg.s1_base + j] = k;
-  if (p % SAMPLE2 == 0) s2[sg.s2_base + p / SAMPLE2] = k;
+  const int i1 = min(i0 + SORT_TILE, sg.len);
+  float* fk = const_cast<float*>(kx.fkeys) + sg.out_base;
+  for (int p = i0 + (int)threadIdx.x; p < i1; p += SAMPLE_THREADS) {
+    const uint64_t k = __ldg(kx.keys + sg.out_base + p);
+    const float f = __double2float_rd(value_of(k));
+    fk[p] = f;
+    if (p % SAMPLE1 == 0) {
+      const_cast<uint64_t*>(kx.s1)[sg.s1_base + p / SAMPLE1] = k;
+      const_cast<float*>(kx.fs1)[sg.s1_base + p / SAMPLE1] = f;
+      if (p % SAMPLE2 == 0) {
+        const_cast<uint64_t*>(kx.s2)[sg.s2_base + p / SAMPLE2] = k;
+        const_cast<float*>(kx.fs2)[sg.s2_base + p / SAMPLE2] = f;
+      }
+    }
+  }
 }
 static_assert(SORT_TILE % SAMPLE1 == 0, "sample grid");
 
@@ -415,18 +425,16 @@ void launch_wm_build(const WmJob* jobs_d, int njobs, int total_tiles, int max_le
 }
 
 void launch_wm_count(const TaskDev* tasks_d, const WmJob* jobs_d, int njobs, int total_blocks,
-                     const uint64_t* sorted_keys, const uint64_t* samples1,
-                     const uint64_t* samples2, const int32_t* sorted_vals, cudaStream_t st) {
+                     const KeyIndex& kx, const int32_t* sorted_vals, cudaStream_t st) {
   if (njobs <= 0 || total_blocks <= 0) return;
-  wm_count_kernel<<<total_blocks, WM_QBLOCK, 0, st>>>(tasks_d, jobs_d, njobs, sorted_keys, samples1,
-                                                      samples2, sorted_vals);
+  wm_count_kernel<<<total_blocks, WM_QBLOCK, 0, st>>>(tasks_d, jobs_d, njobs, kx, sorted_vals);
   count_launch();
 }
 
-void launch_samples(const SortSeg* segs_d, const int32_t* blk_seg_d, int nblk,
-                    const uint64_t* keys, uint64_t* samples1, uint64_t* samples2, cudaStream_t st) {
+void launch_samples(const SortSeg* segs_d, const int32_t* blk_seg_d, int nblk, const KeyIndex& kx,
+                    cudaStream_t st) {
   if (nblk <= 0) return;
-  samples_kernel<<<nblk, SORT_TILE / SAMPLE1, 0, st>>>(segs_d, blk_seg_d, keys, samples1, samples2);
+  samples_kernel<<<nblk, SAMPLE_THREADS, 0, st>>>(segs_d, blk_seg_d, kx);
   count_launch();
 }
 
