@@ -59,7 +59,9 @@ constexpr int SLAB_MIN = 4096;        // shorter multi-D segments use brute forc
 constexpr int NPHASE = 7;
 constexpr int NKTIME = 6;   // kNN tile, kNN deferred, count tile, count deferred,
                             // radix sort, 1-D counts
-constexpr int NSTATS = 13;
+constexpr int NSTATS = 14;
+// finish_batch: the batch must run again with the full sort (not a public code)
+constexpr int RC_SORT_RETRY = 1;
 
 // Digamma of a positive integer with the reference's formula
 // (ennemi/_entropy_estimators.py:341-348): the SciPy constant for psi(1),
@@ -135,6 +137,7 @@ struct ReplayState {
   size_t tab_bytes = 0, zr_bytes = 0;
   int nchunks = 0;
   int64_t sort_keys = 0, sort_segs = 0;  // keys and segments of the batch's radix sort
+  int64_t sort_passes = 0;                // its 8-bit digit passes
 };
 
 }  // namespace
@@ -273,7 +276,9 @@ int finish_batch(egb_ctx* ctx, const ReplayState& R, const char* H, int64_t laun
     ctx->stats[9] = R.sort_keys;
     ctx->stats[10] = R.sort_segs;
   }
+  ctx->stats[13] = R.sort_passes;
   const uint32_t dev_err = *(const uint32_t*)(H + R.pin_zr + R.zr_err);
+  if (dev_err == DERR_SORT_TIES) return RC_SORT_RETRY;
   if (dev_err) {
     char buf[128];
     std::snprintf(buf, sizeof buf, "device error word 0x%x (%s)", dev_err,
@@ -391,8 +396,10 @@ uint64_t replay_key(const egb_ctx* ctx, const egb_task* tasks, int ntasks, int f
 }
 
 // extra: per-task extras for the internal kinds (radius for KIND_COUNT_ONLY)
-int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_result* results,
-              const double* count_radius) {
+// One batch.  sort_first: the first 8-bit key digit the batch sort passes
+// over (2: the high 48 bits and a repair of tied runs; 0: all eight).
+int run_batch_sorted(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags,
+                     egb_result* results, const double* count_radius, int sort_first) {
   if (!ctx) return EGB_ERR_ARG;
   if (ntasks < 0 || (ntasks > 0 && !tasks)) return fail(ctx, EGB_ERR_ARG, "invalid task list");
   if (ntasks == 0) return EGB_OK;
@@ -1535,7 +1542,7 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   if (timing) EGB_CUDA(cudaEventRecord(ctx->kev[8], st));
   launch_sort(tasks_d, (const SortSeg*)dtab(tab_segs), (const int32_t*)dtab(tab_blkseg), nblk_sort,
               (int)segs.size(), keys, (uint64_t*)(A + off_keys_b), vals, (int32_t*)(A + off_vals_b),
-              A + off_sweep, err_d, st);
+              A + off_sweep, sort_first, err_d, st);
   const KeyIndex kx{keys, (const float*)(A + off_fk), (const uint64_t*)(A + off_s1),
                     (const uint64_t*)(A + off_s2), (const float*)(A + off_fs1),
                     (const float*)(A + off_fs2)};
@@ -1744,6 +1751,7 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   R.zr_bytes = zr_bytes;
   R.sort_keys = sort_total;
   R.sort_segs = (int64_t)segs.size();
+  R.sort_passes = 8 - sort_first;
   const int64_t launches =
       use_graph ? (int64_t)ctx->graph_launches : (int64_t)(g_launches.load() - launches0);
   const int rc_fin = finish_batch(ctx, R, H, launches, results);
@@ -1759,6 +1767,16 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
     ctx->replay = std::move(R);
   }
   return EGB_OK;
+}
+
+// A batch whose sort met keys tied in their high 48 bits over a run too long
+// to repair (finish_batch: RC_SORT_RETRY) runs again with the full sort,
+// planned and issued directly.
+int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_result* results,
+              const double* count_radius) {
+  const int rc = run_batch_sorted(ctx, tasks, ntasks, flags, results, count_radius, 2);
+  if (rc != RC_SORT_RETRY) return rc;
+  return run_batch_sorted(ctx, tasks, ntasks, flags & ~EGB_GRAPH, results, count_radius, 0);
 }
 
 }  // namespace

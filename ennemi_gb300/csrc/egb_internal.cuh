@@ -31,6 +31,8 @@ enum DevErr : uint32_t {
   DERR_NONE = 0,
   DERR_WAIT_TIMEOUT = 1u << 0,  // a bounded mbarrier wait gave up
   DERR_BAD_INDEX = 1u << 1,     // an index guard tripped
+  DERR_SORT_TIES = 1u << 2,     // keys equal in their high 48 bits need the
+                                // full sort: the host runs the batch again
 };
 
 // Per-job flag bits (JobDev::jflags).
@@ -486,12 +488,16 @@ void launch_radix_pass(const SortSeg* segs_d, const int32_t* blk_seg_d, int nblk
                        const uint64_t* kin, const int32_t* vin, uint64_t* kout, int32_t* vout,
                        int shift, uint32_t* hist, uint32_t* scan_tmp, cudaStream_t st);
 size_t sort_scan_tmp_elems(int nblk);
-// The batch sort: single-sweep LSD passes; `sweep` (sort_sweep_bytes, zeroed
-// before the launch) holds its look-back flags, digit totals and tile counters.
+// The batch sort: single-sweep LSD passes over the 8-bit digits first..7 of
+// the keys (first = 0: all; first = 2: the high 48 bits, then a repair of
+// the rare runs tied there, which sets DERR_SORT_TIES when one is too long);
+// `sweep` (sort_sweep_bytes, zeroed before the launch) holds its look-back
+// flags, digit totals and tile counters.  `first` is even: the result is in
+// keys_a / vals_a.
 size_t sort_sweep_bytes(int nblk, int nseg);
 void launch_sort(const TaskDev* tasks_d, const SortSeg* segs_d, const int32_t* blk_seg_d,
                  int nblk, int nseg, uint64_t* keys_a, uint64_t* keys_b, int32_t* vals_a,
-                 int32_t* vals_b, void* sweep, uint32_t* err, cudaStream_t st);
+                 int32_t* vals_b, void* sweep, int first, uint32_t* err, cudaStream_t st);
 constexpr int SORTED_BLOCK = 256;
 void launch_sorted_jobs(const TaskDev* tasks_d, const SortedJob* jobs_d, int njobs,
                         int total_blocks, const KeyIndex& kx, const int32_t* perm, cudaStream_t st);

@@ -194,7 +194,7 @@ __device__ __forceinline__ uint64_t key_of_bits(uint64_t u) {
 __global__ void __launch_bounds__(SORT_THREADS)
 onesweep_load_kernel(const TaskDev* __restrict__ tasks, const SortSeg* __restrict__ segs,
                      const int32_t* __restrict__ blk_seg, uint64_t* __restrict__ keys,
-                     int32_t* __restrict__ vals, uint32_t* __restrict__ seg_hist) {
+                     int32_t* __restrict__ vals, uint32_t* __restrict__ seg_hist, int first) {
   __shared__ uint32_t h[OS_PASSES * 256];
   const int b = blockIdx.x;
   const int si = blk_seg[b];
@@ -211,7 +211,8 @@ onesweep_load_kernel(const TaskDev* __restrict__ tasks, const SortSeg* __restric
     keys[s.out_base + i] = k;
     vals[s.out_base + i] = s.src_begin + i;
 #pragma unroll
-    for (int p = 0; p < OS_PASSES; ++p) atomicAdd(&h[p * 256 + (uint32_t)((k >> (8 * p)) & 255u)], 1u);
+    for (int p = 0; p < OS_PASSES; ++p)
+      if (p >= first) atomicAdd(&h[p * 256 + (uint32_t)((k >> (8 * p)) & 255u)], 1u);
   }
   __syncthreads();
   uint32_t* g = seg_hist + (size_t)si * OS_PASSES * 256;
@@ -333,6 +334,64 @@ onesweep_pass_kernel(const SortSeg* __restrict__ segs, const int32_t* __restrict
       vout[s.out_base + pos] = sv[t];
     } else {
       atomicOr(err, DERR_BAD_INDEX);
+    }
+  }
+}
+
+// ----------------------------------------------------------- tie repair --
+// After the passes over digits 2..7 the keys of a segment are ordered by
+// their high 48 bits (sign, exponent and 36 mantissa bits of the value),
+// stably.  Keys equal there but not in the low 16 bits -- values within a
+// relative 2^-36 of each other -- are rare, and sit in short runs: the first
+// thread of a run of at most TIE_RUN keys sorts it by the whole key with an
+// insertion sort (stable, so equal keys keep their input order and the
+// result is the permutation of the eight-pass sort).  A longer run that is
+// out of order is not repaired: its threads set DERR_SORT_TIES and the host
+// runs the batch again with all eight passes.  Repairs permute keys only
+// within runs, so the high bits read at any position never change while the
+// kernel runs: run boundaries are read race-free.
+constexpr int TIE_RUN = 32;
+
+__global__ void __launch_bounds__(SORT_THREADS)
+tie_fix_kernel(const SortSeg* __restrict__ segs, const int32_t* __restrict__ blk_seg,
+               uint64_t* keys_all, int32_t* vals_all, uint32_t* __restrict__ err) {
+  const SortSeg sg = segs[blk_seg[blockIdx.x]];
+  const int len = sg.len;
+  const int i0 = ((int)blockIdx.x - sg.blk0) * SORT_TILE;
+  const int i1 = min(i0 + SORT_TILE, len);
+  uint64_t* keys = keys_all + sg.out_base;  // written by run owners: no __restrict__
+  int32_t* vals = vals_all + sg.out_base;
+  for (int q = i0 + (int)threadIdx.x; q < i1; q += SORT_THREADS) {
+    const uint64_t k = keys[q];
+    const uint64_t hi = k >> 16;
+    const bool starts = q == 0 || (keys[q - 1] >> 16) != hi;
+    if (!starts) {
+      // inside a run: out of order against the previous key and the run
+      // too long to be repaired -> the batch needs the full sort
+      if (k < keys[q - 1]) {
+        int s = q - 1, e = q + 1;
+        while (s > 0 && (keys[s - 1] >> 16) == hi && q - s <= TIE_RUN) --s;
+        while (e < len && (keys[e] >> 16) == hi && e - s <= TIE_RUN) ++e;
+        if (e - s > TIE_RUN) atomicOr(err, (uint32_t)DERR_SORT_TIES);
+      }
+      continue;
+    }
+    if (q + 1 >= len || (keys[q + 1] >> 16) != hi) continue;  // a run of one
+    int e = q + 1;
+    while (e < len && (keys[e] >> 16) == hi && e - q <= TIE_RUN) ++e;
+    if (e - q > TIE_RUN) continue;
+    for (int i = q + 1; i < e; ++i) {  // stable insertion sort of [q, e)
+      const uint64_t ki = keys[i];
+      if (ki >= keys[i - 1]) continue;
+      const int32_t vi = vals[i];
+      int j = i;
+      while (j > q && keys[j - 1] > ki) {
+        keys[j] = keys[j - 1];
+        vals[j] = vals[j - 1];
+        --j;
+      }
+      keys[j] = ki;
+      vals[j] = vi;
     }
   }
 }
@@ -611,27 +670,32 @@ size_t sort_sweep_bytes(int nblk, int nseg) {
 
 void launch_sort(const TaskDev* tasks_d, const SortSeg* segs_d, const int32_t* blk_seg_d,
                  int nblk, int nseg, uint64_t* keys_a, uint64_t* keys_b, int32_t* vals_a,
-                 int32_t* vals_b, void* sweep, uint32_t* err, cudaStream_t st) {
+                 int32_t* vals_b, void* sweep, int first, uint32_t* err, cudaStream_t st) {
   if (nblk <= 0) return;
   // sweep (zeroed by the caller): flag words, segment digit totals, tile counters
   unsigned long long* flags = (unsigned long long*)sweep;
   uint32_t* seg_hist = (uint32_t*)(flags + 256 * (size_t)nblk);
   int* counters = (int*)(seg_hist + OS_PASSES * 256 * (size_t)std::max(nseg, 1));
   onesweep_load_kernel<<<nblk, SORT_THREADS, 0, st>>>(tasks_d, segs_d, blk_seg_d, keys_a, vals_a,
-                                                     seg_hist);
+                                                     seg_hist, first);
   count_launch();
   uint64_t* kin = keys_a;
   uint64_t* kout = keys_b;
   int32_t* vin = vals_a;
   int32_t* vout = vals_b;
-  for (int pass = 0; pass < OS_PASSES; ++pass) {
+  for (int pass = first; pass < OS_PASSES; ++pass) {
     onesweep_pass_kernel<<<nblk, SORT_THREADS, 0, st>>>(segs_d, blk_seg_d, kin, vin, kout, vout,
                                                        pass, seg_hist, flags, counters + pass, err);
     count_launch();
     uint64_t* tk = kin; kin = kout; kout = tk;
     int32_t* tv = vin; vin = vout; vout = tv;
   }
-  // eight passes: the sorted keys and values are back in keys_a / vals_a
+  // an even number of passes: the sorted keys and values are back in
+  // keys_a / vals_a
+  if (first > 0) {
+    tie_fix_kernel<<<nblk, SORT_THREADS, 0, st>>>(segs_d, blk_seg_d, keys_a, vals_a, err);
+    count_launch();
+  }
 }
 
 void launch_radix_pass(const SortSeg* segs_d, const int32_t* blk_seg_d, int nblk,

@@ -236,7 +236,10 @@ int egb_last_transfer(const egb_ctx* ctx, int64_t* h2d_bytes, int64_t* d2h_bytes
  * d differences, d max-of-abs, one compare), [8] kernels launched, [9] keys
  * and [10] segments of the batch's radix sort, [11] 1 if the batch was
  * planned on the host (0: an EGB_GRAPH replay without planning), [12] 1 if
- * its device work ran as a CUDA graph.  Returns the number written. */
+ * its device work ran as a CUDA graph, [13] the sort's 8-bit digit passes
+ * (6: the high 48 bits of the keys, then a repair of the runs tied there; 8:
+ * the batch ran again with the full sort because such a run was too long to
+ * repair).  Returns the number written. */
 int egb_last_stats(const egb_ctx* ctx, int64_t* out, int32_t max);
 
 /*

@@ -58,3 +58,21 @@ def test_injected_error_bypasses_graph_replay():
     replay = N.run_tasks(dev, flags=N.INPUT_DEVICE | N.GRAPH)
     assert ctx.stats()["planned"] == 0
     assert np.array_equal(first, again) and np.array_equal(first, replay)
+
+
+def test_sort_tie_report_reruns_batch_with_full_sort():
+    """DERR_SORT_TIES (a run of keys tied in their high 48 bits too long for
+    the in-kernel repair) is not an error: the batch runs again, planned and
+    without a graph, with all eight digit passes, and returns the same
+    results as the six-pass sort."""
+    tasks, n = _tasks()
+    ctx = N.context(0)
+    base = N.run_tasks(tasks, flags=N.KEEP_INTERNALS)
+    base_eps = N.fetch(0, 0, n)
+    assert ctx.stats()["sort_passes"] == 6
+    ctx.inject_device_error(4)
+    again = N.run_tasks(tasks, flags=N.KEEP_INTERNALS)
+    st = ctx.stats()
+    assert st["sort_passes"] == 8 and st["planned"] == 1 and st["graph"] == 0
+    assert np.array_equal(base, again)
+    assert np.array_equal(base_eps, N.fetch(0, 0, n))

@@ -246,6 +246,46 @@ def test_public_estimators_on_gpu():
     assert abs(h - 0.5 * np.log(2 * np.pi * np.e)) < 0.05
 
 
+def _tie_cases():
+    """Columns whose sort keys tie in their high 48 bits (values within a
+    relative 2^-36): the six-pass sort repairs short runs in place and sends
+    a long run out of order to the full sort; long runs already in order
+    (exact duplicates, or ascending input) need neither."""
+    rng = np.random.default_rng(31)
+    n = 6000
+    v = rng.normal(size=n // 3)
+    near = np.concatenate([v, np.nextafter(v, np.inf), np.nextafter(np.nextafter(v, -np.inf), -np.inf)])
+    yield "short_runs", rng.permutation(near), 6
+    yield "long_run_shuffled", 1.0 + rng.permutation(n) * 2.0 ** -52, 8
+    yield "long_run_ascending", 1.0 + np.arange(n) * 2.0 ** -52, 6
+    yield "duplicates", rng.integers(0, 7, size=n).astype(np.float64), 6
+    mixed = rng.normal(size=n)
+    mixed[: n // 2] = 3.0 + rng.permutation(n // 2) * 2.0 ** -51
+    yield "half_long_run", rng.permutation(mixed), 8
+
+
+TIES = list(_tie_cases())
+
+
+@pytest.mark.parametrize("kind", ["mi", "ent", "cmi"])
+@pytest.mark.parametrize("case", TIES, ids=[c[0] for c in TIES])
+def test_sort_ties_in_high_bits(oracle, case, kind):
+    name, x, passes = case
+    rng = np.random.default_rng(5)
+    n = len(x)
+    y = rng.normal(size=n) + 0.5 * np.argsort(np.argsort(x)) / n
+    inp = dict(x=x, y=y, z=rng.normal(size=(n, 1)) + x[:, None] * 0)
+    if kind == "ent":
+        inp = dict(x=x)
+    ref_value, ref = _oracle_case(oracle, kind, 3, inp)
+    task = make_task(kind, 3, inp)
+    ctx = N.context(0)
+    vals = N.run_tasks([task], flags=N.KEEP_INTERNALS)
+    assert ctx.stats()["sort_passes"] == passes
+    check_internals(0, kind, task.n, ref["eps"], ref)
+    assert same_value(vals[0], ref_value), (vals[0], ref_value)
+
+
 def test_graph_replay_matches_direct_launch():
     """The streaming pattern: capture once, then refill the same device
     buffers and replay without planning.  The expected values of both data
