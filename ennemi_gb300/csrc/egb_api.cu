@@ -147,6 +147,10 @@ struct egb_ctx {
   int num_sms = 1;
   cudaStream_t own_stream = nullptr;
   cudaStream_t stream = nullptr;
+  // second stream of a batch: the rank-space matrices build on it while the
+  // grid layouts and the kNN run on `stream` (fork / join events)
+  cudaStream_t side_stream = nullptr;
+  cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
   std::string err;
   void* arena = nullptr;
   size_t arena_cap = 0;
@@ -1534,7 +1538,8 @@ int run_batch_sorted(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags,
                    (const int32_t*)dtab(tab_pwlevels), (double*)(A + off_pw_scratch),
                    (double2*)(A + off_pw_ms), ctx->noise_d, zero_d, st);
   launch_prepare(tasks_d, (const int32_t*)dtab(tab_coltask), (const int32_t*)dtab(tab_colidx),
-                 ncols_total, (unsigned long long*)(A + off_minmax), (double*)(A + off_centers), st);
+                 ncols_total, max_n, (unsigned long long*)(A + off_minmax), (double*)(A + off_centers),
+                 st);
   if (timing) EGB_CUDA(cudaEventRecord(ctx->ev[2], st));
 
   uint64_t* keys = (uint64_t*)(A + off_keys_a);
@@ -1547,6 +1552,16 @@ int run_batch_sorted(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags,
                     (const uint64_t*)(A + off_s2), (const float*)(A + off_fs1),
                     (const float*)(A + off_fs2)};
   launch_samples((const SortSeg*)dtab(tab_segs), (const int32_t*)dtab(tab_blkseg), nblk_sort, kx, st);
+  // the rank-space matrices need only the sorted values: they build on the
+  // side stream, joined back before their counts
+  const bool fork_wm = !wbuild.empty();
+  if (fork_wm) {
+    EGB_CUDA(cudaEventRecord(ctx->fork_ev, st));
+    EGB_CUDA(cudaStreamWaitEvent(ctx->side_stream, ctx->fork_ev, 0));
+    launch_wm_build((const WmJob*)dtab(tab_wbuild), (int)wbuild.size(), wm_tiles, wm_levels, vals,
+                    ctx->side_stream);
+    EGB_CUDA(cudaEventRecord(ctx->join_ev, ctx->side_stream));
+  }
   if (timing) EGB_CUDA(cudaEventRecord(ctx->kev[9], st));
   launch_materialize(tasks_d, (const JobDev*)dtab(tab_jobs), (int)jobs.size(), vals,
                      (const SortSeg*)dtab(tab_segs), max_lds, st);
@@ -1582,7 +1597,6 @@ int run_batch_sorted(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags,
                             max_gkey > 256 ? gva : gvb, (const SortSeg*)dtab(tab_gsegs),
                             max_lds, st);
   }
-  launch_wm_build((const WmJob*)dtab(tab_wbuild), (int)wbuild.size(), wm_tiles, wm_levels, vals, st);
   if (timing) EGB_CUDA(cudaEventRecord(ctx->ev[3], st));
 
   launch_sorted_jobs(tasks_d, (const SortedJob*)dtab(tab_sjk), (int)sj_knn.size(), blk_knn, kx, vals,
@@ -1628,6 +1642,7 @@ int run_batch_sorted(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags,
   if (timing) EGB_CUDA(cudaEventRecord(ctx->kev[4], st));
   launch_groups(tasks_d, (const GroupJob*)dtab(tab_gbjobs), (int)gbjobs.size(), gb_blocks, err_d, st);
   launch_level_checks((const LevelCheck*)dtab(tab_lchecks), (int)lchecks.size(), lcheck_max_n, st);
+  if (fork_wm) EGB_CUDA(cudaStreamWaitEvent(st, ctx->join_ev, 0));
   launch_wm_count(tasks_d, (const WmJob*)dtab(tab_wjobs), (int)wjobs.size(), wm_qblocks, kx, vals, st);
   for (size_t g = 0; g < groups.size(); ++g) {
     Group& G = groups[g];
@@ -1789,8 +1804,14 @@ int egb_create(int device, egb_ctx** out) {
   egb_ctx* ctx = new egb_ctx();
   ctx->device = device;
   if (cudaSetDevice(device) != cudaSuccess ||
-      cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking) != cudaSuccess) {
+      cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&ctx->side_stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&ctx->fork_ev, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&ctx->join_ev, cudaEventDisableTiming) != cudaSuccess) {
     cudaGetLastError();
+    if (ctx->fork_ev) cudaEventDestroy(ctx->fork_ev);
+    if (ctx->side_stream) cudaStreamDestroy(ctx->side_stream);
+    if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
     delete ctx;
     return EGB_ERR_CUDA;
   }
@@ -1821,6 +1842,9 @@ void egb_destroy(egb_ctx* ctx) {
     if (e) cudaEventDestroy(e);
   for (auto& e : ctx->kev)
     if (e) cudaEventDestroy(e);
+  if (ctx->fork_ev) cudaEventDestroy(ctx->fork_ev);
+  if (ctx->join_ev) cudaEventDestroy(ctx->join_ev);
+  if (ctx->side_stream) cudaStreamDestroy(ctx->side_stream);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
   delete ctx;
 }

@@ -429,8 +429,8 @@ void count_launch();
 void launch_gather(const TaskDev* tasks_d, const GatherCol* cols_d, int ncols,
                    int64_t max_ld, cudaStream_t st);
 void launch_prepare(const TaskDev* tasks_d, const int32_t* col_task_d, const int32_t* col_idx_d,
-                    int ncols_total, unsigned long long* minmax_d, double* centers_d,
-                    cudaStream_t st);
+                    int ncols_total, int64_t max_n, unsigned long long* minmax_d,
+                    double* centers_d, cudaStream_t st);
 void launch_materialize(const TaskDev* tasks_d, const JobDev* jobs_d, int njobs,
                         const int32_t* sorted_vals, const SortSeg* segs_d, int64_t max_lds,
                         cudaStream_t st);

@@ -192,8 +192,15 @@ __global__ void minmax_kernel(const TaskDev* __restrict__ tasks,
     const TaskDev t = tasks[col_task[g]];
     const double* x = t.x64 + (int64_t)col_idx[g] * t.ld;
     unsigned long long lo = ~0ull, hi = 0ull;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < t.n;
-         i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    for (; i + 3 * stride < t.n; i += 4 * stride) {  // four loads in flight
+      const double v0 = x[i], v1 = x[i + stride], v2 = x[i + 2 * stride], v3 = x[i + 3 * stride];
+      const unsigned long long k0 = key_of(v0), k1 = key_of(v1), k2 = key_of(v2), k3 = key_of(v3);
+      lo = min(min(lo, k0), min(k1, min(k2, k3)));
+      hi = max(max(hi, k0), max(k1, max(k2, k3)));
+    }
+    for (; i < t.n; i += stride) {
       const unsigned long long k = key_of(x[i]);
       lo = k < lo ? k : lo;
       hi = k > hi ? k : hi;
@@ -460,15 +467,15 @@ void launch_rescale(const TaskDev* tasks_d, const RescaleStat* stats_d, int nsta
 }
 
 void launch_prepare(const TaskDev* tasks_d, const int32_t* col_task_d, const int32_t* col_idx_d,
-                    int ncols_total, unsigned long long* minmax_d, double* centers_d,
-                    cudaStream_t st) {
+                    int ncols_total, int64_t max_n, unsigned long long* minmax_d,
+                    double* centers_d, cudaStream_t st) {
   if (ncols_total <= 0) return;
   // slot 2g holds the min key (starts all-ones), slot 2g+1 the max key
   // (starts at zero)
   cudaMemsetAsync(minmax_d, 0, sizeof(unsigned long long) * 2 * ncols_total, st);
   cudaMemset2DAsync(minmax_d, 2 * sizeof(unsigned long long), 0xff, sizeof(unsigned long long),
                     ncols_total, st);
-  dim3 grid(64, grid_y_for(ncols_total));
+  dim3 grid(grid_x_for((max_n + 7) / 8), grid_y_for(ncols_total));  // eight values a thread
   minmax_kernel<<<grid, PREP_THREADS, 0, st>>>(tasks_d, col_task_d, col_idx_d, ncols_total,
                                                 minmax_d);
   count_launch();
