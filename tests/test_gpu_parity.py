@@ -229,6 +229,16 @@ def test_host_columns_read_in_place_match_staged_copies():
         staged = N.run_tasks(tasks, flags=N.STAGE_HOST | extra)
         default = N.run_tasks(tasks, flags=extra)
         assert np.array_equal(staged, default), extra
+    # odd lengths, and a column 8 bytes off a 16-byte boundary (read one
+    # value per request instead of pairs)
+    n2 = 40001
+    buf = np.empty(n2 + 1)
+    off = buf[1:]
+    off[:] = rng.normal(size=n2)
+    c = rng.normal(size=n2) + 0.4 * off
+    assert c.ctypes.data % 16 == 0 and off.ctypes.data % 16 == 8
+    odd = [E.mi_task(c, off, 3), E.cmi_task(off, c, c[::-1].copy(), 3), E.entropy_task(c, 3)]
+    assert np.array_equal(N.run_tasks(odd, flags=N.STAGE_HOST), N.run_tasks(odd))
     pts = np.ascontiguousarray(m[:, :2])
     r = N.knn_eps(pts, 3)
     assert np.array_equal(r, N.knn_eps(pts, 3, flags=N.STAGE_HOST))
