@@ -486,12 +486,12 @@ def main():
     # The dominant kernel (largest share of the step in the ncu launch list)
     # is the radix sort's pass, HBM-bound: per launch it reads and writes
     # every key (8 B) and index (4 B) of the batch's sort once.  Its time per
-    # launch is the event-timed sort (load kernel + 8 passes) over 8, which
-    # slightly overstates it.  DRAM traffic per launch from one ncu capture
-    # of this workload (cold cache): 143.3 MB read + 89.2 MB written.
+    # launch is the event-timed run of the batch's digit passes over their
+    # number.  DRAM traffic per launch from one ncu capture of this workload
+    # (cold cache): 143.3 MB read + 89.2 MB written.
     keys = work_stats.get("sort_keys", 0)
-    sort_ms = phases.get("sort_radix", 0.0)
-    pass_ms = sort_ms / 8.0
+    npass = work_stats.get("sort_passes", 0) or 8
+    pass_ms = phases.get("sort_passes", 0.0) / npass
     pass_bytes = 24.0 * keys
     pass_gbs = pass_bytes / (pass_ms / 1000.0) / 1e9 if pass_ms > 0 else 0.0
     roofline = {"bound": "hbm", "kernel": "onesweep_pass_kernel (radix sort pass)",
@@ -499,7 +499,7 @@ def main():
                 "traffic": (143.31 + 89.22) * 1e6 if args.n == 1_000_000 else None,
                 "traffic_unit": "bytes per launch (ncu, cold cache)",
                 "algorithmic_bytes_per_launch": pass_bytes, "ms_per_launch": pass_ms,
-                "launches_per_step": 8, "peak_source": hbm_src}
+                "launches_per_step": npass, "peak_source": hbm_src}
 
     # the multi-D kernels: latency- and L1-bound, far from any pipe or HBM
     # roofline; counted algorithmic operations ((2d+1) per screened
@@ -537,7 +537,7 @@ def main():
     sort_ms, c1_ms = phases.get("sort_radix", 0.0), phases.get("count_1d", 0.0)
     ss_bytes = 32.0 * args.n * n1d
     ss_gbs = ss_bytes / ((sort_ms + c1_ms) / 1000.0) / 1e9 if sort_ms + c1_ms > 0 else 0.0
-    roofline_sort = {"bound": "hbm", "kernels": "radix sort (load + 8 single-sweep passes) + "
+    roofline_sort = {"bound": "hbm", "kernels": f"radix sort (load + {npass} single-sweep passes) + "
                                                 "sorted_jobs_kernel 1-D counts",
                      "marginals_1d": n1d, "algorithmic_bytes": ss_bytes,
                      "sort_ms": sort_ms, "count_1d_ms": c1_ms,

@@ -55,7 +55,8 @@ def policy_index(search: int, d: int, K: int, length: int) -> int:
 
 
 PHASES = ("upload", "prepare", "sort", "knn", "counts", "combine", "total",
-          "knn_tile", "knn_defer", "count_tile", "count_defer", "sort_radix", "count_1d")
+          "knn_tile", "knn_defer", "count_tile", "count_defer", "sort_radix", "count_1d",
+          "sort_passes")
 
 
 class EgbColumn(ctypes.Structure):

@@ -57,8 +57,8 @@ constexpr int KIND_KNN_ONLY = 100;    // egb_knn_eps
 constexpr int KIND_COUNT_ONLY = 101;  // egb_ball_count
 constexpr int SLAB_MIN = 4096;        // shorter multi-D segments use brute force
 constexpr int NPHASE = 7;
-constexpr int NKTIME = 6;   // kNN tile, kNN deferred, count tile, count deferred,
-                            // radix sort, 1-D counts
+constexpr int NKTIME = 7;   // kNN tile, kNN deferred, count tile, count deferred,
+                            // radix sort, 1-D counts, the sort's digit passes
 constexpr int NSTATS = 14;
 // finish_batch: the batch must run again with the full sort (not a public code)
 constexpr int RC_SORT_RETRY = 1;
@@ -147,10 +147,12 @@ struct egb_ctx {
   int num_sms = 1;
   cudaStream_t own_stream = nullptr;
   cudaStream_t stream = nullptr;
-  // second stream of a batch: the rank-space matrices build on it while the
-  // grid layouts and the kNN run on `stream` (fork / join events)
+  // second stream of a batch, with fork / join events: [0] the rank-space
+  // matrices build there beside the grid layouts, [1] kNN groups after the
+  // first run there beside it, [2] the 1-D counts run there beside the
+  // rank-space and multi-D counts
   cudaStream_t side_stream = nullptr;
-  cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
+  cudaEvent_t fork_ev[3] = {}, join_ev[3] = {};
   std::string err;
   void* arena = nullptr;
   size_t arena_cap = 0;
@@ -1547,7 +1549,7 @@ int run_batch_sorted(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags,
   if (timing) EGB_CUDA(cudaEventRecord(ctx->kev[8], st));
   launch_sort(tasks_d, (const SortSeg*)dtab(tab_segs), (const int32_t*)dtab(tab_blkseg), nblk_sort,
               (int)segs.size(), keys, (uint64_t*)(A + off_keys_b), vals, (int32_t*)(A + off_vals_b),
-              A + off_sweep, sort_first, err_d, st);
+              A + off_sweep, sort_first, err_d, st, timing ? ctx->kev + 12 : nullptr);
   const KeyIndex kx{keys, (const float*)(A + off_fk), (const uint64_t*)(A + off_s1),
                     (const uint64_t*)(A + off_s2), (const float*)(A + off_fs1),
                     (const float*)(A + off_fs2)};
@@ -1556,11 +1558,11 @@ int run_batch_sorted(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags,
   // side stream, joined back before their counts
   const bool fork_wm = !wbuild.empty();
   if (fork_wm) {
-    EGB_CUDA(cudaEventRecord(ctx->fork_ev, st));
-    EGB_CUDA(cudaStreamWaitEvent(ctx->side_stream, ctx->fork_ev, 0));
+    EGB_CUDA(cudaEventRecord(ctx->fork_ev[0], st));
+    EGB_CUDA(cudaStreamWaitEvent(ctx->side_stream, ctx->fork_ev[0], 0));
     launch_wm_build((const WmJob*)dtab(tab_wbuild), (int)wbuild.size(), wm_tiles, wm_levels, vals,
                     ctx->side_stream);
-    EGB_CUDA(cudaEventRecord(ctx->join_ev, ctx->side_stream));
+    EGB_CUDA(cudaEventRecord(ctx->join_ev[0], ctx->side_stream));
   }
   if (timing) EGB_CUDA(cudaEventRecord(ctx->kev[9], st));
   launch_materialize(tasks_d, (const JobDev*)dtab(tab_jobs), (int)jobs.size(), vals,
@@ -1602,25 +1604,41 @@ int run_batch_sorted(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags,
   launch_sorted_jobs(tasks_d, (const SortedJob*)dtab(tab_sjk), (int)sj_knn.size(), blk_knn, kx, vals,
                      st);
   if (timing) EGB_CUDA(cudaEventRecord(ctx->kev[0], st));
+  // kNN groups after the first run on the side stream: each persistent
+  // launch fills the GPU, so the next one starts in the previous one's tail
+  // (a timed batch keeps them in line)
+  int knn_groups = 0;
+  for (const Group& G : groups) knn_groups += (G.is_knn && G.nitems > 0) ? 1 : 0;
+  const bool fork_knn = !timing && knn_groups > 1;
+  if (fork_knn) {
+    EGB_CUDA(cudaEventRecord(ctx->fork_ev[1], st));
+    EGB_CUDA(cudaStreamWaitEvent(ctx->side_stream, ctx->fork_ev[1], 0));
+  }
+  int knn_seen = 0;
   for (size_t g = 0; g < groups.size(); ++g) {
     Group& G = groups[g];
     if (!G.is_knn || G.nitems == 0) continue;
+    cudaStream_t gs = (fork_knn && knn_seen++ > 0) ? ctx->side_stream : st;
     if (G.sel)
       launch_knn_select((const JobDev*)dtab(tab_jobs), items_of(G),
-                        (int)G.nitems, err_d, ctx->num_sms, st);
+                        (int)G.nitems, err_d, ctx->num_sms, gs);
     else if (G.mode == 3)
       launch_knn_wgrid((const JobDev*)dtab(tab_jobs), items_of(G),
                        (int)G.nitems, G.kclass, G.dclass, plain, G.dmax, counters + 2 * g,
-                       ctx->num_sms, st);
+                       ctx->num_sms, gs);
     else if (G.mode == 2)
       launch_knn_grid((const JobDev*)dtab(tab_jobs), items_of(G),
                       (int)G.nitems, G.kclass, G.dclass, plain, G.dmax, counters + 2 * g,
-                      err_d, (DeferEntry*)(A + G.off_defer), counters + 2 * g + 1, ctx->num_sms, st);
+                      err_d, (DeferEntry*)(A + G.off_defer), counters + 2 * g + 1, ctx->num_sms, gs);
     else
       launch_knn_tile((const JobDev*)dtab(tab_jobs), items_of(G),
                       (int)G.nitems, G.kclass, G.dclass, plain, G.slab, G.dmax,
                       counters + 2 * g, err_d, (DeferEntry*)(A + G.off_defer),
-                      counters + 2 * g + 1, ctx->num_sms, st);
+                      counters + 2 * g + 1, ctx->num_sms, gs);
+  }
+  if (fork_knn) {
+    EGB_CUDA(cudaEventRecord(ctx->join_ev[1], ctx->side_stream));
+    EGB_CUDA(cudaStreamWaitEvent(st, ctx->join_ev[1], 0));
   }
   if (timing) EGB_CUDA(cudaEventRecord(ctx->kev[1], st));
   if (timing) EGB_CUDA(cudaEventRecord(ctx->kev[2], st));
@@ -1636,13 +1654,21 @@ int run_batch_sorted(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags,
 
   launch_radius(tasks_d, ntasks, max_ld, st);
   if (timing) EGB_CUDA(cudaEventRecord(ctx->kev[10], st));
+  // the 1-D counts overlap the rank-space and multi-D counts on the side
+  // stream (a timed batch keeps them in line, for their own event times)
+  const bool fork_1d = !timing && !sj_cnt.empty() && (!wjobs.empty() || !groups.empty());
+  if (fork_1d) {
+    EGB_CUDA(cudaEventRecord(ctx->fork_ev[2], st));
+    EGB_CUDA(cudaStreamWaitEvent(ctx->side_stream, ctx->fork_ev[2], 0));
+  }
   launch_sorted_jobs(tasks_d, (const SortedJob*)dtab(tab_sjc), (int)sj_cnt.size(), blk_cnt, kx, vals,
-                     st);
+                     fork_1d ? ctx->side_stream : st);
+  if (fork_1d) EGB_CUDA(cudaEventRecord(ctx->join_ev[2], ctx->side_stream));
   if (timing) EGB_CUDA(cudaEventRecord(ctx->kev[11], st));
   if (timing) EGB_CUDA(cudaEventRecord(ctx->kev[4], st));
   launch_groups(tasks_d, (const GroupJob*)dtab(tab_gbjobs), (int)gbjobs.size(), gb_blocks, err_d, st);
   launch_level_checks((const LevelCheck*)dtab(tab_lchecks), (int)lchecks.size(), lcheck_max_n, st);
-  if (fork_wm) EGB_CUDA(cudaStreamWaitEvent(st, ctx->join_ev, 0));
+  if (fork_wm) EGB_CUDA(cudaStreamWaitEvent(st, ctx->join_ev[0], 0));
   launch_wm_count(tasks_d, (const WmJob*)dtab(tab_wjobs), (int)wjobs.size(), wm_qblocks, kx, vals, st);
   for (size_t g = 0; g < groups.size(); ++g) {
     Group& G = groups[g];
@@ -1677,6 +1703,7 @@ int run_batch_sorted(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags,
                        counters + 2 * g + 1, (int)G.defer_cap, G.dclass, plain, ctx->num_sms, st);
   }
   if (timing) EGB_CUDA(cudaEventRecord(ctx->kev[7], st));
+  if (fork_1d) EGB_CUDA(cudaStreamWaitEvent(st, ctx->join_ev[2], 0));
   if (timing) EGB_CUDA(cudaEventRecord(ctx->ev[5], st));
 
   launch_combine(tasks_d, (const CombineJob*)dtab(tab_cjobs), (const int32_t*)dtab(tab_chunkjob),
@@ -1794,6 +1821,22 @@ int run_batch(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags, egb_re
   return run_batch_sorted(ctx, tasks, ntasks, flags & ~EGB_GRAPH, results, count_radius, 0);
 }
 
+bool create_fork_events(egb_ctx* ctx) {
+  for (int i = 0; i < 3; ++i)
+    if (cudaEventCreateWithFlags(&ctx->fork_ev[i], cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->join_ev[i], cudaEventDisableTiming) != cudaSuccess)
+      return false;
+  return true;
+}
+
+void destroy_fork_events(egb_ctx* ctx) {
+  for (int i = 0; i < 3; ++i) {
+    if (ctx->fork_ev[i]) cudaEventDestroy(ctx->fork_ev[i]);
+    if (ctx->join_ev[i]) cudaEventDestroy(ctx->join_ev[i]);
+    ctx->fork_ev[i] = ctx->join_ev[i] = nullptr;
+  }
+}
+
 }  // namespace
 
 extern "C" {
@@ -1806,10 +1849,9 @@ int egb_create(int device, egb_ctx** out) {
   if (cudaSetDevice(device) != cudaSuccess ||
       cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaStreamCreateWithFlags(&ctx->side_stream, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaEventCreateWithFlags(&ctx->fork_ev, cudaEventDisableTiming) != cudaSuccess ||
-      cudaEventCreateWithFlags(&ctx->join_ev, cudaEventDisableTiming) != cudaSuccess) {
+      !create_fork_events(ctx)) {
     cudaGetLastError();
-    if (ctx->fork_ev) cudaEventDestroy(ctx->fork_ev);
+    destroy_fork_events(ctx);
     if (ctx->side_stream) cudaStreamDestroy(ctx->side_stream);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
     delete ctx;
@@ -1842,8 +1884,7 @@ void egb_destroy(egb_ctx* ctx) {
     if (e) cudaEventDestroy(e);
   for (auto& e : ctx->kev)
     if (e) cudaEventDestroy(e);
-  if (ctx->fork_ev) cudaEventDestroy(ctx->fork_ev);
-  if (ctx->join_ev) cudaEventDestroy(ctx->join_ev);
+  destroy_fork_events(ctx);
   if (ctx->side_stream) cudaStreamDestroy(ctx->side_stream);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
   delete ctx;

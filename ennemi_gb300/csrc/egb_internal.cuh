@@ -497,7 +497,8 @@ size_t sort_scan_tmp_elems(int nblk);
 size_t sort_sweep_bytes(int nblk, int nseg);
 void launch_sort(const TaskDev* tasks_d, const SortSeg* segs_d, const int32_t* blk_seg_d,
                  int nblk, int nseg, uint64_t* keys_a, uint64_t* keys_b, int32_t* vals_a,
-                 int32_t* vals_b, void* sweep, int first, uint32_t* err, cudaStream_t st);
+                 int32_t* vals_b, void* sweep, int first, uint32_t* err, cudaStream_t st,
+                 cudaEvent_t* pass_events = nullptr);  // recorded around the passes alone
 constexpr int SORTED_BLOCK = 256;
 void launch_sorted_jobs(const TaskDev* tasks_d, const SortedJob* jobs_d, int njobs,
                         int total_blocks, const KeyIndex& kx, const int32_t* perm, cudaStream_t st);

@@ -670,7 +670,8 @@ size_t sort_sweep_bytes(int nblk, int nseg) {
 
 void launch_sort(const TaskDev* tasks_d, const SortSeg* segs_d, const int32_t* blk_seg_d,
                  int nblk, int nseg, uint64_t* keys_a, uint64_t* keys_b, int32_t* vals_a,
-                 int32_t* vals_b, void* sweep, int first, uint32_t* err, cudaStream_t st) {
+                 int32_t* vals_b, void* sweep, int first, uint32_t* err, cudaStream_t st,
+                 cudaEvent_t* pass_events) {
   if (nblk <= 0) return;
   // sweep (zeroed by the caller): flag words, segment digit totals, tile counters
   unsigned long long* flags = (unsigned long long*)sweep;
@@ -683,6 +684,7 @@ void launch_sort(const TaskDev* tasks_d, const SortSeg* segs_d, const int32_t* b
   uint64_t* kout = keys_b;
   int32_t* vin = vals_a;
   int32_t* vout = vals_b;
+  if (pass_events) cudaEventRecord(pass_events[0], st);
   for (int pass = first; pass < OS_PASSES; ++pass) {
     onesweep_pass_kernel<<<nblk, SORT_THREADS, 0, st>>>(segs_d, blk_seg_d, kin, vin, kout, vout,
                                                        pass, seg_hist, flags, counters + pass, err);
@@ -690,6 +692,7 @@ void launch_sort(const TaskDev* tasks_d, const SortSeg* segs_d, const int32_t* b
     uint64_t* tk = kin; kin = kout; kout = tk;
     int32_t* tv = vin; vin = vout; vout = tv;
   }
+  if (pass_events) cudaEventRecord(pass_events[1], st);
   // an even number of passes: the sorted keys and values are back in
   // keys_a / vals_a
   if (first > 0) {

@@ -220,8 +220,9 @@ int egb_ball_count(egb_ctx* ctx, const double* points, int64_t n, int32_t d,
  * [5] combine+download, [6] whole batch; then the multi-D kernels alone:
  * [7] kNN tile kernels, [8] kNN deferred-query kernels, [9] count tile
  * kernels, [10] count deferred-query kernels; then [11] the radix sort of
- * the batch's columns (part of [2]) and [12] the 1-D counts on the sorted
- * columns (part of [4]).  Returns the number written.
+ * the batch's columns (part of [2]), [12] the 1-D counts on the sorted
+ * columns (part of [4]) and [13] the sort's digit passes alone (part of
+ * [11]).  Returns the number written.
  */
 int egb_timings(const egb_ctx* ctx, double* ms, int32_t max);
 
