@@ -942,6 +942,22 @@ int run_batch_sorted(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags,
   int wm_tiles = 0, wm_qblocks = 0, wm_levels = 0;
   size_t wmz_bytes = 0;
   std::vector<size_t> wm_tc_off;  // per build: offset of its sums in the zeroed block
+  // The b ball of a rank-space count is the ball of the task's 1-D count
+  // over the same sorted segment, when it has one (the condition z of a
+  // conditional MI: nz, n_xz and n_yz share it): that count keeps it, by
+  // working index, and the rank-space counts read it instead of searching.
+  std::vector<size_t> sj_ranges(sj_cnt.size(), 0);  // arena offset per 1-D count job, 0 = none
+  auto b_ranges_of = [&](const WmPlan& w) -> const int2* {
+    for (size_t k = 0; k < sorted_cnt.size(); ++k) {
+      const Space& c = sorted_cnt[k].second;
+      if (sorted_cnt[k].first != w.seg_b || c.task != w.s.task || c.b != w.s.b || c.e != w.s.e)
+        continue;
+      if (!sj_ranges[k])
+        sj_ranges[k] = dl.take(sizeof(int2) * (size_t)P[(size_t)w.s.task].ld);
+      return (const int2*)(uintptr_t)sj_ranges[k];  // an offset until the arena is known
+    }
+    return nullptr;
+  };
   for (const WmPlan& w : wplans) {
     const auto bkey = std::make_pair(w.seg_a, w.seg_b);
     auto bit = build_of.find(bkey);
@@ -949,6 +965,7 @@ int run_batch_sorted(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags,
       WmJob Q = wbuild[bit->second];
       Q.task = w.s.task;
       Q.slot = w.s.slot;
+      Q.brange = b_ranges_of(w);
       Q.qblk0 = wm_qblocks;
       wm_qblocks += (int)((Q.len + WM_QBLOCK - 1) / WM_QBLOCK);
       wjobs.push_back(Q);
@@ -958,6 +975,7 @@ int run_batch_sorted(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags,
     const int64_t len = w.s.e - w.s.b;
     J.task = w.s.task;
     J.slot = w.s.slot;
+    J.brange = b_ranges_of(w);
     J.len = (int32_t)len;
     int D = 1;
     while (((int64_t)1 << (2 * D)) <= len) ++D;   // 4^D > len
@@ -1375,6 +1393,8 @@ int run_batch_sorted(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags,
   if (!grid_jobs.empty())
     std::memcpy(H + tab_gridjobs, grid_jobs.data(), sizeof(int32_t) * grid_jobs.size());
   if (!sj_knn.empty()) std::memcpy(H + tab_sjk, sj_knn.data(), sizeof(SortedJob) * sj_knn.size());
+  for (size_t k = 0; k < sj_cnt.size(); ++k)
+    sj_cnt[k].ranges = sj_ranges[k] ? (int2*)(A + sj_ranges[k]) : nullptr;
   if (!sj_cnt.empty()) std::memcpy(H + tab_sjc, sj_cnt.data(), sizeof(SortedJob) * sj_cnt.size());
   for (size_t j = 0; j < jobs.size(); ++j) {
     JobDev J = jobs[j];
@@ -1438,6 +1458,7 @@ int run_batch_sorted(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags,
       J.seq0 = (int32_t*)(A + (uintptr_t)J.seq0);
       J.seq1 = (int32_t*)(A + (uintptr_t)J.seq1);
       J.inv_b = (int32_t*)(A + (uintptr_t)J.inv_b);
+      if (J.brange) J.brange = (const int2*)(A + (uintptr_t)J.brange);
       J.tcount = (uint32_t*)(A + off_wmz + wm_tc_off[bi]);
       J.scount = J.tcount + 4 * (size_t)J.D * (size_t)J.ntiles;
       return J;
@@ -1656,7 +1677,9 @@ int run_batch_sorted(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags,
   if (timing) EGB_CUDA(cudaEventRecord(ctx->kev[10], st));
   // the 1-D counts overlap the rank-space and multi-D counts on the side
   // stream (a timed batch keeps them in line, for their own event times)
-  const bool fork_1d = !timing && !sj_cnt.empty() && (!wjobs.empty() || !groups.empty());
+  bool wm_reads_1d = false;  // rank-space counts that read the 1-D counts' balls
+  for (const WmJob& J : wjobs) wm_reads_1d |= J.brange != nullptr;
+  const bool fork_1d = !timing && !wm_reads_1d && !sj_cnt.empty() && (!wjobs.empty() || !groups.empty());
   if (fork_1d) {
     EGB_CUDA(cudaEventRecord(ctx->fork_ev[2], st));
     EGB_CUDA(cudaStreamWaitEvent(ctx->side_stream, ctx->fork_ev[2], 0));

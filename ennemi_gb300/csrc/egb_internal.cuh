@@ -353,6 +353,9 @@ struct SortedJob {
   int64_t s2_base;
   int32_t len;            // its length
   int32_t blk0;           // first block of this job in the launch
+  int2* ranges;           // count jobs: [lo, hi) of each query's ball in the
+                          // segment, by working index (null: not kept), for
+                          // the rank-space counts whose b order it is
 };
 
 struct SortSeg {          // one segment of the batched radix sort
@@ -593,6 +596,9 @@ struct WmJob {
   int32_t tile0;          // first block of the job in the level launches
   int32_t qblk0;          // first block of the job in the count launch
   int32_t seg_begin;      // first working index of the space
+  const int2* brange;     // the b order's ball of each query, by working
+                          // index, kept by the task's 1-D count of that
+                          // column (null: searched here)
 };
 // Build (after the batch sort): inverse b order, the level-0 sequence, then
 // one launch per level for every job at once (max_levels launches).

@@ -489,6 +489,7 @@ __global__ void sorted_jobs_kernel(const TaskDev* __restrict__ tasks,
     int lo, hi;
     ball_positions(seg_view(kx, jb.base, jb.s1_base, jb.s2_base, (int)len), q, r, (int)p, lo, hi);
     count = (int32_t)(hi - lo);
+    if (jb.ranges) jb.ranges[i] = make_int2(lo, hi);
   }
   t.cnt[jb.slot][i] = count;
 }

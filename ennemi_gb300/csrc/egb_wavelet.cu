@@ -373,11 +373,17 @@ wm_count_kernel(const TaskDev* __restrict__ tasks, const WmJob* __restrict__ job
     count = len;
   } else {
     const SegView va = seg_view(kx, J.base_a, J.s1_a, J.s2_a, len);
-    const SegView vb = seg_view(kx, J.base_b, J.s1_b, J.s2_b, len);
-    const int jb = min(max(J.inv_b[w - J.seg_begin], 0), len - 1);
     int alo, ahi, blo, bhi;
     ball_positions(va, value_of(va.keys[i]), r, -1, alo, ahi);
-    ball_positions(vb, value_of(__ldg(vb.keys + jb)), r, -1, blo, bhi);
+    if (J.brange) {  // the b ball, as the 1-D count of column b found it
+      const int2 br = __ldg(J.brange + w);
+      blo = br.x;
+      bhi = br.y;
+    } else {
+      const SegView vb = seg_view(kx, J.base_b, J.s1_b, J.s2_b, len);
+      const int jb = min(max(J.inv_b[w - J.seg_begin], 0), len - 1);
+      ball_positions(vb, value_of(__ldg(vb.keys + jb)), r, -1, blo, bhi);
+    }
     count = wm_rect(J, alo, ahi, blo, bhi);
   }
   t.cnt[J.slot][w] = count;
