@@ -178,7 +178,7 @@ class Context:
         names = ("knn_tile_pairs", "knn_defer_pairs", "knn_deferred",
                  "count_tile_pairs", "count_defer_pairs", "count_deferred",
                  "knn_tile_ops", "count_tile_ops", "kernel_launches", "sort_keys", "sort_segments",
-                 "planned", "graph", "sort_passes")
+                 "planned", "graph", "sort_passes", "plan_us", "issue_us")
         buf = (ctypes.c_int64 * len(names))()
         n = self.lib.egb_last_stats(self.h, buf, len(names))
         return {names[i]: int(buf[i]) for i in range(n)}

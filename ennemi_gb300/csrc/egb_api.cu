@@ -30,6 +30,7 @@
 #include <algorithm>
 #include <array>
 #include <atomic>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -59,7 +60,7 @@ constexpr int SLAB_MIN = 4096;        // shorter multi-D segments use brute forc
 constexpr int NPHASE = 7;
 constexpr int NKTIME = 7;   // kNN tile, kNN deferred, count tile, count deferred,
                             // radix sort, 1-D counts, the sort's digit passes
-constexpr int NSTATS = 14;
+constexpr int NSTATS = 16;
 // finish_batch: the batch must run again with the full sort (not a public code)
 constexpr int RC_SORT_RETRY = 1;
 
@@ -409,6 +410,11 @@ int run_batch_sorted(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags,
   if (!ctx) return EGB_ERR_ARG;
   if (ntasks < 0 || (ntasks > 0 && !tasks)) return fail(ctx, EGB_ERR_ARG, "invalid task list");
   if (ntasks == 0) return EGB_OK;
+  using clk = std::chrono::steady_clock;
+  const clk::time_point t_entry = clk::now();
+  auto us_since = [](clk::time_point t) {
+    return (int64_t)std::chrono::duration_cast<std::chrono::microseconds>(clk::now() - t).count();
+  };
   const bool dev_in = (flags & EGB_INPUT_DEVICE) != 0;
   const int plain = (flags & EGB_PLAIN_FP64) ? 1 : 0;
   const bool force_brute = (flags & EGB_FORCE_BRUTE) != 0;
@@ -1739,6 +1745,8 @@ int run_batch_sorted(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags,
   return EGB_OK;
   };
 
+  const int64_t plan_us = us_since(t_entry);
+  const clk::time_point t_issue = clk::now();
   const bool use_graph = (flags & EGB_GRAPH) != 0 && !timing && !inject;
   if (use_graph) {
     // signature of the batch: the descriptor blob (all device pointers,
@@ -1781,6 +1789,7 @@ int run_batch_sorted(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags,
     if (rc_q != EGB_OK) return rc_q;
   }
   if (timing) EGB_CUDA(cudaEventRecord(ctx->ev[6], st));
+  const int64_t issue_us = us_since(t_issue);
   EGB_CUDA(cudaStreamSynchronize(st));
 
   if (timing) {
@@ -1822,6 +1831,8 @@ int run_batch_sorted(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags,
   const int rc_fin = finish_batch(ctx, R, H, launches, results);
   ctx->stats[11] = 1;
   ctx->stats[12] = use_graph ? 1 : 0;
+  ctx->stats[14] = plan_us;
+  ctx->stats[15] = issue_us;
   if (rc_fin != EGB_OK) return rc_fin;
   if (flags & EGB_KEEP_INTERNALS) {
     ctx->keep = std::move(R.P);

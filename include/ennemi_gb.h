@@ -240,7 +240,9 @@ int egb_last_transfer(const egb_ctx* ctx, int64_t* h2d_bytes, int64_t* d2h_bytes
  * its device work ran as a CUDA graph, [13] the sort's 8-bit digit passes
  * (6: the high 48 bits of the keys, then a repair of the runs tied there; 8:
  * the batch ran again with the full sort because such a run was too long to
- * repair).  Returns the number written. */
+ * repair), [14] microseconds of host planning before the first launch and
+ * [15] of issuing the launches (or the graph) of a planned batch (0 for a
+ * replay without planning).  Returns the number written. */
 int egb_last_stats(const egb_ctx* ctx, int64_t* out, int32_t max);
 
 /*
