@@ -134,6 +134,8 @@ def load():
         lib.egb_normalize.restype = ctypes.c_int
         lib.egb_debug_inject_device_error.argtypes = [vp, ctypes.c_uint32]
         lib.egb_debug_inject_device_error.restype = ctypes.c_int
+        lib.egb_debug_divide.argtypes = [vp, vp, vp, ctypes.c_int64, vp]
+        lib.egb_debug_divide.restype = ctypes.c_int
         lib.egb_version.argtypes = []
         lib.egb_version.restype = ctypes.c_char_p
         _lib = lib
@@ -215,6 +217,17 @@ class Context:
         with self.lock:
             self.check(self.lib.egb_debug_inject_device_error(self.h, int(word)),
                        "egb_debug_inject_device_error")
+
+    def debug_divide(self, a: np.ndarray, b: np.ndarray) -> np.ndarray:
+        """Test hook: a / b through the device division of the rescale
+        (egb_debug_divide)."""
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        out = np.empty_like(a)
+        with self.lock:
+            self.check(self.lib.egb_debug_divide(self.h, a.ctypes.data, b.ctypes.data, a.size,
+                                                 out.ctypes.data), "egb_debug_divide")
+        return out
 
     def get_policy(self) -> np.ndarray:
         m = np.empty(POLICY_ENTRIES, dtype=np.int8)

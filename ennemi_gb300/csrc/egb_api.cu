@@ -733,14 +733,16 @@ int run_batch_sorted(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags,
   // caller data ranges (host input), deduplicated by address range.  Where
   // the device reads pageable host memory directly, the gather kernel reads a
   // range in place when every column in it is contiguous and read in order
-  // (one pass over the link, no staging copy); strided columns (re-read once
-  // per column) and class-permuted ones (scattered reads) are staged in the
+  // and the columns together read it about once (one pass over the link, no
+  // staging copy); strided columns (re-read once per column), class-permuted
+  // ones (scattered reads) and ranges that several columns read (the lagged
+  // views of one series, a column shared by many pairs) are staged in the
   // arena with one copy per range.
-  struct Range { uintptr_t lo, hi; size_t dev_off; bool stage; };
+  struct Range { uintptr_t lo, hi; size_t dev_off; bool stage; uint64_t used; };
   std::vector<Range> ranges;
   const bool direct_ok = !dev_in && ctx->host_direct && !(flags & EGB_STAGE_HOST);
   if (!dev_in) {
-    struct Span { uintptr_t lo, hi; bool stage; };
+    struct Span { uintptr_t lo, hi; bool stage; uint64_t used; };
     std::vector<Span> rs;
     for (int t = 0; t < ntasks; ++t)
       for (int c = 0; c < P[(size_t)t].ncol; ++c) {
@@ -748,7 +750,8 @@ int run_batch_sorted(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags,
         const uintptr_t lo = (uintptr_t)col.data;
         const uintptr_t hi =
             lo + (uintptr_t)(((P[(size_t)t].src_len - 1) * col.stride + 1) * sizeof(double));
-        rs.push_back({lo, hi, !direct_ok || col.stride != 1 || !P[(size_t)t].perm.empty()});
+        rs.push_back({lo, hi, !direct_ok || col.stride != 1 || !P[(size_t)t].perm.empty(),
+                      (uint64_t)(P[(size_t)t].n * (int64_t)sizeof(double))});
       }
     std::sort(rs.begin(), rs.end(), [](const Span& a, const Span& b) {
       return a.lo < b.lo || (a.lo == b.lo && a.hi < b.hi);
@@ -757,11 +760,13 @@ int run_batch_sorted(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags,
       if (!ranges.empty() && r.lo <= ranges.back().hi) {
         ranges.back().hi = std::max(ranges.back().hi, r.hi);
         ranges.back().stage = ranges.back().stage || r.stage;
+        ranges.back().used += r.used;
       } else {
-        ranges.push_back({r.lo, r.hi, 0, r.stage});
+        ranges.push_back({r.lo, r.hi, 0, r.stage, r.used});
       }
     }
     for (auto& r : ranges) {
+      if (2 * r.used > 3 * (uint64_t)(r.hi - r.lo)) r.stage = true;  // read 1.5 times or more
       // keep the element alignment of the source within the 256-byte block
       const size_t mis = r.lo & 255u;
       if (r.stage) r.dev_off = dl.take(r.hi - r.lo + mis) + mis;
@@ -1565,7 +1570,7 @@ int run_batch_sorted(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags,
                    (const RescaleCol*)dtab(tab_rcols), (int)rcols.size(),
                    (const PwTree*)dtab(tab_pwtrees), (const int2*)dtab(tab_pwnodes),
                    (const int32_t*)dtab(tab_pwlevels), (double*)(A + off_pw_scratch),
-                   (double2*)(A + off_pw_ms), ctx->noise_d, zero_d, st);
+                   (double2*)(A + off_pw_ms), ctx->noise_d, zero_d, max_n, st);
   launch_prepare(tasks_d, (const int32_t*)dtab(tab_coltask), (const int32_t*)dtab(tab_colidx),
                  ncols_total, max_n, (unsigned long long*)(A + off_minmax), (double*)(A + off_centers),
                  st);
@@ -2139,6 +2144,27 @@ int egb_normalize(egb_ctx* ctx, const double* mi, int64_t n, int32_t flags, doub
   launch_normalize(in_d, n, out_d, st);
   EGB_CUDA(cudaGetLastError());
   if (!dev) EGB_CUDA(cudaMemcpyAsync(out, out_d, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost, st));
+  EGB_CUDA(cudaStreamSynchronize(st));
+  return EGB_OK;
+}
+
+int egb_debug_divide(egb_ctx* ctx, const double* a, const double* b, int64_t n, double* out) {
+  if (!ctx) return EGB_ERR_ARG;
+  if (n < 0 || (n > 0 && (!a || !b || !out))) return fail(ctx, EGB_ERR_ARG, "egb_debug_divide: invalid arguments");
+  if (n == 0) return EGB_OK;
+  cudaSetDevice(ctx->device);
+  cudaStream_t st = ctx->stream;
+  const size_t part = align_up(sizeof(double) * (size_t)n, 256);
+  const int rc = ensure_aux(ctx, 3 * part);
+  if (rc) return rc;
+  double* a_d = (double*)ctx->aux;
+  double* b_d = (double*)((char*)ctx->aux + part);
+  double* o_d = (double*)((char*)ctx->aux + 2 * part);
+  EGB_CUDA(cudaMemcpyAsync(a_d, a, sizeof(double) * (size_t)n, cudaMemcpyHostToDevice, st));
+  EGB_CUDA(cudaMemcpyAsync(b_d, b, sizeof(double) * (size_t)n, cudaMemcpyHostToDevice, st));
+  launch_divide(a_d, b_d, n, o_d, st);
+  EGB_CUDA(cudaGetLastError());
+  EGB_CUDA(cudaMemcpyAsync(out, o_d, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost, st));
   EGB_CUDA(cudaStreamSynchronize(st));
   return EGB_OK;
 }

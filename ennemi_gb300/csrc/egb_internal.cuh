@@ -410,7 +410,9 @@ constexpr uint32_t RESCALE_CONSTANT = 1u << 31;
 void launch_rescale(const TaskDev* tasks_d, const RescaleStat* stats_d, int nstats,
                     const RescaleCol* cols_d, int ncols, const PwTree* trees_d,
                     const int2* nodes_d, const int32_t* levels_d, double* scratch, double2* ms,
-                    const double* noise, uint32_t* zero_flags, cudaStream_t st);
+                    const double* noise, uint32_t* zero_flags, int64_t max_n, cudaStream_t st);
+// egb_debug_divide: the rescale's division (div_rn) over n pairs
+void launch_divide(const double* a_d, const double* b_d, int64_t n, double* out_d, cudaStream_t st);
 
 struct CombineJob {       // per-task reduction of per-sample terms
   int32_t task;

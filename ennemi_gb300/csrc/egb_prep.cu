@@ -164,24 +164,92 @@ rescale_stats_kernel(const TaskDev* __restrict__ tasks, const RescaleStat* __res
   if (threadIdx.x == 0) ms[blockIdx.x] = make_double2(mean, sd);
 }
 
+// RN(a / b) without a division per element.  q = RN(a * rb) (rb = RN(1/b))
+// is within two ulps of the quotient; the remainder a - q b from one FMA is
+// exact once q is within one ulp (the remainder of a faithful quotient is
+// representable: Boldo and Daumas, 2003), and the quotient lies above the
+// midpoint between q and its successor exactly when that remainder exceeds
+// half an ulp of q times b -- a power-of-two multiple of b, built by integer
+// exponent arithmetic.  q steps one ulp at a time until the remainder lies
+// between the two midpoints; a remainder equal to one of them is a tie,
+// rounded to the even neighbour.  Magnitudes throughout, the sign applied at
+// the end (round to nearest is symmetric).  Operands outside the exponent
+// range where no step can underflow or overflow take the division itself.
+// One FP64 multiply and one or two FMAs per element, against the FP64 pipe's
+// few operations per clock per SM.
+__device__ __forceinline__ double div_rn(double a, double b, double rb) {
+  const uint64_t ua = (uint64_t)__double_as_longlong(a), ub = (uint64_t)__double_as_longlong(b);
+  const uint64_t sign = (ua ^ ub) & 0x8000000000000000ull;
+  const uint64_t ma = ua & 0x7fffffffffffffffull, mb = ub & 0x7fffffffffffffffull;
+  const int ea = (int)(ma >> 52), eb = (int)(mb >> 52);
+  if (ea < 1023 - 900 || ea > 1023 + 900 || eb < 1023 - 900 || eb > 1023 + 900 ||
+      abs(ea - eb) > 1000)
+    return __ddiv_rn(a, b);
+  const double A = __longlong_as_double((long long)ma), B = __longlong_as_double((long long)mb);
+  const int64_t half_b = (int64_t)mb - ((int64_t)1 << 52);  // bits of B / 2
+  double q = __dmul_rn(A, fabs(rb));
+  for (int it = 0; it < 4; ++it) {
+    const double e = __fma_rn(-q, B, A);  // A - q B
+    const uint64_t uq = (uint64_t)__double_as_longlong(q);
+    const int eq = (int)(uq >> 52);
+    // half an ulp of q above (and below: half that at a power of two) times B
+    const uint64_t h_up = (uint64_t)(half_b + ((int64_t)(eq - 1075) << 52));
+    const uint64_t h_dn = (uq & 0xfffffffffffffull) ? h_up : h_up - (1ull << 52);
+    const uint64_t ue = (uint64_t)__double_as_longlong(e);
+    const uint64_t me = ue & 0x7fffffffffffffffull;
+    const bool neg = (ue >> 63) != 0 && me != 0;
+    if (!neg && me > h_up) { q = __longlong_as_double((long long)(uq + 1)); continue; }
+    if (neg && me > h_dn) { q = __longlong_as_double((long long)(uq - 1)); continue; }
+    if (!neg && me == h_up) q = __longlong_as_double((long long)((uq & 1) ? uq + 1 : uq));
+    else if (neg && me == h_dn) q = __longlong_as_double((long long)((uq & 1) ? uq - 1 : uq));
+    return __longlong_as_double((long long)((uint64_t)__double_as_longlong(q) | sign));
+  }
+  return __ddiv_rn(a, b);  // not settled in four steps (not met in the fast range)
+}
+
+// x = RN(RN(RN(x - mean) / sd) + noise) per sample of a task column (one
+// y-row of blocks per column, four samples in flight per thread)
 __global__ void __launch_bounds__(PREP_THREADS)
 rescale_apply_kernel(const TaskDev* __restrict__ tasks, const RescaleCol* __restrict__ cols,
                      const double2* __restrict__ ms, const double* __restrict__ noise,
                      uint32_t* __restrict__ zero_flags) {
-  const RescaleCol rc = cols[blockIdx.x];
+  const RescaleCol rc = cols[blockIdx.y];
   const TaskDev t = tasks[rc.task];
   double* x = const_cast<double*>(t.x64) + (int64_t)rc.col * t.ld;
   const double2 m = ms[rc.stat];
   const double mean = m.x, sd = m.y;
   if (fabs(sd) < 1e-20) {  // np.abs(std) < 1e-20: the reference warns and keeps x
-    if (threadIdx.x == 0) atomicOr(zero_flags + rc.task, RESCALE_CONSTANT);
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(zero_flags + rc.task, RESCALE_CONSTANT);
     return;
   }
+  const double rsd = __ddiv_rn(1.0, sd);
   const double* nz = noise + rc.noise_pos;
-  for (int i = threadIdx.x; i < t.n; i += blockDim.x) {  // sample i
-    const int w = rc.inv ? rc.inv[i] : i;
-    x[w] = __dadd_rn(__ddiv_rn(__dsub_rn(x[w], mean), sd), nz[(int64_t)i * rc.group]);
+  const int64_t step = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i0 < t.n; i0 += 4 * step) {
+    int w[4];
+    double v[4], z[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {  // sample i0 + u * step
+      const int64_t i = i0 + u * step;
+      w[u] = -1;
+      if (i < t.n) {
+        w[u] = rc.inv ? rc.inv[i] : (int)i;
+        v[u] = x[w[u]];
+        z[u] = nz[i * rc.group];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      if (w[u] >= 0) x[w[u]] = __dadd_rn(div_rn(__dsub_rn(v[u], mean), sd, rsd), z[u]);
   }
+}
+
+// egb_debug_divide: div_rn over n pairs (one thread per pair)
+__global__ void divide_kernel(const double* __restrict__ a, const double* __restrict__ b, int64_t n,
+                              double* __restrict__ out) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = div_rn(a[i], b[i], __ddiv_rn(1.0, b[i]));
 }
 
 __global__ void minmax_kernel(const TaskDev* __restrict__ tasks,
@@ -457,12 +525,19 @@ void launch_gather(const TaskDev* tasks_d, const GatherCol* cols_d, int ncols, i
 void launch_rescale(const TaskDev* tasks_d, const RescaleStat* stats_d, int nstats,
                     const RescaleCol* cols_d, int ncols, const PwTree* trees_d,
                     const int2* nodes_d, const int32_t* levels_d, double* scratch, double2* ms,
-                    const double* noise, uint32_t* zero_flags, cudaStream_t st) {
+                    const double* noise, uint32_t* zero_flags, int64_t max_n, cudaStream_t st) {
   if (ncols <= 0 || nstats <= 0) return;
   rescale_stats_kernel<<<nstats, PREP_THREADS, 0, st>>>(tasks_d, stats_d, trees_d, nodes_d, levels_d,
                                                         scratch, ms);
   count_launch();
-  rescale_apply_kernel<<<ncols, PREP_THREADS, 0, st>>>(tasks_d, cols_d, ms, noise, zero_flags);
+  const dim3 agrid(grid_x_for((max_n + 3) / 4 / 8), grid_y_for(ncols));  // 32 samples a thread
+  rescale_apply_kernel<<<agrid, PREP_THREADS, 0, st>>>(tasks_d, cols_d, ms, noise, zero_flags);
+  count_launch();
+}
+
+void launch_divide(const double* a_d, const double* b_d, int64_t n, double* out_d, cudaStream_t st) {
+  if (n <= 0) return;
+  divide_kernel<<<grid_x_for(n), PREP_THREADS, 0, st>>>(a_d, b_d, n, out_d);
   count_launch();
 }
 

@@ -382,6 +382,11 @@ int egb_last_groups(const egb_ctx* ctx, int32_t task, int64_t* out, int32_t max)
  */
 int egb_debug_inject_device_error(egb_ctx* ctx, uint32_t word);
 
+/* Test hook: out[i] = a[i] / b[i] (host arrays) through the device division
+ * that the rescale of EGB_RESCALE uses in place of one FP64 divide per
+ * sample -- round to nearest even, as IEEE division.  Returns 0. */
+int egb_debug_divide(egb_ctx* ctx, const double* a, const double* b, int64_t n, double* out);
+
 /* Name of the context's CUDA device (cudaDeviceProp::name) into name[0 ..
  * len), NUL-terminated; *sms = its multiprocessor count.  Returns 0. */
 int egb_device_info(const egb_ctx* ctx, char* name, int32_t len, int32_t* sms);

@@ -131,3 +131,37 @@ def test_public_api_same_with_device_and_host_preparation(case, monkeypatch):
     monkeypatch.setattr(_driver, "device_prep", False)
     host = calls[case]()
     assert np.array_equal(dev, host, equal_nan=True)
+
+
+def _division_cases():
+    rng = np.random.default_rng(77)
+    n = 400_000
+    # random mantissas and signs over the exponents of rescaled data and far beyond
+    a = rng.uniform(1, 2, n) * 2.0 ** rng.integers(-60, 60, n) * rng.choice([-1, 1], n)
+    b = rng.uniform(1, 2, n) * 2.0 ** rng.integers(-60, 60, n) * rng.choice([-1, 1], n)
+    # quotients at and beside binade edges and exact multiples
+    k = rng.integers(-8, 9, 50_000)
+    bb = rng.uniform(1, 2, 50_000) * 2.0 ** rng.integers(-30, 30, 50_000)
+    edge_a = bb * (1.0 + k * 2.0 ** -52)
+    edge_a2 = bb * 2.0 ** rng.integers(-5, 5, 50_000)
+    ones = np.full(1000, np.nextafter(2.0, 0.0))                      # all-ones mantissa
+    # the division's own domain: huge, tiny, subnormal, zeros, inf, nan
+    spec = np.array([0.0, -0.0, 1e300, -1e300, 1e-300, 5e-324, -5e-324, np.inf, -np.inf, np.nan,
+                     1.0, -1.0, 3.0, 2.0 ** 1000, 2.0 ** -1000, 1e-20, 1e20])
+    sa, sb = np.meshgrid(spec, spec)
+    return (np.concatenate([a, edge_a, edge_a2, ones * 3.0, ones, sa.ravel()]),
+            np.concatenate([b, bb, bb, ones, ones * 3.0, sb.ravel()]))
+
+
+def test_device_division_is_ieee_division():
+    """The rescale divides by the column's standard deviation without an FP64
+    divide per sample (reciprocal, exact FMA remainder, midpoint test); it
+    must give IEEE division's round-to-nearest-even bits everywhere."""
+    a, b = _division_cases()
+    got = N.context(0).debug_divide(a, b)
+    with np.errstate(all="ignore"):
+        want = a / b
+    bad = np.flatnonzero(got.view(np.uint64) != want.view(np.uint64))
+    nan_both = np.isnan(got[bad]) & np.isnan(want[bad])
+    bad = bad[~nan_both]
+    assert bad.size == 0, list(zip(a[bad[:5]], b[bad[:5]], got[bad[:5]], want[bad[:5]]))
