@@ -222,7 +222,10 @@ rescale_apply_kernel(const TaskDev* __restrict__ tasks, const RescaleCol* __rest
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(zero_flags + rc.task, RESCALE_CONSTANT);
     return;
   }
-  const double rsd = __ddiv_rn(1.0, sd);
+  __shared__ double rsd_s;  // RN(1 / sd), once per block
+  if (threadIdx.x == 0) rsd_s = __ddiv_rn(1.0, sd);
+  __syncthreads();
+  const double rsd = rsd_s;
   const double* nz = noise + rc.noise_pos;
   const int64_t step = (int64_t)gridDim.x * blockDim.x;
   for (int64_t i0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i0 < t.n; i0 += 4 * step) {
@@ -280,10 +283,24 @@ __global__ void minmax_kernel(const TaskDev* __restrict__ tasks,
       lo = a < lo ? a : lo;
       hi = b > hi ? b : hi;
     }
-    if ((threadIdx.x & 31) == 0) {
+    // one pair of atomics per block (per warp they queue up at the column's
+    // two words)
+    __shared__ unsigned long long wlo[PREP_THREADS / 32], whi[PREP_THREADS / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) {
+      wlo[warp] = lo;
+      whi[warp] = hi;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      for (int w = 1; w < PREP_THREADS / 32; ++w) {
+        lo = wlo[w] < lo ? wlo[w] : lo;
+        hi = whi[w] > hi ? whi[w] : hi;
+      }
       atomicMin(&minmax[2 * g], lo);
       atomicMax(&minmax[2 * g + 1], hi);
     }
+    __syncthreads();
   }
 }
 
