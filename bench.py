@@ -282,14 +282,20 @@ def run_config(args, torch, N, ctx, dev):
     import ennemi_gb300 as eg
     from ennemi_gb300 import _driver, synthetic
     from ennemi_gb300 import _entropy_estimators as ee
-    if args.config == "lags":
+    if args.config in ("lags", "lags_nan"):
         y, x, lags, mask = synthetic.lagged_ar(seed=args.seed + 3)
         if args.lags:  # a smaller case of the same workload (first lags only)
             lags = lags[:args.lags]
-        calls = [lambda: eg.estimate_mi(y, x, lag=lags, mask=mask)]
+        if args.config == "lags_nan":  # uneven task lengths: NaN runs, drop_nan=True
+            xn = synthetic.with_nan_runs(x)
+            calls = [lambda: eg.estimate_mi(y, xn, lag=lags, mask=mask, drop_nan=True)]
+        else:
+            calls = [lambda: eg.estimate_mi(y, x, lag=lags, mask=mask)]
         ntask = len(lags) * x.shape[1]
         desc = ("16 coupled AR(1) series, length 200,000, estimate_mi of series 0 vs all at lags "
                 f"0..{len(lags) - 1} with a ~10 % mask in runs of 1-50 (one batch)")
+        if args.config == "lags_nan":
+            desc += "; NaN runs of 1-50 in ~2 % of every x series, drop_nan=True (uneven N)"
     elif args.config == "pairwise":
         data, cond = synthetic.pairwise_mix(seed=args.seed + 4)
         calls = [lambda: eg.pairwise_mi(data), lambda: eg.pairwise_mi(data, cond=cond)]
@@ -392,7 +398,8 @@ def main():
     ap.add_argument("--profile", action="store_true", help="device-resident steps only (ncu)")
     ap.add_argument("--lags", type=int, default=0,
                     help="--config lags: the first LAGS lags only (0: all 49)")
-    ap.add_argument("--config", default="large", choices=["large", "lags", "pairwise", "semidiscrete"],
+    ap.add_argument("--config", default="large",
+                    choices=["large", "lags", "lags_nan", "pairwise", "semidiscrete"],
                     help="large: the headline workload; the others time one public-API call "
                          "of the batched lag / pairwise / semidiscrete workloads")
     args = ap.parse_args()

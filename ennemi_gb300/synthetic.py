@@ -105,6 +105,23 @@ def lagged_ar(length: int = 200_000, nseries: int = 16, seed: int = 3):
     return x[:, 0].copy(), x, np.arange(49), mask
 
 
+def with_nan_runs(x: np.ndarray, frac: float = 0.02, seed: int = 9) -> np.ndarray:
+    """A copy of x (2-D) with runs of U{1..50} NaNs in every column, about
+    `frac` of each column, at different places per column: with
+    drop_nan=True every task of a lagged estimate_mi keeps its own rows, so
+    the tasks of one call have different lengths."""
+    rng = np.random.default_rng(seed)
+    out = np.array(x, dtype=np.float64, copy=True)
+    n = out.shape[0]
+    for c in range(out.shape[1]):
+        bad = np.zeros(n, dtype=bool)
+        while bad.sum() < int(frac * n):
+            start = int(rng.integers(0, n))
+            bad[start:start + int(rng.integers(1, 51))] = True
+        out[bad, c] = np.nan
+    return out
+
+
 def _random_corr(k: int, rng) -> np.ndarray:
     a = rng.normal(size=(k, k + 2))
     c = a @ a.T

@@ -70,6 +70,26 @@ def test_lagged_batch_vs_oracle(oracle, monkeypatch):
     assert cond.shape == (len(lags), 3)
 
 
+def test_lagged_batch_nan_runs_full_size(monkeypatch):
+    """The lag workload with NaN runs in every x series and drop_nan=True:
+    each task keeps its own rows, so the 784 tasks of the batch have
+    different lengths."""
+    y, x, lags, mask = synthetic.lagged_ar()
+    xn = synthetic.with_nan_runs(x)
+    res = _variants(monkeypatch, lambda: eg.estimate_mi(y, xn, lag=lags, mask=mask, drop_nan=True))
+    assert res.shape == (49, 16) and np.all(np.isfinite(res))
+    assert np.argmax(res[:, 0]) == 0
+
+
+def test_lagged_batch_nan_runs_vs_oracle(oracle, monkeypatch):
+    y, x, _, mask = synthetic.lagged_ar(length=1500, nseries=4, seed=8)
+    xn = synthetic.with_nan_runs(x, frac=0.05)
+    lags = np.arange(0, 49, 6)
+    res = _gpu_and_oracle(oracle, monkeypatch,
+                          lambda: eg.estimate_mi(y, xn, lag=lags, mask=mask, drop_nan=True))
+    assert res.shape == (len(lags), 4) and np.all(np.isfinite(res))
+
+
 # --------------------------------------------------------- batched pairwise --
 
 def test_pairwise_full_size(monkeypatch):
