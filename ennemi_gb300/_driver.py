@@ -350,7 +350,7 @@ def _estimate_mi(y: FloatArray, x: FloatArray, lag: FloatArray, k: int,
                               cond, cond_lag[li], discrete_x, discrete_y, preprocess, drop_nan,
                               share_x=False))
     if _device_prep_ok((x, y) + (() if cond is None else (cond,)), cond, preprocess, drop_nan,
-                       discrete_x or discrete_y):
+                       discrete_x or discrete_y, nan_rows_ok=True):
         lo, hi = min(min_lag, 0), max(max_lag, 0)
         n = len(y) - hi + lo if prep.idx is None else len(prep.idx)
         specs = []
@@ -366,7 +366,11 @@ def _estimate_mi(y: FloatArray, x: FloatArray, lag: FloatArray, k: int,
                     zv = zcols[zkey] = [_native.Col(cond[hi - cond_lag[li][c]:, c])
                                         for c in range(cond.shape[1])]
             specs.append((_native.Col(xv[hi - lag[li]:]), ycol, zv))
-        values = _run_device_prep(specs, n, k, prep.idx, jobs, max_threads)
+        rows = None
+        if drop_nan:
+            rows = _kept_rows(x, y, cond, lag, cond_lag, indices, hi, len(y) - hi + lo, prep.idx,
+                              max_threads)
+        values = _run_device_prep(specs, n, k, prep.idx, jobs, max_threads, rows)
     else:
         batch = _Batch()
         slots = [_add_prepared(batch, p) for p in _prepare_all(jobs, max_threads)]
@@ -591,29 +595,63 @@ def _numpy_sums_pairwise() -> bool:
     return _pairwise_checked
 
 
-def _device_prep_ok(arrays, cond, preprocess: bool, drop_nan: bool, any_discrete: bool) -> bool:
-    if not (device_prep and preprocess) or drop_nan or any_discrete:
+def _device_prep_ok(arrays, cond, preprocess: bool, drop_nan: bool, any_discrete: bool,
+                    nan_rows_ok: bool = False) -> bool:
+    """Whether the call's columns can be prepared on the device: continuous
+    float64 data, preprocessing on; NaNs only where the caller drops their rows
+    (drop_nan) and the call gives every task its own rows (nan_rows_ok: the
+    lagged estimate_mi)."""
+    if not (device_prep and preprocess) or any_discrete or (drop_nan and not nan_rows_ok):
         return False
     for a in arrays:
-        if a.dtype != np.float64 or np.isnan(a).any():
+        if a.dtype != np.float64 or (not drop_nan and np.isnan(a).any()):
             return False
     return _numpy_sums_pairwise()
 
 
-def _run_device_prep(specs, n: int, k: int, idx, jobs, max_threads) -> np.ndarray:
+def _kept_rows(x, y, cond, lag, cond_lag, indices, hi: int, n0: int, idx, max_threads):
+    """Per task of a lagged estimate_mi with drop_nan: the sample index of
+    the rows it keeps -- the masked rows (idx; None: all n0) whose x, y and
+    condition values in the task's lagged views are all numbers, the rows
+    _apply_masks keeps (_driver.py:834-854) -- or None where that is every
+    masked row (such tasks share the call's index)."""
+    base = None if idx is None else np.asarray(idx, dtype=np.int32)
+    cols = lambda a: [a] if a.ndim == 1 else [a[:, c] for c in range(a.shape[1])]
+    fin_x = [~np.isnan(c) for c in cols(x)]
+    fin_y = ~np.isnan(y[hi: hi + n0])
+    fin_z = [] if cond is None else [~np.isnan(c) for c in cols(cond)]
+
+    def one(li, vi):
+        keep = fin_x[vi][hi - lag[li]: hi - lag[li] + n0] & fin_y
+        for c, fz in enumerate(fin_z):
+            keep &= fz[hi - cond_lag[li][c]: hi - cond_lag[li][c] + n0]
+        if base is not None:
+            keep = keep[base]
+        if keep.all():
+            return None
+        return base[keep] if base is not None else np.flatnonzero(keep).astype(np.int32)
+
+    jobs = [lambda li=li, vi=vi: one(li, vi) for li, vi in indices]
+    return _prepare_all(jobs, max_threads)
+
+
+def _run_device_prep(specs, n: int, k: int, idx, jobs, max_threads, rows=None) -> np.ndarray:
     """Estimates of the tasks (x, y, condition columns or None): the columns
     are lagged views of the caller's arrays, sample w at view[idx[w]] (idx
-    None: the first n), rescaled on the device.  Tasks with a constant column
+    None: the first n), rescaled on the device.  rows: per task, its own
+    sample index (drop_nan) or None for idx.  Tasks with a constant column
     are prepared on the host (`jobs`, same order) and run in a second batch."""
-    if n <= k:
-        raise ValueError(K_TOO_LARGE_MSG)
     index = None if idx is None else np.ascontiguousarray(idx, dtype=np.int32)
     tasks = []
-    for xv, yv, zv in specs:
+    for t, (xv, yv, zv) in enumerate(specs):
+        own = None if rows is None else rows[t]
+        tn, tix = (n, index) if own is None else (len(own), own)
+        if tn <= k:  # the first task in order that keeps too few rows raises
+            raise ValueError(K_TOO_LARGE_MSG)
         if zv is None:
-            tasks.append(_native.Task(_native.MI, k, [xv], [yv], n=n, index=index))
+            tasks.append(_native.Task(_native.MI, k, [xv], [yv], n=tn, index=tix))
         else:
-            tasks.append(_native.Task(_native.CMI, k, [xv], [yv], list(zv), n=n, index=index))
+            tasks.append(_native.Task(_native.CMI, k, [xv], [yv], list(zv), n=tn, index=tix))
     res = []
     values = _native.run_tasks(tasks, flags=run_flags | _native.RESCALE, results_out=res,
                                noise=lambda m: _noise.take(0, (m,)))

@@ -225,7 +225,8 @@ def test_shared_preparation_is_bit_identical(monkeypatch, case):
 
 
 @pytest.mark.parametrize("case", ["lags_mask", "lags_nomask", "lags_cond1", "lags_cond2",
-                                  "pairwise", "pairwise_cond_mask", "constant", "nan_elsewhere"])
+                                  "pairwise", "pairwise_cond_mask", "constant", "nan_elsewhere",
+                                  "lags_dropnan", "lags_cond_dropnan", "pairwise_dropnan"])
 def test_device_preprocessing_matches_host_preparation(oracle, monkeypatch, case):
     """The EGB_RESCALE path (lagged views + shared sample index, rescaled in the
     library) gives what the host preparation gives; the library is stood in for
@@ -238,6 +239,10 @@ def test_device_preprocessing_matches_host_preparation(oracle, monkeypatch, case
     mask = rng.random(n) > 0.2
     xn = x.copy()
     xn[-3:, 1] = np.nan                     # after every lagged slice below (lags 5, 6)
+    xd, yd, cd = x.copy(), y.copy(), cond.copy()   # NaN rows dropped per task
+    xd[rng.random((n, 3)) < 0.03] = np.nan
+    yd[rng.random(n) < 0.03] = np.nan
+    cd[rng.random((n, 2)) < 0.03] = np.nan
     calls = {
         "lags_mask": lambda: eg.estimate_mi(y, x, lag=[0, 1, 5, -2], mask=mask),
         "lags_nomask": lambda: eg.estimate_mi(y, x, lag=[0, 2, -3]),
@@ -248,6 +253,10 @@ def test_device_preprocessing_matches_host_preparation(oracle, monkeypatch, case
         "pairwise_cond_mask": lambda: eg.pairwise_mi(x, cond=cond[:, 1], mask=mask),
         "constant": lambda: eg.pairwise_mi(np.column_stack((x[:, :2], np.ones(n)))),
         "nan_elsewhere": lambda: eg.estimate_mi(y, xn, lag=[5, 6]),
+        "lags_dropnan": lambda: eg.estimate_mi(yd, xd, lag=[0, 1, 5, -2], mask=mask, drop_nan=True),
+        "lags_cond_dropnan": lambda: eg.estimate_mi(yd, xd, lag=[0, 2], cond=cd, cond_lag=[[1, 0], [3, 2]],
+                                                    drop_nan=True),
+        "pairwise_dropnan": lambda: eg.pairwise_mi(xd, drop_nan=True),
     }
     flags_seen = []
     run = oracle_run_tasks(oracle)
@@ -269,8 +278,9 @@ def test_device_preprocessing_matches_host_preparation(oracle, monkeypatch, case
         host = calls[case]()
     assert np.array_equal(dev, host, equal_nan=True)
     assert len(w_dev) == len(w_host)
-    # the device path is taken exactly where its conditions hold
-    assert used == (case != "nan_elsewhere")
+    # the device path is taken exactly where its conditions hold (NaNs: only
+    # where the lagged estimate_mi drops their rows per task)
+    assert used == (case not in ("nan_elsewhere", "pairwise_dropnan"))
 
 
 def test_numpy_sums_in_pairwise_order():
@@ -282,7 +292,7 @@ def test_numpy_sums_in_pairwise_order():
 
 
 @pytest.mark.parametrize("case", ["lags_mask", "lags_nomask", "lags_negative", "lags_cond2",
-                                  "pairwise_cond_mask"])
+                                  "pairwise_cond_mask", "lags_mask_dropnan", "lags_cond2_dropnan"])
 def test_device_preprocessing_columns_are_the_reference_slices(monkeypatch, case):
     """Every task of the EGB_RESCALE path reads, through its column views and
     shared sample index, exactly the lagged and masked samples the reference's
@@ -294,6 +304,12 @@ def test_device_preprocessing_columns_are_the_reference_slices(monkeypatch, case
     y = rng.normal(size=n)
     cond = rng.normal(size=(n, 2))
     mask = rng.random(n) > 0.25
+    drop = case.endswith("_dropnan")
+    if drop:  # NaNs in every variable; each task keeps its own rows
+        x[rng.random((n, 3)) < 0.04] = np.nan
+        y[rng.random(n) < 0.04] = np.nan
+        cond[rng.random((n, 2)) < 0.04] = np.nan
+        case = case[:-len("_dropnan")]
     lags = {"lags_mask": [0, 1, 5], "lags_nomask": [0, 2, 7], "lags_negative": [-2, 0, 3],
             "lags_cond2": [0, 4]}
     seen = []
@@ -316,7 +332,7 @@ def test_device_preprocessing_columns_are_the_reference_slices(monkeypatch, case
         c2 = case == "lags_cond2"
         cond_lag = [[1, 0], [3, 2]] if c2 else None
         eg.estimate_mi(y, x, lag=lag, mask=None if case == "lags_nomask" else mask,
-                       cond=cond if c2 else None, cond_lag=cond_lag if c2 else 0)
+                       cond=cond if c2 else None, cond_lag=cond_lag if c2 else 0, drop_nan=drop)
         m = None if case == "lags_nomask" else mask
         lo = min(min(lag), 0 if not c2 else min(min(r) for r in cond_lag))
         hi = max(max(lag), 0 if not c2 else max(max(r) for r in cond_lag))
@@ -327,7 +343,7 @@ def test_device_preprocessing_columns_are_the_reference_slices(monkeypatch, case
                 ys = y[hi: n + lo]
                 zs = (np.column_stack([cond[hi - cond_lag[li][i]: n - cond_lag[li][i] + lo, i]
                                        for i in range(2)]) if c2 else None)
-                xs, ys, zs = _driver._apply_masks(xs, ys, zs, m, lo, hi, False)
+                xs, ys, zs = _driver._apply_masks(xs, ys, zs, m, lo, hi, drop)
                 want.append([xs, ys] + ([zs[:, 0], zs[:, 1]] if c2 else []))
     else:
         eg.pairwise_mi(x, cond=cond, mask=mask)
