@@ -2,14 +2,14 @@
 // 1-D estimator kernels that run on the sorted arrays.
 //
 // Sort.  Every requested (task, column, segment) is one segment of a single
-// concatenated key array (the single-sweep passes below; the three-kernel
-// pass -- histogram, scan, scatter -- serves the strip-key passes of the
-// grid layouts).  Keys are the order-preserving uint64 image of the
-// FP64 value (key_of), the payload is the working index of the point.  Eight
-// stable 8-bit LSD passes; each pass is histogram -> exclusive scan ->
-// stable scatter.  Per-block histograms are laid out segment-major,
-// digit-next, block-minor, so ONE global exclusive scan yields absolute
-// output positions that never leave a segment.
+// concatenated key array.  Keys are the order-preserving uint64 image of the
+// FP64 value (key_of), the payload is the working index of the point.  The
+// batch sort takes stable 8-bit single-sweep LSD passes over the high 48 key
+// bits and repairs the rare runs tied there (below); the three-kernel pass
+// -- histogram, exclusive scan, stable scatter -- serves the strip-key
+// passes of the grid layouts: its per-block histograms are laid out
+// segment-major, digit-next, block-minor, so ONE global exclusive scan
+// yields absolute output positions that never leave a segment.
 //
 // 1-D kNN (entropy of one column, Ross MI with 1-D x): for the point at
 // sorted position p the (k+1)-th smallest |x_j - x_p| (self included) is
@@ -169,9 +169,9 @@ sort_scatter_kernel(const SortSeg* __restrict__ segs, const int32_t* __restrict_
 }
 
 // ------------------------------------------------------- single sweep --
-// The batch sort proper: eight stable 8-bit LSD passes, one launch each,
+// The batch sort proper: stable 8-bit LSD passes, one launch each,
 // after Adinets and Merrill's single-sweep radix sort (Onesweep, 2022).  The
-// load kernel computes the digit totals of all eight passes per segment at
+// load kernel computes the digit totals of all the passes per segment at
 // once; each pass then needs, per tile and digit, only the count of that
 // digit in the segment's earlier tiles.  A tile takes its id from an atomic
 // counter (so every earlier tile of its segment has started), publishes its
