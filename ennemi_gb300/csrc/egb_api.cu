@@ -713,7 +713,7 @@ int run_batch_sorted(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags,
     }
   }
   int64_t sort_total = 0, s1_total = 0, s2_total = 0;
-  int nblk_sort = 0;
+  int nblk_sort = 0, nblk_os = 0;
   for (SortSeg& s : segs) {
     s.out_base = sort_total;
     s.s1_base = s1_total;
@@ -722,8 +722,11 @@ int run_batch_sorted(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags,
     s2_total += samples2_of(s.len);
     s.blk0 = nblk_sort;
     s.nblk = (s.len + SORT_TILE - 1) / SORT_TILE;
+    s.os_blk0 = nblk_os;
+    s.os_nblk = (s.len + OS_TILE - 1) / OS_TILE;
     sort_total += s.len;
     nblk_sort += s.nblk;
+    nblk_os += s.os_nblk;
   }
   if (sort_total >= ((int64_t)1 << 31)) return fail(ctx, EGB_ERR_ARG, "batch too large for one sort");
 
@@ -803,7 +806,7 @@ int run_batch_sorted(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags,
   const size_t off_fk = dl.take(sizeof(float) * (size_t)std::max<int64_t>(sort_total, 1));
   const size_t off_fs1 = dl.take(sizeof(float) * (size_t)std::max<int64_t>(s1_total, 1));
   const size_t off_fs2 = dl.take(sizeof(float) * (size_t)std::max<int64_t>(s2_total, 1));
-  const size_t sweep_bytes = sort_sweep_bytes(nblk_sort, (int)segs.size());
+  const size_t sweep_bytes = sort_sweep_bytes(nblk_os, (int)segs.size());
   const size_t off_sweep = dl.take(sweep_bytes);
 
   // multi-D job blocks
@@ -1267,6 +1270,7 @@ int run_batch_sorted(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags,
   const size_t tab_colidx = tl.take(sizeof(int32_t) * (size_t)ncols_total);
   const size_t tab_segs = tl.take(sizeof(SortSeg) * std::max<size_t>(segs.size(), 1));
   const size_t tab_blkseg = tl.take(sizeof(int32_t) * (size_t)std::max(nblk_sort, 1));
+  const size_t tab_osblkseg = tl.take(sizeof(int32_t) * (size_t)std::max(nblk_os, 1));
   const size_t tab_sjk = tl.take(sizeof(SortedJob) * std::max<size_t>(sj_knn.size(), 1));
   const size_t tab_sjc = tl.take(sizeof(SortedJob) * std::max<size_t>(sj_cnt.size(), 1));
   const size_t tab_jobs = tl.take(sizeof(JobDev) * std::max<size_t>(jobs.size(), 1));
@@ -1392,8 +1396,11 @@ int run_batch_sorted(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags,
   if (!segs.empty()) std::memcpy(H + tab_segs, segs.data(), sizeof(SortSeg) * segs.size());
   {
     int32_t* bs = (int32_t*)(H + tab_blkseg);
-    for (size_t s = 0; s < segs.size(); ++s)
+    int32_t* os = (int32_t*)(H + tab_osblkseg);
+    for (size_t s = 0; s < segs.size(); ++s) {
       for (int b = 0; b < segs[s].nblk; ++b) bs[segs[s].blk0 + b] = (int32_t)s;
+      for (int b = 0; b < segs[s].os_nblk; ++b) os[segs[s].os_blk0 + b] = (int32_t)s;
+    }
   }
   if (!gsegs.empty()) std::memcpy(H + tab_gsegs, gsegs.data(), sizeof(SortSeg) * gsegs.size());
   {
@@ -1580,8 +1587,9 @@ int run_batch_sorted(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags,
   int32_t* vals = (int32_t*)(A + off_vals_a);
   if (timing) EGB_CUDA(cudaEventRecord(ctx->kev[8], st));
   launch_sort(tasks_d, (const SortSeg*)dtab(tab_segs), (const int32_t*)dtab(tab_blkseg), nblk_sort,
-              (int)segs.size(), keys, (uint64_t*)(A + off_keys_b), vals, (int32_t*)(A + off_vals_b),
-              A + off_sweep, sort_first, err_d, st, timing ? ctx->kev + 12 : nullptr);
+              (const int32_t*)dtab(tab_osblkseg), nblk_os, (int)segs.size(), keys,
+              (uint64_t*)(A + off_keys_b), vals, (int32_t*)(A + off_vals_b), A + off_sweep,
+              sort_first, err_d, st, timing ? ctx->kev + 12 : nullptr);
   const KeyIndex kx{keys, (const float*)(A + off_fk), (const uint64_t*)(A + off_s1),
                     (const uint64_t*)(A + off_s2), (const float*)(A + off_fs1),
                     (const float*)(A + off_fs2)};
@@ -1885,7 +1893,7 @@ int egb_create(int device, egb_ctx** out) {
   *out = nullptr;
   egb_ctx* ctx = new egb_ctx();
   ctx->device = device;
-  if (cudaSetDevice(device) != cudaSuccess ||
+  if (cudaSetDevice(device) != cudaSuccess || init_sort_kernels() != (int)cudaSuccess ||
       cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaStreamCreateWithFlags(&ctx->side_stream, cudaStreamNonBlocking) != cudaSuccess ||
       !create_fork_events(ctx)) {

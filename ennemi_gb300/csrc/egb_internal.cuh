@@ -368,6 +368,8 @@ struct SortSeg {          // one segment of the batched radix sort
   int32_t task;
   int32_t col;            // source column of the task
   int32_t src_begin;      // first working index of the segment
+  int32_t os_blk0;        // its first tile of the single-sweep passes (OS_TILE keys)
+  int32_t os_nblk;
 };
 
 struct GatherCol {        // working column <- caller column (strided, permuted)
@@ -452,6 +454,7 @@ void launch_combine(const TaskDev* tasks_d, const CombineJob* jobs_d, const int3
 
 // egb_sort.cu
 constexpr int SORT_TILE = 2048;
+constexpr int OS_TILE = 4096;   // keys per tile of the batch sort's single-sweep passes
 // The batch's sorted keys and the arrays searched in their place: each
 // key's value rounded down to FP32 (exact comparisons against FP32 bounds in
 // half the bytes), and samples of both (egb_search.cuh), at each segment's
@@ -499,10 +502,16 @@ size_t sort_scan_tmp_elems(int nblk);
 // `sweep` (sort_sweep_bytes, zeroed before the launch) holds its look-back
 // flags, digit totals and tile counters.  `first` is even: the result is in
 // keys_a / vals_a.
-size_t sort_sweep_bytes(int nblk, int nseg);
+// blk_seg_d / nblk: the segments' SORT_TILE tiles (load and repair
+// kernels); os_blk_seg_d / os_nblk: their OS_TILE tiles (the passes).
+size_t sort_sweep_bytes(int os_nblk, int nseg);
+// Once per context, on its device: lets the passes use their shared memory
+// (above the 48 KB default); returns the cudaError_t.
+int init_sort_kernels();
 void launch_sort(const TaskDev* tasks_d, const SortSeg* segs_d, const int32_t* blk_seg_d,
-                 int nblk, int nseg, uint64_t* keys_a, uint64_t* keys_b, int32_t* vals_a,
-                 int32_t* vals_b, void* sweep, int first, uint32_t* err, cudaStream_t st,
+                 int nblk, const int32_t* os_blk_seg_d, int os_nblk, int nseg, uint64_t* keys_a,
+                 uint64_t* keys_b, int32_t* vals_a, int32_t* vals_b, void* sweep, int first,
+                 uint32_t* err, cudaStream_t st,
                  cudaEvent_t* pass_events = nullptr);  // recorded around the passes alone
 constexpr int SORTED_BLOCK = 256;
 void launch_sorted_jobs(const TaskDev* tasks_d, const SortedJob* jobs_d, int njobs,

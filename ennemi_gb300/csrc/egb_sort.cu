@@ -220,33 +220,71 @@ onesweep_load_kernel(const TaskDev* __restrict__ tasks, const SortSeg* __restric
     if (h[i]) atomicAdd(g + i, h[i]);
 }
 
-__global__ void __launch_bounds__(SORT_THREADS)
-onesweep_pass_kernel(const SortSeg* __restrict__ segs, const int32_t* __restrict__ blk_seg,
+// A pass tile is OS_TILE keys on OS_THREADS threads (eight keys a thread);
+// its staging arrays exceed the 48 KB of static shared memory.
+constexpr int OS_THREADS = 512;
+constexpr int OS_NW = OS_THREADS / 32;
+struct OsSmem {
+  uint32_t wcnt[OS_NW][256];  // per-warp digit counts, then offsets
+  uint32_t dstart[256];       // first tile slot of each digit
+  uint32_t gbase[256];        // first output position of each digit
+  uint32_t ws[8];             // digit-scan scratch
+  int tile;
+  uint64_t sk[OS_TILE];
+  int32_t sv[OS_TILE];
+};
+static_assert(OS_TILE % OS_NW == 0 && (OS_TILE / OS_NW) % 32 == 0, "whole warp rounds");
+
+// Exclusive scan over the 256 digits, one value per digit thread (tid <
+// 256: warps 0-7); every thread of the block calls it.
+__device__ __forceinline__ uint32_t digit_excl_scan(uint32_t v, uint32_t* ws) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  uint32_t x = v;
+  if (tid < 256) {
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) ws[warp] = x;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t w = lane < 8 ? ws[lane] : 0u;
+#pragma unroll
+    for (int o = 1; o < 8; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    if (lane < 8) ws[lane] = w;
+  }
+  __syncthreads();
+  const uint32_t r = tid < 256 ? (warp ? ws[warp - 1] : 0u) + x - v : 0u;
+  __syncthreads();
+  return r;
+}
+
+__global__ void __launch_bounds__(OS_THREADS)
+onesweep_pass_kernel(const SortSeg* __restrict__ segs, const int32_t* __restrict__ os_blk_seg,
                      const uint64_t* __restrict__ kin, const int32_t* __restrict__ vin,
                      uint64_t* __restrict__ kout, int32_t* __restrict__ vout, int pass,
                      const uint32_t* __restrict__ seg_hist, unsigned long long* flags,
                      int* tile_counter, uint32_t* err) {
-  constexpr int NW = SORT_THREADS / 32;
-  constexpr int CH = SORT_TILE / NW;  // keys per warp
-  constexpr int R = CH / 32;          // rounds per warp
-  __shared__ uint32_t wcnt[NW][256];  // per-warp digit counts, then offsets
-  __shared__ uint32_t dstart[256];    // first tile slot of each digit
-  __shared__ uint32_t gbase[256];     // first output position of each digit
-  __shared__ uint64_t sk[SORT_TILE];
-  __shared__ int32_t sv[SORT_TILE];
-  __shared__ int tile_s;
+  constexpr int CH = OS_TILE / OS_NW;  // keys per warp
+  constexpr int R = CH / 32;           // rounds per warp
+  extern __shared__ __align__(16) unsigned char os_raw[];
+  OsSmem& S = *reinterpret_cast<OsSmem*>(os_raw);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  if (tid == 0) tile_s = atomicAdd(tile_counter, 1);
-#pragma unroll
-  for (int w = 0; w < NW; ++w) wcnt[w][tid] = 0;
+  if (tid == 0) S.tile = atomicAdd(tile_counter, 1);
+  for (int i = tid; i < OS_NW * 256; i += OS_THREADS) (&S.wcnt[0][0])[i] = 0u;
   __syncthreads();
-  const int b = tile_s;
-  const int si = blk_seg[b];
+  const int b = S.tile;
+  const int si = os_blk_seg[b];
   const SortSeg s = segs[si];
-  const int lb = b - s.blk0;
+  const int lb = b - s.os_blk0;
   const int shift = 8 * pass;
-  const int i0 = lb * SORT_TILE;
-  const int n = min(SORT_TILE, s.len - i0);
+  const int i0 = lb * OS_TILE;
+  const int n = min(OS_TILE, s.len - i0);
   const uint32_t lt = (1u << lane) - 1u;
   uint64_t key[R];
   int32_t val[R];
@@ -265,73 +303,80 @@ onesweep_pass_kernel(const SortSeg* __restrict__ segs, const int32_t* __restrict
       const uint32_t bb = __ballot_sync(0xffffffffu, (d >> bit) & 1u);
       peers &= ((d >> bit) & 1u) ? bb : ~bb;
     }
-    const uint32_t before = valid ? wcnt[warp][d] : 0u;
+    const uint32_t before = valid ? S.wcnt[warp][d] : 0u;
     __syncwarp();
-    if (valid && (peers & lt) == 0) wcnt[warp][d] = before + __popc(peers);
+    if (valid && (peers & lt) == 0) S.wcnt[warp][d] = before + __popc(peers);
     __syncwarp();
     rk[r] = before + __popc(peers & lt);
   }
   __syncthreads();
   uint32_t cnt = 0;  // digit tid: offsets of the warps, then its count in the tile
+  if (tid < 256) {
 #pragma unroll
-  for (int w = 0; w < NW; ++w) {
-    const uint32_t c = wcnt[w][tid];
-    wcnt[w][tid] = cnt;
-    cnt += c;
+    for (int w = 0; w < OS_NW; ++w) {
+      const uint32_t c = S.wcnt[w][tid];
+      S.wcnt[w][tid] = cnt;
+      cnt += c;
+    }
   }
   // publish this tile's count of digit tid, then look back for the count of
   // digit tid in the segment's earlier tiles
-  const unsigned long long tag = (unsigned long long)(pass + 1) << 56;
-  const unsigned long long INCL = 1ull << 55;
-  unsigned long long* mine = flags + (size_t)b * 256 + tid;
   uint32_t excl = 0;
-  if (lb == 0) {
-    atomicExch(mine, tag | INCL | cnt);
-  } else {
-    atomicExch(mine, tag | cnt);
-    int pb = b - 1;
-    for (;;) {
-      const volatile unsigned long long* f = flags + (size_t)pb * 256 + tid;
-      unsigned long long w = *f;
-      int spins = 0;
-      while ((w >> 56) != (unsigned long long)(pass + 1)) {
-        if (++spins > OS_SPIN_LIMIT) {
-          atomicOr(err, DERR_WAIT_TIMEOUT);
-          w = tag | INCL;
-          break;
+  if (tid < 256) {
+    const unsigned long long tag = (unsigned long long)(pass + 1) << 56;
+    const unsigned long long INCL = 1ull << 55;
+    unsigned long long* mine = flags + (size_t)b * 256 + tid;
+    if (lb == 0) {
+      atomicExch(mine, tag | INCL | cnt);
+    } else {
+      atomicExch(mine, tag | cnt);
+      int pb = b - 1;
+      for (;;) {
+        const volatile unsigned long long* f = flags + (size_t)pb * 256 + tid;
+        unsigned long long w = *f;
+        int spins = 0;
+        while ((w >> 56) != (unsigned long long)(pass + 1)) {
+          if (++spins > OS_SPIN_LIMIT) {
+            atomicOr(err, DERR_WAIT_TIMEOUT);
+            w = tag | INCL;
+            break;
+          }
+          w = *f;
         }
-        w = *f;
+        excl += (uint32_t)w;
+        if ((w & INCL) || pb <= s.os_blk0) break;
+        --pb;
       }
-      excl += (uint32_t)w;
-      if ((w & INCL) || pb <= s.blk0) break;
-      --pb;
+      atomicExch(mine, tag | INCL | (excl + cnt));
     }
-    atomicExch(mine, tag | INCL | (excl + cnt));
   }
   // digit tid of the whole segment starts after the smaller digits
-  const uint32_t seg_tot = seg_hist[((size_t)si * OS_PASSES + pass) * 256 + tid];
-  const uint32_t seg_off = block_excl_scan(seg_tot, nullptr);
-  gbase[tid] = seg_off + excl;
-  dstart[tid] = block_excl_scan(cnt, nullptr);
+  const uint32_t seg_tot = tid < 256 ? seg_hist[((size_t)si * OS_PASSES + pass) * 256 + tid] : 0u;
+  const uint32_t seg_off = digit_excl_scan(seg_tot, S.ws);
+  const uint32_t ds = digit_excl_scan(cnt, S.ws);
+  if (tid < 256) {
+    S.gbase[tid] = seg_off + excl;
+    S.dstart[tid] = ds;
+  }
   __syncthreads();
 #pragma unroll
   for (int r = 0; r < R; ++r) {
     const int t = warp * CH + r * 32 + lane;
     if (t < n) {
       const uint32_t d = dg[r];
-      const uint32_t slot = dstart[d] + wcnt[warp][d] + rk[r];
-      sk[slot] = key[r];
-      sv[slot] = val[r];
+      const uint32_t slot = S.dstart[d] + S.wcnt[warp][d] + rk[r];
+      S.sk[slot] = key[r];
+      S.sv[slot] = val[r];
     }
   }
   __syncthreads();
-  for (int t = tid; t < n; t += SORT_THREADS) {
-    const uint64_t k = sk[t];
+  for (int t = tid; t < n; t += OS_THREADS) {
+    const uint64_t k = S.sk[t];
     const uint32_t d = (uint32_t)(k >> shift) & 255u;
-    const uint32_t pos = gbase[d] + ((uint32_t)t - dstart[d]);
+    const uint32_t pos = S.gbase[d] + ((uint32_t)t - S.dstart[d]);
     if (pos < (uint32_t)s.len) {
       kout[s.out_base + pos] = k;
-      vout[s.out_base + pos] = sv[t];
+      vout[s.out_base + pos] = S.sv[t];
     } else {
       atomicOr(err, DERR_BAD_INDEX);
     }
@@ -664,19 +709,24 @@ static void excl_scan(uint32_t* data, int64_t n, uint32_t* tmp, cudaStream_t st)
   count_launch();
 }
 
-size_t sort_sweep_bytes(int nblk, int nseg) {
-  return sizeof(unsigned long long) * 256 * (size_t)std::max(nblk, 1) +
+int init_sort_kernels() {
+  return (int)cudaFuncSetAttribute(onesweep_pass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)sizeof(OsSmem));
+}
+
+size_t sort_sweep_bytes(int os_nblk, int nseg) {
+  return sizeof(unsigned long long) * 256 * (size_t)std::max(os_nblk, 1) +
          sizeof(uint32_t) * OS_PASSES * 256 * (size_t)std::max(nseg, 1) + 64;
 }
 
 void launch_sort(const TaskDev* tasks_d, const SortSeg* segs_d, const int32_t* blk_seg_d,
-                 int nblk, int nseg, uint64_t* keys_a, uint64_t* keys_b, int32_t* vals_a,
-                 int32_t* vals_b, void* sweep, int first, uint32_t* err, cudaStream_t st,
-                 cudaEvent_t* pass_events) {
-  if (nblk <= 0) return;
+                 int nblk, const int32_t* os_blk_seg_d, int os_nblk, int nseg, uint64_t* keys_a,
+                 uint64_t* keys_b, int32_t* vals_a, int32_t* vals_b, void* sweep, int first,
+                 uint32_t* err, cudaStream_t st, cudaEvent_t* pass_events) {
+  if (nblk <= 0 || os_nblk <= 0) return;
   // sweep (zeroed by the caller): flag words, segment digit totals, tile counters
   unsigned long long* flags = (unsigned long long*)sweep;
-  uint32_t* seg_hist = (uint32_t*)(flags + 256 * (size_t)nblk);
+  uint32_t* seg_hist = (uint32_t*)(flags + 256 * (size_t)os_nblk);
   int* counters = (int*)(seg_hist + OS_PASSES * 256 * (size_t)std::max(nseg, 1));
   onesweep_load_kernel<<<nblk, SORT_THREADS, 0, st>>>(tasks_d, segs_d, blk_seg_d, keys_a, vals_a,
                                                      seg_hist, first);
@@ -687,8 +737,8 @@ void launch_sort(const TaskDev* tasks_d, const SortSeg* segs_d, const int32_t* b
   int32_t* vout = vals_b;
   if (pass_events) cudaEventRecord(pass_events[0], st);
   for (int pass = first; pass < OS_PASSES; ++pass) {
-    onesweep_pass_kernel<<<nblk, SORT_THREADS, 0, st>>>(segs_d, blk_seg_d, kin, vin, kout, vout,
-                                                       pass, seg_hist, flags, counters + pass, err);
+    onesweep_pass_kernel<<<os_nblk, OS_THREADS, sizeof(OsSmem), st>>>(
+        segs_d, os_blk_seg_d, kin, vin, kout, vout, pass, seg_hist, flags, counters + pass, err);
     count_launch();
     uint64_t* tk = kin; kin = kout; kout = tk;
     int32_t* tv = vin; vin = vout; vout = tv;
