@@ -505,8 +505,8 @@ def main():
     # every key (8 B) and index (4 B) of the batch's sort once.  Its time per
     # launch is the event-timed run of the batch's digit passes over their
     # number.  DRAM traffic per launch from one ncu capture of this workload
-    # (cold cache, the six passes of one batch averaged): 143.2 MB read +
-    # 87.2 MB written.
+    # (cold cache, the six passes of one batch averaged): 137.6 MB read +
+    # 82.5 MB written.
     keys = work_stats.get("sort_keys", 0)
     npass = work_stats.get("sort_passes", 0) or 8
     pass_ms = phases.get("sort_passes", 0.0) / npass
@@ -514,7 +514,7 @@ def main():
     pass_gbs = pass_bytes / (pass_ms / 1000.0) / 1e9 if pass_ms > 0 else 0.0
     roofline = {"bound": "hbm", "kernel": "onesweep_pass_kernel (radix sort pass)",
                 "achieved": pass_gbs, "peak": hbm, "unit": "GB/s", "frac": pass_gbs / hbm,
-                "traffic": (143.19 + 87.20) * 1e6 if args.n == 1_000_000 else None,
+                "traffic": (137.61 + 82.46) * 1e6 if args.n == 1_000_000 else None,
                 "traffic_unit": "bytes per launch (ncu, cold cache)",
                 "algorithmic_bytes_per_launch": pass_bytes, "ms_per_launch": pass_ms,
                 "launches_per_step": npass, "peak_source": hbm_src}
