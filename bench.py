@@ -390,7 +390,7 @@ def main():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--cpu-slices", type=int, default=2,
+    ap.add_argument("--cpu-slices", type=int, default=10,
                     help="query slices (of --cpu-nslices) timed for cpu_baseline")
     ap.add_argument("--cpu-nslices", type=int, default=50)
     ap.add_argument("--plain-steps", type=int, default=5,
