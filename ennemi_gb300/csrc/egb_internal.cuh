@@ -64,6 +64,22 @@ __host__ __device__ __forceinline__ double value_of(uint64_t k) {
   return v;
 }
 
+// A count radius by its bits, with integer compares (GB300 issues FP64,
+// comparisons included, at a few operations per clock per SM): 0 = no ball
+// (negative or NaN: the count is 0), 1 = finite and >= 0 (-0 included),
+// 2 = +inf (every point).
+__host__ __device__ __forceinline__ int radius_class(double r) {
+  uint64_t u;
+#ifdef __CUDA_ARCH__
+  u = (uint64_t)__double_as_longlong(r);
+#else
+  __builtin_memcpy(&u, &r, 8);
+#endif
+  if (u == 0x7ff0000000000000ull) return 2;
+  if (u < 0x7ff0000000000000ull || u == 0x8000000000000000ull) return 1;
+  return 0;
+}
+
 #ifdef __CUDACC__
 // Smallest float >= the non-negative double with bit pattern u (integer
 // operations only: GB300 issues FP64 at 2 lanes per clock per SM, so this

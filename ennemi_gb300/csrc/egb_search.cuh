@@ -166,7 +166,9 @@ __device__ __forceinline__ void ball_positions(const SegView& v, double q, doubl
   const float rn = __int_as_float(__float_as_int(ru) + 1);         // next float above ru
   const float a1 = __fadd_rd(qd, rd), b1 = __fadd_ru(qu, rn);
   const float a0 = __fsub_rd(qd, rn), b0 = __fsub_ru(qu, rd);
-  bool exact = isfinite(a1) && isfinite(b1) && isfinite(a0) && isfinite(b0) && isfinite(q);
+  const uint64_t qb = (uint64_t)__double_as_longlong(q);
+  bool exact = isfinite(a1) && isfinite(b1) && isfinite(a0) && isfinite(b0) &&
+               ((qb >> 52) & 0x7ffu) != 0x7ffu;  // q finite, by its exponent bits
   auto fbound = [&](float a) {  // first position whose value is >= a
     return g >= 0 ? sampled_bound_from<float, false>(v.fk, v.fs1, len, a, g)
                   : sampled_bound<float, false>(v.fk, v.fs1, v.fs2, len, a);

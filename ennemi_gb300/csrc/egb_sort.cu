@@ -523,10 +523,11 @@ __global__ void sorted_jobs_kernel(const TaskDev* __restrict__ tasks,
   }
 
   const double r = t.rad[i];
+  const int rc = radius_class(r);
   int32_t count;
-  if (!(r >= 0.0)) {
+  if (rc == 0) {
     count = 0;
-  } else if (r == INF) {
+  } else if (rc == 2) {
     count = (int32_t)len;
   } else {
     // The ball is one run of sorted positions; its ends come from FP32

@@ -366,10 +366,11 @@ wm_count_kernel(const TaskDev* __restrict__ tasks, const WmJob* __restrict__ job
   const TaskDev& t = tasks[J.task];
   const int32_t w = vals_all[J.base_a + i];          // working index of the query
   const double r = t.rad[w];
+  const int rc = radius_class(r);
   int32_t count;
-  if (!(r >= 0.0)) {
+  if (rc == 0) {
     count = 0;
-  } else if (isinf(r)) {
+  } else if (rc == 2) {
     count = len;
   } else {
     const SegView va = seg_view(kx, J.base_a, J.s1_a, J.s2_a, len);
