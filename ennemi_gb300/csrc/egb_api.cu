@@ -1590,10 +1590,11 @@ int run_batch_sorted(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags,
               (const int32_t*)dtab(tab_osblkseg), nblk_os, (int)segs.size(), keys,
               (uint64_t*)(A + off_keys_b), vals, (int32_t*)(A + off_vals_b), A + off_sweep,
               sort_first, err_d, st, timing ? ctx->kev + 12 : nullptr);
-  const KeyIndex kx{keys, (const float*)(A + off_fk), (const uint64_t*)(A + off_s1),
-                    (const uint64_t*)(A + off_s2), (const float*)(A + off_fs1),
-                    (const float*)(A + off_fs2)};
-  launch_samples((const SortSeg*)dtab(tab_segs), (const int32_t*)dtab(tab_blkseg), nblk_sort, kx, st);
+  const KeyIndexOut ko{(float*)(A + off_fk), (uint64_t*)(A + off_s1), (uint64_t*)(A + off_s2),
+                       (float*)(A + off_fs1), (float*)(A + off_fs2)};
+  const KeyIndex kx{keys, ko.fkeys, ko.s1, ko.s2, ko.fs1, ko.fs2};
+  launch_samples((const SortSeg*)dtab(tab_segs), (const int32_t*)dtab(tab_blkseg), nblk_sort, keys,
+                 ko, st);
   // the rank-space matrices need only the sorted values: they build on the
   // side stream, joined back before their counts
   const bool fork_wm = !wbuild.empty();

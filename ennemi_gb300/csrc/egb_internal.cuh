@@ -634,10 +634,17 @@ void launch_wm_build(const WmJob* jobs_d, int njobs, int total_tiles, int max_le
 // Counts: one thread per query, in the a order; writes cnt[slot] of the task.
 void launch_wm_count(const TaskDev* tasks_d, const WmJob* jobs_d, int njobs, int total_blocks,
                      const KeyIndex& kx, const int32_t* sorted_vals, cudaStream_t st);
-// The FP32 copy and the samples of every sorted segment (KeyIndex), after
-// the sort.
-void launch_samples(const SortSeg* segs_d, const int32_t* blk_seg_d, int nblk, const KeyIndex& kx,
-                    cudaStream_t st);
+// The arrays launch_samples writes: the FP32 copy and the samples of every
+// sorted segment (read back through a KeyIndex), after the sort.
+struct KeyIndexOut {
+  float* fkeys;
+  uint64_t* s1;
+  uint64_t* s2;
+  float* fs1;
+  float* fs2;
+};
+void launch_samples(const SortSeg* segs_d, const int32_t* blk_seg_d, int nblk,
+                    const uint64_t* keys, const KeyIndexOut& out, cudaStream_t st);
 
 // egb_discrete.cu: exact group-by of the rows of one column subset of a
 // discrete task: the rows equal to each row, into count slot `slot`.

@@ -395,21 +395,21 @@ wm_count_kernel(const TaskDev* __restrict__ tasks, const WmJob* __restrict__ job
 // One block of SAMPLE_THREADS per 2048-key tile of the sort.
 constexpr int SAMPLE_THREADS = 256;
 __global__ void __launch_bounds__(SAMPLE_THREADS)
-samples_kernel(const SortSeg* __restrict__ segs, const int32_t* __restrict__ blk_seg, KeyIndex kx) {
+samples_kernel(const SortSeg* __restrict__ segs, const int32_t* __restrict__ blk_seg,
+               const uint64_t* __restrict__ keys, KeyIndexOut out) {
   const SortSeg sg = segs[blk_seg[blockIdx.x]];
   const int i0 = ((int)blockIdx.x - sg.blk0) * SORT_TILE;
   const int i1 = min(i0 + SORT_TILE, sg.len);
-  float* fk = const_cast<float*>(kx.fkeys) + sg.out_base;
   for (int p = i0 + (int)threadIdx.x; p < i1; p += SAMPLE_THREADS) {
-    const uint64_t k = __ldg(kx.keys + sg.out_base + p);
+    const uint64_t k = __ldg(keys + sg.out_base + p);
     const float f = __double2float_rd(value_of(k));
-    fk[p] = f;
+    out.fkeys[sg.out_base + p] = f;
     if (p % SAMPLE1 == 0) {
-      const_cast<uint64_t*>(kx.s1)[sg.s1_base + p / SAMPLE1] = k;
-      const_cast<float*>(kx.fs1)[sg.s1_base + p / SAMPLE1] = f;
+      out.s1[sg.s1_base + p / SAMPLE1] = k;
+      out.fs1[sg.s1_base + p / SAMPLE1] = f;
       if (p % SAMPLE2 == 0) {
-        const_cast<uint64_t*>(kx.s2)[sg.s2_base + p / SAMPLE2] = k;
-        const_cast<float*>(kx.fs2)[sg.s2_base + p / SAMPLE2] = f;
+        out.s2[sg.s2_base + p / SAMPLE2] = k;
+        out.fs2[sg.s2_base + p / SAMPLE2] = f;
       }
     }
   }
@@ -438,10 +438,10 @@ void launch_wm_count(const TaskDev* tasks_d, const WmJob* jobs_d, int njobs, int
   count_launch();
 }
 
-void launch_samples(const SortSeg* segs_d, const int32_t* blk_seg_d, int nblk, const KeyIndex& kx,
-                    cudaStream_t st) {
+void launch_samples(const SortSeg* segs_d, const int32_t* blk_seg_d, int nblk,
+                    const uint64_t* keys, const KeyIndexOut& out, cudaStream_t st) {
   if (nblk <= 0) return;
-  samples_kernel<<<nblk, SAMPLE_THREADS, 0, st>>>(segs_d, blk_seg_d, kx);
+  samples_kernel<<<nblk, SAMPLE_THREADS, 0, st>>>(segs_d, blk_seg_d, keys, out);
   count_launch();
 }
 
