@@ -816,7 +816,7 @@ int run_batch_sorted(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags,
   int64_t gsort_total = 0, max_glen = 1;
   bool any_nested = false;
   int64_t max_gkey = 1;  // largest strip / cell key of the grid jobs
-  int nblk_grid = 0, nblk_os_grid = 0;
+  int nblk_grid = 0;
   int64_t max_lds = 32;
   for (size_t j = 0; j < mjobs.size(); ++j) {
     const MJob& m = mjobs[j];
@@ -906,29 +906,24 @@ int run_batch_sorted(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags,
       g.len = (int32_t)len;
       g.blk0 = nblk_grid;
       g.nblk = (int32_t)((len + SORT_TILE - 1) / SORT_TILE);
-      g.os_blk0 = nblk_os_grid;
-      g.os_nblk = (int32_t)((len + OS_TILE - 1) / OS_TILE);
       g.task = m.s.task;
       gsegs.push_back(g);
       grid_jobs.push_back((int32_t)j);
       gsort_total += len;
       nblk_grid += g.nblk;
-      nblk_os_grid += g.os_nblk;
       max_glen = std::max(max_glen, len);
     }
   }
 
-  // strip / cell key sorts of the grid jobs (single-sweep passes, each sort
-  // with its own zeroed sweep region)
+  // strip-key sort of the grid jobs (one extra 8-bit radix pass)
   const size_t off_gkeys_a = dl.take(sizeof(uint64_t) * (size_t)std::max<int64_t>(gsort_total, 1));
   const size_t off_gkeys_b = dl.take(sizeof(uint64_t) * (size_t)std::max<int64_t>(gsort_total, 1));
   const size_t off_gvals_a = dl.take(sizeof(int32_t) * (size_t)std::max<int64_t>(gsort_total, 1));
   const size_t off_gvals_b = dl.take(sizeof(int32_t) * (size_t)std::max<int64_t>(gsort_total, 1));
   const size_t off_ginv = dl.take(sizeof(int32_t) * (size_t)std::max<int64_t>(gsort_total, 1));
   const size_t off_gsub = any_nested ? dl.take(sizeof(int32_t) * (size_t)std::max<int64_t>(gsort_total, 1)) : 0;
-  const size_t gsweep_bytes = sort_sweep_bytes(nblk_os_grid, (int)gsegs.size());
-  const size_t off_gsweep_nest = dl.take(gsweep_bytes);
-  const size_t off_gsweep_key = dl.take(gsweep_bytes);
+  const size_t off_ghist = dl.take(sizeof(uint32_t) * 256 * (size_t)std::max(nblk_grid, 1));
+  const size_t off_gscan = dl.take(sizeof(uint32_t) * sort_scan_tmp_elems(std::max(nblk_grid, 1)));
 
   // sorted jobs
   std::vector<SortedJob> sj_knn, sj_cnt;
@@ -1281,7 +1276,6 @@ int run_batch_sorted(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags,
   const size_t tab_jobs = tl.take(sizeof(JobDev) * std::max<size_t>(jobs.size(), 1));
   const size_t tab_gsegs = tl.take(sizeof(SortSeg) * std::max<size_t>(gsegs.size(), 1));
   const size_t tab_blkgseg = tl.take(sizeof(int32_t) * (size_t)std::max(nblk_grid, 1));
-  const size_t tab_osblkgseg = tl.take(sizeof(int32_t) * (size_t)std::max(nblk_os_grid, 1));
   const size_t tab_gridjobs = tl.take(sizeof(int32_t) * std::max<size_t>(grid_jobs.size(), 1));
   const size_t tab_pwtrees = tl.take(sizeof(PwTree) * std::max<size_t>(pw_trees.size(), 1));
   const size_t tab_pwnodes = tl.take(sizeof(int2) * std::max<size_t>(pw_nodes.size(), 1));
@@ -1411,11 +1405,8 @@ int run_batch_sorted(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags,
   if (!gsegs.empty()) std::memcpy(H + tab_gsegs, gsegs.data(), sizeof(SortSeg) * gsegs.size());
   {
     int32_t* bs = (int32_t*)(H + tab_blkgseg);
-    int32_t* os = (int32_t*)(H + tab_osblkgseg);
-    for (size_t g = 0; g < gsegs.size(); ++g) {
+    for (size_t g = 0; g < gsegs.size(); ++g)
       for (int b = 0; b < gsegs[g].nblk; ++b) bs[gsegs[g].blk0 + b] = (int32_t)g;
-      for (int b = 0; b < gsegs[g].os_nblk; ++b) os[gsegs[g].os_blk0 + b] = (int32_t)g;
-    }
   }
   if (!grid_jobs.empty())
     std::memcpy(H + tab_gridjobs, grid_jobs.data(), sizeof(int32_t) * grid_jobs.size());
@@ -1560,10 +1551,6 @@ int run_batch_sorted(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags,
   if (wmz_bytes) EGB_CUDA(cudaMemsetAsync(A + off_wmz, 0, wmz_bytes, st));
   if (gbz_bytes) EGB_CUDA(cudaMemsetAsync(A + off_gbz, 0, gbz_bytes, st));
   if (nblk_sort) EGB_CUDA(cudaMemsetAsync(A + off_sweep, 0, sweep_bytes, st));
-  if (nblk_grid) {
-    EGB_CUDA(cudaMemsetAsync(A + off_gsweep_nest, 0, gsweep_bytes, st));
-    EGB_CUDA(cudaMemsetAsync(A + off_gsweep_key, 0, gsweep_bytes, st));
-  }
   if (inject)  // the device error word as if a kernel had set these bits
     for (int i = 0; i < 4; ++i)
       EGB_CUDA(cudaMemsetAsync((char*)err_d + i, (int)((inject >> (8 * i)) & 0xffu), 1, st));
@@ -1631,8 +1618,8 @@ int run_batch_sorted(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags,
     uint64_t* gkb = (uint64_t*)(A + off_gkeys_b);
     int32_t* gva = (int32_t*)(A + off_gvals_a);
     int32_t* gvb = (int32_t*)(A + off_gvals_b);
-    const int32_t* osblkg_d = (const int32_t*)dtab(tab_osblkgseg);
-    const int ngseg = (int)gsegs.size();
+    uint32_t* ghist = (uint32_t*)(A + off_ghist);
+    uint32_t* gscan = (uint32_t*)(A + off_gscan);
     int32_t* ginv = (int32_t*)(A + off_ginv);
     int32_t* gsub = any_nested ? (int32_t*)(A + off_gsub) : nullptr;
     launch_grid_inv(jobs_d, gj_d, ngrid, gsegs_d, vals, (const SortSeg*)dtab(tab_segs), ginv, max_glen, st);
@@ -1640,16 +1627,14 @@ int run_batch_sorted(egb_ctx* ctx, const egb_task* tasks, int ntasks, int flags,
       // strips of the column-2 order -> cell of every point within its strip
       launch_nest_key(jobs_d, gj_d, ngrid, gsegs_d, vals, (const SortSeg*)dtab(tab_segs), ginv, gka,
                       gva, max_glen, st);
-      launch_key_sort(gsegs_d, blkg_d, nblk_grid, osblkg_d, nblk_os_grid, ngseg, gka, gva, gkb, gvb,
-                      1, A + off_gsweep_nest, err_d, st);  // strips < 256: one digit
+      launch_radix_pass(gsegs_d, blkg_d, nblk_grid, gka, gva, gkb, gvb, 0, ghist, gscan, st);
       launch_nest_sub(tasks_d, jobs_d, gj_d, ngrid, gsegs_d, gkb, gvb, gsub, max_glen, st);
     }
     launch_grid_key(jobs_d, gj_d, ngrid, gsegs_d, vals, (const SortSeg*)dtab(tab_segs), ginv, gsub, gka,
                     gva, max_glen, st);
-    // strip / cell keys below 2^16: one digit, or two above 8 bits (then the
-    // result is back in gka / gva)
-    launch_key_sort(gsegs_d, blkg_d, nblk_grid, osblkg_d, nblk_os_grid, ngseg, gka, gva, gkb, gvb,
-                    max_gkey > 256 ? 2 : 1, A + off_gsweep_key, err_d, st);
+    launch_radix_pass(gsegs_d, blkg_d, nblk_grid, gka, gva, gkb, gvb, 0, ghist, gscan, st);
+    if (max_gkey > 256)  // strip / cell keys above 8 bits: second digit
+      launch_radix_pass(gsegs_d, blkg_d, nblk_grid, gkb, gvb, gka, gva, 8, ghist, gscan, st);
     launch_materialize_grid(tasks_d, (const JobDev*)dtab(tab_jobs), (const int32_t*)dtab(tab_gridjobs),
                             (int)grid_jobs.size(), vals, (const SortSeg*)dtab(tab_segs),
                             max_gkey > 256 ? gva : gvb, (const SortSeg*)dtab(tab_gsegs),

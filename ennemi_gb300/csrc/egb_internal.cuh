@@ -508,15 +508,10 @@ void launch_nest_key(const JobDev* jobs_d, const int32_t* grid_jobs_d, int ngrid
 void launch_nest_sub(const TaskDev* tasks_d, const JobDev* jobs_d, const int32_t* grid_jobs_d,
                      int ngrid, const SortSeg* gsegs_d, const uint64_t* keys_sorted,
                      const int32_t* vals_sorted, int32_t* sub, int64_t max_len, cudaStream_t st);
-// Stable sort of given keys (< 2^(8 npass), npass <= 2) with their values,
-// per segment (the grid layouts' strip / cell keys): npass single-sweep
-// passes from keys_a / vals_a, ping-ponging with keys_b / vals_b (npass odd:
-// the result is in keys_b / vals_b).  `sweep` (sort_sweep_bytes(os_nblk,
-// nseg), zeroed before the launch) is this sort's own.
-void launch_key_sort(const SortSeg* segs_d, const int32_t* blk_seg_d, int nblk,
-                     const int32_t* os_blk_seg_d, int os_nblk, int nseg, uint64_t* keys_a,
-                     int32_t* vals_a, uint64_t* keys_b, int32_t* vals_b, int npass, void* sweep,
-                     uint32_t* err, cudaStream_t st);
+void launch_radix_pass(const SortSeg* segs_d, const int32_t* blk_seg_d, int nblk,
+                       const uint64_t* kin, const int32_t* vin, uint64_t* kout, int32_t* vout,
+                       int shift, uint32_t* hist, uint32_t* scan_tmp, cudaStream_t st);
+size_t sort_scan_tmp_elems(int nblk);
 // The batch sort: single-sweep LSD passes over the 8-bit digits first..7 of
 // the keys (first = 0: all; first = 2: the high 48 bits, then a repair of
 // the rare runs tied there, which sets DERR_SORT_TIES when one is too long);

@@ -5,8 +5,11 @@
 // concatenated key array.  Keys are the order-preserving uint64 image of the
 // FP64 value (key_of), the payload is the working index of the point.  The
 // batch sort takes stable 8-bit single-sweep LSD passes over the high 48 key
-// bits and repairs the rare runs tied there (below); the strip / cell keys
-// of the grid layouts take one or two passes of the same kernel.
+// bits and repairs the rare runs tied there (below); the three-kernel pass
+// -- histogram, exclusive scan, stable scatter -- serves the strip-key
+// passes of the grid layouts: its per-block histograms are laid out
+// segment-major, digit-next, block-minor, so ONE global exclusive scan
+// yields absolute output positions that never leave a segment.
 //
 // 1-D kNN (entropy of one column, Ross MI with 1-D x): for the point at
 // sorted position p the (k+1)-th smallest |x_j - x_p| (self included) is
@@ -27,7 +30,143 @@ namespace egb {
 namespace {
 
 constexpr int SORT_THREADS = 256;
+constexpr int SCAN_THREADS = 256;
+constexpr int SCAN_ITEMS = 16;
+constexpr int SCAN_CHUNK = SCAN_THREADS * SCAN_ITEMS;
 constexpr int SORTED_THREADS = SORTED_BLOCK;
+
+__device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* total) {
+  __shared__ uint32_t ws[SCAN_THREADS / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) ws[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t w = lane < SCAN_THREADS / 32 ? ws[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    if (lane < SCAN_THREADS / 32) ws[lane] = w;
+  }
+  __syncthreads();
+  const uint32_t wprefix = warp ? ws[warp - 1] : 0;
+  if (total) *total = ws[SCAN_THREADS / 32 - 1];
+  const uint32_t r = wprefix + x - v;
+  __syncthreads();
+  return r;
+}
+
+__global__ void sort_hist_kernel(const SortSeg* __restrict__ segs,
+                                 const int32_t* __restrict__ blk_seg,
+                                 const uint64_t* __restrict__ keys, int shift,
+                                 uint32_t* __restrict__ hist) {
+  __shared__ uint32_t h[256];
+  const int b = blockIdx.x;
+  const SortSeg s = segs[blk_seg[b]];
+  h[threadIdx.x] = 0;
+  __syncthreads();
+  const int i0 = (b - s.blk0) * SORT_TILE;
+  const int i1 = min(i0 + SORT_TILE, s.len);
+  for (int i = i0 + threadIdx.x; i < i1; i += SORT_THREADS)
+    atomicAdd(&h[(uint32_t)(keys[s.out_base + i] >> shift) & 255u], 1u);
+  __syncthreads();
+  const int lb = b - s.blk0;
+  hist[(int64_t)256 * s.blk0 + (int64_t)threadIdx.x * s.nblk + lb] = h[threadIdx.x];
+}
+
+// Stable scatter of one tile.  Warp w ranks the keys [w * CH, (w + 1) * CH)
+// of the tile in rounds of 32: per-bit ballots give a key's rank among the
+// equal digits of its round, per-warp counters carry the rank across rounds.  One
+// block scan then turns the per-warp digit counts into the tile's layout in
+// digit order, staged in shared memory and written out so that consecutive
+// threads store to consecutive addresses of each digit's output run.
+// offs[] holds absolute positions in the concatenated buffer.
+__global__ void __launch_bounds__(SORT_THREADS)
+sort_scatter_kernel(const SortSeg* __restrict__ segs, const int32_t* __restrict__ blk_seg,
+                    const uint64_t* __restrict__ kin, const int32_t* __restrict__ vin, int shift,
+                    const uint32_t* __restrict__ offs, uint64_t* __restrict__ kout,
+                    int32_t* __restrict__ vout) {
+  constexpr int NW = SORT_THREADS / 32;
+  constexpr int CH = SORT_TILE / NW;  // keys per warp
+  constexpr int R = CH / 32;          // rounds per warp
+  static_assert(SORT_THREADS == 256 && SCAN_THREADS == 256, "one thread per digit");
+  __shared__ uint32_t wcnt[NW][256];  // per-warp digit counts, then offsets
+  __shared__ uint32_t dstart[256];    // first tile slot of each digit
+  __shared__ uint32_t gbase[256];     // first output position of each digit
+  __shared__ uint64_t sk[SORT_TILE];
+  __shared__ int32_t sv[SORT_TILE];
+  const int b = blockIdx.x;
+  const SortSeg s = segs[blk_seg[b]];
+  const int lb = b - s.blk0;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  gbase[tid] = offs[(int64_t)256 * s.blk0 + (int64_t)tid * s.nblk + lb];
+#pragma unroll
+  for (int w = 0; w < NW; ++w) wcnt[w][tid] = 0;
+  __syncthreads();
+  const int i0 = lb * SORT_TILE;
+  const int n = min(SORT_TILE, s.len - i0);
+  const uint32_t lt = (1u << lane) - 1u;
+  uint64_t key[R];
+  int32_t val[R];
+  uint32_t dg[R], rk[R];
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const int t = warp * CH + r * 32 + lane;
+    const bool valid = t < n;
+    key[r] = valid ? kin[s.out_base + i0 + t] : 0ull;
+    val[r] = valid ? vin[s.out_base + i0 + t] : 0;
+    const uint32_t d = valid ? (uint32_t)(key[r] >> shift) & 255u : 256u + lane;
+    dg[r] = d;
+    // lanes with the same digit (9 bits: invalid lanes carry 256 + lane),
+    // from one ballot per bit (measured faster than match_any here)
+    uint32_t peers = 0xffffffffu;
+#pragma unroll
+    for (int bit = 0; bit < 9; ++bit) {
+      const uint32_t bb = __ballot_sync(0xffffffffu, (d >> bit) & 1u);
+      peers &= ((d >> bit) & 1u) ? bb : ~bb;
+    }
+    const uint32_t before = valid ? wcnt[warp][d] : 0u;
+    __syncwarp();
+    if (valid && (peers & lt) == 0) wcnt[warp][d] = before + __popc(peers);
+    __syncwarp();
+    rk[r] = before + __popc(peers & lt);
+  }
+  __syncthreads();
+  uint32_t run = 0;  // digit tid: offsets of the warps, then of the digit
+#pragma unroll
+  for (int w = 0; w < NW; ++w) {
+    const uint32_t c = wcnt[w][tid];
+    wcnt[w][tid] = run;
+    run += c;
+  }
+  dstart[tid] = block_excl_scan(run, nullptr);
+  __syncthreads();
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const int t = warp * CH + r * 32 + lane;
+    if (t < n) {
+      const uint32_t d = dg[r];
+      const uint32_t slot = dstart[d] + wcnt[warp][d] + rk[r];
+      sk[slot] = key[r];
+      sv[slot] = val[r];
+    }
+  }
+  __syncthreads();
+  for (int t = tid; t < n; t += SORT_THREADS) {
+    const uint64_t k = sk[t];
+    const uint32_t d = (uint32_t)(k >> shift) & 255u;
+    const uint32_t pos = gbase[d] + ((uint32_t)t - dstart[d]);
+    kout[pos] = k;
+    vout[pos] = sv[t];
+  }
+}
 
 // ------------------------------------------------------- single sweep --
 // The batch sort proper: stable 8-bit LSD passes, one launch each,
@@ -78,28 +217,6 @@ onesweep_load_kernel(const TaskDev* __restrict__ tasks, const SortSeg* __restric
   __syncthreads();
   uint32_t* g = seg_hist + (size_t)si * OS_PASSES * 256;
   for (int i = threadIdx.x; i < OS_PASSES * 256; i += SORT_THREADS)
-    if (h[i]) atomicAdd(g + i, h[i]);
-}
-
-// Digit totals of the first npass (<= 2) passes of given keys, per segment
-// (the strip / cell keys of the grid layouts).
-__global__ void __launch_bounds__(SORT_THREADS)
-key_hist_kernel(const SortSeg* __restrict__ segs, const int32_t* __restrict__ blk_seg,
-                const uint64_t* __restrict__ keys, int npass, uint32_t* __restrict__ seg_hist) {
-  __shared__ uint32_t h[2 * 256];
-  const int si = blk_seg[blockIdx.x];
-  const SortSeg s = segs[si];
-  for (int i = threadIdx.x; i < 2 * 256; i += SORT_THREADS) h[i] = 0;
-  __syncthreads();
-  const int i0 = ((int)blockIdx.x - s.blk0) * SORT_TILE;
-  const int i1 = min(i0 + SORT_TILE, s.len);
-  for (int i = i0 + threadIdx.x; i < i1; i += SORT_THREADS) {
-    const uint64_t k = keys[s.out_base + i];
-    for (int p = 0; p < npass; ++p) atomicAdd(&h[p * 256 + (uint32_t)((k >> (8 * p)) & 255u)], 1u);
-  }
-  __syncthreads();
-  uint32_t* g = seg_hist + (size_t)si * OS_PASSES * 256;
-  for (int i = threadIdx.x; i < npass * 256; i += SORT_THREADS)
     if (h[i]) atomicAdd(g + i, h[i]);
 }
 
@@ -324,6 +441,53 @@ tie_fix_kernel(const SortSeg* __restrict__ segs, const int32_t* __restrict__ blk
   }
 }
 
+// ------------------------------------------------------------------ scan --
+__global__ void scan_reduce_kernel(const uint32_t* __restrict__ in, int64_t n,
+                                   uint32_t* __restrict__ sums) {
+  const int64_t c0 = (int64_t)blockIdx.x * SCAN_CHUNK;
+  uint32_t s = 0;
+  for (int j = 0; j < SCAN_ITEMS; ++j) {
+    const int64_t i = c0 + (int64_t)j * SCAN_THREADS + threadIdx.x;
+    if (i < n) s += in[i];
+  }
+  uint32_t tot;
+  block_excl_scan(s, &tot);
+  if (threadIdx.x == 0) sums[blockIdx.x] = tot;
+}
+
+__global__ void scan_top_kernel(uint32_t* __restrict__ sums, int nchunks) {
+  uint32_t carry = 0;
+  for (int c0 = 0; c0 < nchunks; c0 += SCAN_THREADS) {
+    const int i = c0 + threadIdx.x;
+    const uint32_t v = i < nchunks ? sums[i] : 0;
+    uint32_t tot;
+    const uint32_t ex = block_excl_scan(v, &tot);
+    if (i < nchunks) sums[i] = carry + ex;
+    carry += tot;
+  }
+}
+
+__global__ void scan_down_kernel(uint32_t* __restrict__ data, int64_t n,
+                                 const uint32_t* __restrict__ sums) {
+  const int64_t c0 = (int64_t)blockIdx.x * SCAN_CHUNK;
+  // blocked arrangement: thread t owns items [t*ITEMS, (t+1)*ITEMS)
+  uint32_t v[SCAN_ITEMS];
+  uint32_t s = 0;
+#pragma unroll
+  for (int j = 0; j < SCAN_ITEMS; ++j) {
+    const int64_t i = c0 + (int64_t)threadIdx.x * SCAN_ITEMS + j;
+    v[j] = i < n ? data[i] : 0;
+    s += v[j];
+  }
+  uint32_t run = block_excl_scan(s, nullptr) + sums[blockIdx.x];
+#pragma unroll
+  for (int j = 0; j < SCAN_ITEMS; ++j) {
+    const int64_t i = c0 + (int64_t)threadIdx.x * SCAN_ITEMS + j;
+    if (i < n) data[i] = run;
+    run += v[j];
+  }
+}
+
 // --------------------------------------------------------- sorted jobs ----
 __global__ void sorted_jobs_kernel(const TaskDev* __restrict__ tasks,
                                    const SortedJob* __restrict__ jobs, int njobs,
@@ -531,6 +695,21 @@ void launch_nest_sub(const TaskDev* tasks_d, const JobDev* jobs_d, const int32_t
   count_launch();
 }
 
+size_t sort_scan_tmp_elems(int nblk) {
+  const int64_t n = (int64_t)256 * nblk;
+  return (size_t)((n + SCAN_CHUNK - 1) / SCAN_CHUNK) + 1;
+}
+
+static void excl_scan(uint32_t* data, int64_t n, uint32_t* tmp, cudaStream_t st) {
+  const int nchunks = (int)((n + SCAN_CHUNK - 1) / SCAN_CHUNK);
+  scan_reduce_kernel<<<nchunks, SCAN_THREADS, 0, st>>>(data, n, tmp);
+  count_launch();
+  scan_top_kernel<<<1, SCAN_THREADS, 0, st>>>(tmp, nchunks);
+  count_launch();
+  scan_down_kernel<<<nchunks, SCAN_THREADS, 0, st>>>(data, n, tmp);
+  count_launch();
+}
+
 int init_sort_kernels() {
   return (int)cudaFuncSetAttribute(onesweep_pass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)sizeof(OsSmem));
@@ -574,27 +753,16 @@ void launch_sort(const TaskDev* tasks_d, const SortSeg* segs_d, const int32_t* b
   }
 }
 
-void launch_key_sort(const SortSeg* segs_d, const int32_t* blk_seg_d, int nblk,
-                     const int32_t* os_blk_seg_d, int os_nblk, int nseg, uint64_t* keys_a,
-                     int32_t* vals_a, uint64_t* keys_b, int32_t* vals_b, int npass, void* sweep,
-                     uint32_t* err, cudaStream_t st) {
-  if (nblk <= 0 || os_nblk <= 0 || npass <= 0) return;
-  unsigned long long* flags = (unsigned long long*)sweep;
-  uint32_t* seg_hist = (uint32_t*)(flags + 256 * (size_t)os_nblk);
-  int* counters = (int*)(seg_hist + OS_PASSES * 256 * (size_t)std::max(nseg, 1));
-  key_hist_kernel<<<nblk, SORT_THREADS, 0, st>>>(segs_d, blk_seg_d, keys_a, npass, seg_hist);
+void launch_radix_pass(const SortSeg* segs_d, const int32_t* blk_seg_d, int nblk,
+                       const uint64_t* kin, const int32_t* vin, uint64_t* kout, int32_t* vout,
+                       int shift, uint32_t* hist, uint32_t* scan_tmp, cudaStream_t st) {
+  if (nblk <= 0) return;
+  sort_hist_kernel<<<nblk, SORT_THREADS, 0, st>>>(segs_d, blk_seg_d, kin, shift, hist);
   count_launch();
-  uint64_t* kin = keys_a;
-  uint64_t* kout = keys_b;
-  int32_t* vin = vals_a;
-  int32_t* vout = vals_b;
-  for (int pass = 0; pass < npass; ++pass) {
-    onesweep_pass_kernel<<<os_nblk, OS_THREADS, sizeof(OsSmem), st>>>(
-        segs_d, os_blk_seg_d, kin, vin, kout, vout, pass, seg_hist, flags, counters + pass, err);
-    count_launch();
-    uint64_t* tk = kin; kin = kout; kout = tk;
-    int32_t* tv = vin; vin = vout; vout = tv;
-  }
+  excl_scan(hist, (int64_t)256 * nblk, scan_tmp, st);
+  sort_scatter_kernel<<<nblk, SORT_THREADS, 0, st>>>(segs_d, blk_seg_d, kin, vin, shift, hist,
+                                                     kout, vout);
+  count_launch();
 }
 
 void launch_sorted_jobs(const TaskDev* tasks_d, const SortedJob* jobs_d, int njobs,
