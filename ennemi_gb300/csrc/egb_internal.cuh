@@ -529,7 +529,7 @@ void launch_sort(const TaskDev* tasks_d, const SortSeg* segs_d, const int32_t* b
                  uint64_t* keys_b, int32_t* vals_a, int32_t* vals_b, void* sweep, int first,
                  uint32_t* err, cudaStream_t st,
                  cudaEvent_t* pass_events = nullptr);  // recorded around the passes alone
-constexpr int SORTED_BLOCK = 256;
+constexpr int SORTED_BLOCK = 128;
 void launch_sorted_jobs(const TaskDev* tasks_d, const SortedJob* jobs_d, int njobs,
                         int total_blocks, const KeyIndex& kx, const int32_t* perm, cudaStream_t st);
 
@@ -594,7 +594,7 @@ void launch_count_wgrid(const JobDev* jobs_d, const WorkItem* items_d, int nitem
 // <= 0, <= 1, <= 2 before the block, so a rank is one block read.
 constexpr int WM_TILE = 2048;      // values per block of the level passes
 constexpr int WM_SUPER = 64;       // tiles per super tile (prefix sums of digits)
-constexpr int WM_QBLOCK = 256;     // queries per block of the count kernel
+constexpr int WM_QBLOCK = 128;     // queries per block of the count kernel
 struct WmBlock {                   // 64 digits of one level
   uint32_t hi[2];                  // bit 1 of digit j at bit j % 32 of hi[j / 32]
   uint32_t lo[2];                  // bit 0
